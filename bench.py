@@ -1,0 +1,400 @@
+#!/usr/bin/env python
+"""Benchmark of the GB300 Reconflow solver: 720p frame pairs per second.
+
+Workload (default ``720p``): one 1280x720 float32 gray frame pair from the
+seeded synthetic scene generator (8 planes, depth 2-10 m, blob + 1/f
+texture, pose <= 2 deg / 0.1 m, N(0, 0.01) noise), 6 pyramid levels (x0.5),
+5 warps, 100 primal-dual iterations per warp, lambda = 50, theta = 0.33
+(alpha_tv = 1/theta), tau = 0.25, with the reference demo's projection weights
+(alpha_proj = 60, lambdaf = 0.1, lambdams = 100) and the K-pyramid fix.  One
+step = one full ReconFlow solve (flow, 3D points; inverse depth derived).
+
+``value``: pairs/s with the frames already in HBM (CUDA events on the solve
+stream, L2 flushed between steps).  ``e2e``: the same through the C ABI with
+host buffers: pinned upload of both frames, solve, download of flow, inverse
+depth and 3D points, every step.  ``roofline``: the dominant kernel at level
+0, timed live with CUDA events on its stream.  ``cpu_baseline``: the oracle's
+FP32 reference-semantics path on this host's cores, on a bounded sample.
+
+``--impl reference`` times the reference semantics on the host CPU (the FP32
+oracle; the reference itself cannot be built: it needs OpenCV and the texture
+reference API that CUDA 12 removed).  Several GPUs run independent replicas.
+"""
+from __future__ import annotations
+
+import argparse
+import ctypes
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+WORKLOADS = {
+    # 1280x720, 6 levels, 5 warps, 100 iterations: the headline workload
+    "720p": dict(width=1280, height=720, levels=6, warps=5, iters=100, seed=0),
+    # 640x480, 5 levels, 3 warps, 50 iterations (small case for profiling)
+    "480p": dict(width=640, height=480, levels=5, warps=3, iters=50, seed=0),
+}
+SOLVER = dict(method=14, lam=50.0, theta=0.33, tau=0.25, alpha_proj=60.0, lambdaf=0.1,
+              lambdams=100.0, fix_quirks=1)
+# algorithmic bytes per pixel per launch of the two inner-iteration kernels:
+# A reads u,v,duhat(2),p(4),uproj(2),sk(2),Ix,Iy,Iz,X,Y,Z = 18 floats, writes
+# duhat(2),uproj(2),X1,Y1,Z1 = 7; B reads duhat(2),p(4),X1(3),sk(2),u,v,uproj(2)
+# = 15, writes p(4),X,Y,Z,sk(2) = 9.
+ALG_BYTES = {"recon_a": 25 * 4, "recon_b": 24 * 4}
+L2_FLUSH_BYTES = 512 << 20
+
+
+def load_peaks():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        with open(p) as f:
+            d = json.load(f)
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+class ClockSampler:
+    """nvidia-smi clock / throttle samples while the timed region runs."""
+
+    Q = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.hw_slowdown,"
+         "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+         "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index=0):
+        self.index = index
+        self.proc = None
+        self.lines = []
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.index), f"--query-gpu={self.Q}",
+                 "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.thread = threading.Thread(target=self._read, daemon=True)
+            self.thread.start()
+        except OSError:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def __exit__(self, *a):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+            self.thread.join(timeout=2)
+
+    def summary(self):
+        sm, mx, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            parts = [x.strip() for x in ln.split(",")]
+            if len(parts) < 7:
+                continue
+            try:
+                sm.append(float(parts[0]))
+                mx.append(float(parts[1]))
+            except ValueError:
+                continue
+            for n, v in zip(names, parts[3:7]):
+                if v.lower() == "active":
+                    reasons.add(n)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": [], "samples": 0}
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(mx),
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def dist_setup(args):
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if world > 1:
+        import torch
+        import torch.distributed as dist
+
+        backend = "nccl" if torch.cuda.is_available() else "gloo"
+        if torch.cuda.is_available():
+            torch.cuda.set_device(local)
+        dist.init_process_group(backend)
+    return world, rank, local
+
+
+def barrier(world):
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.barrier()
+
+
+def max_over_ranks(x, world):
+    if world == 1:
+        return x
+    import torch
+    import torch.distributed as dist
+
+    t = torch.tensor([x], dtype=torch.float64,
+                     device="cuda" if torch.cuda.is_available() else "cpu")
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def make_inputs(wl):
+    from reconflow_gb300.scene import make_scene
+
+    sc = make_scene(wl["width"], wl["height"], seed=wl["seed"])
+    s = (wl["width"] + 31) // 32 * 32
+    pad = lambda a: np.pad(a, ((0, 0), (0, s - a.shape[1]))).astype(np.float32)  # noqa: E731
+    return sc, pad(sc["I0"]), pad(sc["I1"]), s
+
+
+def cpu_sample(wl, sc, I0, I1, threads=None):
+    """FP32 reference-semantics oracle on this host: the full schedule at 1
+    and 5 inner iterations, extrapolated linearly to the workload's count."""
+    from oracle import oracle as O
+
+    O.build()
+    if threads:
+        O.set_num_threads(threads)
+
+    def run(iters):
+        p = O.make_params(wl["width"], wl["height"], wl["levels"], method=SOLVER["method"],
+                          lam=SOLVER["lam"], lambdaf=SOLVER["lambdaf"],
+                          lambdams=SOLVER["lambdams"], alpha_tv=1.0 / SOLVER["theta"],
+                          alpha_proj=SOLVER["alpha_proj"], tau=SOLVER["tau"],
+                          n_warp_iters=wl["warps"], n_solver_iters=iters,
+                          fix_quirks=SOLVER["fix_quirks"])
+        t0 = time.perf_counter()
+        O.solve(p, I0, I1, K0=sc["K"], K1=sc["K"], R1=sc["R"], t1=sc["t"], dtype=np.float32)
+        return time.perf_counter() - t0
+
+    return run, O.num_threads()
+
+
+def extrapolate(t1, t5, iters):
+    per_iter = max(t5 - t1, 1e-9) / 4.0
+    return t1 + per_iter * (iters - 1)
+
+
+def run_reference(args, wl, world, rank):
+    if rank != 0:
+        return
+    sc, I0, I1, s = make_inputs(wl)
+    run, cores = cpu_sample(wl, sc, I0, I1)
+    t1 = min(run(1) for _ in range(max(1, args.warmup)))
+    per_pair = []
+    for _ in range(args.steps):
+        per_pair.append(extrapolate(t1, run(5), wl["iters"]))
+    total = sum(per_pair)
+    value = args.steps / total
+    sample = (f"{wl['width']}x{wl['height']} pair, full {wl['levels']}-level x {wl['warps']}-warp "
+              f"schedule at 1 and 5 inner iterations, extrapolated linearly to {wl['iters']}")
+    line = {
+        "impl": "reference", "metric": "720p frame pairs/s (ReconFlow flow + depth)",
+        "value": value, "unit": "pairs/s", "n_gpus": args.gpus, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": 1000.0 * total / args.steps,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+        "data": "synthetic (seeded scene generator)", "config": config_of(wl),
+        "cpu_baseline": {"value": value, "unit": "pairs/s", "cores": cores, "kind": "port",
+                         "sample": sample},
+        "e2e": {"value": value, "unit": "pairs/s", "h2d_bytes_per_step": 0,
+                "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+
+
+def config_of(wl):
+    return {"workload": f"reconflow_{wl['width']}x{wl['height']}_L{wl['levels']}_w{wl['warps']}"
+                        f"_i{wl['iters']}",
+            "width": wl["width"], "height": wl["height"], "pyramid_levels": wl["levels"],
+            "warps": wl["warps"], "iters": wl["iters"], "pairs_per_step": 1,
+            "method": "METHODR_TVL1_MS", "lambda": SOLVER["lam"], "theta": SOLVER["theta"],
+            "tau": SOLVER["tau"], "alpha_proj": SOLVER["alpha_proj"], "lambdaf": SOLVER["lambdaf"],
+            "lambdams": SOLVER["lambdams"], "fix_quirks": SOLVER["fix_quirks"],
+            "scene_seed": wl["seed"], "l2": "flushed between steps (512 MiB write)",
+            "parallelism": "replicas"}
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--workload", default="720p", choices=sorted(WORKLOADS))
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--solve-only", action="store_true",
+                    help="only warm-up + timed solves (for profiler launch lists)")
+    args = ap.parse_args()
+    wl = WORKLOADS[args.workload]
+    world, rank, local = dist_setup(args)
+    if args.impl == "reference":
+        run_reference(args, wl, world, rank)
+        return
+
+    import torch
+
+    import reconflow_gb300 as R
+
+    if not torch.cuda.is_available():
+        raise SystemExit("bench.py: no CUDA device (the solver has no CPU path)")
+    torch.cuda.set_device(local)
+    lib = R.load()
+    sc, I0, I1, s = make_inputs(wl)
+    f = R.ReconFlow()
+    f.initializeR(wl["width"], wl["height"], 1, wl["levels"], 2.0, SOLVER["method"], SOLVER["lam"],
+                  0.0, SOLVER["lambdaf"], SOLVER["lambdams"], 1.0 / SOLVER["theta"],
+                  SOLVER["alpha_proj"], 0.5, SOLVER["tau"], wl["warps"], wl["iters"], cvType=5,
+                  fix_quirks=SOLVER["fix_quirks"])
+    stream = torch.cuda.Stream()
+    f.setStream(stream.cuda_stream)
+    f.setCameraMatrices(sc["K"], sc["K"])
+    f.copyImagesToDevice(I0, I1)
+    flush = torch.empty(L2_FLUSH_BYTES // 4, dtype=torch.float32, device="cuda")
+
+    def solve():
+        f.solveR(sc["R"], sc["t"], 5.0)
+
+    with torch.cuda.stream(stream):
+        for _ in range(args.warmup):
+            solve()
+        torch.cuda.synchronize()
+        barrier(world)
+        launches0 = f.kernelLaunches()
+        evs = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
+               for _ in range(args.steps)]
+        with ClockSampler(local) as clk:
+            torch.cuda.synchronize()
+            wall0 = time.perf_counter()
+            for a, b in evs:
+                flush.zero_()
+                a.record(stream)
+                solve()
+                b.record(stream)
+            torch.cuda.synchronize()
+            wall = time.perf_counter() - wall0
+        launches = f.kernelLaunches() - launches0
+        step_ms = [a.elapsed_time(b) for a, b in evs]
+        total_s = max_over_ranks(sum(step_ms) / 1000.0, world)
+        barrier(world)
+    value = world * args.steps / total_s
+    if args.solve_only:
+        if rank == 0:
+            print(json.dumps({"metric": "720p frame pairs/s", "value": value, "unit": "pairs/s",
+                              "note": "solve-only run"}), flush=True)
+        return
+
+    # accuracy of the last solve against the generator's ground truth
+    u, v = f.copyOpticalFlowToHost()
+    X, Y, Z = f.copy3dToHost()
+    w, h = wl["width"], wl["height"]
+    val = sc["valid"]
+    epe = np.sqrt((u[:, :w] - sc["flow"][..., 0]) ** 2 + (v[:, :w] - sc["flow"][..., 1]) ** 2)[val]
+    with np.errstate(divide="ignore", invalid="ignore"):
+        inv = 1.0 / Z[:, :w]
+        rel = np.abs(inv - sc["inv_depth"]) / sc["inv_depth"]
+    accuracy = {"epe_mean_px": float(epe.mean()), "epe_median_px": float(np.median(epe)),
+                "inv_depth_rel_err_median": float(np.nanmedian(rel[val]))}
+
+    # end to end through the C ABI with pinned host buffers
+    e2e = None
+    if not args.no_e2e:
+        nbytes_plane = h * s * 4
+        hosts = []
+        for _ in range(8):
+            p = ctypes.c_void_p()
+            R._native.check(lib.rf_host_alloc(nbytes_plane, ctypes.byref(p)))
+            hosts.append(p)
+        np_h = [np.ctypeslib.as_array(ctypes.cast(p, ctypes.POINTER(ctypes.c_float)),
+                                      shape=(h, s)) for p in hosts]
+        np_h[0][:] = I0
+        np_h[1][:] = I1
+        hnd = f._handle()
+
+        def e2e_step():
+            R._native.check(lib.rf_upload_images(hnd, hosts[0], hosts[1], s))
+            f.solveR(sc["R"], sc["t"], 5.0)
+            R._native.check(lib.rf_download_flow(hnd, hosts[2], hosts[3], s))
+            R._native.check(lib.rf_download_inv_depth(hnd, hosts[4], s))
+            R._native.check(lib.rf_download_points(hnd, hosts[5], hosts[6], hosts[7], s))
+
+        for _ in range(max(1, args.warmup)):
+            e2e_step()
+        barrier(world)
+        times = []
+        for _ in range(args.steps):
+            flush.zero_()
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            e2e_step()
+            times.append(time.perf_counter() - t0)
+        e2e_total = max_over_ranks(sum(times), world)
+        e2e = {"value": world * args.steps / e2e_total, "unit": "pairs/s",
+               "h2d_bytes_per_step": 2 * w * h * 4, "d2h_bytes_per_step": 6 * w * h * 4}
+        for p in hosts:
+            lib.rf_host_free(p)
+
+    # roofline of the dominant kernel: level-0 inner iterations, CUDA events
+    ms = (ctypes.c_float * 2)()
+    f.solveR(sc["R"], sc["t"], 5.0)
+    R._native.check(lib.rf_profile_iterations(f._handle(), 0, 20, ms))
+    names = ["recon_a", "recon_b"]
+    dom = 0 if ms[0] >= ms[1] else 1
+    px = w * h
+    achieved = ALG_BYTES[names[dom]] * px / (ms[dom] * 1e-3) / 1e9
+    peak, peak_kind = load_peaks()
+    traffic = None
+    tpath = os.path.join(ROOT, "profiles", "traffic_720p.json")
+    if os.path.exists(tpath):
+        with open(tpath) as fh:
+            traffic = json.load(fh).get(names[dom])
+    roofline = {"bound": "hbm", "kernel": names[dom], "achieved": achieved, "peak": peak,
+                "peak_kind": peak_kind, "unit": "GB/s", "frac": achieved / peak,
+                "traffic": traffic, "alg_bytes_per_launch": ALG_BYTES[names[dom]] * px,
+                "launch_ms": {names[0]: ms[0], names[1]: ms[1]}}
+
+    cpu = None
+    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+        run, cores = cpu_sample(wl, sc, I0, I1)
+        t1 = run(1)
+        t5 = run(5)
+        per_pair = extrapolate(t1, t5, wl["iters"])
+        cpu = {"value": 1.0 / per_pair, "unit": "pairs/s", "cores": cores, "kind": "port",
+               "sample": f"{w}x{h} pair, full schedule at 1 and 5 inner iterations "
+                         f"({t1:.2f} s, {t5:.2f} s), extrapolated linearly to {wl['iters']}"}
+
+    if rank == 0:
+        line = {
+            "metric": "720p frame pairs/s (ReconFlow flow + depth)", "value": value,
+            "unit": "pairs/s", "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": 1000.0 * total_s / args.steps, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+            "data": "synthetic (seeded scene generator)", "config": config_of(wl),
+            "e2e": e2e, "roofline": roofline, "cpu_baseline": cpu,
+            "clocks": clk.summary(), "gpu_launches": int(launches),
+            "wall_s_timed": wall, "accuracy": accuracy,
+            "step_ms": {"min": min(step_ms), "median": statistics.median(step_ms),
+                        "max": max(step_ms)},
+        }
+        print(json.dumps(line), flush=True)
+    f.close()
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,240 @@
+/*
+ * reconflow_gb300 — C ABI of the GB300 (sm_103a) simultaneous optical-flow and
+ * depth solver.
+ *
+ * This is the drop-in boundary for the reference's ReconFlow / CudaFlow class
+ * surface (menandro/Reconflow, reconflow/Reconflow.h:9-160 and
+ * reconflow/Cudaflow.h:17-362).  Every entry point is plain C: handles,
+ * pointers, sizes and status codes; no CUDA, OpenCV or torch types appear in
+ * the signatures.  Each declaration names the reference member it replaces.
+ *
+ * Layout: every image and field is a row-major float32 plane with `stride`
+ * elements per row, stride = width aligned up to `stride_alignment` (32), as
+ * the reference pads its cv::Mat buffers (test_reconflow/main.cpp:57-67).
+ * Host buffers passed to the upload / download calls have a caller-chosen
+ * row pitch in elements (pass rf_stride(h) to match the reference exactly).
+ *
+ * Errors: every call returns an rf_status; the message of the last failure on
+ * the calling thread is available from rf_last_error_string().  The reference
+ * returns 0 unconditionally and aborts inside checkCudaErrors instead.
+ *
+ * Threading: handles share no global state; one host thread per handle.  All
+ * device work of a handle is ordered on the handle's CUDA stream.
+ */
+#ifndef RECONFLOW_GB300_H
+#define RECONFLOW_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define RF_API __attribute__((visibility("default")))
+
+typedef enum rf_status {
+    RF_OK = 0,
+    RF_ERR_INVALID_ARG = 1,  /* bad size, null pointer, mismatched dims */
+    RF_ERR_UNSUPPORTED = 2,  /* method / input type not implemented */
+    RF_ERR_CUDA = 3,         /* a CUDA runtime call failed */
+    RF_ERR_OOM = 4,          /* device or pinned allocation failed */
+    RF_ERR_STATE = 5,        /* call out of order (e.g. solve before upload) */
+    RF_ERR_NO_DEVICE = 6     /* no CUDA device visible */
+} rf_status;
+
+/* Method codes, numerically equal to the reference's constants
+ * (Cudaflow.h:20-28, Reconflow.h:46-52). */
+enum {
+    RF_METHOD_TVL1 = 0,            /* CudaFlow::METHOD_TVL1, plain TV-L1 flow */
+    RF_METHODR_TVL1_MS = 14,       /* ReconFlow::METHODR_TVL1_MS, flow + 3D */
+    RF_METHODR_TVL1_MS_FN = 17,    /* + dense prior flow term */
+    RF_METHODR_TVL1_MS_FNSPARSE = 20 /* + masked (sparse) prior flow term */
+};
+
+/* Input image types (the reference's cvType argument, Cudaflow.cu:288-311). */
+enum {
+    RF_INPUT_F32 = 0,   /* CV_32F gray, used as is (rgbToGray.cu:66-77) */
+    RF_INPUT_RGB8 = 1,  /* CV_8UC3, gray = (r+g+b)/3/256 (rgbToGray.cu:3-19) */
+    RF_INPUT_U8 = 2,    /* CV_8U, gray = v/256 (rgbToGray.cu:21-36) */
+    RF_INPUT_U16 = 3    /* CV_16U, gray = v/65536 (rgbToGray.cu:38-52) */
+};
+
+/* Reference behaviours that can be switched off (bit flags of fix_quirks).
+ * 0 reproduces the reference. */
+enum {
+    /* pK[l] (l >= 1) starts from zeros, so K[2][2] = 0 and the third rows of
+     * P and Q vanish at coarse levels (Reconflow.cu:98-110).  Set to use 1. */
+    RF_FIX_K_PYRAMID = 1,
+    /* X, Y, Z are not resampled at a level change; the coarse flat arrays are
+     * re-read with the finer stride (Reconflow.cu:424-458).  Set to resample
+     * them bilinearly instead. */
+    RF_FIX_XYZ_UPSCALE = 2
+};
+
+/* Solver parameters: the arguments of CudaFlow::initialize (Cudaflow.h:36-46)
+ * and ReconFlow::initializeR (Reconflow.h:67-70) in one POD block. */
+typedef struct rf_params {
+    int width, height;        /* level-0 image size */
+    int channels;             /* informational (reference `channels`) */
+    int input_type;           /* RF_INPUT_* */
+    int n_levels;             /* pyramid levels */
+    float scale;              /* pyramid factor fScale (2.0) */
+    int method;               /* RF_METHOD* */
+    float lambda;             /* data weight */
+    float lambdagrad;         /* accepted, unused by the implemented methods */
+    float lambdaf;            /* 3D / epipolar coupling weight */
+    float lambdams;           /* minimal-surface-area weight */
+    float alpha_tv;           /* ReconFlow: thetaTv = 1/alpha_tv */
+    float alpha_proj;         /* projection coupling */
+    float alpha_fn;           /* prior-flow weight (methods 17, 20) */
+    float tau;                /* dual step */
+    float theta;              /* plain TV-L1 coupling (method 0) */
+    int n_warp_iters;
+    int n_solver_iters;
+    int stride_alignment;     /* 32 in the reference */
+    int block_width, block_height; /* reference ctor launch shape; accepted, unused */
+    int fix_quirks;           /* RF_FIX_* bit flags, 0 = reference behaviour */
+} rf_params;
+
+typedef struct rf_handle rf_handle;
+
+/* Defaults of ReconFlow::initializeR (Reconflow.cu:15-18) for
+ * method != RF_METHOD_TVL1, of CudaFlow::initialize (Cudaflow.cu:16-18)
+ * otherwise; width/height/n_levels are left 0 for the caller. */
+RF_API rf_status rf_params_default(rf_params* p, int method);
+
+/* ReconFlow::ReconFlow + initializeR / CudaFlow::initialize
+ * (Reconflow.cu:9-63, Cudaflow.cu:99-269): validates the parameters and
+ * allocates every device buffer once, at level-0 size. */
+RF_API rf_status rf_create(const rf_params* p, rf_handle** out);
+
+/* ~ReconFlow / ~CudaFlow (Reconflow.cu:479-509, Cudaflow.cu:873-978). */
+RF_API rf_status rf_destroy(rf_handle* h);
+
+/* CudaFlow::iAlignUp(width) (Cudaflow.cu:984-994): the row stride in elements. */
+RF_API int rf_stride(const rf_handle* h);
+
+/* Level sizes of the pyramid (Cudaflow.cu:146-171); arrays of n_levels ints. */
+RF_API rf_status rf_pyramid_dims(const rf_handle* h, int* W, int* H, int* S);
+
+/* ReconFlow::setCameraMatrices(K0, K1) (Reconflow.cu:78-116): 3x3 row-major
+ * intrinsics of both cameras. */
+RF_API rf_status rf_set_cameras(rf_handle* h, const double K0[9], const double K1[9]);
+
+/* CudaFlow::copyImagesToDevice (Cudaflow.cu:288-311): host images of the
+ * handle's input type, `pitch` elements per row (pixels for RGB8). */
+RF_API rf_status rf_upload_images(rf_handle* h, const void* i0, const void* i1, int pitch);
+
+/* Same from device memory (no host copy; e.g. frames already in HBM). */
+RF_API rf_status rf_upload_images_device(rf_handle* h, const void* i0, const void* i1, int pitch);
+
+/* CudaFlow::copySparseOpticalFlowToDevice(u, v[, mask]) /
+ * copyInitialOpticalFlowToDevice (Cudaflow.cu:327-343): the prior flow of
+ * methods 17 and 20; mask may be NULL (all ones). */
+RF_API rf_status rf_set_prior_flow(rf_handle* h, const float* u, const float* v,
+                                   const float* mask, int pitch);
+
+/* ReconFlow::solveR(R0, t0, R1, t1, flowScale) -> solveReconFlow
+ * (Reconflow.cu:134-466).  R row-major 3x3, t 3x1, camera j maps a world
+ * point X to R_j X + t_j.  R0/t0 may be NULL (identity / zero, as
+ * solveR(R1, t1) does at Reconflow.cu:138-144).  Asynchronous on the
+ * handle's stream. */
+RF_API rf_status rf_solve(rf_handle* h, const double R0[9], const double t0[3],
+                          const double R1[9], const double t1[3]);
+
+/* CudaFlow::solveOpticalFlow (Cudaflow.cu:394-621): plain TV-L1 flow. */
+RF_API rf_status rf_solve_flow(rf_handle* h);
+
+/* CudaFlow::copyOpticalFlowToHost(u, v) (Cudaflow.cu:320-325). Blocking. */
+RF_API rf_status rf_download_flow(rf_handle* h, float* u, float* v, int pitch);
+
+/* ReconFlow::copy3dToHost(X, Y, Z) (Reconflow.cu:65-70). Blocking. */
+RF_API rf_status rf_download_points(rf_handle* h, float* X, float* Y, float* Z, int pitch);
+
+/* Inverse depth 1/Z of camera 0 (no reference counterpart: derived from
+ * d_Z, Reconflow.h:26).  Blocking. */
+RF_API rf_status rf_download_inv_depth(rf_handle* h, float* inv_depth, int pitch);
+
+/* CudaFlow::copyOpticalFlowToHost(u, v, uvrgb) colour part
+ * (Cudaflow.cu:313-318) via FlowToHSV (flowToHSV.cu:194-311): float RGB
+ * triples (B, G, R order as the reference's float3 x, y, z), 3*pitch floats
+ * per row. */
+RF_API rf_status rf_download_flow_color(rf_handle* h, float flow_scale, float* rgb, int pitch);
+
+/* ReconFlow::removeEdgeArtifacts3D (Reconflow.cu:468-477). */
+RF_API rf_status rf_remove_edge_artifacts(rf_handle* h, int surface_width, float max_area);
+
+/* Device pointers of the results (level-0 planes, rf_stride() per row);
+ * valid until the next solve or destroy.  Any pointer argument may be NULL. */
+RF_API rf_status rf_device_results(rf_handle* h, const float** u, const float** v,
+                                   const float** X, const float** Y, const float** Z);
+
+/* Use a caller's CUDA stream (cudaStream_t passed as void*; NULL = the
+ * handle's own stream). */
+RF_API rf_status rf_set_stream(rf_handle* h, void* stream);
+RF_API rf_status rf_synchronize(rf_handle* h);
+
+/* Pinned host memory for fast uploads/downloads. */
+RF_API rf_status rf_host_alloc(size_t bytes, void** ptr);
+RF_API rf_status rf_host_free(void* ptr);
+
+/* Timing hook (no reference counterpart): after a solve, run `n_iters` more
+ * inner iterations of the fused kernels at pyramid level `level` on the
+ * handle's stream, each launch bracketed by CUDA events, and return the mean
+ * duration of each kernel in milliseconds (ms[0] = data/projection/
+ * triangulation kernel, ms[1] = dual/median/clean-up kernel; plain TV-L1:
+ * data, dual).  Changes the solver state; results of the last solve are no
+ * longer valid afterwards. */
+RF_API rf_status rf_profile_iterations(rf_handle* h, int level, int n_iters, float* ms);
+
+/* Kernel launches issued by this handle so far (count of this library's
+ * kernels, graph nodes included). */
+RF_API uint64_t rf_kernel_launches(const rf_handle* h);
+
+/* Message of the last failing call on this thread ("" if none). */
+RF_API const char* rf_last_error_string(void);
+
+/* Library version string. */
+RF_API const char* rf_version(void);
+
+/* ------------------------------------------------------------------------
+ * Kernel-level entry points (device pointers, caller's stream).  Each runs
+ * one reference kernel's computation on one pyramid level so it can be
+ * checked against the oracle in isolation.  Arrays are stride-major planes.
+ * ---------------------------------------------------------------------- */
+
+/* DownscaleKernel / DownscaleScalingKernel (downscale.cu:6-48). */
+RF_API rf_status rfk_downscale(const float* src, int w, int h, int s, int nw, int nh, int ns,
+                               float scale, int scaled, float* out, void* stream);
+/* UpscaleKernel (upscale.cu:14-27). */
+RF_API rf_status rfk_upscale(const float* src, int w, int h, int s, int nw, int nh, int ns,
+                             float scale, float* out, void* stream);
+/* WarpingKernel (warpImage.cu:15-29). */
+RF_API rf_status rfk_warp(const float* src, int w, int h, int s, const float* u, const float* v,
+                          float* out, void* stream);
+/* ComputeDerivativesKernel (computeDerivatives.cu:8-57). */
+RF_API rf_status rfk_derivatives(const float* I0, const float* I1w, int w, int h, int s,
+                                 float* Ix, float* Iy, float* Iz, void* stream);
+/* MedianFilterKernel5 (medianFilter.cu:3-75). */
+RF_API rf_status rfk_median5(const float* u, const float* v, int w, int h, int s, float* ou,
+                             float* ov, void* stream);
+/* MedianFilter3DKernel3 (medianFilter.cu:166-243). */
+RF_API rf_status rfk_median3d(const float* X, const float* Y, const float* Z, int w, int h, int s,
+                              float* X1, float* Y1, float* Z1, void* stream);
+/* rgbaToGrayKernel (rgbToGray.cu:3-19). */
+RF_API rf_status rfk_rgb_to_gray(const uint8_t* rgb, int w, int h, int s, float* out,
+                                 void* stream);
+/* RemoveEdgeArtifacts3DKernel (solve3dMinimalArea.cu:320-378). */
+RF_API rf_status rfk_remove_edge_artifacts(const float* X, const float* Y, const float* Z,
+                                           int range, float max_area, int w, int h, int s,
+                                           float* X1, float* Y1, float* Z1, void* stream);
+/* ComputeColorKernel (flowToHSV.cu:194-302). */
+RF_API rf_status rfk_flow_to_color(const float* u, const float* v, int w, int h, int s,
+                                   float flow_scale, float* rgb, void* stream);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* RECONFLOW_GB300_H */

@@ -1,0 +1,113 @@
+"""ctypes binding of the C ABI (``include/reconflow_gb300.h``).
+
+The CUDA library is built in-tree (``reconflow_gb300/lib/librfgb300.so``).  If
+it is missing or cannot be loaded, every call raises: there is no CPU
+fallback.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+
+_HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(_HERE, "lib", "librfgb300.so")
+
+RF_OK = 0
+STATUS_NAMES = {0: "RF_OK", 1: "RF_ERR_INVALID_ARG", 2: "RF_ERR_UNSUPPORTED", 3: "RF_ERR_CUDA",
+                4: "RF_ERR_OOM", 5: "RF_ERR_STATE", 6: "RF_ERR_NO_DEVICE"}
+
+METHOD_TVL1 = 0
+METHODR_TVL1_MS = 14
+METHODR_TVL1_MS_FN = 17
+METHODR_TVL1_MS_FNSPARSE = 20
+
+INPUT_F32, INPUT_RGB8, INPUT_U8, INPUT_U16 = 0, 1, 2, 3
+FIX_K_PYRAMID, FIX_XYZ_UPSCALE = 1, 2
+
+
+class RfError(RuntimeError):
+    def __init__(self, status: int, message: str):
+        super().__init__(f"{STATUS_NAMES.get(status, status)}: {message}")
+        self.status = status
+
+
+class RfParams(ctypes.Structure):
+    _fields_ = [
+        ("width", ctypes.c_int), ("height", ctypes.c_int), ("channels", ctypes.c_int),
+        ("input_type", ctypes.c_int), ("n_levels", ctypes.c_int), ("scale", ctypes.c_float),
+        ("method", ctypes.c_int), ("lambda_", ctypes.c_float), ("lambdagrad", ctypes.c_float),
+        ("lambdaf", ctypes.c_float), ("lambdams", ctypes.c_float), ("alpha_tv", ctypes.c_float),
+        ("alpha_proj", ctypes.c_float), ("alpha_fn", ctypes.c_float), ("tau", ctypes.c_float),
+        ("theta", ctypes.c_float), ("n_warp_iters", ctypes.c_int), ("n_solver_iters", ctypes.c_int),
+        ("stride_alignment", ctypes.c_int), ("block_width", ctypes.c_int),
+        ("block_height", ctypes.c_int), ("fix_quirks", ctypes.c_int),
+    ]
+
+
+# (name, restype, argtypes) of every exported entry point
+_VP, _I, _F, _D = ctypes.c_void_p, ctypes.c_int, ctypes.c_float, ctypes.c_void_p
+_SIGS = [
+    ("rf_params_default", _I, [ctypes.POINTER(RfParams), _I]),
+    ("rf_create", _I, [ctypes.POINTER(RfParams), ctypes.POINTER(_VP)]),
+    ("rf_destroy", _I, [_VP]),
+    ("rf_stride", _I, [_VP]),
+    ("rf_pyramid_dims", _I, [_VP, _VP, _VP, _VP]),
+    ("rf_set_cameras", _I, [_VP, _D, _D]),
+    ("rf_upload_images", _I, [_VP, _VP, _VP, _I]),
+    ("rf_upload_images_device", _I, [_VP, _VP, _VP, _I]),
+    ("rf_set_prior_flow", _I, [_VP, _VP, _VP, _VP, _I]),
+    ("rf_solve", _I, [_VP, _D, _D, _D, _D]),
+    ("rf_solve_flow", _I, [_VP]),
+    ("rf_download_flow", _I, [_VP, _VP, _VP, _I]),
+    ("rf_download_points", _I, [_VP, _VP, _VP, _VP, _I]),
+    ("rf_download_inv_depth", _I, [_VP, _VP, _I]),
+    ("rf_download_flow_color", _I, [_VP, _F, _VP, _I]),
+    ("rf_remove_edge_artifacts", _I, [_VP, _I, _F]),
+    ("rf_device_results", _I, [_VP, _VP, _VP, _VP, _VP, _VP]),
+    ("rf_set_stream", _I, [_VP, _VP]),
+    ("rf_synchronize", _I, [_VP]),
+    ("rf_host_alloc", _I, [ctypes.c_size_t, ctypes.POINTER(_VP)]),
+    ("rf_host_free", _I, [_VP]),
+    ("rf_profile_iterations", _I, [_VP, _I, _I, _VP]),
+    ("rf_kernel_launches", ctypes.c_uint64, [_VP]),
+    ("rf_last_error_string", ctypes.c_char_p, []),
+    ("rf_version", ctypes.c_char_p, []),
+    ("rfk_downscale", _I, [_VP, _I, _I, _I, _I, _I, _I, _F, _I, _VP, _VP]),
+    ("rfk_upscale", _I, [_VP, _I, _I, _I, _I, _I, _I, _F, _VP, _VP]),
+    ("rfk_warp", _I, [_VP, _I, _I, _I, _VP, _VP, _VP, _VP]),
+    ("rfk_derivatives", _I, [_VP, _VP, _I, _I, _I, _VP, _VP, _VP, _VP]),
+    ("rfk_median5", _I, [_VP, _VP, _I, _I, _I, _VP, _VP, _VP]),
+    ("rfk_median3d", _I, [_VP, _VP, _VP, _I, _I, _I, _VP, _VP, _VP, _VP]),
+    ("rfk_rgb_to_gray", _I, [_VP, _I, _I, _I, _VP, _VP]),
+    ("rfk_remove_edge_artifacts", _I, [_VP, _VP, _VP, _I, _F, _I, _I, _I, _VP, _VP, _VP, _VP]),
+    ("rfk_flow_to_color", _I, [_VP, _VP, _I, _I, _I, _F, _VP, _VP]),
+]
+
+EXPORTED = [s[0] for s in _SIGS]
+
+_lib = None
+
+
+def load(path: str | None = None):
+    """Load the CUDA library (building it first if absent); raises if impossible."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    path = path or LIB_PATH
+    if not os.path.exists(path):
+        from . import build as _build
+
+        _build.build()
+    lib = ctypes.CDLL(path)
+    for name, res, args in _SIGS:
+        fn = getattr(lib, name)
+        fn.restype = res
+        fn.argtypes = args
+    _lib = lib
+    return lib
+
+
+def check(status: int) -> None:
+    if status != RF_OK:
+        msg = load().rf_last_error_string().decode(errors="replace")
+        raise RfError(status, msg)

@@ -1,0 +1,87 @@
+"""Build the in-tree CUDA library ``reconflow_gb300/lib/librfgb300.so``.
+
+Every translation unit is compiled for sm_103a only, in parallel, with
+``-fmad=false`` for the solver kernels (IEEE division / square root and no
+multiply-add contraction, so results are a deterministic function of the
+inputs) and linked into one shared library with the C ABI of
+``include/reconflow_gb300.h``.
+"""
+from __future__ import annotations
+
+import os
+import shutil
+import subprocess
+import sys
+from concurrent.futures import ThreadPoolExecutor
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ROOT = os.path.dirname(HERE)
+CSRC = os.path.join(HERE, "csrc")
+LIB_DIR = os.path.join(HERE, "lib")
+LIB_PATH = os.path.join(LIB_DIR, "librfgb300.so")
+OBJ_DIR = os.path.join(HERE, "_build")
+
+ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
+# per-file flags: the solver keeps exact IEEE arithmetic without contraction
+SOURCES = {
+    "rf_kernels.cu": ["-fmad=false"],
+    "rf_solver.cu": ["-fmad=false"],
+}
+COMMON = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC,-ffp-contract=off,-fvisibility=hidden",
+          "--expt-relaxed-constexpr", "-I" + os.path.join(ROOT, "include"), "-I" + CSRC]
+
+
+def nvcc() -> str:
+    for cand in (os.environ.get("NVCC"), shutil.which("nvcc"), "/usr/local/cuda/bin/nvcc"):
+        if cand and os.path.exists(cand):
+            return cand
+    raise RuntimeError("nvcc not found: the CUDA toolkit is required to build reconflow_gb300")
+
+
+def _stale(target: str, deps) -> bool:
+    if not os.path.exists(target):
+        return True
+    t = os.path.getmtime(target)
+    return any(os.path.getmtime(d) > t for d in deps)
+
+
+def _headers():
+    out = [os.path.join(ROOT, "include", f) for f in os.listdir(os.path.join(ROOT, "include"))]
+    out += [os.path.join(CSRC, f) for f in os.listdir(CSRC) if f.endswith((".cuh", ".h"))]
+    return out
+
+
+def build(force: bool = False, verbose: bool = False) -> str:
+    os.makedirs(LIB_DIR, exist_ok=True)
+    os.makedirs(OBJ_DIR, exist_ok=True)
+    nv = nvcc()
+    hdrs = _headers()
+    jobs = []
+    objs = []
+    for src, flags in SOURCES.items():
+        s = os.path.join(CSRC, src)
+        o = os.path.join(OBJ_DIR, src.replace(".cu", ".o"))
+        objs.append(o)
+        if force or _stale(o, [s] + hdrs):
+            jobs.append([nv, "-c", s, "-o", o] + ARCH + COMMON + flags)
+
+    def run(cmd):
+        if verbose:
+            print(" ".join(cmd), flush=True)
+        r = subprocess.run(cmd, capture_output=True, text=True)
+        if r.returncode != 0:
+            raise RuntimeError(f"nvcc failed:\n{' '.join(cmd)}\n{r.stdout}\n{r.stderr}")
+        return r.stdout + r.stderr
+
+    with ThreadPoolExecutor(max_workers=max(1, len(jobs))) as ex:
+        for log in ex.map(run, jobs):
+            if verbose and log.strip():
+                print(log)
+    if force or jobs or _stale(LIB_PATH, objs):
+        run([nv, "-shared", "-o", LIB_PATH] + objs + ARCH + ["-Xcompiler", "-fPIC", "-lcudart_static",
+                                                              "-ldl", "-lrt", "-lpthread"])
+    return LIB_PATH
+
+
+if __name__ == "__main__":
+    print(build(force="--force" in sys.argv, verbose=True))

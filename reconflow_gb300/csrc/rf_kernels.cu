@@ -1,0 +1,727 @@
+// CUDA kernels of the Reconflow flow + depth path for sm_103a.
+//
+// Layout: float32 planes, row-major, `s` elements per row, every buffer sized
+// for level 0 plus one zero guard row; level l uses the first h_l rows with
+// stride s_l (the reference's flat reuse, Reconflow.cu:42-61).
+//
+// One ReconFlow inner iteration (Reconflow.cu:284-406, eight launches in the
+// reference) runs as two kernels:
+//   recon_a: data step (solveReconDataL1.cu:4-102), projection blend
+//            (solveUVProj.cu:4-22) with uc recomputed from the current 3D
+//            state (solveUcSk.cu:3-35), and the per-pixel 3x3 triangulation
+//            (solve3dMinimalArea.cu:3-193);
+//   recon_b: dual TV step (solveSmoothDualTVGlobal.cu:4-65), 3x3 median of
+//            the 3D points (medianFilter.cu:166-243), outlier clean-up
+//            (solve3dMinimalArea.cu:248-297) and the multiplier update
+//            (solveUcSk.cu:80-97).
+// All pixel-local state (duhat, p, uproj, sk) is updated in place: each is
+// read at a neighbour only by the other kernel of the pair.
+#include <cstdint>
+
+#include "rf_kernels.cuh"
+
+namespace rf {
+
+namespace {
+
+constexpr int BX = 32;
+constexpr int BY = 8;
+
+inline dim3 grid_for(int w, int h) { return dim3((w + BX - 1) / BX, (h + BY - 1) / BY); }
+
+inline int check_launch() { return cudaGetLastError() == cudaSuccess ? 0 : 1; }
+
+// ---------------------------------------------------------------------------
+// Input conversion (rgbToGray.cu:3-77)
+// ---------------------------------------------------------------------------
+__global__ void k_convert(const void* __restrict__ in, int type, int w, int h, int in_pitch,
+                          float* __restrict__ out, int s) {
+    int ix = blockIdx.x * blockDim.x + threadIdx.x;
+    int iy = blockIdx.y * blockDim.y + threadIdx.y;
+    if (ix >= w || iy >= h) return;
+    size_t i = (size_t)ix + (size_t)iy * in_pitch;
+    float g;
+    if (type == 1) {
+        const uint8_t* p = static_cast<const uint8_t*>(in) + 3 * i;
+        g = ((float)p[0] + (float)p[1] + (float)p[2]) / 3.0f;
+        g = g / 256.0f;
+    } else if (type == 2) {
+        g = (float)static_cast<const uint8_t*>(in)[i] / 256.0f;
+    } else if (type == 3) {
+        g = (float)static_cast<const uint16_t*>(in)[i] / 65536.0f;
+    } else {
+        g = static_cast<const float*>(in)[i];
+    }
+    out[ix + iy * s] = g;
+}
+
+// ---------------------------------------------------------------------------
+// Pyramid (downscale.cu:6-48, upscale.cu:14-27)
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ float downscale_px(const float* __restrict__ src, LevelDims f, int nw,
+                                              int nh, int ix, int iy) {
+    float dx = 1.0f / (float)nw;
+    float dy = 1.0f / (float)nh;
+    float x = ((float)ix + 0.5f) * dx;
+    float y = ((float)iy + 0.5f) * dy;
+    return tex2d(src, f.w, f.h, f.s, x - dx * 0.25f, y) + tex2d(src, f.w, f.h, f.s, x + dx * 0.25f, y) +
+           tex2d(src, f.w, f.h, f.s, x, y - dy * 0.25f) + tex2d(src, f.w, f.h, f.s, x, y + dy * 0.25f);
+}
+
+__global__ void k_downscale2(const float* __restrict__ a, const float* __restrict__ b, LevelDims f,
+                             LevelDims c, float* __restrict__ oa, float* __restrict__ ob) {
+    int ix = blockIdx.x * blockDim.x + threadIdx.x;
+    int iy = blockIdx.y * blockDim.y + threadIdx.y;
+    if (ix >= c.w || iy >= c.h) return;
+    oa[ix + iy * c.s] = 0.25f * downscale_px(a, f, c.w, c.h, ix, iy);
+    ob[ix + iy * c.s] = 0.25f * downscale_px(b, f, c.w, c.h, ix, iy);
+}
+
+__global__ void k_downscale(const float* __restrict__ src, LevelDims f, LevelDims c, float scale,
+                            int scaled, float* __restrict__ out) {
+    int ix = blockIdx.x * blockDim.x + threadIdx.x;
+    int iy = blockIdx.y * blockDim.y + threadIdx.y;
+    if (ix >= c.w || iy >= c.h) return;
+    float sum = downscale_px(src, f, c.w, c.h, ix, iy);
+    out[ix + iy * c.s] = scaled ? scale * 0.25f * sum : 0.25f * sum;
+}
+
+struct UpscaleArgs {
+    const float* src[12];
+    float* dst[12];
+    float scale[12];
+    int n;
+};
+
+__global__ void k_upscale_fields(UpscaleArgs a, LevelDims c, LevelDims f) {
+    int ix = blockIdx.x * blockDim.x + threadIdx.x;
+    int iy = blockIdx.y * blockDim.y + threadIdx.y;
+    if (ix >= f.w || iy >= f.h) return;
+    float x = ((float)ix + 0.5f) / (float)f.w;
+    float y = ((float)iy + 0.5f) / (float)f.h;
+    Taps tx = taps_of(x, c.w);
+    Taps ty = taps_of(y, c.h);
+    int pos = ix + iy * f.s;
+#pragma unroll 1
+    for (int i = 0; i < a.n; i++) a.dst[i][pos] = bilerp(a.src[i], c.s, tx, ty) * a.scale[i];
+}
+
+// ---------------------------------------------------------------------------
+// Warp and derivatives (warpImage.cu:15-29, computeDerivatives.cu:8-57)
+// ---------------------------------------------------------------------------
+__global__ void k_warp(const float* __restrict__ I1, const float* __restrict__ u,
+                       const float* __restrict__ v, LevelDims d, float* __restrict__ out) {
+    int ix = blockIdx.x * blockDim.x + threadIdx.x;
+    int iy = blockIdx.y * blockDim.y + threadIdx.y;
+    if (ix >= d.w || iy >= d.h) return;
+    int pos = ix + iy * d.s;
+    float x = ((float)ix + u[pos] + 0.5f) / (float)d.w;
+    float y = ((float)iy + v[pos] + 0.5f) / (float)d.h;
+    out[pos] = tex2d(I1, d.w, d.h, d.s, x, y);
+}
+
+__device__ __forceinline__ float deriv5(float m2, float m1, float p1, float p2) {
+    float t = m2;
+    t -= m1 * 8.0f;
+    t += p1 * 8.0f;
+    t -= p2;
+    t /= 12.0f;
+    return t;
+}
+
+__global__ void k_derivatives(const float* __restrict__ I0, const float* __restrict__ I1,
+                              LevelDims d, float* __restrict__ Ix, float* __restrict__ Iy,
+                              float* __restrict__ Iz) {
+    int ix = blockIdx.x * blockDim.x + threadIdx.x;
+    int iy = blockIdx.y * blockDim.y + threadIdx.y;
+    if (ix >= d.w || iy >= d.h) return;
+    int row = iy * d.s;
+    int pos = ix + row;
+    int xm2 = mirror_index(ix - 2, d.w) + row, xm1 = mirror_index(ix - 1, d.w) + row;
+    int xp1 = mirror_index(ix + 1, d.w) + row, xp2 = mirror_index(ix + 2, d.w) + row;
+    int ym2 = ix + mirror_index(iy - 2, d.h) * d.s, ym1 = ix + mirror_index(iy - 1, d.h) * d.s;
+    int yp1 = ix + mirror_index(iy + 1, d.h) * d.s, yp2 = ix + mirror_index(iy + 2, d.h) * d.s;
+    float t0 = deriv5(I0[xm2], I0[xm1], I0[xp1], I0[xp2]);
+    float t1 = deriv5(I1[xm2], I1[xm1], I1[xp1], I1[xp2]);
+    Ix[pos] = (t0 + t1) * 0.5f;
+    Iz[pos] = I1[pos] - I0[pos];
+    t0 = deriv5(I0[ym2], I0[ym1], I0[yp1], I0[yp2]);
+    t1 = deriv5(I1[ym2], I1[ym1], I1[yp1], I1[yp2]);
+    Iy[pos] = (t0 + t1) * 0.5f;
+}
+
+// ---------------------------------------------------------------------------
+// ReconFlow inner iteration, part A: data step, projection blend, Solve3d
+// ---------------------------------------------------------------------------
+template <int PRIOR>
+__global__ void __launch_bounds__(BX* BY) k_recon_a(ReconFields f, const LevelConsts* __restrict__ lcp,
+                                                    Weights wt, LevelDims d, int first,
+                                                    int uc_from_buffer) {
+    int ix = blockIdx.x * blockDim.x + threadIdx.x;
+    int iy = blockIdx.y * blockDim.y + threadIdx.y;
+    if (ix >= d.w || iy >= d.h) return;
+    const int s = d.s;
+    const int pos = ix + iy * s;
+    const LevelConsts& c = *lcp;
+
+    // --- data step (solveReconDataL1.cu:24-100) ---
+    float u = f.u[pos], v = f.v[pos];
+    float dix = f.Ix[pos], diy = f.Iy[pos], dit = f.Iz[pos];
+    float uproj = f.uproj[pos], vproj = f.vproj[pos];
+    float sku = f.sku[pos], skv = f.skv[pos];
+    float duhat = 0.0f, dvhat = 0.0f;
+    float pu1 = 0.0f, pu2 = 0.0f, pv1 = 0.0f, pv2 = 0.0f;
+    float pu1l = 0.0f, pv1l = 0.0f, pu2d = 0.0f, pv2d = 0.0f;
+    if (!first) {
+        duhat = f.duhat[pos];
+        dvhat = f.dvhat[pos];
+        pu1 = f.pu1[pos];
+        pu2 = f.pu2[pos];
+        pv1 = f.pv1[pos];
+        pv2 = f.pv2[pos];
+        if (ix > 0) {
+            pu1l = f.pu1[pos - 1];
+            pv1l = f.pv1[pos - 1];
+        }
+        if (iy > 0) {
+            pu2d = f.pu2[pos - s];
+            pv2d = f.pv2[pos - s];
+        }
+    }
+    float A, dusub, dvsub;
+    if (PRIOR == 0) {
+        A = wt.A;
+        dusub = (wt.alpha_tv * duhat + wt.alpha_proj * (uproj - u - sku)) / A;
+        dvsub = (wt.alpha_tv * dvhat + wt.alpha_proj * (vproj - v - skv)) / A;
+    } else {
+        float alphaFn = PRIOR == 2 ? wt.alpha_fn * f.mask[pos] : wt.alpha_fn;
+        float ufn = f.ufn[pos], vfn = f.vfn[pos];
+        A = wt.alpha_tv + wt.alpha_proj + alphaFn;
+        dusub = (alphaFn * (ufn - u) + wt.alpha_tv * duhat + wt.alpha_proj * (uproj - u - sku)) / A;
+        dvsub = (alphaFn * (vfn - v) + wt.alpha_tv * dvhat + wt.alpha_proj * (vproj - v - skv)) / A;
+    }
+    float du, dv;
+    l1_threshold(dusub, dvsub, dix, diy, dit, wt.lambda, A, du, dv);
+    float divpu = divergence(pu1, pu1l, pu2, pu2d, ix, iy);
+    float divpv = divergence(pv1, pv1l, pv2, pv2d, ix, iy);
+    float duhat1 = du + divpu / A;
+    float dvhat1 = dv + divpv / A;
+    f.duhat[pos] = duhat1;
+    f.dvhat[pos] = dvhat1;
+
+    // --- projection blend (solveUVProj.cu:13-21), uc from the current 3D ---
+    float Xn[5], Yn[5], Zn[5];
+    Xn[0] = f.X[pos];
+    Yn[0] = f.Y[pos];
+    Zn[0] = f.Z[pos];
+    float uc, vc;
+    if (uc_from_buffer) {
+        uc = f.uc[pos];
+        vc = f.vc[pos];
+    } else {
+        project_uc(c, Xn[0], Yn[0], Zn[0], ix, iy, uc, vc);
+    }
+    float uproj1 = (wt.lambdaf * uc + wt.alpha_proj * (u + duhat1 + sku)) / wt.proj_den;
+    float vproj1 = (wt.lambdaf * vc + wt.alpha_proj * (v + dvhat1 + skv)) / wt.proj_den;
+    f.uproj[pos] = uproj1;
+    f.vproj[pos] = vproj1;
+
+    // --- triangulation with minimal-area smoothing (solve3dMinimalArea.cu:23-184) ---
+    // x+1 / y+1 are read at flat pos+1 / pos+s even on the last column / row.
+    Xn[1] = f.X[pos + 1];
+    Yn[1] = f.Y[pos + 1];
+    Zn[1] = f.Z[pos + 1];
+    Xn[2] = f.X[pos + s];
+    Yn[2] = f.Y[pos + s];
+    Zn[2] = f.Z[pos + s];
+    Xn[3] = Yn[3] = Zn[3] = 0.0f;
+    Xn[4] = Yn[4] = Zn[4] = 0.0f;
+    if (ix > 0) {
+        Xn[3] = f.X[pos - 1];
+        Yn[3] = f.Y[pos - 1];
+        Zn[3] = f.Z[pos - 1];
+    }
+    if (iy > 0) {
+        Xn[4] = f.X[pos - s];
+        Yn[4] = f.Y[pos - s];
+        Zn[4] = f.Z[pos - s];
+    }
+    float Xo, Yo, Zo;
+    solve3d_pixel(c, uproj1, vproj1, ix, iy, Xn, Yn, Zn, wt.lambdaf, wt.lambdams, Xo, Yo, Zo);
+    f.X1[pos] = Xo;
+    f.Y1[pos] = Yo;
+    f.Z1[pos] = Zo;
+}
+
+// 3x3 tap of the reference's 3D median with its border rules
+// (medianFilter.cu:181-214): left / top clamp, right / bottom and corners 0.
+__device__ __forceinline__ int median3_tap(int col, int row, int w, int h, int s) {
+    if (col >= 0 && col < w && row >= 0 && row < h) return col + s * row;
+    if (col < 0 && row >= 0 && row < h) return s * row;
+    if (col >= 0 && col < w && row < 0) return col;
+    return -1;
+}
+
+// ---------------------------------------------------------------------------
+// ReconFlow inner iteration, part B: dual step, 3D median, clean-up, sk
+// ---------------------------------------------------------------------------
+__global__ void __launch_bounds__(BX* BY) k_recon_b(ReconFields f, Weights wt, LevelDims d,
+                                                    int first) {
+    int ix = blockIdx.x * blockDim.x + threadIdx.x;
+    int iy = blockIdx.y * blockDim.y + threadIdx.y;
+    if (ix >= d.w || iy >= d.h) return;
+    const int s = d.s, w = d.w, h = d.h;
+    const int pos = ix + iy * s;
+
+    // --- dual TV step (solveSmoothDualTVGlobal.cu:26-64) ---
+    float duhat = f.duhat[pos], dvhat = f.dvhat[pos];
+    float dux, duy, dvx, dvy;
+    if ((ix + 1) >= w) {
+        dux = 0.0f;
+        dvx = 0.0f;
+    } else {
+        dux = f.duhat[pos + 1] - duhat;
+        dvx = f.dvhat[pos + 1] - dvhat;
+    }
+    if ((iy + 1) >= h) {
+        duy = 0.0f;
+        dvy = 0.0f;
+    } else {
+        duy = f.duhat[pos + s] - duhat;
+        dvy = f.dvhat[pos + s] - dvhat;
+    }
+    float pu1 = 0.0f, pu2 = 0.0f, pv1 = 0.0f, pv2 = 0.0f;
+    if (!first) {
+        pu1 = f.pu1[pos];
+        pu2 = f.pu2[pos];
+        pv1 = f.pv1[pos];
+        pv2 = f.pv2[pos];
+    }
+    dual_step(dux, duy, wt.fac, pu1, pu2);
+    dual_step(dvx, dvy, wt.fac, pv1, pv2);
+    f.pu1[pos] = pu1;
+    f.pu2[pos] = pu2;
+    f.pv1[pos] = pv1;
+    f.pv2[pos] = pv2;
+
+    // --- 3x3 median of the triangulated points, then clean-up ---
+    float mX[9], mY[9], mZ[9];
+#pragma unroll
+    for (int j = 0; j < 3; j++) {
+#pragma unroll
+        for (int i = 0; i < 3; i++) {
+            int at = median3_tap(ix + i - 1, iy + j - 1, w, h, s);
+            int k = j * 3 + i;
+            if (at >= 0) {
+                mX[k] = f.X1[at];
+                mY[k] = f.Y1[at];
+                mZ[k] = f.Z1[at];
+            } else {
+                mX[k] = 0.0f;
+                mY[k] = 0.0f;
+                mZ[k] = 0.0f;
+            }
+        }
+    }
+    float X1 = mX[4], Y1 = mY[4], Z1 = mZ[4];
+    float Xm = median9_exchange(mX);
+    float Ym = median9_exchange(mY);
+    float Zm = median9_exchange(mZ);
+    float Xo, Yo, Zo;
+    cleanup_pixel(X1, Y1, Z1, Xm, Ym, Zm, Xo, Yo, Zo);
+    f.X[pos] = Xo;
+    f.Y[pos] = Yo;
+    f.Z[pos] = Zo;
+
+    // --- multiplier update (solveUcSk.cu:94-95) ---
+    f.sku[pos] = f.sku[pos] + f.u[pos] + duhat - f.uproj[pos];
+    f.skv[pos] = f.skv[pos] + f.v[pos] + dvhat - f.vproj[pos];
+}
+
+// ---------------------------------------------------------------------------
+// Plain TV-L1 (solveDataL1.cu:4-91 + solveSmoothDualTVGlobal.cu:4-65)
+// ---------------------------------------------------------------------------
+__global__ void k_plain_data(float* __restrict__ duhat0, float* __restrict__ dvhat0,
+                             const float* __restrict__ pu1, const float* __restrict__ pu2,
+                             const float* __restrict__ pv1, const float* __restrict__ pv2,
+                             const float* __restrict__ Ix, const float* __restrict__ Iy,
+                             const float* __restrict__ Iz, Weights wt, LevelDims d, int first) {
+    int ix = blockIdx.x * blockDim.x + threadIdx.x;
+    int iy = blockIdx.y * blockDim.y + threadIdx.y;
+    if (ix >= d.w || iy >= d.h) return;
+    const int s = d.s;
+    const int pos = ix + iy * s;
+    float duhat = 0.0f, dvhat = 0.0f;
+    float p1u = 0.0f, p2u = 0.0f, p1v = 0.0f, p2v = 0.0f, p1ul = 0.0f, p1vl = 0.0f, p2ud = 0.0f,
+          p2vd = 0.0f;
+    if (!first) {
+        duhat = duhat0[pos];
+        dvhat = dvhat0[pos];
+        p1u = pu1[pos];
+        p2u = pu2[pos];
+        p1v = pv1[pos];
+        p2v = pv2[pos];
+        if (ix > 0) {
+            p1ul = pu1[pos - 1];
+            p1vl = pv1[pos - 1];
+        }
+        if (iy > 0) {
+            p2ud = pu2[pos - s];
+            p2vd = pv2[pos - s];
+        }
+    }
+    float du, dv;
+    l1_threshold_plain(duhat, dvhat, Ix[pos], Iy[pos], Iz[pos], wt.lambda, wt.theta, du, dv);
+    float divpu = divergence(p1u, p1ul, p2u, p2ud, ix, iy);
+    float divpv = divergence(p1v, p1vl, p2v, p2vd, ix, iy);
+    duhat0[pos] = du + wt.theta * divpu;
+    dvhat0[pos] = dv + wt.theta * divpv;
+}
+
+__global__ void k_plain_tv(const float* __restrict__ duhat, const float* __restrict__ dvhat,
+                           float* __restrict__ pu1, float* __restrict__ pu2,
+                           float* __restrict__ pv1, float* __restrict__ pv2, Weights wt,
+                           LevelDims d, int first) {
+    int ix = blockIdx.x * blockDim.x + threadIdx.x;
+    int iy = blockIdx.y * blockDim.y + threadIdx.y;
+    if (ix >= d.w || iy >= d.h) return;
+    const int s = d.s;
+    const int pos = ix + iy * s;
+    float du0 = duhat[pos], dv0 = dvhat[pos];
+    float dux = 0.0f, duy = 0.0f, dvx = 0.0f, dvy = 0.0f;
+    if (ix + 1 < d.w) {
+        dux = duhat[pos + 1] - du0;
+        dvx = dvhat[pos + 1] - dv0;
+    }
+    if (iy + 1 < d.h) {
+        duy = duhat[pos + s] - du0;
+        dvy = dvhat[pos + s] - dv0;
+    }
+    float a = 0.0f, b = 0.0f, c = 0.0f, e = 0.0f;
+    if (!first) {
+        a = pu1[pos];
+        b = pu2[pos];
+        c = pv1[pos];
+        e = pv2[pos];
+    }
+    dual_step(dux, duy, wt.fac, a, b);
+    dual_step(dvx, dvy, wt.fac, c, e);
+    pu1[pos] = a;
+    pu2[pos] = b;
+    pv1[pos] = c;
+    pv2[pos] = e;
+}
+
+// ---------------------------------------------------------------------------
+// 5x5 medians (medianFilter.cu:3-75): taps clamp along one axis, 0 at corners
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ int median5_tap(int col, int row, int w, int h, int s) {
+    bool cin = col >= 0 && col < w, rin = row >= 0 && row < h;
+    if (cin && rin) return col + s * row;
+    if (col < 0 && rin) return s * row;
+    if (col >= w && rin) return w - 1 + s * row;
+    if (cin && row < 0) return col;
+    if (cin && row >= h) return col + s * (h - 1);
+    return -1;
+}
+
+__device__ __forceinline__ void median5_pair(const float* __restrict__ a,
+                                             const float* __restrict__ b, int ix, int iy,
+                                             LevelDims d, float& ma, float& mb) {
+    float mu[25], mv[25];
+#pragma unroll
+    for (int j = 0; j < 5; j++) {
+#pragma unroll
+        for (int i = 0; i < 5; i++) {
+            int at = median5_tap(ix + i - 2, iy + j - 2, d.w, d.h, d.s);
+            mu[j * 5 + i] = at >= 0 ? a[at] : 0.0f;
+            mv[j * 5 + i] = at >= 0 ? b[at] : 0.0f;
+        }
+    }
+    ma = median25_exchange(mu);
+    mb = median25_exchange(mv);
+}
+
+// u + median5(duhat): MedianFilter then Add (Reconflow.cu:410-416)
+__global__ void k_median_add(const float* __restrict__ duhat, const float* __restrict__ dvhat,
+                             const float* u, const float* v, float* ou, float* ov, LevelDims d) {
+    int ix = blockIdx.x * blockDim.x + threadIdx.x;
+    int iy = blockIdx.y * blockDim.y + threadIdx.y;
+    if (ix >= d.w || iy >= d.h) return;
+    float mu, mv;
+    median5_pair(duhat, dvhat, ix, iy, d, mu, mv);
+    int pos = ix + iy * d.s;
+    float a = u[pos] + mu;
+    float b = v[pos] + mv;
+    ou[pos] = a;
+    ov[pos] = b;
+}
+
+__global__ void k_median5(const float* __restrict__ u, const float* __restrict__ v,
+                          float* __restrict__ ou, float* __restrict__ ov, LevelDims d) {
+    int ix = blockIdx.x * blockDim.x + threadIdx.x;
+    int iy = blockIdx.y * blockDim.y + threadIdx.y;
+    if (ix >= d.w || iy >= d.h) return;
+    float mu, mv;
+    median5_pair(u, v, ix, iy, d, mu, mv);
+    ou[ix + iy * d.s] = mu;
+    ov[ix + iy * d.s] = mv;
+}
+
+__global__ void k_median3d(const float* __restrict__ X, const float* __restrict__ Y,
+                           const float* __restrict__ Z, float* __restrict__ X1,
+                           float* __restrict__ Y1, float* __restrict__ Z1, LevelDims d) {
+    int ix = blockIdx.x * blockDim.x + threadIdx.x;
+    int iy = blockIdx.y * blockDim.y + threadIdx.y;
+    if (ix >= d.w || iy >= d.h) return;
+    float mX[9], mY[9], mZ[9];
+#pragma unroll
+    for (int j = 0; j < 3; j++)
+#pragma unroll
+        for (int i = 0; i < 3; i++) {
+            int at = median3_tap(ix + i - 1, iy + j - 1, d.w, d.h, d.s);
+            int k = j * 3 + i;
+            mX[k] = at >= 0 ? X[at] : 0.0f;
+            mY[k] = at >= 0 ? Y[at] : 0.0f;
+            mZ[k] = at >= 0 ? Z[at] : 0.0f;
+        }
+    int pos = ix + iy * d.s;
+    X1[pos] = median9_exchange(mX);
+    Y1[pos] = median9_exchange(mY);
+    Z1[pos] = median9_exchange(mZ);
+}
+
+__global__ void k_solve_uc(const float* __restrict__ X, const float* __restrict__ Y,
+                           const float* __restrict__ Z, const LevelConsts* __restrict__ lc,
+                           LevelDims d, float* __restrict__ uc, float* __restrict__ vc) {
+    int ix = blockIdx.x * blockDim.x + threadIdx.x;
+    int iy = blockIdx.y * blockDim.y + threadIdx.y;
+    if (ix >= d.w || iy >= d.h) return;
+    int pos = ix + iy * d.s;
+    float a, b;
+    project_uc(*lc, X[pos], Y[pos], Z[pos], ix, iy, a, b);
+    uc[pos] = a;
+    vc[pos] = b;
+}
+
+__global__ void k_inv_depth(const float* __restrict__ Z, LevelDims d, float* __restrict__ out) {
+    int ix = blockIdx.x * blockDim.x + threadIdx.x;
+    int iy = blockIdx.y * blockDim.y + threadIdx.y;
+    if (ix >= d.w || iy >= d.h) return;
+    int pos = ix + iy * d.s;
+    out[pos] = 1.0f / Z[pos];
+}
+
+// RemoveEdgeArtifacts3DKernel (solve3dMinimalArea.cu:320-378)
+__global__ void k_remove_edge(const float* __restrict__ X0, const float* __restrict__ Y0,
+                              const float* __restrict__ Z0, int range, float maxArea, LevelDims d,
+                              float* __restrict__ X1, float* __restrict__ Y1,
+                              float* __restrict__ Z1) {
+    int ix = blockIdx.x * blockDim.x + threadIdx.x;
+    int iy = blockIdx.y * blockDim.y + threadIdx.y;
+    if (ix >= d.w || iy >= d.h) return;
+    const int s = d.s, pos = ix + iy * s;
+    float Xx, Yx, Zx, Xy, Yy, Zy;
+    if (ix + range > d.w) {
+        int a = ix - range + iy * s;
+        Xx = -X0[a] + X0[pos]; Yx = -Y0[a] + Y0[pos]; Zx = -Z0[a] + Z0[pos];
+    } else {
+        int a = ix + range + iy * s;
+        Xx = X0[a] - X0[pos]; Yx = Y0[a] - Y0[pos]; Zx = Z0[a] - Z0[pos];
+    }
+    if (iy + range > d.h) {
+        int a = ix + (iy - range) * s;
+        Xy = -X0[a] + X0[pos]; Yy = -Y0[a] + Y0[pos]; Zy = -Z0[a] + Z0[pos];
+    } else {
+        int a = ix + (iy + range) * s;
+        Xy = X0[a] - X0[pos]; Yy = Y0[a] - Y0[pos]; Zy = Z0[a] - Z0[pos];
+    }
+    float area = sqrtf((Yx * Zy - Zx * Yy) * (Yx * Zy - Zx * Yy) +
+                       (Zx * Xy - Xx * Zy) * (Zx * Xy - Xx * Zy) +
+                       (Xx * Yy - Yx * Xy) * (Xx * Yy - Yx * Xy));
+    if (area > maxArea) {
+        X1[pos] = 0.0f; Y1[pos] = 0.0f; Z1[pos] = 0.0f;
+    } else {
+        X1[pos] = X0[pos]; Y1[pos] = Y0[pos]; Z1[pos] = Z0[pos];
+    }
+}
+
+// Middlebury colour wheel (flowToHSV.cu:194-302); entry 55 (reached when the
+// angle term rounds to exactly one) wraps to entry 0.
+__constant__ float c_wheel[3][55] = {
+    {255, 255, 255, 255, 255, 255, 255, 255, 255, 255, 255, 255, 255, 255, 255, 255, 213, 170, 128,
+     85,  43,  0,   0,   0,   0,   0,   0,   0,   0,   0,   0,   0,   0,   0,   0,   0,   0,   19,
+     39,  58,  78,  98,  117, 137, 156, 176, 196, 215, 235, 255, 255, 255, 255, 255, 255},
+    {0,   17,  34,  51,  68,  85,  102, 119, 136, 153, 170, 187, 204, 221, 238, 255, 255, 255, 255,
+     255, 255, 255, 255, 255, 255, 255, 232, 209, 186, 163, 140, 116, 93,  70,  47,  24,  0,   0,
+     0,   0,   0,   0,   0,   0,   0,   0,   0,   0,   0,   0,   0,   0,   0,   0,   0},
+    {0,   0,   0,   0,   0,   0,   0,   0,   0,   0,   0,   0,   0,   0,   0,   0,   0,   0,   0,
+     0,   0,   0,   63,  127, 191, 255, 255, 255, 255, 255, 255, 255, 255, 255, 255, 255, 255, 255,
+     255, 255, 255, 255, 255, 255, 255, 255, 255, 255, 255, 255, 213, 170, 128, 85,  43}};
+
+__global__ void k_flow_color(const float* __restrict__ u, const float* __restrict__ v,
+                             LevelDims d, float flow_scale, float* __restrict__ rgb) {
+    int c = blockIdx.x * blockDim.x + threadIdx.x;
+    int r = blockIdx.y * blockDim.y + threadIdx.y;
+    if (c >= d.w || r >= d.h) return;
+    int pos = c + d.s * r;
+    float du = u[pos] / flow_scale;
+    float dv = v[pos] / flow_scale;
+    const int ncols = 55;
+    float rad = sqrtf(du * du + dv * dv);
+    float a = atan2f(-dv, -du) / 3.14159f;
+    float fk = (a + 1) / 2 * ((float)ncols - 1) + 1;
+    int k0 = (int)floorf(fk);
+    int k1 = k0 + 1;
+    if (k1 == ncols + 1) k1 = 1;
+    float fr = fk - (float)k0;
+    k0 %= ncols;
+    k1 %= ncols;
+    float col[3];
+#pragma unroll
+    for (int ch = 0; ch < 3; ch++) {
+        float cv = (1 - fr) * (c_wheel[ch][k0] / 255.0f) + fr * (c_wheel[ch][k1] / 255.0f);
+        if (rad <= 1) cv = 1 - rad * (1 - cv);
+        else cv = cv * 0.75f;
+        col[ch] = cv;
+    }
+    // float3 (x, y, z) = (B, G, R) as the reference stores it
+    rgb[3 * pos + 0] = col[2];
+    rgb[3 * pos + 1] = col[1];
+    rgb[3 * pos + 2] = col[0];
+}
+
+}  // namespace
+
+// ---------------------------------------------------------------------------
+// Launchers
+// ---------------------------------------------------------------------------
+int launch_convert(const void* in, int type, int w, int h, int in_pitch, float* out, int s,
+                   cudaStream_t st) {
+    k_convert<<<grid_for(w, h), dim3(BX, BY), 0, st>>>(in, type, w, h, in_pitch, out, s);
+    return check_launch();
+}
+
+int launch_downscale2(const float* a, const float* b, LevelDims fine, LevelDims coarse, float* oa,
+                      float* ob, cudaStream_t st) {
+    k_downscale2<<<grid_for(coarse.w, coarse.h), dim3(BX, BY), 0, st>>>(a, b, fine, coarse, oa, ob);
+    return check_launch();
+}
+
+int launch_downscale(const float* src, LevelDims fine, LevelDims coarse, float scale, bool scaled,
+                     float* out, cudaStream_t st) {
+    k_downscale<<<grid_for(coarse.w, coarse.h), dim3(BX, BY), 0, st>>>(src, fine, coarse, scale,
+                                                                      scaled ? 1 : 0, out);
+    return check_launch();
+}
+
+int launch_warp(const float* I1, const float* u, const float* v, LevelDims d, float* out,
+                cudaStream_t st) {
+    k_warp<<<grid_for(d.w, d.h), dim3(BX, BY), 0, st>>>(I1, u, v, d, out);
+    return check_launch();
+}
+
+int launch_derivatives(const float* I0, const float* I1w, LevelDims d, float* Ix, float* Iy,
+                       float* Iz, cudaStream_t st) {
+    k_derivatives<<<grid_for(d.w, d.h), dim3(BX, BY), 0, st>>>(I0, I1w, d, Ix, Iy, Iz);
+    return check_launch();
+}
+
+int launch_recon_a(const ReconFields& f, const LevelConsts* lc, const Weights& wt, LevelDims d,
+                   bool first, bool uc_from_buffer, int prior, cudaStream_t st) {
+    dim3 g = grid_for(d.w, d.h), b(BX, BY);
+    if (prior == 1)
+        k_recon_a<1><<<g, b, 0, st>>>(f, lc, wt, d, first, uc_from_buffer);
+    else if (prior == 2)
+        k_recon_a<2><<<g, b, 0, st>>>(f, lc, wt, d, first, uc_from_buffer);
+    else
+        k_recon_a<0><<<g, b, 0, st>>>(f, lc, wt, d, first, uc_from_buffer);
+    return check_launch();
+}
+
+int launch_recon_b(const ReconFields& f, const Weights& wt, LevelDims d, bool first,
+                   cudaStream_t st) {
+    k_recon_b<<<grid_for(d.w, d.h), dim3(BX, BY), 0, st>>>(f, wt, d, first);
+    return check_launch();
+}
+
+int launch_plain_data(float* duhat, float* dvhat, const float* pu1, const float* pu2,
+                      const float* pv1, const float* pv2, const float* Ix, const float* Iy,
+                      const float* Iz, const Weights& wt, LevelDims d, bool first,
+                      cudaStream_t st) {
+    k_plain_data<<<grid_for(d.w, d.h), dim3(BX, BY), 0, st>>>(duhat, dvhat, pu1, pu2, pv1, pv2,
+                                                             Ix, Iy, Iz, wt, d, first);
+    return check_launch();
+}
+
+int launch_plain_tv(const float* duhat, const float* dvhat, float* pu1, float* pu2, float* pv1,
+                    float* pv2, const Weights& wt, LevelDims d, bool first, cudaStream_t st) {
+    k_plain_tv<<<grid_for(d.w, d.h), dim3(BX, BY), 0, st>>>(duhat, dvhat, pu1, pu2, pv1, pv2, wt,
+                                                           d, first);
+    return check_launch();
+}
+
+int launch_median_add(const float* duhat, const float* dvhat, const float* u, const float* v,
+                      float* ou, float* ov, LevelDims d, cudaStream_t st) {
+    k_median_add<<<grid_for(d.w, d.h), dim3(BX, BY), 0, st>>>(duhat, dvhat, u, v, ou, ov, d);
+    return check_launch();
+}
+
+int launch_median5(const float* u, const float* v, float* ou, float* ov, LevelDims d,
+                   cudaStream_t st) {
+    k_median5<<<grid_for(d.w, d.h), dim3(BX, BY), 0, st>>>(u, v, ou, ov, d);
+    return check_launch();
+}
+
+int launch_median3d(const float* X, const float* Y, const float* Z, float* X1, float* Y1,
+                    float* Z1, LevelDims d, cudaStream_t st) {
+    k_median3d<<<grid_for(d.w, d.h), dim3(BX, BY), 0, st>>>(X, Y, Z, X1, Y1, Z1, d);
+    return check_launch();
+}
+
+int launch_solve_uc(const float* X, const float* Y, const float* Z, const LevelConsts* lc,
+                    LevelDims d, float* uc, float* vc, cudaStream_t st) {
+    k_solve_uc<<<grid_for(d.w, d.h), dim3(BX, BY), 0, st>>>(X, Y, Z, lc, d, uc, vc);
+    return check_launch();
+}
+
+int launch_upscale_fields(int n, const float* const* src, float* const* dst, const float* scales,
+                          LevelDims coarse, LevelDims fine, cudaStream_t st) {
+    if (n < 1 || n > 12) return 1;
+    UpscaleArgs a;
+    a.n = n;
+    for (int i = 0; i < n; i++) {
+        a.src[i] = src[i];
+        a.dst[i] = dst[i];
+        a.scale[i] = scales[i];
+    }
+    k_upscale_fields<<<grid_for(fine.w, fine.h), dim3(BX, BY), 0, st>>>(a, coarse, fine);
+    return check_launch();
+}
+
+int launch_upscale(const float* src, LevelDims coarse, LevelDims fine, float scale, float* out,
+                   cudaStream_t st) {
+    float* dst[1] = {out};
+    const float* s[1] = {src};
+    return launch_upscale_fields(1, s, dst, &scale, coarse, fine, st);
+}
+
+int launch_inv_depth(const float* Z, LevelDims d, float* out, cudaStream_t st) {
+    k_inv_depth<<<grid_for(d.w, d.h), dim3(BX, BY), 0, st>>>(Z, d, out);
+    return check_launch();
+}
+
+int launch_remove_edge(const float* X, const float* Y, const float* Z, int range, float max_area,
+                       LevelDims d, float* X1, float* Y1, float* Z1, cudaStream_t st) {
+    k_remove_edge<<<grid_for(d.w, d.h), dim3(BX, BY), 0, st>>>(X, Y, Z, range, max_area, d, X1,
+                                                              Y1, Z1);
+    return check_launch();
+}
+
+int launch_flow_color(const float* u, const float* v, LevelDims d, float flow_scale, float* rgb,
+                      cudaStream_t st) {
+    k_flow_color<<<grid_for(d.w, d.h), dim3(BX, BY), 0, st>>>(u, v, d, flow_scale, rgb);
+    return check_launch();
+}
+
+}  // namespace rf

@@ -1,0 +1,98 @@
+// Launch interface of the solver kernels (rf_kernels.cu), used by the host
+// orchestration (rf_solver.cu) and the kernel-level C entry points.
+#pragma once
+
+#include <cstdint>
+
+#include <cuda_runtime.h>
+
+#include "rf_math.cuh"
+
+namespace rf {
+
+struct LevelDims {
+    int w, h, s;
+};
+
+// Scalar solver weights in the exact float forms the kernels use.
+struct Weights {
+    float lambda;
+    float alpha_tv, alpha_proj, alpha_fn;
+    float A;          // alpha_tv + alpha_proj (data-term denominator)
+    float fac;        // tau / thetaTv (dual step), or tau / theta in plain mode
+    float lambdaf, lambdams;
+    float proj_den;   // lambdaf + alpha_proj
+    float theta;      // plain TV-L1 theta
+};
+
+// Fields of one ReconFlow inner iteration.
+struct ReconFields {
+    const float* u;
+    const float* v;
+    float* duhat;     // in place: read at the pixel, written by the data step
+    float* dvhat;
+    float* pu1;       // dual field, in place
+    float* pu2;
+    float* pv1;
+    float* pv2;
+    float* uproj;     // in place
+    float* vproj;
+    float* sku;       // in place
+    float* skv;
+    const float* Ix;
+    const float* Iy;
+    const float* Iz;
+    float* X;         // post-cleanup 3D state (flat level-0 buffer)
+    float* Y;
+    float* Z;
+    float* X1;        // Solve3d output (before median / cleanup)
+    float* Y1;
+    float* Z1;
+    const float* uc;  // buffer read only when uc_from_buffer
+    const float* vc;
+    const float* ufn; // prior flow at this level (methods 17 / 20)
+    const float* vfn;
+    const float* mask;
+};
+
+int launch_convert(const void* in, int type, int w, int h, int in_pitch, float* out, int s,
+                   cudaStream_t st);
+int launch_downscale2(const float* a, const float* b, LevelDims fine, LevelDims coarse,
+                      float* oa, float* ob, cudaStream_t st);
+int launch_downscale(const float* src, LevelDims fine, LevelDims coarse, float scale, bool scaled,
+                     float* out, cudaStream_t st);
+int launch_warp(const float* I1, const float* u, const float* v, LevelDims d, float* out,
+                cudaStream_t st);
+int launch_derivatives(const float* I0, const float* I1w, LevelDims d, float* Ix, float* Iy,
+                       float* Iz, cudaStream_t st);
+int launch_recon_a(const ReconFields& f, const LevelConsts* lc, const Weights& wt, LevelDims d,
+                   bool first, bool uc_from_buffer, int prior, cudaStream_t st);
+int launch_recon_b(const ReconFields& f, const Weights& wt, LevelDims d, bool first,
+                   cudaStream_t st);
+int launch_plain_data(float* duhat, float* dvhat, const float* pu1, const float* pu2,
+                      const float* pv1, const float* pv2, const float* Ix, const float* Iy,
+                      const float* Iz, const Weights& wt, LevelDims d, bool first,
+                      cudaStream_t st);
+int launch_plain_tv(const float* duhat, const float* dvhat, float* pu1, float* pu2, float* pv1,
+                    float* pv2, const Weights& wt, LevelDims d, bool first, cudaStream_t st);
+// out = u + median5(duhat) (out may alias u)
+int launch_median_add(const float* duhat, const float* dvhat, const float* u, const float* v,
+                      float* ou, float* ov, LevelDims d, cudaStream_t st);
+int launch_median5(const float* u, const float* v, float* ou, float* ov, LevelDims d,
+                   cudaStream_t st);
+int launch_median3d(const float* X, const float* Y, const float* Z, float* X1, float* Y1,
+                    float* Z1, LevelDims d, cudaStream_t st);
+int launch_solve_uc(const float* X, const float* Y, const float* Z, const LevelConsts* lc,
+                    LevelDims d, float* uc, float* vc, cudaStream_t st);
+// Upscale n fields by one pyramid step; scales[i] multiplies field i.
+int launch_upscale_fields(int n, const float* const* src, float* const* dst, const float* scales,
+                          LevelDims coarse, LevelDims fine, cudaStream_t st);
+int launch_upscale(const float* src, LevelDims coarse, LevelDims fine, float scale, float* out,
+                   cudaStream_t st);
+int launch_inv_depth(const float* Z, LevelDims d, float* out, cudaStream_t st);
+int launch_remove_edge(const float* X, const float* Y, const float* Z, int range, float max_area,
+                       LevelDims d, float* X1, float* Y1, float* Z1, cudaStream_t st);
+int launch_flow_color(const float* u, const float* v, LevelDims d, float flow_scale, float* rgb,
+                      cudaStream_t st);
+
+}  // namespace rf

@@ -1,0 +1,323 @@
+// Per-pixel arithmetic of the Reconflow update equations, as __device__ code.
+//
+// Every expression keeps the reference kernels' operation order and is built
+// with -fmad=false (IEEE division / square root, no contraction), so a result
+// is a deterministic function of its inputs.  The texture fetches of the
+// reference (normalized coordinates, mirror addressing, linear filtering;
+// downscale.cu:50-67, upscale.cu:42-58, warpImage.cu:33-50,
+// computeDerivatives.cu:60-84) are replaced by explicit exact bilinear
+// interpolation with half-sample-symmetric tap indices.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <math.h>
+
+namespace rf {
+
+// Half-sample-symmetric extension of a tap index (period 2n): -1 -> 0,
+// -2 -> 1, n -> n-1, n+1 -> n-2.
+__device__ __forceinline__ int mirror_index(int i, int n) {
+    if (i >= 0 && i < n) return i;
+    int p = 2 * n;
+    i %= p;
+    if (i < 0) i += p;
+    return i < n ? i : p - 1 - i;
+}
+
+// Mirror addressing of a normalized coordinate (period 2, reflected into
+// [0, 1]); a non-finite coordinate reads at 0.
+__device__ __forceinline__ float mirror_coord(float t) {
+    if (t >= 0.0f && t <= 1.0f) return t;
+    if (!isfinite(t)) return 0.0f;
+    if (t < 0.0f) t = -t;
+    t = fmodf(t, 2.0f);
+    if (t > 1.0f) t = 2.0f - t;
+    return t;
+}
+
+// Tap indices and weights of one linear fetch along an axis of n texels.
+struct Taps {
+    int i0, i1;
+    float a;
+};
+
+__device__ __forceinline__ Taps taps_of(float tn, int n) {
+    float tm = mirror_coord(tn);
+    float tx = tm * (float)n - 0.5f;
+    float f = floorf(tx);
+    Taps t;
+    int x0 = (int)f;
+    t.a = tx - f;
+    t.i0 = mirror_index(x0, n);
+    t.i1 = mirror_index(x0 + 1, n);
+    return t;
+}
+
+__device__ __forceinline__ float bilerp(const float* __restrict__ src, int s, const Taps& tx,
+                                        const Taps& ty) {
+    float r0 = (1.0f - tx.a) * src[tx.i0 + ty.i0 * s] + tx.a * src[tx.i1 + ty.i0 * s];
+    float r1 = (1.0f - tx.a) * src[tx.i0 + ty.i1 * s] + tx.a * src[tx.i1 + ty.i1 * s];
+    return (1.0f - ty.a) * r0 + ty.a * r1;
+}
+
+__device__ __forceinline__ float tex2d(const float* __restrict__ src, int W, int H, int S,
+                                       float xn, float yn) {
+    Taps tx = taps_of(xn, W);
+    Taps ty = taps_of(yn, H);
+    return bilerp(src, S, tx, ty);
+}
+
+__device__ __forceinline__ bool finite3(float a, float b, float c) {
+    return isfinite(a) && isfinite(b) && isfinite(c);
+}
+
+// Divergence of the dual field with one-sided borders
+// (solveReconDataL1.cu:66-97).  l = p1 at x-1, d = p2 at y-1.
+__device__ __forceinline__ float divergence(float p1, float p1l, float p2, float p2d, int ix,
+                                            int iy) {
+    if (ix - 1 < 0) {
+        if (iy - 1 < 0) return p1 + p2;
+        return p1 + p2 - p2d;
+    }
+    if (iy - 1 < 0) return p1 - p1l + p2;
+    return p1 - p1l + p2 - p2d;
+}
+
+// L1 threshold step of the ReconFlow data term (solveReconDataL1.cu:36-63).
+// A = alphaTv + alphaProj (+ alphaFn); `upper` = lambda*g/A.
+__device__ __forceinline__ void l1_threshold(float dusub, float dvsub, float dix, float diy,
+                                             float dit, float lambda, float A, float& du,
+                                             float& dv) {
+    float rho = (dix * dusub + diy * dvsub + dit);
+    float upper = lambda * (dix * dix + diy * diy) / A;
+    float lower = -upper;  // == -lambda*g/A exactly (negation is exact)
+    du = dusub;
+    dv = dvsub;
+    if ((rho <= upper) && (rho >= lower)) {
+        float magi = dix * dix + diy * diy;
+        if (magi != 0) {
+            du = dusub - rho * dix / magi;
+            dv = dvsub - rho * diy / magi;
+        }
+    } else if (rho < lower) {
+        du = dusub + lambda * dix / A;
+        dv = dvsub + lambda * diy / A;
+    } else if (rho > upper) {
+        du = dusub - lambda * dix / A;
+        dv = dvsub - lambda * diy / A;
+    }
+}
+
+// Plain TV-L1 threshold step (solveDataL1.cu:27-51); lt = lambda*theta.
+__device__ __forceinline__ void l1_threshold_plain(float duhat, float dvhat, float dix, float diy,
+                                                   float dit, float lambda, float theta,
+                                                   float& du, float& dv) {
+    float rho = (dix * duhat + diy * dvhat + dit);
+    float upper = lambda * theta * (dix * dix + diy * diy);
+    float lower = -lambda * theta * (dix * dix + diy * diy);
+    du = duhat;
+    dv = dvhat;
+    if ((rho <= upper) && (rho >= lower)) {
+        float magi = dix * dix + diy * diy;
+        if (magi != 0) {
+            du = duhat - rho * dix / magi;
+            dv = dvhat - rho * diy / magi;
+        }
+    } else if (rho < lower) {
+        du = duhat + lambda * theta * dix;
+        dv = dvhat + lambda * theta * diy;
+    } else if (rho > upper) {
+        du = duhat - lambda * theta * dix;
+        dv = dvhat - lambda * theta * diy;
+    }
+}
+
+// Semi-implicit dual step (solveSmoothDualTVGlobal.cu:46-60); fac = tau/theta.
+__device__ __forceinline__ void dual_step(float dx, float dy, float fac, float& p1, float& p2) {
+    float mag = sqrtf(dx * dx + dy * dy);
+    float den = 1.0f + fac * mag;
+    p1 = (p1 + fac * dx) / den;
+    p2 = (p2 + fac * dy) / den;
+}
+
+// Per-level camera constants (float copies, as the reference passes them:
+// solve3dMinimalArea.cu:204-228, solveUcSk.cu:42-56).
+struct LevelConsts {
+    float P[12];
+    float Q[12];
+    float R1[9];
+    float t1[3];
+    float focal, cx, cy;
+    float pad;
+};
+
+// SolveUcKernel (solveUcSk.cu:21-33).
+__device__ __forceinline__ void project_uc(const LevelConsts& c, float X, float Y, float Z, int ix,
+                                           int iy, float& uc, float& vc) {
+    float X2 = c.R1[0] * X + c.R1[1] * Y + c.R1[2] * Z + c.t1[0];
+    float Y2 = c.R1[3] * X + c.R1[4] * Y + c.R1[5] * Z + c.t1[1];
+    float Z2 = c.R1[6] * X + c.R1[7] * Y + c.R1[8] * Z + c.t1[2];
+    float xproj = c.focal * X2 / Z2 + c.cx;
+    float yproj = c.focal * Y2 / Z2 + c.cy;
+    uc = xproj - (float)ix;
+    vc = yproj - (float)iy;
+}
+
+// Solve3dMinimalAreaKernel body (solve3dMinimalArea.cu:23-184).  nb[] holds
+// X0, Y0, Z0 at: 0 = pos, 1 = x+1 (flat pos+1), 2 = y+1 (flat pos+stride),
+// 3 = x-1, 4 = y-1 (3, 4 unused at the left / top border).
+__device__ __forceinline__ void solve3d_pixel(const LevelConsts& c, float uproj, float vproj,
+                                              int ix, int iy, const float (&Xn)[5],
+                                              const float (&Yn)[5], const float (&Zn)[5],
+                                              float lambdaf, float lambdams, float& Xo, float& Yo,
+                                              float& Zo) {
+    const float* P = c.P;
+    const float* Q = c.Q;
+    float x1 = (float)ix;
+    float y1 = (float)iy;
+    float x2 = (float)ix + uproj;
+    float y2 = (float)iy + vproj;
+
+    float p1 = x1 * P[8] - P[0], p2 = x1 * P[9] - P[1], p3 = x1 * P[10] - P[2], p4 = x1 * P[11] - P[3];
+    float q1 = y1 * P[8] - P[4], q2 = y1 * P[9] - P[5], q3 = y1 * P[10] - P[6], q4 = y1 * P[11] - P[7];
+    float r1 = x2 * Q[8] - Q[0], r2 = x2 * Q[9] - Q[1], r3 = x2 * Q[10] - Q[2], r4 = x2 * Q[11] - Q[3];
+    float s1 = y2 * Q[8] - Q[4], s2 = y2 * Q[9] - Q[5], s3 = y2 * Q[10] - Q[6], s4 = y2 * Q[11] - Q[7];
+
+    float ax = lambdaf * (p1 * p1 + q1 * q1 + r1 * r1 + s1 * s1);
+    float bx = lambdaf * (p1 * p2 + q1 * q2 + r1 * r2 + s1 * s2);
+    float cx = lambdaf * (p1 * p3 + q1 * q3 + r1 * r3 + s1 * s3);
+    float dx = lambdaf * (p1 * p4 + q1 * q4 + r1 * r4 + s1 * s4);
+    float ay = lambdaf * (p2 * p1 + q2 * q1 + r2 * r1 + s2 * s1);
+    float by = lambdaf * (p2 * p2 + q2 * q2 + r2 * r2 + s2 * s2);
+    float cy = lambdaf * (p2 * p3 + q2 * q3 + r2 * r3 + s2 * s3);
+    float dy = lambdaf * (p2 * p4 + q2 * q4 + r2 * r4 + s2 * s4);
+    float az = lambdaf * (p3 * p1 + q3 * q1 + r3 * r1 + s3 * s1);
+    float bz = lambdaf * (p3 * p2 + q3 * q2 + r3 * r2 + s3 * s2);
+    float cz = lambdaf * (p3 * p3 + q3 * q3 + r3 * r3 + s3 * s3);
+    float dz = lambdaf * (p3 * p4 + q3 * q4 + r3 * r4 + s3 * s4);
+
+    float Xx = Xn[1] - Xn[0], Yx = Yn[1] - Yn[0], Zx = Zn[1] - Zn[0];
+    float Xy = Xn[2] - Xn[0], Yy = Yn[2] - Yn[0], Zy = Zn[2] - Zn[0];
+
+    float lambetams = lambdams / sqrtf((Yx * Zy - Zx * Yy) * (Yx * Zy - Zx * Yy) +
+                                       (Zx * Xy - Xx * Zy) * (Zx * Xy - Xx * Zy) +
+                                       (Xx * Yy - Yx * Xy) * (Xx * Yy - Yx * Xy) + 0.001f);
+
+    float Xibar, Yibar, Zibar, Xjbar, Yjbar, Zjbar;
+    if (ix - 1 < 0) {
+        Xibar = Xn[1];
+        Yibar = Yn[1];
+        Zibar = Zn[1];
+    } else {
+        Xibar = 0.5f * Xn[3] + 0.5f * Xn[1];
+        Yibar = 0.5f * Yn[3] + 0.5f * Yn[1];
+        Zibar = 0.5f * Zn[3] + 0.5f * Zn[1];
+    }
+    if (iy - 1 < 0) {
+        Xjbar = Xn[2];
+        Yjbar = Yn[2];
+        Zjbar = Zn[2];
+    } else {
+        Xjbar = 0.5f * Xn[4] + 0.5f * Xn[2];
+        Yjbar = 0.5f * Yn[4] + 0.5f * Yn[2];
+        Zjbar = 0.5f * Zn[4] + 0.5f * Zn[2];
+    }
+
+    float a11 = ax + lambetams * (Yx * Yx + Zx * Zx + Yy * Yy + Zy * Zy);
+    float a12 = bx - lambetams * (Xx * Yx + Xy * Yy);
+    float a13 = cx - lambetams * (Xx * Zx + Xy * Zy);
+    float a21 = ay - lambetams * (Xx * Yx + Xy * Yy);
+    float a22 = by + lambetams * (Xx * Xx + Zx * Zx + Xy * Xy + Zy * Zy);
+    float a23 = cy - lambetams * (Yx * Zx + Yy * Zy);
+    float a31 = az - lambetams * (Xx * Zx + Xy * Zy);
+    float a32 = bz - lambetams * (Yx * Zx + Yy * Zy);
+    float a33 = cz + lambetams * (Xx * Xx + Yx * Yx + Xy * Xy + Yy * Yy);
+
+    float detA = a11 * (a22 * a33 - a23 * a32) - a12 * (a21 * a33 - a23 * a31) +
+                 a13 * (a21 * a32 - a22 * a31);
+
+    float E11 = a22 * a33 - a23 * a32;
+    float E12 = a13 * a32 - a12 * a33;
+    float E13 = a12 * a23 - a13 * a22;
+    float E21 = a23 * a31 - a21 * a33;
+    float E22 = a11 * a33 - a13 * a31;
+    float E23 = a13 * a21 - a11 * a23;
+    float E31 = a21 * a32 - a22 * a31;
+    float E32 = a12 * a31 - a11 * a32;
+    float E33 = a11 * a22 - a12 * a21;
+
+    float b1 = lambetams * ((Zy * Zy + Yy * Yy) * Xibar + (Zx * Zx + Yx * Yx) * Xjbar -
+                            (Xy * Yy) * Yibar - (Xx * Yx) * Yjbar - (Xy * Zy) * Zibar -
+                            (Xx * Zx) * Zjbar) -
+               dx;
+    float b2 = lambetams * (-(Xy * Yy) * Xibar - (Xx * Yx) * Xjbar + (Xy * Xy + Zy * Zy) * Yibar +
+                            (Xx * Xx + Zx * Zx) * Yjbar - (Yy * Zy) * Zibar - (Yx * Zx) * Zjbar) -
+               dy;
+    float b3 = lambetams * (-(Xy * Zy) * Xibar - (Xx * Zx) * Xjbar - (Yy * Zy) * Yibar -
+                            (Yx * Zx) * Yjbar + (Xy * Xy + Yy * Yy) * Zibar +
+                            (Xx * Xx + Yx * Yx) * Zjbar) -
+               dz;
+
+    float Xsub = (E11 * b1 + E12 * b2 + E13 * b3) / detA;
+    float Ysub = (E21 * b1 + E22 * b2 + E23 * b3) / detA;
+    float Zsub = (E31 * b1 + E32 * b2 + E33 * b3) / detA;
+
+    if (finite3(Xsub, Ysub, Zsub)) {
+        Xo = Xsub;
+        Yo = Ysub;
+        Zo = Zsub;
+    } else {
+        Xo = Xn[0];
+        Yo = Yn[0];
+        Zo = Zn[0];
+    }
+}
+
+// Exchange-selection median of 9 (medianFilter.cu:216-242): 5 passes, the
+// reference's compare order, so ties (+0/-0) resolve identically.
+__device__ __forceinline__ float median9_exchange(float (&m)[9]) {
+#pragma unroll
+    for (int j = 0; j < 5; j++) {
+#pragma unroll
+        for (int i = j + 1; i < 9; i++) {
+            if (m[j] > m[i]) {
+                float t = m[j];
+                m[j] = m[i];
+                m[i] = t;
+            }
+        }
+    }
+    return m[4];
+}
+
+// Exchange-selection median of 25 (medianFilter.cu:55-74): 13 passes.
+__device__ __forceinline__ float median25_exchange(float (&m)[25]) {
+#pragma unroll
+    for (int j = 0; j < 13; j++) {
+#pragma unroll
+        for (int i = j + 1; i < 25; i++) {
+            if (m[j] > m[i]) {
+                float t = m[j];
+                m[j] = m[i];
+                m[i] = t;
+            }
+        }
+    }
+    return m[12];
+}
+
+// CleanUp3DKernel body (solve3dMinimalArea.cu:259-295).
+__device__ __forceinline__ void cleanup_pixel(float X, float Y, float Z, float Xm, float Ym,
+                                              float Zm, float& Xo, float& Yo, float& Zo) {
+    if (finite3(X, Y, Z) && finite3(Xm, Ym, Zm)) {
+        Xo = fabsf(Xm - X) > 5.0f ? Xm : X;
+        Yo = fabsf(Ym - Y) > 5.0f ? Ym : Y;
+        Zo = fabsf(Zm - Z) > 5.0f ? Zm : Z;
+    } else {
+        Xo = 0.0f;
+        Yo = 0.0f;
+        Zo = 0.0f;
+    }
+}
+
+}  // namespace rf

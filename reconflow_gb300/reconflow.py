@@ -1,0 +1,270 @@
+"""Python mirror of the reference's ``CudaFlow`` / ``ReconFlow`` classes.
+
+Same method names, argument meaning and call order as
+``reconflow/Cudaflow.h:17-362`` and ``reconflow/Reconflow.h:9-160``
+(``test_reconflow/main.cpp:24-106`` shows the order): construct, initialize,
+set cameras, copy images (and prior flow) to the device, solve, copy results
+to the host.  Host images are numpy arrays of shape (height, pitch[, 3]); a
+result is written into a caller's array when one is passed (the reference's
+pre-allocated ``cv::Mat``) or returned as a new (height, stride) array.
+
+Every call goes through the C ABI of the CUDA library; a failure raises
+``RfError`` (the reference aborts the process inside ``checkCudaErrors``).
+"""
+from __future__ import annotations
+
+import ctypes
+
+import numpy as np
+
+from . import _native as N
+from ._native import RfError
+
+__all__ = ["CudaFlow", "ReconFlow", "RfError"]
+
+# OpenCV type codes accepted by initialize(cvType=...) (Cudaflow.cu:288-311)
+CV_8U, CV_16U, CV_32F, CV_8UC3 = 0, 2, 5, 16
+_CV_TO_INPUT = {CV_8UC3: N.INPUT_RGB8, CV_8U: N.INPUT_U8, CV_16U: N.INPUT_U16, CV_32F: N.INPUT_F32}
+_INPUT_DTYPE = {N.INPUT_F32: np.float32, N.INPUT_RGB8: np.uint8, N.INPUT_U8: np.uint8,
+                N.INPUT_U16: np.uint16}
+
+
+def _ptr(a: np.ndarray):
+    return ctypes.c_void_p(a.ctypes.data)
+
+
+def _dbl(a, n):
+    a = np.ascontiguousarray(np.asarray(a, np.float64).reshape(n))
+    return a, _ptr(a)
+
+
+class CudaFlow:
+    """Plain TV-L1 optical flow (Cudaflow.h:17-362)."""
+
+    METHOD_TVL1 = N.METHOD_TVL1
+
+    def __init__(self, BlockWidth: int = 32, BlockHeight: int = 12, StrideAlignment: int = 32):
+        self._lib = N.load()
+        self.BlockWidth, self.BlockHeight, self.StrideAlignment = BlockWidth, BlockHeight, StrideAlignment
+        self._h = None
+        self.params = None
+
+    # -- lifecycle ---------------------------------------------------------
+    def _create(self, params: N.RfParams) -> int:
+        self.close()
+        h = ctypes.c_void_p()
+        N.check(self._lib.rf_create(ctypes.byref(params), ctypes.byref(h)))
+        self._h = h
+        self.params = params
+        self.width, self.height = params.width, params.height
+        self.stride = self._lib.rf_stride(h)
+        self.nLevels = params.n_levels
+        return 0
+
+    def close(self) -> int:
+        if self._h is not None:
+            self._lib.rf_destroy(self._h)
+            self._h = None
+        return 0
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def _handle(self):
+        if self._h is None:
+            raise RfError(5, "not initialized")
+        return self._h
+
+    def iAlignUp(self, n: int) -> int:
+        m = self.StrideAlignment
+        return n + m - n % m if n % m else n
+
+    def pyramid(self):
+        """(pW, pH, pS) level sizes (Cudaflow.cu:146-171)."""
+        L = self.nLevels
+        W, H, S = (ctypes.c_int * L)(), (ctypes.c_int * L)(), (ctypes.c_int * L)()
+        N.check(self._lib.rf_pyramid_dims(self._handle(), W, H, S))
+        return list(W), list(H), list(S)
+
+    def initialize(self, width, height, channels, cvType=CV_8UC3, nLevels=1, scale=2.0,
+                   method=METHOD_TVL1, lambda_=100.0, lambdagrad=400.0, theta=0.33, tau=0.25,
+                   nWarpIters=1, nSolverIters=100, withVisualization=True):
+        """CudaFlow::initialize (Cudaflow.cu:99-269)."""
+        if cvType not in _CV_TO_INPUT:
+            raise RfError(2, f"unsupported cvType {cvType}")
+        p = N.RfParams()
+        N.check(self._lib.rf_params_default(ctypes.byref(p), int(method)))
+        p.width, p.height, p.channels = int(width), int(height), int(channels)
+        p.input_type = _CV_TO_INPUT[cvType]
+        p.n_levels, p.scale, p.method = int(nLevels), float(scale), int(method)
+        p.lambda_, p.lambdagrad, p.theta, p.tau = lambda_, lambdagrad, theta, tau
+        p.n_warp_iters, p.n_solver_iters = int(nWarpIters), int(nSolverIters)
+        p.stride_alignment = self.StrideAlignment
+        p.block_width, p.block_height = self.BlockWidth, self.BlockHeight
+        self.withVisualization = withVisualization
+        return self._create(p)
+
+    # -- copies ------------------------------------------------------------
+    def _input(self, img):
+        dt = _INPUT_DTYPE[self.params.input_type]
+        a = np.ascontiguousarray(img, dtype=dt)
+        if a.shape[0] != self.height or a.shape[1] < self.width:
+            raise RfError(1, f"image shape {a.shape} does not match {self.height}x{self.width}")
+        return a
+
+    def copyImagesToDevice(self, i0, i1) -> int:
+        """CudaFlow::copyImagesToDevice (Cudaflow.cu:288-311)."""
+        a, b = self._input(i0), self._input(i1)
+        N.check(self._lib.rf_upload_images(self._handle(), _ptr(a), _ptr(b), a.shape[1]))
+        return 0
+
+    def copyImagesToDeviceFromDevice(self, ptr0: int, ptr1: int, pitch: int) -> int:
+        """Images already in device memory (e.g. torch tensors' data_ptr())."""
+        N.check(self._lib.rf_upload_images_device(self._handle(), ctypes.c_void_p(ptr0),
+                                                  ctypes.c_void_p(ptr1), int(pitch)))
+        return 0
+
+    def _out(self, out, ch=1):
+        shape = (self.height, self.stride) if ch == 1 else (self.height, self.stride, ch)
+        if out is None:
+            return np.zeros(shape, np.float32)
+        if out.dtype != np.float32 or not out.flags.c_contiguous or out.shape[0] != self.height:
+            raise RfError(1, "output must be a C-contiguous float32 array of `height` rows")
+        return out
+
+    def copyOpticalFlowToHost(self, u=None, v=None, uvrgb=None):
+        """CudaFlow::copyOpticalFlowToHost (Cudaflow.cu:313-325); returns (u, v[, uvrgb])."""
+        u, v = self._out(u), self._out(v)
+        N.check(self._lib.rf_download_flow(self._handle(), _ptr(u), _ptr(v), u.shape[1]))
+        if uvrgb is not None:
+            N.check(self._lib.rf_download_flow_color(self._handle(), ctypes.c_float(self.flowScale),
+                                                     _ptr(uvrgb), uvrgb.shape[1]))
+            return u, v, uvrgb
+        return u, v
+
+    def copyFlowColorToHost(self, flowScale: float = 5.0, uvrgb=None):
+        uvrgb = self._out(uvrgb, 3)
+        N.check(self._lib.rf_download_flow_color(self._handle(), ctypes.c_float(flowScale),
+                                                 _ptr(uvrgb), uvrgb.shape[1]))
+        return uvrgb
+
+    # -- solve -------------------------------------------------------------
+    def solveOpticalFlow(self, flowScale: float = 5.0) -> int:
+        """CudaFlow::solveOpticalFlow (Cudaflow.cu:394-621)."""
+        self.flowScale = flowScale
+        N.check(self._lib.rf_solve_flow(self._handle()))
+        return 0
+
+    def synchronize(self) -> int:
+        N.check(self._lib.rf_synchronize(self._handle()))
+        return 0
+
+    def kernelLaunches(self) -> int:
+        return int(self._lib.rf_kernel_launches(self._handle()))
+
+    def deviceResults(self):
+        """Device pointers (u, v, X, Y, Z) of the last solve (0 when absent)."""
+        ptrs = [ctypes.c_void_p() for _ in range(5)]
+        N.check(self._lib.rf_device_results(self._handle(), *[ctypes.byref(p) for p in ptrs]))
+        return [p.value or 0 for p in ptrs]
+
+    def setStream(self, stream_ptr: int | None) -> int:
+        N.check(self._lib.rf_set_stream(self._handle(), ctypes.c_void_p(stream_ptr or 0)))
+        return 0
+
+
+class ReconFlow(CudaFlow):
+    """Simultaneous flow + 3D reconstruction (Reconflow.h:9-160)."""
+
+    METHODR_TVL1_MS = N.METHODR_TVL1_MS
+    METHODR_TVL1_MS_FN = N.METHODR_TVL1_MS_FN
+    METHODR_TVL1_MS_FNSPARSE = N.METHODR_TVL1_MS_FNSPARSE
+
+    def initializeR(self, width, height, channels, nLevels, scale, method, lambda_=100.0,
+                    lambdagrad=400.0, lambdaf=100.0, lambdams=100.0, alphaTv=3.0, alphaProj=1.0,
+                    alphaFn=0.5, tau=0.25, nWarpIters=1, nSolverIters=100, cvType=None,
+                    fix_quirks=0):
+        """ReconFlow::initializeR (Reconflow.cu:15-63).  The reference forces
+        CV_8UC3 input (Cudaflow.cu:16-25); cvType=CV_32F selects float gray."""
+        p = N.RfParams()
+        N.check(self._lib.rf_params_default(ctypes.byref(p), int(method)))
+        cvType = CV_8UC3 if cvType is None else cvType
+        if cvType not in _CV_TO_INPUT:
+            raise RfError(2, f"unsupported cvType {cvType}")
+        p.width, p.height, p.channels = int(width), int(height), int(channels)
+        p.input_type = _CV_TO_INPUT[cvType]
+        p.n_levels, p.scale, p.method = int(nLevels), float(scale), int(method)
+        p.lambda_, p.lambdagrad, p.lambdaf, p.lambdams = lambda_, lambdagrad, lambdaf, lambdams
+        p.alpha_tv, p.alpha_proj, p.alpha_fn, p.tau = alphaTv, alphaProj, alphaFn, tau
+        p.theta = 1.0 / alphaTv
+        p.n_warp_iters, p.n_solver_iters = int(nWarpIters), int(nSolverIters)
+        p.stride_alignment = self.StrideAlignment
+        p.block_width, p.block_height = self.BlockWidth, self.BlockHeight
+        p.fix_quirks = int(fix_quirks)
+        return self._create(p)
+
+    def setCameraMatrices(self, intrinsic0, intrinsic1=None) -> int:
+        """ReconFlow::setCameraMatrices (Reconflow.cu:78-116)."""
+        intrinsic1 = intrinsic0 if intrinsic1 is None else intrinsic1
+        k0, p0 = _dbl(intrinsic0, 9)
+        k1, p1 = _dbl(intrinsic1, 9)
+        N.check(self._lib.rf_set_cameras(self._handle(), p0, p1))
+        return 0
+
+    def copySparseOpticalFlowToDevice(self, u, v, mask=None) -> int:
+        """CudaFlow::copySparseOpticalFlowToDevice (Cudaflow.cu:327-343)."""
+        u = np.ascontiguousarray(u, np.float32)
+        v = np.ascontiguousarray(v, np.float32)
+        m = None if mask is None else np.ascontiguousarray(mask, np.float32)
+        N.check(self._lib.rf_set_prior_flow(self._handle(), _ptr(u), _ptr(v),
+                                            None if m is None else _ptr(m), u.shape[1]))
+        return 0
+
+    copyInitialOpticalFlowToDevice = copySparseOpticalFlowToDevice
+
+    def solveR(self, *args) -> int:
+        """solveR(R1, t1, flowScale) or solveR(R0, t0, R1, t1, flowScale)
+        (Reconflow.cu:130-144)."""
+        if len(args) in (2, 3):
+            R0 = t0 = None
+            R1, t1 = args[0], args[1]
+            fs = args[2] if len(args) == 3 else 5.0
+        elif len(args) in (4, 5):
+            R0, t0, R1, t1 = args[:4]
+            fs = args[4] if len(args) == 5 else 5.0
+        else:
+            raise RfError(1, "solveR(R1, t1[, flowScale]) or solveR(R0, t0, R1, t1[, flowScale])")
+        self.flowScale = fs
+        keep = []
+        ptrs = []
+        for a, n in ((R0, 9), (t0, 3), (R1, 9), (t1, 3)):
+            if a is None:
+                ptrs.append(None)
+            else:
+                arr, p = _dbl(a, n)
+                keep.append(arr)
+                ptrs.append(p)
+        N.check(self._lib.rf_solve(self._handle(), *ptrs))
+        return 0
+
+    solveReconFlow = solveR
+
+    def copy3dToHost(self, X=None, Y=None, Z=None):
+        """ReconFlow::copy3dToHost (Reconflow.cu:65-70); returns (X, Y, Z)."""
+        X, Y, Z = self._out(X), self._out(Y), self._out(Z)
+        N.check(self._lib.rf_download_points(self._handle(), _ptr(X), _ptr(Y), _ptr(Z), X.shape[1]))
+        return X, Y, Z
+
+    def copyInverseDepthToHost(self, out=None):
+        out = self._out(out)
+        N.check(self._lib.rf_download_inv_depth(self._handle(), _ptr(out), out.shape[1]))
+        return out
+
+    def removeEdgeArtifacts3D(self, surfaceWidth: int, maxSurfaceArea: float) -> int:
+        """ReconFlow::removeEdgeArtifacts3D (Reconflow.cu:468-477)."""
+        N.check(self._lib.rf_remove_edge_artifacts(self._handle(), int(surfaceWidth),
+                                                   ctypes.c_float(maxSurfaceArea)))
+        return 0

@@ -1,0 +1,203 @@
+"""Seeded synthetic stereo scenes with analytic ground truth.
+
+A scene is a piecewise-planar surface seen by camera 0 (at the origin) and a
+second camera moved rigidly (X1 = R X + t, the convention of the reference's
+SolveUc, ``reconflow/solveUcSk.cu:25-33``):
+
+* depth: 8 planes over a Voronoi partition of camera 0's image, each plane's
+  inverse depth linear in pixel coordinates with depth inside [2, 10] m over
+  the image;
+* texture: 200 Gaussian blobs plus 1/f noise, an analytic function of camera-0
+  pixel coordinates, normalised to [0, 1];
+* frame 2: every camera-1 pixel is ray-cast against the planes (nearest hit
+  whose camera-0 projection lies in that plane's cell) and takes the texture
+  there;
+* pose: rotation <= 2 degrees about a random axis, |t| = 0.1 m;
+* N(0, 0.01) pixel noise on both frames.
+
+K defaults to fx = fy = 500 * w / 640, cx = w / 2, cy = h / 2 (500, 320, 240
+at 640x480).  Ground truth: flow of every camera-0 pixel, inverse depth, and
+a validity mask (in view and not occluded in camera 1).
+"""
+from __future__ import annotations
+
+import math
+
+import numpy as np
+
+__all__ = ["make_scene", "intrinsics_for", "random_pose", "render_pair"]
+
+
+def intrinsics_for(width: int, height: int) -> np.ndarray:
+    f = 500.0 * width / 640.0
+    return np.array([[f, 0.0, width / 2.0], [0.0, f, height / 2.0], [0.0, 0.0, 1.0]])
+
+
+def _rodrigues(axis: np.ndarray, angle: float) -> np.ndarray:
+    a = axis / np.linalg.norm(axis)
+    K = np.array([[0, -a[2], a[1]], [a[2], 0, -a[0]], [-a[1], a[0], 0]])
+    return np.eye(3) + math.sin(angle) * K + (1 - math.cos(angle)) * (K @ K)
+
+
+def random_pose(rng: np.random.Generator, max_rot_deg: float = 2.0, trans: float = 0.1):
+    axis = rng.normal(size=3)
+    ang = math.radians(rng.uniform(0.0, max_rot_deg))
+    R = _rodrigues(axis, ang)
+    d = rng.normal(size=3)
+    t = trans * d / np.linalg.norm(d)
+    return R, t
+
+
+class _Texture:
+    """Gaussian blobs + 1/f noise, analytic in camera-0 pixel coordinates."""
+
+    def __init__(self, rng, width, height, n_blobs=200, n_waves=48):
+        w, h = float(width), float(height)
+        m = 0.15  # blobs also cover a margin around the image
+        self.cx = rng.uniform(-m * w, (1 + m) * w, n_blobs)
+        self.cy = rng.uniform(-m * h, (1 + m) * h, n_blobs)
+        self.sig = np.exp(rng.uniform(math.log(0.004 * w), math.log(0.05 * w), n_blobs))
+        self.amp = rng.uniform(-1.0, 1.0, n_blobs)
+        fmin, fmax = 1.0 / w, 0.2
+        self.freq = np.exp(rng.uniform(math.log(fmin), math.log(fmax), n_waves))
+        th = rng.uniform(0, 2 * math.pi, n_waves)
+        self.kx = 2 * math.pi * self.freq * np.cos(th)
+        self.ky = 2 * math.pi * self.freq * np.sin(th)
+        self.ph = rng.uniform(0, 2 * math.pi, n_waves)
+        self.wamp = 0.6 * (fmin / self.freq) ** 0.5
+        self.lo, self.hi = 0.0, 1.0
+
+    def raw(self, x: np.ndarray, y: np.ndarray) -> np.ndarray:
+        x = x.astype(np.float64).ravel()
+        y = y.astype(np.float64).ravel()
+        out = np.zeros_like(x)
+        for i in range(len(self.amp)):
+            r = 4.0 * self.sig[i]
+            sel = np.nonzero((np.abs(x - self.cx[i]) < r) & (np.abs(y - self.cy[i]) < r))[0]
+            if sel.size == 0:
+                continue
+            dx = x[sel] - self.cx[i]
+            dy = y[sel] - self.cy[i]
+            out[sel] += self.amp[i] * np.exp(-(dx * dx + dy * dy) / (2 * self.sig[i] ** 2))
+        for i in range(len(self.freq)):
+            out += self.wamp[i] * np.cos(self.kx[i] * x + self.ky[i] * y + self.ph[i])
+        return out
+
+    def __call__(self, x, y):
+        shape = np.shape(x)
+        v = (self.raw(x, y) - self.lo) / (self.hi - self.lo)
+        return np.clip(v, 0.0, 1.0).reshape(shape)
+
+
+class _Planes:
+    """Inverse depth a + b x + c y over Voronoi cells of camera 0's image."""
+
+    def __init__(self, rng, width, height, K, n_planes=8, zmin=2.0, zmax=10.0):
+        w, h = float(width), float(height)
+        self.seeds = np.stack([rng.uniform(0, w, n_planes), rng.uniform(0, h, n_planes)], 1)
+        lo, hi = 1.0 / zmax, 1.0 / zmin
+        abc = []
+        for _ in range(n_planes):
+            while True:
+                d00, d10, d01 = rng.uniform(lo, hi, 3)
+                d11 = d10 + d01 - d00
+                if lo <= d11 <= hi:
+                    break
+            b = (d10 - d00) / w
+            c = (d01 - d00) / h
+            abc.append((d00, b, c))
+        self.abc = np.array(abc)
+        fx, fy, cx, cy = K[0, 0], K[1, 1], K[0, 2], K[1, 2]
+        a, b, c = self.abc.T
+        # inverse depth plane -> 3D plane n . X = 1 in camera-0 coordinates
+        self.n = np.stack([b * fx, c * fy, a + b * cx + c * cy], 1)
+
+    def label(self, x, y):
+        d = (x[..., None] - self.seeds[:, 0]) ** 2 + (y[..., None] - self.seeds[:, 1]) ** 2
+        return np.argmin(d, axis=-1)
+
+    def inv_depth(self, x, y):
+        k = self.label(x, y)
+        a, b, c = self.abc[k, 0], self.abc[k, 1], self.abc[k, 2]
+        return a + b * x + c * y
+
+
+def _raycast(planes: _Planes, K, Kinv, R, t, xs, ys):
+    """Nearest valid plane hit for camera-1 pixels; returns (X in camera 0, ok)."""
+    C = -R.T @ t
+    rays = np.stack([xs.ravel(), ys.ravel(), np.ones(xs.size)], 0)
+    d = R.T @ (Kinv @ rays)  # directions in camera-0 coordinates, (3, N)
+    best = np.full(xs.size, np.inf)
+    hit = np.zeros((3, xs.size))
+    nC = planes.n @ C
+    nd = planes.n @ d  # (P, N)
+    for k in range(planes.n.shape[0]):
+        with np.errstate(divide="ignore", invalid="ignore"):
+            lam = (1.0 - nC[k]) / nd[k]
+        X = C[:, None] + lam[None, :] * d
+        z = X[2]
+        ok = (lam > 0) & (z > 1e-6) & np.isfinite(lam)
+        with np.errstate(divide="ignore", invalid="ignore"):
+            px = K[0, 0] * X[0] / z + K[0, 2]
+            py = K[1, 1] * X[1] / z + K[1, 2]
+        ok &= planes.label(np.where(ok, px, 0.0), np.where(ok, py, 0.0)) == k
+        better = ok & (lam < best)
+        best = np.where(better, lam, best)
+        hit[:, better] = X[:, better]
+    found = np.isfinite(best)
+    return hit, found
+
+
+def render_pair(width, height, K, R, t, planes, tex, rng, noise=0.01):
+    """Render both frames and the ground truth of one pose."""
+    Kinv = np.linalg.inv(K)
+    ys, xs = np.mgrid[0:height, 0:width].astype(np.float64)
+    inv_depth = planes.inv_depth(xs, ys)
+    Z = 1.0 / inv_depth
+    I0 = tex(xs, ys)
+    # camera 1: ray-cast every pixel
+    X, found = _raycast(planes, K, Kinv, R, t, xs, ys)
+    with np.errstate(divide="ignore", invalid="ignore"):
+        px = K[0, 0] * X[0] / X[2] + K[0, 2]
+        py = K[1, 1] * X[1] / X[2] + K[1, 2]
+    px = np.where(found, px, xs.ravel())
+    py = np.where(found, py, ys.ravel())
+    I1 = tex(px, py).reshape(height, width)
+    # ground-truth flow of camera-0 pixels
+    P0 = np.stack([xs.ravel() * Z.ravel(), ys.ravel() * Z.ravel(), Z.ravel()], 0)
+    X0 = Kinv @ P0
+    X1 = R @ X0 + t[:, None]
+    u1 = K[0, 0] * X1[0] / X1[2] + K[0, 2]
+    v1 = K[1, 1] * X1[1] / X1[2] + K[1, 2]
+    flow = np.stack([(u1 - xs.ravel()).reshape(height, width),
+                     (v1 - ys.ravel()).reshape(height, width)], -1)
+    # validity: lands inside camera 1 and is the surface camera 1 sees there
+    inb = (u1 >= 0) & (u1 <= width - 1) & (v1 >= 0) & (v1 <= height - 1)
+    Xv, fv = _raycast(planes, K, Kinv, R, t, u1, v1)
+    same = fv & (np.linalg.norm(Xv - X0, axis=0) < 1e-3 * np.maximum(X0[2], 1.0))
+    valid = (inb & same).reshape(height, width)
+    I0 = I0 + rng.normal(0.0, noise, I0.shape)
+    I1 = I1 + rng.normal(0.0, noise, I1.shape)
+    return {
+        "I0": I0.astype(np.float32), "I1": I1.astype(np.float32),
+        "flow": flow.astype(np.float32), "inv_depth": inv_depth.astype(np.float32),
+        "depth": Z.astype(np.float32), "valid": valid,
+    }
+
+
+def make_scene(width: int, height: int, seed: int = 0, K=None, n_planes: int = 8,
+               n_blobs: int = 200, max_rot_deg: float = 2.0, trans: float = 0.1,
+               noise: float = 0.01) -> dict:
+    """One seeded frame pair with ground truth (see module docstring)."""
+    rng = np.random.default_rng(seed)
+    K = intrinsics_for(width, height) if K is None else np.asarray(K, np.float64)
+    planes = _Planes(rng, width, height, K, n_planes)
+    tex = _Texture(rng, width, height, n_blobs)
+    # normalise the texture once, from a coarse sample of camera 0's view
+    gy, gx = np.mgrid[0:height:4, 0:width:4].astype(np.float64)
+    raw = tex.raw(gx, gy)
+    tex.lo, tex.hi = float(np.percentile(raw, 0.5)), float(np.percentile(raw, 99.5))
+    R, t = random_pose(rng, max_rot_deg, trans)
+    out = render_pair(width, height, K, R, t, planes, tex, rng, noise)
+    out.update({"K": K, "R": R, "t": t, "seed": seed})
+    return out
