@@ -40,8 +40,11 @@ sys.path.insert(0, ROOT)
 WORKLOADS = {
     # 1280x720, 6 levels, 5 warps, 100 iterations: the headline workload
     "720p": dict(width=1280, height=720, levels=6, warps=5, iters=100, seed=0),
-    # 640x480, 5 levels, 3 warps, 50 iterations (small case for profiling)
+    # 640x480, 5 levels, 3 warps, 50 iterations
     "480p": dict(width=640, height=480, levels=5, warps=3, iters=50, seed=0),
+    # profiling case: the 720p pair at its finest level only, 1 warp, 4 iterations
+    # (a dozen launches, so a profiler capture ends in seconds)
+    "720p-l0": dict(width=1280, height=720, levels=1, warps=1, iters=4, seed=0),
 }
 SOLVER = dict(method=14, lam=50.0, theta=0.33, tau=0.25, alpha_proj=60.0, lambdaf=0.1,
               lambdams=100.0, fix_quirks=1)

@@ -201,7 +201,9 @@ RF_API const char* rf_version(void);
 /* ------------------------------------------------------------------------
  * Kernel-level entry points (device pointers, caller's stream).  Each runs
  * one reference kernel's computation on one pyramid level so it can be
- * checked against the oracle in isolation.  Arrays are stride-major planes.
+ * checked against the oracle in isolation.  Arrays are stride-major planes
+ * of (h + 1) * s floats: kernels that read the row below or the column right
+ * of the image (as the reference does) touch row h and column w. 
  * ---------------------------------------------------------------------- */
 
 /* DownscaleKernel / DownscaleScalingKernel (downscale.cu:6-48). */

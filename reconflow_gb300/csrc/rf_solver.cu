@@ -702,7 +702,8 @@ rf_status rf_remove_edge_artifacts(rf_handle* h, int surface_width, float max_ar
     if (!h) return fail(RF_ERR_INVALID_ARG, "rf_remove_edge_artifacts: null handle");
     if (h->p.method == RF_METHOD_TVL1 || !h->solved)
         return fail(RF_ERR_STATE, "rf_remove_edge_artifacts: needs a ReconFlow solve");
-    if (surface_width < 0 || surface_width >= h->p.width || surface_width >= h->p.height)
+    // ix - range stays >= 0 wherever ix + range > width only if 2*range <= width
+    if (surface_width < 0 || 2 * surface_width > h->p.width || 2 * surface_width > h->p.height)
         return fail(RF_ERR_INVALID_ARG, "rf_remove_edge_artifacts: surface_width out of range");
     LevelDims d{h->W[0], h->H[0], h->S[0]};
     if (launch_remove_edge(h->X, h->Y, h->Z, surface_width, max_area, d, h->X1, h->Y1, h->Z1,
@@ -878,7 +879,7 @@ rf_status rfk_remove_edge_artifacts(const float* X, const float* Y, const float*
                                     float max_area, int w, int h, int s, float* X1, float* Y1,
                                     float* Z1, void* stream) {
     RFK_CHECK(X && Y && Z && X1 && Y1 && Z1 && w > 0 && h > 0 && s >= w && range >= 0 &&
-                  range < w && range < h,
+                  2 * range <= w && 2 * range <= h,
               "rfk_remove_edge_artifacts");
     RFK_RET(launch_remove_edge(X, Y, Z, range, max_area, LevelDims{w, h, s}, X1, Y1, Z1,
                                (cudaStream_t)stream),

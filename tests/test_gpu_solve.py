@@ -235,3 +235,19 @@ def test_device_results_and_inverse_depth(rf):
     np.testing.assert_array_equal(inv[:, :w], (np.float32(1) / Z[:, :w]))
     ptrs = f.deviceResults()
     assert all(p != 0 for p in ptrs)
+
+
+def test_degenerate_baseline_nan_parity(oracle, rf):
+    """Pure sideways baseline (t_z = 0, R = I): the reference's projection
+    divides 0/0 wherever a point is reset to the origin, so NaNs appear; the
+    GPU must still match the oracle everywhere (NaN for NaN)."""
+    w, h, L = 96, 72, 3
+    rng = np.random.default_rng(0)
+    y, x = np.mgrid[0:h, 0:w].astype(np.float64)
+    I0 = (0.5 + 0.2 * np.sin(0.31 * x + 0.17 * y) + rng.normal(0, 0.01, (h, w))).astype(np.float32)
+    I1 = np.roll(I0, 1, axis=1)
+    K = _K(w, h)
+    kw = dict(warps=2, iters=5, fix=1)
+    got, _ = run_gpu(rf, w, h, L, 14, I0, I1, K, np.eye(3), np.array([-0.1, 0.0, 0.0]), **kw)
+    want = run_oracle(oracle, w, h, L, 14, I0, I1, K, np.eye(3), np.array([-0.1, 0.0, 0.0]), **kw)
+    compare(got, want, w, h)
