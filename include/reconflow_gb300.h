@@ -224,6 +224,13 @@ RF_API rf_status rfk_median5(const float* u, const float* v, int w, int h, int s
 /* MedianFilter3DKernel3 (medianFilter.cu:166-243). */
 RF_API rf_status rfk_median3d(const float* X, const float* Y, const float* Z, int w, int h, int s,
                               float* X1, float* Y1, float* Z1, void* stream);
+/* The per-warp flow update of ReconFlow (Reconflow.cu:410-420): median of
+ * duhat (MedianFilterKernel5), u += it (AddKernel), median of u.  The
+ * intermediate u + median(duhat) goes to the caller's scratch planes
+ * (tmp_u, tmp_v, (h + 1) * s floats each); results to out_u, out_v. */
+RF_API rf_status rfk_warp_update(const float* duhat, const float* dvhat, const float* u,
+                                 const float* v, int w, int h, int s, float* tmp_u, float* tmp_v,
+                                 float* out_u, float* out_v, void* stream);
 /* rgbaToGrayKernel (rgbToGray.cu:3-19). */
 RF_API rf_status rfk_rgb_to_gray(const uint8_t* rgb, int w, int h, int s, float* out,
                                  void* stream);

@@ -869,6 +869,18 @@ rf_status rfk_median3d(const float* X, const float* Y, const float* Z, int w, in
             "rfk_median3d");
 }
 
+rf_status rfk_warp_update(const float* duhat, const float* dvhat, const float* u, const float* v,
+                          int w, int h, int s, float* tmp_u, float* tmp_v, float* out_u,
+                          float* out_v, void* stream) {
+    RFK_CHECK(duhat && dvhat && u && v && tmp_u && tmp_v && out_u && out_v && w > 0 && h > 0 &&
+                  s >= w,
+              "rfk_warp_update");
+    LevelDims d{w, h, s};
+    if (launch_median_add(duhat, dvhat, u, v, tmp_u, tmp_v, d, (cudaStream_t)stream) != 0)
+        return cuda_fail(cudaGetLastError(), "rfk_warp_update");
+    RFK_RET(launch_median5(tmp_u, tmp_v, out_u, out_v, d, (cudaStream_t)stream), "rfk_warp_update");
+}
+
 rf_status rfk_rgb_to_gray(const uint8_t* rgb, int w, int h, int s, float* out, void* stream) {
     RFK_CHECK(rgb && out && w > 0 && h > 0 && s >= w, "rfk_rgb_to_gray");
     RFK_RET(launch_convert(rgb, RF_INPUT_RGB8, w, h, s, out, s, (cudaStream_t)stream),

@@ -200,3 +200,23 @@ def test_flow_color_matches_formula(rf, torch_cuda):
     np.testing.assert_allclose(got[..., 2], col[0], atol=2e-5)
     np.testing.assert_allclose(got[..., 1], col[1], atol=2e-5)
     np.testing.assert_allclose(got[..., 0], col[2], atol=2e-5)
+
+
+@pytest.mark.parametrize("w,h,s", SIZES)
+def test_warp_update_bitexact(oracle, rf, torch_cuda, w, h, s):
+    """median5(duhat) -> u += it -> median5(u) (Reconflow.cu:410-420)."""
+    rng = np.random.default_rng(w * 13 + h)
+    n = (h + 1) * s
+    du, dv = (rng.normal(size=n).astype(np.float32) for _ in range(2))
+    u, v = ((rng.normal(size=n) * 3).astype(np.float32) for _ in range(2))
+    lib = rf.load()
+    d = [dev(torch_cuda, a) for a in (du, dv, u, v)]
+    tmp = [torch_cuda.zeros_like(d[0]) for _ in range(2)]
+    out = [torch_cuda.zeros_like(d[0]) for _ in range(2)]
+    ok(rf, lib.rfk_warp_update(*[P(t) for t in d], w, h, s, *[P(t) for t in tmp],
+                               *[P(t) for t in out], None))
+    mu, mv = oracle.median5(du, dv, w, h, s)
+    tu, tv = u + mu, v + mv
+    wu, wv = oracle.median5(tu, tv, w, h, s)
+    for got, want, nm in ((out[0], wu, "u"), (out[1], wv, "v")):
+        assert_bitexact(host(got).reshape(h + 1, s), want.reshape(h + 1, s), nm, region=(h, w))
