@@ -31,7 +31,7 @@ int main() {
         const double f = 125.0;
         const double K[9] = {f, 0, width / 2.0, 0, f, height / 2.0, 0, 0, 1};
         const double R[9] = {1, 0, 0, 0, 1, 0, 0, 0, 1};
-        const double t[3] = {-0.1, 0.001, 0.001};
+        const double t[3] = {0.1, 0.001, 0.001};  // content moves +1 px: depth f*b/d = 12.5
         flow.setCameraMatrices(K, K);
         flow.copyImagesToDevice(i0.data(), i1.data(), stride);
         flow.solveR(R, t, 50.0f);

@@ -37,4 +37,5 @@ def test_cpp_demo_runs_on_gpu(tmp_path):
     out = r.stdout.strip().split()
     assert r.returncode == 0 and out[0] == "ok", r.stdout + r.stderr
     med_u, med_z = float(out[1]), float(out[2])
-    assert abs(med_u - 1.0) < 0.2 and med_z > 0
+    # one-pixel disparity, baseline 0.1, focal 125: depth 12.5
+    assert abs(med_u - 1.0) < 0.2 and abs(med_z - 12.5) < 1.5, (med_u, med_z)
