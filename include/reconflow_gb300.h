@@ -231,6 +231,23 @@ RF_API rf_status rfk_median3d(const float* X, const float* Y, const float* Z, in
 RF_API rf_status rfk_warp_update(const float* duhat, const float* dvhat, const float* u,
                                  const float* v, int w, int h, int s, float* tmp_u, float* tmp_v,
                                  float* out_u, float* out_v, void* stream);
+/* Largest height * stride (floats per plane) that rfk_warp_update_noalloc
+ * accepts: 1920x1088 fits. */
+#define RF_NOALLOC_MAX_PLANE (1u << 21)
+
+/* rfk_warp_update without caller scratch and without any allocation, for
+ * callers that cannot allocate device memory where this step runs (a
+ * real-time pipeline that forbids cudaMalloc after start-up, or a host
+ * framework that owns the device memory budget).  No counterpart in the
+ * reference.  The intermediate planes live in a static 16 MiB device array
+ * that every call on a device shares: calls that overlap on the GPU race, so
+ * order them on one stream.  height * stride above RF_NOALLOC_MAX_PLANE is
+ * rejected with RF_ERR_INVALID_ARG.  The first call on each device looks up
+ * the array's device address with that device current; make it before any
+ * stream capture on that device. */
+RF_API rf_status rfk_warp_update_noalloc(const float* duhat, const float* dvhat, const float* u,
+                                         const float* v, int w, int h, int s, float* out_u,
+                                         float* out_v, void* stream);
 /* rgbaToGrayKernel (rgbToGray.cu:3-19). */
 RF_API rf_status rfk_rgb_to_gray(const uint8_t* rgb, int w, int h, int s, float* out,
                                  void* stream);

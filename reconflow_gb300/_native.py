@@ -79,6 +79,7 @@ _SIGS = [
     ("rfk_median5", _I, [_VP, _VP, _I, _I, _I, _VP, _VP, _VP]),
     ("rfk_median3d", _I, [_VP, _VP, _VP, _I, _I, _I, _VP, _VP, _VP, _VP]),
     ("rfk_warp_update", _I, [_VP, _VP, _VP, _VP, _I, _I, _I, _VP, _VP, _VP, _VP, _VP]),
+    ("rfk_warp_update_noalloc", _I, [_VP, _VP, _VP, _VP, _I, _I, _I, _VP, _VP, _VP]),
     ("rfk_rgb_to_gray", _I, [_VP, _I, _I, _I, _VP, _VP]),
     ("rfk_remove_edge_artifacts", _I, [_VP, _VP, _VP, _I, _F, _I, _I, _I, _VP, _VP, _VP, _VP]),
     ("rfk_flow_to_color", _I, [_VP, _VP, _I, _I, _I, _F, _VP, _VP]),

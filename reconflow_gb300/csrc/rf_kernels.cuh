@@ -55,6 +55,9 @@ struct ReconFields {
     const float* mask;
 };
 
+// Records `msg` as the calling thread's rf_last_error_string(); returns st.
+int set_last_error(int st, const char* msg);
+
 int launch_convert(const void* in, int type, int w, int h, int in_pitch, float* out, int s,
                    cudaStream_t st);
 int launch_downscale2(const float* a, const float* b, LevelDims fine, LevelDims coarse,

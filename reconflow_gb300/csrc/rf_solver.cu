@@ -20,6 +20,10 @@
 
 using namespace rf;
 
+namespace rf {
+int set_last_error(int st, const char* msg);
+}
+
 namespace {
 
 thread_local std::string g_err;
@@ -28,6 +32,15 @@ rf_status fail(rf_status st, const std::string& msg) {
     g_err = msg;
     return st;
 }
+
+}  // namespace
+
+int rf::set_last_error(int st, const char* msg) {
+    g_err = msg;
+    return st;
+}
+
+namespace {
 
 rf_status cuda_fail(cudaError_t e, const char* what) {
     g_err = std::string(what) + ": " + cudaGetErrorString(e);
