@@ -290,6 +290,44 @@ __device__ __forceinline__ float median9_exchange(float (&m)[9]) {
     return m[4];
 }
 
+// Median of 9 finite values with the 19-comparator min/max network for the
+// 3x3 median (A. Paeth, "Median finding on a 3x3 grid", Graphics Gems, 1990,
+// in N. Devillard's ordering).  For finite inputs its value equals the
+// exchange selection's; the two can differ only in the sign of a zero
+// result, so a zero result is recomputed with the reference's exchange order.
+// Inputs must not be NaN (the 3D state fed to it is finite by construction).
+__device__ __forceinline__ float median9_finite(const float (&in)[9]) {
+    float p0 = in[0], p1 = in[1], p2 = in[2], p3 = in[3], p4 = in[4], p5 = in[5], p6 = in[6],
+          p7 = in[7], p8 = in[8];
+#define RF_SORT2(a, b)            \
+    {                             \
+        float lo__ = fminf(a, b); \
+        b = fmaxf(a, b);          \
+        a = lo__;                 \
+    }
+    RF_SORT2(p1, p2); RF_SORT2(p4, p5); RF_SORT2(p7, p8);
+    RF_SORT2(p0, p1); RF_SORT2(p3, p4); RF_SORT2(p6, p7);
+    RF_SORT2(p1, p2); RF_SORT2(p4, p5); RF_SORT2(p7, p8);
+    p3 = fmaxf(p0, p3);
+    p5 = fminf(p5, p8);
+    RF_SORT2(p4, p7);
+    p6 = fmaxf(p3, p6);
+    p4 = fmaxf(p1, p4);
+    p2 = fminf(p2, p5);
+    p4 = fminf(p4, p7);
+    RF_SORT2(p4, p2);
+    p4 = fmaxf(p6, p4);
+    p4 = fminf(p4, p2);
+#undef RF_SORT2
+    if (p4 == 0.0f) {
+        float m[9];
+#pragma unroll
+        for (int k = 0; k < 9; k++) m[k] = in[k];
+        return median9_exchange(m);
+    }
+    return p4;
+}
+
 // Exchange-selection median of 25 (medianFilter.cu:55-74): 13 passes.
 __device__ __forceinline__ float median25_exchange(float (&m)[25]) {
 #pragma unroll
