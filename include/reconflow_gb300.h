@@ -199,6 +199,42 @@ RF_API const char* rf_last_error_string(void);
 RF_API const char* rf_version(void);
 
 /* ------------------------------------------------------------------------
+ * Batched solve (no reference counterpart; the reference solves one pair per
+ * object).  Many independent frame pairs, each with its own size, cameras and
+ * pose, share one parameter block (methods 0 and 14, float32 gray input) and
+ * are solved together: every step of the schedule is one launch covering all
+ * pairs, captured in one CUDA graph.  A pair's results are bit-identical to
+ * solving it alone with rf_solve / rf_solve_flow.
+ * ---------------------------------------------------------------------- */
+typedef struct rf_batch rf_batch;
+
+RF_API rf_status rf_batch_create(const rf_params* p, int n_pairs, const int* widths,
+                                 const int* heights, rf_batch** out);
+RF_API rf_status rf_batch_destroy(rf_batch* b);
+/* stride (elements per row) of pair `pair`'s planes */
+RF_API int rf_batch_stride(const rf_batch* b, int pair);
+RF_API rf_status rf_batch_set_cameras(rf_batch* b, int pair, const double K0[9],
+                                      const double K1[9]);
+RF_API rf_status rf_batch_upload_images(rf_batch* b, int pair, const float* i0, const float* i1,
+                                        int pitch);
+RF_API rf_status rf_batch_upload_images_device(rf_batch* b, int pair, const float* i0,
+                                               const float* i1, int pitch);
+/* R0, t0 may be NULL (identity / zero for every pair); otherwise arrays of
+ * n_pairs x 9 and n_pairs x 3 doubles, pair-major. */
+RF_API rf_status rf_batch_solve(rf_batch* b, const double* R0, const double* t0, const double* R1,
+                                const double* t1);
+RF_API rf_status rf_batch_solve_flow(rf_batch* b);
+RF_API rf_status rf_batch_download_flow(rf_batch* b, int pair, float* u, float* v, int pitch);
+RF_API rf_status rf_batch_download_points(rf_batch* b, int pair, float* X, float* Y, float* Z,
+                                          int pitch);
+RF_API rf_status rf_batch_download_inv_depth(rf_batch* b, int pair, float* inv_depth, int pitch);
+RF_API rf_status rf_batch_device_results(rf_batch* b, int pair, const float** u, const float** v,
+                                         const float** X, const float** Y, const float** Z);
+RF_API rf_status rf_batch_set_stream(rf_batch* b, void* stream);
+RF_API rf_status rf_batch_synchronize(rf_batch* b);
+RF_API uint64_t rf_batch_kernel_launches(const rf_batch* b);
+
+/* ------------------------------------------------------------------------
  * Kernel-level entry points (device pointers, caller's stream).  Each runs
  * one reference kernel's computation on one pyramid level so it can be
  * checked against the oracle in isolation.  Arrays are stride-major planes

@@ -6,6 +6,6 @@ the reference's ``CudaFlow`` / ``ReconFlow`` class surface, the in-tree build
 of the CUDA library and the seeded synthetic scene generator.
 """
 from ._native import RfError, load  # noqa: F401
-from .reconflow import CudaFlow, ReconFlow  # noqa: F401
+from .reconflow import CudaFlow, ReconFlow, ReconFlowBatch  # noqa: F401
 
-__all__ = ["CudaFlow", "ReconFlow", "RfError", "load"]
+__all__ = ["CudaFlow", "ReconFlow", "ReconFlowBatch", "RfError", "load"]

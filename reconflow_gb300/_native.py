@@ -72,6 +72,21 @@ _SIGS = [
     ("rf_kernel_launches", ctypes.c_uint64, [_VP]),
     ("rf_last_error_string", ctypes.c_char_p, []),
     ("rf_version", ctypes.c_char_p, []),
+    ("rf_batch_create", _I, [ctypes.POINTER(RfParams), _I, _VP, _VP, ctypes.POINTER(_VP)]),
+    ("rf_batch_destroy", _I, [_VP]),
+    ("rf_batch_stride", _I, [_VP, _I]),
+    ("rf_batch_set_cameras", _I, [_VP, _I, _D, _D]),
+    ("rf_batch_upload_images", _I, [_VP, _I, _VP, _VP, _I]),
+    ("rf_batch_upload_images_device", _I, [_VP, _I, _VP, _VP, _I]),
+    ("rf_batch_solve", _I, [_VP, _D, _D, _D, _D]),
+    ("rf_batch_solve_flow", _I, [_VP]),
+    ("rf_batch_download_flow", _I, [_VP, _I, _VP, _VP, _I]),
+    ("rf_batch_download_points", _I, [_VP, _I, _VP, _VP, _VP, _I]),
+    ("rf_batch_download_inv_depth", _I, [_VP, _I, _VP, _I]),
+    ("rf_batch_device_results", _I, [_VP, _I, _VP, _VP, _VP, _VP, _VP]),
+    ("rf_batch_set_stream", _I, [_VP, _VP]),
+    ("rf_batch_synchronize", _I, [_VP]),
+    ("rf_batch_kernel_launches", ctypes.c_uint64, [_VP]),
     ("rfk_downscale", _I, [_VP, _I, _I, _I, _I, _I, _I, _F, _I, _VP, _VP]),
     ("rfk_upscale", _I, [_VP, _I, _I, _I, _I, _I, _I, _F, _VP, _VP]),
     ("rfk_warp", _I, [_VP, _I, _I, _I, _VP, _VP, _VP, _VP]),

@@ -27,6 +27,7 @@ SOURCES = {
     "rf_kernels.cu": ["-fmad=false"],
     "rf_solver.cu": ["-fmad=false"],
     "rf_noalloc.cu": ["-fmad=false"],
+    "rf_batch.cu": ["-fmad=false"],
 }
 COMMON = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC,-ffp-contract=off,-fvisibility=hidden",
           "--expt-relaxed-constexpr", "-I" + os.path.join(ROOT, "include"), "-I" + CSRC]

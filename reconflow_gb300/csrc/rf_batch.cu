@@ -1,0 +1,698 @@
+// Batched solver: many independent frame pairs, of different sizes, solved
+// together.  Every step of the coarse-to-fine schedule (Reconflow.cu:147-466
+// for ReconFlow, Cudaflow.cu:403-621 for plain TV-L1) is ONE launch covering
+// that step for every pair, so small pyramid levels fill the GPU and the
+// per-launch cost is paid once per step instead of once per pair.  The whole
+// batch schedule is captured into one CUDA graph.
+//
+// Layout: each pair owns a run of level-0-sized planes (its stride x (height
+// + 1) floats, aligned to 64 floats) in one pool; plane k of pair i starts at
+// base_i + k * plane_i, and all pairs use the same plane indices for the same
+// role, so a launch names its fields by plane index.  Blocks map to pairs
+// through a per-level prefix sum of tile counts (32x8 tiles).
+//
+// Per-pixel arithmetic is the shared code of the single-pair kernels
+// (rf_ops.cuh), so a pair solved in a batch is bit-identical to the same pair
+// solved alone.
+#include <algorithm>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include <cuda_runtime.h>
+
+#include "../../include/reconflow_gb300.h"
+#include "rf_kernels.cuh"
+#include "rf_ops.cuh"
+
+using namespace rf;
+
+namespace rf_batch_impl {
+
+constexpr int BX = 32;
+constexpr int BY = 8;
+constexpr int kMaxLevels = 16;
+
+struct BatchPair {
+    float* base;
+    size_t plane;  // floats per plane
+    LevelDims dims[kMaxLevels];
+};
+
+struct BatchCtx {
+    const BatchPair* pairs;
+    const int* prefix;          // [level][n + 1] tile prefix sums
+    const LevelConsts* consts;  // [pair][level]
+    int n;
+    int L;
+};
+
+__device__ __forceinline__ float* plane_ptr(const BatchPair& bp, int k) {
+    return bp.base + (size_t)k * bp.plane;
+}
+
+// One block = one 32x8 tile of one pair at `level`.
+template <class Op>
+__global__ void __launch_bounds__(BX* BY) k_batch(BatchCtx ctx, int level, Op op) {
+    const int* pre = ctx.prefix + level * (ctx.n + 1);
+    const int b = blockIdx.x;
+    int lo = 0, hi = ctx.n - 1;
+    while (lo < hi) {
+        int mid = (lo + hi + 1) >> 1;
+        if (pre[mid] <= b)
+            lo = mid;
+        else
+            hi = mid - 1;
+    }
+    const BatchPair& bp = ctx.pairs[lo];
+    const LevelDims d = bp.dims[level];
+    const int t = b - pre[lo];
+    const int tw = (d.w + BX - 1) / BX;
+    const int ix = (t % tw) * BX + threadIdx.x, iy = (t / tw) * BY + threadIdx.y;
+    if (ix >= d.w || iy >= d.h) return;
+    op(ctx, bp, lo, level, d, ix, iy);
+}
+
+// ---- per-step operations (plane indices resolved per pair) ----------------
+struct OpDownscale2 {
+    int a, b, oa, ob;  // fine planes (level-1) -> coarse planes (level)
+    __device__ void operator()(const BatchCtx&, const BatchPair& bp, int, int level, LevelDims c,
+                               int ix, int iy) const {
+        LevelDims f = bp.dims[level - 1];
+        plane_ptr(bp, oa)[ix + iy * c.s] = 0.25f * downscale_px(plane_ptr(bp, a), f, c.w, c.h, ix, iy);
+        plane_ptr(bp, ob)[ix + iy * c.s] = 0.25f * downscale_px(plane_ptr(bp, b), f, c.w, c.h, ix, iy);
+    }
+};
+
+struct OpWarp {
+    int I1, u, v, out;
+    __device__ void operator()(const BatchCtx&, const BatchPair& bp, int, int, LevelDims d, int ix,
+                               int iy) const {
+        warp_px(plane_ptr(bp, I1), plane_ptr(bp, u), plane_ptr(bp, v), d, plane_ptr(bp, out), ix, iy);
+    }
+};
+
+struct OpDeriv {
+    int I0, I1w, Ix, Iy, Iz;
+    __device__ void operator()(const BatchCtx&, const BatchPair& bp, int, int, LevelDims d, int ix,
+                               int iy) const {
+        derivatives_px(plane_ptr(bp, I0), plane_ptr(bp, I1w), d, plane_ptr(bp, Ix), plane_ptr(bp, Iy),
+                       plane_ptr(bp, Iz), ix, iy);
+    }
+};
+
+struct ReconIdx {
+    int u, v, duhat, dvhat, pu1, pu2, pv1, pv2, uproj, vproj, sku, skv, Ix, Iy, Iz, X, Y, Z, X1,
+        Y1, Z1, uc, vc;
+};
+
+__device__ __forceinline__ ReconFields resolve(const BatchPair& bp, const ReconIdx& r) {
+    ReconFields f{};
+    f.u = plane_ptr(bp, r.u); f.v = plane_ptr(bp, r.v);
+    f.duhat = plane_ptr(bp, r.duhat); f.dvhat = plane_ptr(bp, r.dvhat);
+    f.pu1 = plane_ptr(bp, r.pu1); f.pu2 = plane_ptr(bp, r.pu2);
+    f.pv1 = plane_ptr(bp, r.pv1); f.pv2 = plane_ptr(bp, r.pv2);
+    f.uproj = plane_ptr(bp, r.uproj); f.vproj = plane_ptr(bp, r.vproj);
+    f.sku = plane_ptr(bp, r.sku); f.skv = plane_ptr(bp, r.skv);
+    f.Ix = plane_ptr(bp, r.Ix); f.Iy = plane_ptr(bp, r.Iy); f.Iz = plane_ptr(bp, r.Iz);
+    f.X = plane_ptr(bp, r.X); f.Y = plane_ptr(bp, r.Y); f.Z = plane_ptr(bp, r.Z);
+    f.X1 = plane_ptr(bp, r.X1); f.Y1 = plane_ptr(bp, r.Y1); f.Z1 = plane_ptr(bp, r.Z1);
+    f.uc = plane_ptr(bp, r.uc); f.vc = plane_ptr(bp, r.vc);
+    return f;
+}
+
+struct OpReconA {
+    ReconIdx r;
+    Weights wt;
+    int first, ucb;
+    __device__ void operator()(const BatchCtx& ctx, const BatchPair& bp, int pair, int level,
+                               LevelDims d, int ix, int iy) const {
+        ReconFields f = resolve(bp, r);
+        recon_a_px<0>(f, ctx.consts[pair * ctx.L + level], wt, d, ix, iy, first, ucb);
+    }
+};
+
+struct OpReconB {
+    ReconIdx r;
+    Weights wt;
+    int first;
+    __device__ void operator()(const BatchCtx&, const BatchPair& bp, int, int, LevelDims d, int ix,
+                               int iy) const {
+        ReconFields f = resolve(bp, r);
+        recon_b_px(f, wt, d, ix, iy, first);
+    }
+};
+
+struct OpPlainData {
+    int duhat, dvhat, pu1, pu2, pv1, pv2, Ix, Iy, Iz;
+    Weights wt;
+    int first;
+    __device__ void operator()(const BatchCtx&, const BatchPair& bp, int, int, LevelDims d, int ix,
+                               int iy) const {
+        plain_data_px(plane_ptr(bp, duhat), plane_ptr(bp, dvhat), plane_ptr(bp, pu1),
+                      plane_ptr(bp, pu2), plane_ptr(bp, pv1), plane_ptr(bp, pv2), plane_ptr(bp, Ix),
+                      plane_ptr(bp, Iy), plane_ptr(bp, Iz), wt, d, first, ix, iy);
+    }
+};
+
+struct OpPlainTV {
+    int duhat, dvhat, pu1, pu2, pv1, pv2;
+    Weights wt;
+    int first;
+    __device__ void operator()(const BatchCtx&, const BatchPair& bp, int, int, LevelDims d, int ix,
+                               int iy) const {
+        plain_tv_px(plane_ptr(bp, duhat), plane_ptr(bp, dvhat), plane_ptr(bp, pu1),
+                    plane_ptr(bp, pu2), plane_ptr(bp, pv1), plane_ptr(bp, pv2), wt, d, first, ix,
+                    iy);
+    }
+};
+
+// u + median5(duhat) (Reconflow.cu:410-416); out may be u itself
+struct OpMedianAdd {
+    int duhat, dvhat, u, v, ou, ov;
+    __device__ void operator()(const BatchCtx&, const BatchPair& bp, int, int, LevelDims d, int ix,
+                               int iy) const {
+        float mu, mv;
+        median5_pair(plane_ptr(bp, duhat), plane_ptr(bp, dvhat), ix, iy, d, mu, mv);
+        int pos = ix + iy * d.s;
+        float a = plane_ptr(bp, u)[pos] + mu;
+        float b = plane_ptr(bp, v)[pos] + mv;
+        plane_ptr(bp, ou)[pos] = a;
+        plane_ptr(bp, ov)[pos] = b;
+    }
+};
+
+struct OpMedian5 {
+    int u, v, ou, ov;
+    __device__ void operator()(const BatchCtx&, const BatchPair& bp, int, int, LevelDims d, int ix,
+                               int iy) const {
+        float mu, mv;
+        median5_pair(plane_ptr(bp, u), plane_ptr(bp, v), ix, iy, d, mu, mv);
+        plane_ptr(bp, ou)[ix + iy * d.s] = mu;
+        plane_ptr(bp, ov)[ix + iy * d.s] = mv;
+    }
+};
+
+struct OpSolveUc {
+    int X, Y, Z, uc, vc;
+    __device__ void operator()(const BatchCtx& ctx, const BatchPair& bp, int pair, int level,
+                               LevelDims d, int ix, int iy) const {
+        int pos = ix + iy * d.s;
+        float a, b;
+        project_uc(ctx.consts[pair * ctx.L + level], plane_ptr(bp, X)[pos], plane_ptr(bp, Y)[pos],
+                   plane_ptr(bp, Z)[pos], ix, iy, a, b);
+        plane_ptr(bp, uc)[pos] = a;
+        plane_ptr(bp, vc)[pos] = b;
+    }
+};
+
+// upscale.cu:14-27 for up to 8 fields: runs on the tiles of the fine level
+// `level`; the coarse level is level + 1.
+struct OpUpscale {
+    int n;
+    int src[8], dst[8];
+    float scale;
+    __device__ void operator()(const BatchCtx&, const BatchPair& bp, int, int level, LevelDims f,
+                               int ix, int iy) const {
+        LevelDims c = bp.dims[level + 1];
+        float x = ((float)ix + 0.5f) / (float)f.w;
+        float y = ((float)iy + 0.5f) / (float)f.h;
+        Taps tx = taps_of(x, c.w);
+        Taps ty = taps_of(y, c.h);
+        int pos = ix + iy * f.s;
+#pragma unroll 1
+        for (int i = 0; i < n; i++)
+            plane_ptr(bp, dst[i])[pos] = bilerp(plane_ptr(bp, src[i]), c.s, tx, ty) * scale;
+    }
+};
+
+struct OpInvDepth {
+    int Z, out;
+    __device__ void operator()(const BatchCtx&, const BatchPair& bp, int, int, LevelDims d, int ix,
+                               int iy) const {
+        int pos = ix + iy * d.s;
+        plane_ptr(bp, out)[pos] = 1.0f / plane_ptr(bp, Z)[pos];
+    }
+};
+
+thread_local std::string g_batch_err;
+
+rf_status bfail(rf_status st, const std::string& msg) {
+    return static_cast<rf_status>(rf::set_last_error(st, msg.c_str()));
+}
+
+int align_up_i(int n, int m) {
+    int mod = n % m;
+    return mod ? n + m - mod : n;
+}
+
+}  // namespace rf_batch_impl
+
+using namespace rf_batch_impl;
+
+struct rf_batch {
+    rf_params p{};
+    int n = 0, L = 0;
+    std::vector<std::vector<LevelDims>> dims;  // [pair][level]
+    std::vector<size_t> plane, base_off;
+    float* pool = nullptr;
+    BatchPair* d_pairs = nullptr;
+    int* d_prefix = nullptr;
+    std::vector<int> prefix;  // host copy: [level][n + 1]
+    LevelConsts* d_consts = nullptr;
+    LevelConsts* h_consts = nullptr;
+    std::vector<double> K0, K1;  // [pair][9]
+    std::vector<char> cams;
+    std::vector<char> imgs;
+    cudaStream_t own = nullptr, stream = nullptr;
+    cudaGraphExec_t graph = nullptr;
+    int graph_kind = -1;
+    uint64_t launches = 0, graph_nodes = 0, enq = 0;
+    int res_u = -1, res_v = -1;
+    bool solved = false;
+    int n_planes = 0;
+    // plane indices
+    int pI0(int l) const { return l; }
+    int pI1(int l) const { return L + l; }
+    int base_idx() const { return 2 * L; }
+};
+
+namespace rf_batch_impl {
+
+enum {
+    P_I1W = 0, P_IX, P_IY, P_IZ, P_DUHAT, P_DVHAT, P_PU1, P_PU2, P_PV1, P_PV2, P_X, P_Y, P_Z, P_X1,
+    P_Y1, P_Z1, P_SCRATCH, P_SPARE0
+};
+constexpr int kSpares = 18;
+
+BatchCtx ctx_of(rf_batch* b) {
+    BatchCtx c;
+    c.pairs = b->d_pairs;
+    c.prefix = b->d_prefix;
+    c.consts = b->d_consts;
+    c.n = b->n;
+    c.L = b->L;
+    return c;
+}
+
+template <class Op>
+int launch_op(rf_batch* b, int level, const Op& op) {
+    int tiles = b->prefix[level * (b->n + 1) + b->n];
+    if (tiles <= 0) return 0;
+    k_batch<Op><<<tiles, dim3(BX, BY), 0, b->stream>>>(ctx_of(b), level, op);
+    b->enq++;
+    return cudaGetLastError() == cudaSuccess ? 0 : 1;
+}
+
+#define BL(expr)                                                                       \
+    do {                                                                               \
+        if ((expr) != 0)                                                               \
+            return bfail(RF_ERR_CUDA, std::string("batch launch: ") +                 \
+                                          cudaGetErrorString(cudaGetLastError()));     \
+    } while (0)
+#define BC(call)                                                                       \
+    do {                                                                               \
+        cudaError_t e__ = (call);                                                      \
+        if (e__ != cudaSuccess)                                                        \
+            return bfail(RF_ERR_CUDA, std::string(#call ": ") + cudaGetErrorString(e__)); \
+    } while (0)
+
+// zero `count` planes starting at index k for every pair
+rf_status memset_planes(rf_batch* b, std::initializer_list<int> ks) {
+    for (int i = 0; i < b->n; i++)
+        for (int k : ks)
+            BC(cudaMemsetAsync(b->pool + b->base_off[i] + (size_t)k * b->plane[i], 0,
+                               b->plane[i] * sizeof(float), b->stream));
+    return RF_OK;
+}
+
+rf_status enqueue_batch(rf_batch* b, int kind) {
+    const rf_params& p = b->p;
+    const Weights wt = solver_weights(&p);
+    const int B0 = b->base_idx();
+    auto P = [&](int k) { return B0 + k; };
+    // pyramid
+    for (int l = 1; l < b->L; l++)
+        BL(launch_op(b, l, OpDownscale2{b->pI0(l - 1), b->pI1(l - 1), b->pI0(l), b->pI1(l)}));
+    int sp[kSpares];
+    for (int i = 0; i < kSpares; i++) sp[i] = P(P_SPARE0 + i);
+    int u = sp[0], v = sp[1], uc = sp[2], vc = sp[3], uproj = sp[4], vproj = sp[5], sku = sp[6],
+        skv = sp[7], tu = sp[8], tv = sp[9];
+    std::vector<int> freep(sp + 10, sp + kSpares);
+    const bool recon = kind == 0;
+    if (recon) {
+        rf_status rs = memset_planes(b, {u, v, uproj, vproj, uc, vc, sku, skv, P(P_X), P(P_Y), P(P_Z)});
+        if (rs != RF_OK) return rs;
+    } else {
+        rf_status rs = memset_planes(b, {u, v});
+        if (rs != RF_OK) return rs;
+    }
+    bool ucb = true;
+    for (int level = b->L - 1; level >= 0; level--) {
+        for (int warp = 0; warp < p.n_warp_iters; warp++) {
+            BL(launch_op(b, level, OpWarp{b->pI1(level), u, v, P(P_I1W)}));
+            BL(launch_op(b, level, OpDeriv{b->pI0(level), P(P_I1W), P(P_IX), P(P_IY), P(P_IZ)}));
+            ReconIdx r{u, v, P(P_DUHAT), P(P_DVHAT), P(P_PU1), P(P_PU2), P(P_PV1), P(P_PV2),
+                       uproj, vproj, sku, skv, P(P_IX), P(P_IY), P(P_IZ), P(P_X), P(P_Y), P(P_Z),
+                       P(P_X1), P(P_Y1), P(P_Z1), uc, vc};
+            for (int iter = 0; iter < p.n_solver_iters; iter++) {
+                const int first = iter == 0;
+                if (recon) {
+                    BL(launch_op(b, level, OpReconA{r, wt, first, ucb ? 1 : 0}));
+                    BL(launch_op(b, level, OpReconB{r, wt, first}));
+                    ucb = false;
+                } else {
+                    BL(launch_op(b, level, OpPlainData{P(P_DUHAT), P(P_DVHAT), P(P_PU1), P(P_PU2),
+                                                       P(P_PV1), P(P_PV2), P(P_IX), P(P_IY),
+                                                       P(P_IZ), wt, first}));
+                    BL(launch_op(b, level, OpPlainTV{P(P_DUHAT), P(P_DVHAT), P(P_PU1), P(P_PU2),
+                                                     P(P_PV1), P(P_PV2), wt, first}));
+                }
+            }
+            if (p.n_solver_iters == 0) {
+                rf_status rs = memset_planes(b, {P(P_DUHAT), P(P_DVHAT)});
+                if (rs != RF_OK) return rs;
+            }
+            if (recon) {
+                BL(launch_op(b, level, OpMedianAdd{P(P_DUHAT), P(P_DVHAT), u, v, tu, tv}));
+                BL(launch_op(b, level, OpMedian5{tu, tv, u, v}));
+            } else {
+                BL(launch_op(b, level, OpMedianAdd{P(P_DUHAT), P(P_DVHAT), u, v, u, v}));
+            }
+        }
+        if (level > 0) {
+            OpUpscale up{};
+            if (recon) {
+                if (!ucb) BL(launch_op(b, level, OpSolveUc{P(P_X), P(P_Y), P(P_Z), uc, vc}));
+                int src[8] = {u, v, uc, vc, uproj, vproj, sku, skv};
+                up.n = 8;
+                for (int i = 0; i < 8; i++) {
+                    up.src[i] = src[i];
+                    up.dst[i] = freep[i];
+                }
+                up.scale = p.scale;
+                BL(launch_op(b, level - 1, up));
+                for (int i = 0; i < 8; i++) freep[i] = src[i];
+                u = up.dst[0]; v = up.dst[1]; uc = up.dst[2]; vc = up.dst[3];
+                uproj = up.dst[4]; vproj = up.dst[5]; sku = up.dst[6]; skv = up.dst[7];
+                ucb = true;
+            } else {
+                up.n = 2;
+                up.src[0] = u; up.src[1] = v;
+                up.dst[0] = freep[0]; up.dst[1] = freep[1];
+                up.scale = p.scale;
+                BL(launch_op(b, level - 1, up));
+                freep[0] = u; freep[1] = v;
+                u = up.dst[0]; v = up.dst[1];
+            }
+        }
+    }
+    b->res_u = u;
+    b->res_v = v;
+    return RF_OK;
+}
+
+rf_status run_batch(rf_batch* b, int kind) {
+    if (b->graph && b->graph_kind != kind) {
+        cudaGraphExecDestroy(b->graph);
+        b->graph = nullptr;
+    }
+    if (!b->graph) {
+        cudaGraph_t g = nullptr;
+        BC(cudaStreamBeginCapture(b->stream, cudaStreamCaptureModeThreadLocal));
+        b->enq = 0;
+        rf_status rs = enqueue_batch(b, kind);
+        cudaError_t ce = cudaStreamEndCapture(b->stream, &g);
+        if (rs != RF_OK) {
+            if (g) cudaGraphDestroy(g);
+            return rs;
+        }
+        if (ce != cudaSuccess) return bfail(RF_ERR_CUDA, std::string("capture: ") + cudaGetErrorString(ce));
+        cudaError_t ie = cudaGraphInstantiate(&b->graph, g, 0);
+        cudaGraphDestroy(g);
+        if (ie != cudaSuccess) {
+            b->graph = nullptr;
+            return bfail(RF_ERR_CUDA, std::string("instantiate: ") + cudaGetErrorString(ie));
+        }
+        b->graph_kind = kind;
+        b->graph_nodes = b->enq;
+    }
+    BC(cudaGraphLaunch(b->graph, b->stream));
+    b->launches += b->graph_nodes;
+    return RF_OK;
+}
+
+float* pair_plane(rf_batch* b, int i, int k) { return b->pool + b->base_off[i] + (size_t)k * b->plane[i]; }
+
+}  // namespace rf_batch_impl
+
+extern "C" {
+
+rf_status rf_batch_create(const rf_params* p, int n_pairs, const int* widths, const int* heights,
+                          rf_batch** out) {
+    if (!p || !widths || !heights || !out || n_pairs < 1)
+        return bfail(RF_ERR_INVALID_ARG, "rf_batch_create: bad argument");
+    *out = nullptr;
+    if (p->method != RF_METHODR_TVL1_MS && p->method != RF_METHOD_TVL1)
+        return bfail(RF_ERR_UNSUPPORTED, "rf_batch_create: batches run methods 0 and 14");
+    if (p->input_type != RF_INPUT_F32)
+        return bfail(RF_ERR_UNSUPPORTED, "rf_batch_create: batches take float32 gray input");
+    if (p->n_levels < 1 || p->n_levels > kMaxLevels || !(p->scale > 1.0f) ||
+        p->stride_alignment < 1 || p->n_warp_iters < 0 || p->n_solver_iters < 0 ||
+        (p->method == RF_METHOD_TVL1 ? !(p->theta != 0.0f) : !(p->alpha_tv != 0.0f)))
+        return bfail(RF_ERR_INVALID_ARG, "rf_batch_create: parameters out of range");
+    rf_batch* b = new rf_batch();
+    b->p = *p;
+    b->n = n_pairs;
+    b->L = p->n_levels;
+    b->dims.resize(n_pairs);
+    size_t total = 0;
+    b->n_planes = 2 * b->L + P_SPARE0 + kSpares;
+    for (int i = 0; i < n_pairs; i++) {
+        int w = widths[i], h = heights[i];
+        if (w < 1 || h < 1 || (long long)w * h > (1LL << 28)) {
+            delete b;
+            return bfail(RF_ERR_INVALID_ARG, "rf_batch_create: pair size out of range");
+        }
+        int nh = h, nw = w, ns = align_up_i(w, p->stride_alignment);
+        for (int l = 0; l < b->L; l++) {
+            if (nw < 1 || nh < 1) {
+                delete b;
+                return bfail(RF_ERR_INVALID_ARG, "rf_batch_create: too many levels for a pair");
+            }
+            b->dims[i].push_back(LevelDims{nw, nh, ns});
+            nh = (int)((float)nh / p->scale);
+            nw = (int)((float)nw / p->scale);
+            ns = align_up_i(nw, p->stride_alignment);
+        }
+        size_t pl = ((size_t)b->dims[i][0].s * (h + 1) + 63) / 64 * 64;
+        b->plane.push_back(pl);
+        b->base_off.push_back(total);
+        total += pl * b->n_planes;
+    }
+    int ndev = 0;
+    if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev < 1) {
+        delete b;
+        return bfail(RF_ERR_NO_DEVICE, "rf_batch_create: no CUDA device");
+    }
+    cudaError_t e = cudaMalloc(&b->pool, total * sizeof(float));
+    if (e == cudaSuccess) e = cudaMemset(b->pool, 0, total * sizeof(float));
+    std::vector<BatchPair> hp(n_pairs);
+    for (int i = 0; i < n_pairs && e == cudaSuccess; i++) {
+        hp[i].base = b->pool + b->base_off[i];
+        hp[i].plane = b->plane[i];
+        for (int l = 0; l < b->L; l++) hp[i].dims[l] = b->dims[i][l];
+    }
+    b->prefix.assign((size_t)b->L * (n_pairs + 1), 0);
+    for (int l = 0; l < b->L; l++)
+        for (int i = 0; i < n_pairs; i++) {
+            const LevelDims& d = b->dims[i][l];
+            int tiles = ((d.w + BX - 1) / BX) * ((d.h + BY - 1) / BY);
+            b->prefix[l * (n_pairs + 1) + i + 1] = b->prefix[l * (n_pairs + 1) + i] + tiles;
+        }
+    if (e == cudaSuccess) e = cudaMalloc(&b->d_pairs, sizeof(BatchPair) * n_pairs);
+    if (e == cudaSuccess)
+        e = cudaMemcpy(b->d_pairs, hp.data(), sizeof(BatchPair) * n_pairs, cudaMemcpyHostToDevice);
+    if (e == cudaSuccess) e = cudaMalloc(&b->d_prefix, sizeof(int) * b->prefix.size());
+    if (e == cudaSuccess)
+        e = cudaMemcpy(b->d_prefix, b->prefix.data(), sizeof(int) * b->prefix.size(),
+                       cudaMemcpyHostToDevice);
+    if (e == cudaSuccess) e = cudaMalloc(&b->d_consts, sizeof(LevelConsts) * n_pairs * b->L);
+    if (e == cudaSuccess) e = cudaMallocHost(&b->h_consts, sizeof(LevelConsts) * n_pairs * b->L);
+    if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&b->own, cudaStreamNonBlocking);
+    if (e != cudaSuccess) {
+        rf_batch_destroy(b);
+        return bfail(RF_ERR_OOM, std::string("rf_batch_create: ") + cudaGetErrorString(e));
+    }
+    b->stream = b->own;
+    b->K0.assign((size_t)9 * n_pairs, 0.0);
+    b->K1.assign((size_t)9 * n_pairs, 0.0);
+    b->cams.assign(n_pairs, 0);
+    b->imgs.assign(n_pairs, 0);
+    *out = b;
+    return RF_OK;
+}
+
+rf_status rf_batch_destroy(rf_batch* b) {
+    if (!b) return RF_OK;
+    if (b->stream) cudaStreamSynchronize(b->stream);
+    if (b->graph) cudaGraphExecDestroy(b->graph);
+    if (b->pool) cudaFree(b->pool);
+    if (b->d_pairs) cudaFree(b->d_pairs);
+    if (b->d_prefix) cudaFree(b->d_prefix);
+    if (b->d_consts) cudaFree(b->d_consts);
+    if (b->h_consts) cudaFreeHost(b->h_consts);
+    if (b->own) cudaStreamDestroy(b->own);
+    delete b;
+    return RF_OK;
+}
+
+int rf_batch_stride(const rf_batch* b, int pair) {
+    if (!b || pair < 0 || pair >= b->n) return -1;
+    return b->dims[pair][0].s;
+}
+
+rf_status rf_batch_set_cameras(rf_batch* b, int pair, const double K0[9], const double K1[9]) {
+    if (!b || !K0 || !K1 || pair < 0 || pair >= b->n)
+        return bfail(RF_ERR_INVALID_ARG, "rf_batch_set_cameras: bad argument");
+    std::memcpy(&b->K0[(size_t)9 * pair], K0, 9 * sizeof(double));
+    std::memcpy(&b->K1[(size_t)9 * pair], K1, 9 * sizeof(double));
+    b->cams[pair] = 1;
+    return RF_OK;
+}
+
+static rf_status batch_upload(rf_batch* b, int pair, const void* i0, const void* i1, int pitch,
+                              cudaMemcpyKind kind) {
+    if (!b || !i0 || !i1 || pair < 0 || pair >= b->n)
+        return bfail(RF_ERR_INVALID_ARG, "rf_batch_upload_images: bad argument");
+    const LevelDims& d = b->dims[pair][0];
+    if (pitch < d.w) return bfail(RF_ERR_INVALID_ARG, "rf_batch_upload_images: pitch < width");
+    BC(cudaMemcpy2DAsync(pair_plane(b, pair, b->pI0(0)), d.s * sizeof(float), i0,
+                         (size_t)pitch * sizeof(float), d.w * sizeof(float), d.h, kind, b->stream));
+    BC(cudaMemcpy2DAsync(pair_plane(b, pair, b->pI1(0)), d.s * sizeof(float), i1,
+                         (size_t)pitch * sizeof(float), d.w * sizeof(float), d.h, kind, b->stream));
+    b->imgs[pair] = 1;
+    return RF_OK;
+}
+
+rf_status rf_batch_upload_images(rf_batch* b, int pair, const float* i0, const float* i1,
+                                 int pitch) {
+    return batch_upload(b, pair, i0, i1, pitch, cudaMemcpyHostToDevice);
+}
+
+rf_status rf_batch_upload_images_device(rf_batch* b, int pair, const float* i0, const float* i1,
+                                        int pitch) {
+    return batch_upload(b, pair, i0, i1, pitch, cudaMemcpyDeviceToDevice);
+}
+
+rf_status rf_batch_solve(rf_batch* b, const double* R0, const double* t0, const double* R1,
+                         const double* t1) {
+    if (!b || !R1 || !t1) return bfail(RF_ERR_INVALID_ARG, "rf_batch_solve: null argument");
+    if (b->p.method == RF_METHOD_TVL1)
+        return bfail(RF_ERR_STATE, "rf_batch_solve: batch was created for plain TV-L1");
+    for (int i = 0; i < b->n; i++)
+        if (!b->cams[i] || !b->imgs[i])
+            return bfail(RF_ERR_STATE, "rf_batch_solve: pair " + std::to_string(i) +
+                                           " has no cameras or images");
+    BC(cudaStreamSynchronize(b->stream));
+    const double I[9] = {1, 0, 0, 0, 1, 0, 0, 0, 1}, z[3] = {0, 0, 0};
+    for (int i = 0; i < b->n; i++)
+        camera_level_consts(&b->K0[(size_t)9 * i], &b->K1[(size_t)9 * i], b->L, b->p.scale,
+                            b->p.fix_quirks, R0 ? R0 + 9 * i : I, t0 ? t0 + 3 * i : z, R1 + 9 * i,
+                            t1 + 3 * i, b->h_consts + (size_t)i * b->L);
+    BC(cudaMemcpyAsync(b->d_consts, b->h_consts, sizeof(LevelConsts) * b->n * b->L,
+                       cudaMemcpyHostToDevice, b->stream));
+    rf_status rs = run_batch(b, 0);
+    b->solved = rs == RF_OK;
+    return rs;
+}
+
+rf_status rf_batch_solve_flow(rf_batch* b) {
+    if (!b) return bfail(RF_ERR_INVALID_ARG, "rf_batch_solve_flow: null batch");
+    if (b->p.method != RF_METHOD_TVL1)
+        return bfail(RF_ERR_STATE, "rf_batch_solve_flow: batch was created for ReconFlow");
+    for (int i = 0; i < b->n; i++)
+        if (!b->imgs[i]) return bfail(RF_ERR_STATE, "rf_batch_solve_flow: missing images");
+    rf_status rs = run_batch(b, 1);
+    b->solved = rs == RF_OK;
+    return rs;
+}
+
+static rf_status batch_down(rf_batch* b, int pair, int k, float* dst, int pitch) {
+    const LevelDims& d = b->dims[pair][0];
+    BC(cudaMemcpy2DAsync(dst, (size_t)pitch * sizeof(float), pair_plane(b, pair, k),
+                         d.s * sizeof(float), d.w * sizeof(float), d.h, cudaMemcpyDeviceToHost,
+                         b->stream));
+    return RF_OK;
+}
+
+rf_status rf_batch_download_flow(rf_batch* b, int pair, float* u, float* v, int pitch) {
+    if (!b || !u || !v || pair < 0 || pair >= b->n)
+        return bfail(RF_ERR_INVALID_ARG, "rf_batch_download_flow: bad argument");
+    if (!b->solved) return bfail(RF_ERR_STATE, "rf_batch_download_flow: no solve has run");
+    if (pitch < b->dims[pair][0].w) return bfail(RF_ERR_INVALID_ARG, "pitch < width");
+    rf_status rs = batch_down(b, pair, b->res_u, u, pitch);
+    if (rs == RF_OK) rs = batch_down(b, pair, b->res_v, v, pitch);
+    if (rs == RF_OK) BC(cudaStreamSynchronize(b->stream));
+    return rs;
+}
+
+rf_status rf_batch_download_points(rf_batch* b, int pair, float* X, float* Y, float* Z,
+                                   int pitch) {
+    if (!b || !X || !Y || !Z || pair < 0 || pair >= b->n)
+        return bfail(RF_ERR_INVALID_ARG, "rf_batch_download_points: bad argument");
+    if (b->p.method == RF_METHOD_TVL1 || !b->solved)
+        return bfail(RF_ERR_STATE, "rf_batch_download_points: needs a ReconFlow solve");
+    if (pitch < b->dims[pair][0].w) return bfail(RF_ERR_INVALID_ARG, "pitch < width");
+    const int B0 = b->base_idx();
+    rf_status rs = batch_down(b, pair, B0 + P_X, X, pitch);
+    if (rs == RF_OK) rs = batch_down(b, pair, B0 + P_Y, Y, pitch);
+    if (rs == RF_OK) rs = batch_down(b, pair, B0 + P_Z, Z, pitch);
+    if (rs == RF_OK) BC(cudaStreamSynchronize(b->stream));
+    return rs;
+}
+
+rf_status rf_batch_download_inv_depth(rf_batch* b, int pair, float* inv, int pitch) {
+    if (!b || !inv || pair < 0 || pair >= b->n)
+        return bfail(RF_ERR_INVALID_ARG, "rf_batch_download_inv_depth: bad argument");
+    if (b->p.method == RF_METHOD_TVL1 || !b->solved)
+        return bfail(RF_ERR_STATE, "rf_batch_download_inv_depth: needs a ReconFlow solve");
+    if (pitch < b->dims[pair][0].w) return bfail(RF_ERR_INVALID_ARG, "pitch < width");
+    const int B0 = b->base_idx();
+    BL(launch_op(b, 0, OpInvDepth{B0 + P_Z, B0 + P_SCRATCH}));
+    b->launches++;
+    rf_status rs = batch_down(b, pair, B0 + P_SCRATCH, inv, pitch);
+    if (rs == RF_OK) BC(cudaStreamSynchronize(b->stream));
+    return rs;
+}
+
+rf_status rf_batch_device_results(rf_batch* b, int pair, const float** u, const float** v,
+                                  const float** X, const float** Y, const float** Z) {
+    if (!b || pair < 0 || pair >= b->n)
+        return bfail(RF_ERR_INVALID_ARG, "rf_batch_device_results: bad argument");
+    if (!b->solved) return bfail(RF_ERR_STATE, "rf_batch_device_results: no solve has run");
+    const int B0 = b->base_idx();
+    if (u) *u = pair_plane(b, pair, b->res_u);
+    if (v) *v = pair_plane(b, pair, b->res_v);
+    if (X) *X = pair_plane(b, pair, B0 + P_X);
+    if (Y) *Y = pair_plane(b, pair, B0 + P_Y);
+    if (Z) *Z = pair_plane(b, pair, B0 + P_Z);
+    return RF_OK;
+}
+
+rf_status rf_batch_set_stream(rf_batch* b, void* stream) {
+    if (!b) return bfail(RF_ERR_INVALID_ARG, "rf_batch_set_stream: null batch");
+    BC(cudaStreamSynchronize(b->stream));
+    b->stream = stream ? static_cast<cudaStream_t>(stream) : b->own;
+    return RF_OK;
+}
+
+rf_status rf_batch_synchronize(rf_batch* b) {
+    if (!b) return bfail(RF_ERR_INVALID_ARG, "rf_batch_synchronize: null batch");
+    BC(cudaStreamSynchronize(b->stream));
+    return RF_OK;
+}
+
+uint64_t rf_batch_kernel_launches(const rf_batch* b) { return b ? b->launches : 0; }
+
+}  // extern "C"

@@ -8,6 +8,8 @@
 
 #include "rf_math.cuh"
 
+struct rf_params;
+
 namespace rf {
 
 struct LevelDims {
@@ -101,6 +103,15 @@ struct FusedFields {
     float* Y1_o;
     float* Z1_o;
 };
+
+// Per-level camera constants of one pair (K pyramid, P = K0 [R0|t0],
+// Q = K1 [R1|t1], float copies), fix_quirks as rf_params.
+void camera_level_consts(const double* K0, const double* K1, int L, float scale, int fix_quirks,
+                         const double* R0, const double* t0, const double* R1, const double* t1,
+                         LevelConsts* out);
+
+// Kernel weights of a parameter block (the exact float forms the kernels use).
+Weights solver_weights(const rf_params* p);
 
 // Records `msg` as the calling thread's rf_last_error_string(); returns st.
 int set_last_error(int st, const char* msg);

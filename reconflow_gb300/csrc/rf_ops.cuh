@@ -1,0 +1,353 @@
+// Per-pixel operations of the Reconflow kernels, shared by the single-pair
+// kernels (rf_kernels.cu) and the batched kernels (rf_batch.cu).  Every
+// function computes one pixel exactly as the reference kernel it cites.
+#pragma once
+
+#include "rf_kernels.cuh"
+
+namespace rf {
+namespace {
+
+// downscale.cu:6-26: sum of the four fetches at +-1/4 coarse texel.
+__device__ __forceinline__ float downscale_px(const float* __restrict__ src, LevelDims f, int nw,
+                                              int nh, int ix, int iy) {
+    float dx = 1.0f / (float)nw;
+    float dy = 1.0f / (float)nh;
+    float x = ((float)ix + 0.5f) * dx;
+    float y = ((float)iy + 0.5f) * dy;
+    return tex2d(src, f.w, f.h, f.s, x - dx * 0.25f, y) + tex2d(src, f.w, f.h, f.s, x + dx * 0.25f, y) +
+           tex2d(src, f.w, f.h, f.s, x, y - dy * 0.25f) + tex2d(src, f.w, f.h, f.s, x, y + dy * 0.25f);
+}
+
+
+// computeDerivatives.cu:26-36: [1, -8, 0, 8, -1] / 12 in the reference's order.
+__device__ __forceinline__ float deriv5(float m2, float m1, float p1, float p2) {
+    float t = m2;
+    t -= m1 * 8.0f;
+    t += p1 * 8.0f;
+    t -= p2;
+    t /= 12.0f;
+    return t;
+}
+
+template <int PRIOR>
+__device__ __forceinline__ void recon_a_px(const ReconFields& f, const LevelConsts& c,
+                                           const Weights& wt, LevelDims d, int ix, int iy,
+                                           int first, int uc_from_buffer) {
+    const int s = d.s;
+    const int pos = ix + iy * s;
+
+    // --- data step (solveReconDataL1.cu:24-100) ---
+    float u = f.u[pos], v = f.v[pos];
+    float dix = f.Ix[pos], diy = f.Iy[pos], dit = f.Iz[pos];
+    float uproj = f.uproj[pos], vproj = f.vproj[pos];
+    float sku = f.sku[pos], skv = f.skv[pos];
+    float duhat = 0.0f, dvhat = 0.0f;
+    float pu1 = 0.0f, pu2 = 0.0f, pv1 = 0.0f, pv2 = 0.0f;
+    float pu1l = 0.0f, pv1l = 0.0f, pu2d = 0.0f, pv2d = 0.0f;
+    if (!first) {
+        duhat = f.duhat[pos];
+        dvhat = f.dvhat[pos];
+        pu1 = f.pu1[pos];
+        pu2 = f.pu2[pos];
+        pv1 = f.pv1[pos];
+        pv2 = f.pv2[pos];
+        if (ix > 0) {
+            pu1l = f.pu1[pos - 1];
+            pv1l = f.pv1[pos - 1];
+        }
+        if (iy > 0) {
+            pu2d = f.pu2[pos - s];
+            pv2d = f.pv2[pos - s];
+        }
+    }
+    float A, dusub, dvsub;
+    if (PRIOR == 0) {
+        A = wt.A;
+        dusub = (wt.alpha_tv * duhat + wt.alpha_proj * (uproj - u - sku)) / A;
+        dvsub = (wt.alpha_tv * dvhat + wt.alpha_proj * (vproj - v - skv)) / A;
+    } else {
+        float alphaFn = PRIOR == 2 ? wt.alpha_fn * f.mask[pos] : wt.alpha_fn;
+        float ufn = f.ufn[pos], vfn = f.vfn[pos];
+        A = wt.alpha_tv + wt.alpha_proj + alphaFn;
+        dusub = (alphaFn * (ufn - u) + wt.alpha_tv * duhat + wt.alpha_proj * (uproj - u - sku)) / A;
+        dvsub = (alphaFn * (vfn - v) + wt.alpha_tv * dvhat + wt.alpha_proj * (vproj - v - skv)) / A;
+    }
+    float du, dv;
+    l1_threshold(dusub, dvsub, dix, diy, dit, wt.lambda, A, du, dv);
+    float divpu = divergence(pu1, pu1l, pu2, pu2d, ix, iy);
+    float divpv = divergence(pv1, pv1l, pv2, pv2d, ix, iy);
+    float duhat1 = du + divpu / A;
+    float dvhat1 = dv + divpv / A;
+    f.duhat[pos] = duhat1;
+    f.dvhat[pos] = dvhat1;
+
+    // --- projection blend (solveUVProj.cu:13-21), uc from the current 3D ---
+    float Xn[5], Yn[5], Zn[5];
+    Xn[0] = f.X[pos];
+    Yn[0] = f.Y[pos];
+    Zn[0] = f.Z[pos];
+    float uc, vc;
+    if (uc_from_buffer) {
+        uc = f.uc[pos];
+        vc = f.vc[pos];
+    } else {
+        project_uc(c, Xn[0], Yn[0], Zn[0], ix, iy, uc, vc);
+    }
+    float uproj1 = (wt.lambdaf * uc + wt.alpha_proj * (u + duhat1 + sku)) / wt.proj_den;
+    float vproj1 = (wt.lambdaf * vc + wt.alpha_proj * (v + dvhat1 + skv)) / wt.proj_den;
+    f.uproj[pos] = uproj1;
+    f.vproj[pos] = vproj1;
+
+    // --- triangulation with minimal-area smoothing (solve3dMinimalArea.cu:23-184) ---
+    // x+1 / y+1 are read at flat pos+1 / pos+s even on the last column / row.
+    Xn[1] = f.X[pos + 1];
+    Yn[1] = f.Y[pos + 1];
+    Zn[1] = f.Z[pos + 1];
+    Xn[2] = f.X[pos + s];
+    Yn[2] = f.Y[pos + s];
+    Zn[2] = f.Z[pos + s];
+    Xn[3] = Yn[3] = Zn[3] = 0.0f;
+    Xn[4] = Yn[4] = Zn[4] = 0.0f;
+    if (ix > 0) {
+        Xn[3] = f.X[pos - 1];
+        Yn[3] = f.Y[pos - 1];
+        Zn[3] = f.Z[pos - 1];
+    }
+    if (iy > 0) {
+        Xn[4] = f.X[pos - s];
+        Yn[4] = f.Y[pos - s];
+        Zn[4] = f.Z[pos - s];
+    }
+    float Xo, Yo, Zo;
+    solve3d_pixel(c, uproj1, vproj1, ix, iy, Xn, Yn, Zn, wt.lambdaf, wt.lambdams, Xo, Yo, Zo);
+    f.X1[pos] = Xo;
+    f.Y1[pos] = Yo;
+    f.Z1[pos] = Zo;
+}
+
+// 3x3 tap of the reference's 3D median with its border rules
+// (medianFilter.cu:181-214): left / top clamp, right / bottom and corners 0.
+__device__ __forceinline__ int median3_tap(int col, int row, int w, int h, int s) {
+    if (col >= 0 && col < w && row >= 0 && row < h) return col + s * row;
+    if (col < 0 && row >= 0 && row < h) return s * row;
+    if (col >= 0 && col < w && row < 0) return col;
+    return -1;
+}
+
+// ---------------------------------------------------------------------------
+// ReconFlow inner iteration, part B: dual step, 3D median, clean-up, sk
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ void recon_b_px(const ReconFields& f, const Weights& wt, LevelDims d,
+                                           int ix, int iy, int first) {
+    const int s = d.s, w = d.w, h = d.h;
+    const int pos = ix + iy * s;
+
+    // --- dual TV step (solveSmoothDualTVGlobal.cu:26-64) ---
+    float duhat = f.duhat[pos], dvhat = f.dvhat[pos];
+    float dux, duy, dvx, dvy;
+    if ((ix + 1) >= w) {
+        dux = 0.0f;
+        dvx = 0.0f;
+    } else {
+        dux = f.duhat[pos + 1] - duhat;
+        dvx = f.dvhat[pos + 1] - dvhat;
+    }
+    if ((iy + 1) >= h) {
+        duy = 0.0f;
+        dvy = 0.0f;
+    } else {
+        duy = f.duhat[pos + s] - duhat;
+        dvy = f.dvhat[pos + s] - dvhat;
+    }
+    float pu1 = 0.0f, pu2 = 0.0f, pv1 = 0.0f, pv2 = 0.0f;
+    if (!first) {
+        pu1 = f.pu1[pos];
+        pu2 = f.pu2[pos];
+        pv1 = f.pv1[pos];
+        pv2 = f.pv2[pos];
+    }
+    dual_step(dux, duy, wt.fac, pu1, pu2);
+    dual_step(dvx, dvy, wt.fac, pv1, pv2);
+    f.pu1[pos] = pu1;
+    f.pu2[pos] = pu2;
+    f.pv1[pos] = pv1;
+    f.pv2[pos] = pv2;
+
+    // --- 3x3 median of the triangulated points, then clean-up ---
+    // (Solve3d outputs are finite: non-finite results fall back to the
+    // previous, finite, state; so the min/max median network applies.)
+    float mX[9], mY[9], mZ[9];
+    if (ix > 0 && iy > 0 && ix + 1 < w && iy + 1 < h) {
+#pragma unroll
+        for (int j = 0; j < 3; j++) {
+#pragma unroll
+            for (int i = 0; i < 3; i++) {
+                int at = pos + (j - 1) * s + (i - 1);
+                mX[j * 3 + i] = f.X1[at];
+                mY[j * 3 + i] = f.Y1[at];
+                mZ[j * 3 + i] = f.Z1[at];
+            }
+        }
+    } else {
+#pragma unroll
+        for (int j = 0; j < 3; j++) {
+#pragma unroll
+            for (int i = 0; i < 3; i++) {
+                int at = median3_tap(ix + i - 1, iy + j - 1, w, h, s);
+                int k = j * 3 + i;
+                mX[k] = at >= 0 ? f.X1[at] : 0.0f;
+                mY[k] = at >= 0 ? f.Y1[at] : 0.0f;
+                mZ[k] = at >= 0 ? f.Z1[at] : 0.0f;
+            }
+        }
+    }
+    float X1 = mX[4], Y1 = mY[4], Z1 = mZ[4];
+    float Xm = median9_finite(mX);
+    float Ym = median9_finite(mY);
+    float Zm = median9_finite(mZ);
+    float Xo, Yo, Zo;
+    cleanup_pixel(X1, Y1, Z1, Xm, Ym, Zm, Xo, Yo, Zo);
+    f.X[pos] = Xo;
+    f.Y[pos] = Yo;
+    f.Z[pos] = Zo;
+
+    // --- multiplier update (solveUcSk.cu:94-95) ---
+    f.sku[pos] = f.sku[pos] + f.u[pos] + duhat - f.uproj[pos];
+    f.skv[pos] = f.skv[pos] + f.v[pos] + dvhat - f.vproj[pos];
+}
+
+__device__ __forceinline__ int median5_tap(int col, int row, int w, int h, int s) {
+    bool cin = col >= 0 && col < w, rin = row >= 0 && row < h;
+    if (cin && rin) return col + s * row;
+    if (col < 0 && rin) return s * row;
+    if (col >= w && rin) return w - 1 + s * row;
+    if (cin && row < 0) return col;
+    if (cin && row >= h) return col + s * (h - 1);
+    return -1;
+}
+
+__device__ __forceinline__ void median5_pair(const float* __restrict__ a,
+                                             const float* __restrict__ b, int ix, int iy,
+                                             LevelDims d, float& ma, float& mb) {
+    float mu[25], mv[25];
+#pragma unroll
+    for (int j = 0; j < 5; j++) {
+#pragma unroll
+        for (int i = 0; i < 5; i++) {
+            int at = median5_tap(ix + i - 2, iy + j - 2, d.w, d.h, d.s);
+            mu[j * 5 + i] = at >= 0 ? a[at] : 0.0f;
+            mv[j * 5 + i] = at >= 0 ? b[at] : 0.0f;
+        }
+    }
+    ma = median25_exchange(mu);
+    mb = median25_exchange(mv);
+}
+
+
+
+// warpImage.cu:15-29
+__device__ __forceinline__ void warp_px(const float* __restrict__ I1, const float* __restrict__ u,
+                                        const float* __restrict__ v, LevelDims d,
+                                        float* __restrict__ out, int ix, int iy) {
+    int pos = ix + iy * d.s;
+    float x = ((float)ix + u[pos] + 0.5f) / (float)d.w;
+    float y = ((float)iy + v[pos] + 0.5f) / (float)d.h;
+    out[pos] = tex2d(I1, d.w, d.h, d.s, x, y);
+}
+
+// computeDerivatives.cu:8-57 (taps on texel centres: mirrored gathers)
+__device__ __forceinline__ void derivatives_px(const float* __restrict__ I0,
+                                               const float* __restrict__ I1, LevelDims d,
+                                               float* __restrict__ Ix, float* __restrict__ Iy,
+                                               float* __restrict__ Iz, int ix, int iy) {
+    int row = iy * d.s;
+    int pos = ix + row;
+    int xm2 = mirror_index(ix - 2, d.w) + row, xm1 = mirror_index(ix - 1, d.w) + row;
+    int xp1 = mirror_index(ix + 1, d.w) + row, xp2 = mirror_index(ix + 2, d.w) + row;
+    int ym2 = ix + mirror_index(iy - 2, d.h) * d.s, ym1 = ix + mirror_index(iy - 1, d.h) * d.s;
+    int yp1 = ix + mirror_index(iy + 1, d.h) * d.s, yp2 = ix + mirror_index(iy + 2, d.h) * d.s;
+    float t0 = deriv5(I0[xm2], I0[xm1], I0[xp1], I0[xp2]);
+    float t1 = deriv5(I1[xm2], I1[xm1], I1[xp1], I1[xp2]);
+    Ix[pos] = (t0 + t1) * 0.5f;
+    Iz[pos] = I1[pos] - I0[pos];
+    t0 = deriv5(I0[ym2], I0[ym1], I0[yp1], I0[yp2]);
+    t1 = deriv5(I1[ym2], I1[ym1], I1[yp1], I1[yp2]);
+    Iy[pos] = (t0 + t1) * 0.5f;
+}
+
+// solveDataL1.cu:4-91 (duhat updated in place: read and written only at the pixel)
+__device__ __forceinline__ void plain_data_px(float* duhat0, float* dvhat0,
+                                              const float* __restrict__ pu1,
+                                              const float* __restrict__ pu2,
+                                              const float* __restrict__ pv1,
+                                              const float* __restrict__ pv2,
+                                              const float* __restrict__ Ix,
+                                              const float* __restrict__ Iy,
+                                              const float* __restrict__ Iz, const Weights& wt,
+                                              LevelDims d, int first, int ix, int iy) {
+    const int s = d.s;
+    const int pos = ix + iy * s;
+    float duhat = 0.0f, dvhat = 0.0f;
+    float p1u = 0.0f, p2u = 0.0f, p1v = 0.0f, p2v = 0.0f, p1ul = 0.0f, p1vl = 0.0f, p2ud = 0.0f,
+          p2vd = 0.0f;
+    if (!first) {
+        duhat = duhat0[pos];
+        dvhat = dvhat0[pos];
+        p1u = pu1[pos];
+        p2u = pu2[pos];
+        p1v = pv1[pos];
+        p2v = pv2[pos];
+        if (ix > 0) {
+            p1ul = pu1[pos - 1];
+            p1vl = pv1[pos - 1];
+        }
+        if (iy > 0) {
+            p2ud = pu2[pos - s];
+            p2vd = pv2[pos - s];
+        }
+    }
+    float du, dv;
+    l1_threshold_plain(duhat, dvhat, Ix[pos], Iy[pos], Iz[pos], wt.lambda, wt.theta, du, dv);
+    float divpu = divergence(p1u, p1ul, p2u, p2ud, ix, iy);
+    float divpv = divergence(p1v, p1vl, p2v, p2vd, ix, iy);
+    duhat0[pos] = du + wt.theta * divpu;
+    dvhat0[pos] = dv + wt.theta * divpv;
+}
+
+// solveSmoothDualTVGlobal.cu:4-65 (p updated in place: read and written only at the pixel)
+__device__ __forceinline__ void plain_tv_px(const float* __restrict__ duhat,
+                                            const float* __restrict__ dvhat, float* pu1,
+                                            float* pu2, float* pv1, float* pv2,
+                                            const Weights& wt, LevelDims d, int first, int ix,
+                                            int iy) {
+    const int s = d.s;
+    const int pos = ix + iy * s;
+    float du0 = duhat[pos], dv0 = dvhat[pos];
+    float dux = 0.0f, duy = 0.0f, dvx = 0.0f, dvy = 0.0f;
+    if (ix + 1 < d.w) {
+        dux = duhat[pos + 1] - du0;
+        dvx = dvhat[pos + 1] - dv0;
+    }
+    if (iy + 1 < d.h) {
+        duy = duhat[pos + s] - du0;
+        dvy = dvhat[pos + s] - dv0;
+    }
+    float a = 0.0f, b = 0.0f, c = 0.0f, e = 0.0f;
+    if (!first) {
+        a = pu1[pos];
+        b = pu2[pos];
+        c = pv1[pos];
+        e = pv2[pos];
+    }
+    dual_step(dux, duy, wt.fac, a, b);
+    dual_step(dvx, dvy, wt.fac, c, e);
+    pu1[pos] = a;
+    pu2[pos] = b;
+    pv1[pos] = c;
+    pv2[pos] = e;
+}
+
+
+}  // namespace
+}  // namespace rf

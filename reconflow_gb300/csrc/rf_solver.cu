@@ -141,6 +141,14 @@ size_t input_elem_bytes(int t) {
     }
 }
 
+Weights make_weights(const rf_params& p);
+
+}  // namespace
+
+Weights rf::solver_weights(const rf_params* p) { return make_weights(*p); }
+
+namespace {
+
 Weights make_weights(const rf_params& p) {
     Weights w{};
     w.lambda = p.lambda;
@@ -161,17 +169,25 @@ Weights make_weights(const rf_params& p) {
     return w;
 }
 
-// Reconflow.cu:98-110 (K pyramid) and :225-226 (P = K [R | t]), in double.
 void level_consts(const rf_handle* h, const double* R0, const double* t0, const double* R1,
                   const double* t1, LevelConsts* out) {
+    rf::camera_level_consts(h->K0, h->K1, h->L, h->p.scale, h->p.fix_quirks, R0, t0, R1, t1, out);
+}
+
+}  // namespace
+
+// Reconflow.cu:98-110 (K pyramid) and :225-226 (P = K [R | t]), in double.
+void rf::camera_level_consts(const double* K0in, const double* K1in, int L, float scale,
+                             int fix_quirks, const double* R0, const double* t0, const double* R1,
+                             const double* t1, LevelConsts* out) {
     double K0[9], K1[9];
-    std::memcpy(K0, h->K0, sizeof K0);
-    std::memcpy(K1, h->K1, sizeof K1);
-    const bool fix_k = (h->p.fix_quirks & RF_FIX_K_PYRAMID) != 0;
-    for (int l = 0; l < h->L; l++) {
+    std::memcpy(K0, K0in, sizeof K0);
+    std::memcpy(K1, K1in, sizeof K1);
+    const bool fix_k = (fix_quirks & RF_FIX_K_PYRAMID) != 0;
+    for (int l = 0; l < L; l++) {
         if (l > 0) {
             double a[9] = {0}, b[9] = {0};
-            const double f = h->p.scale;
+            const double f = scale;
             a[0] = K0[0] / f; a[2] = K0[2] / f; a[4] = K0[4] / f; a[5] = K0[5] / f;
             b[0] = K1[0] / f; b[2] = K1[2] / f; b[4] = K1[4] / f; b[5] = K1[5] / f;
             if (fix_k) a[8] = b[8] = 1.0;
@@ -206,6 +222,8 @@ void level_consts(const rf_handle* h, const double* R0, const double* t0, const 
         c.pad = 0.0f;
     }
 }
+
+namespace {
 
 #define RF_LAUNCH(expr)                                                               \
     do {                                                                              \

@@ -20,7 +20,7 @@ import numpy as np
 from . import _native as N
 from ._native import RfError
 
-__all__ = ["CudaFlow", "ReconFlow", "RfError"]
+__all__ = ["CudaFlow", "ReconFlow", "ReconFlowBatch", "RfError"]
 
 # OpenCV type codes accepted by initialize(cvType=...) (Cudaflow.cu:288-311)
 CV_8U, CV_16U, CV_32F, CV_8UC3 = 0, 2, 5, 16
@@ -268,3 +268,98 @@ class ReconFlow(CudaFlow):
         N.check(self._lib.rf_remove_edge_artifacts(self._handle(), int(surfaceWidth),
                                                    ctypes.c_float(maxSurfaceArea)))
         return 0
+
+
+class ReconFlowBatch:
+    """Many frame pairs solved together (rf_batch_* C ABI): one launch per
+    schedule step covers every pair.  Pairs may differ in size, cameras and
+    pose; they share the solver parameters.  Float32 gray input; methods
+    METHODR_TVL1_MS (14) and METHOD_TVL1 (0)."""
+
+    def __init__(self, sizes, nLevels, scale=2.0, method=N.METHODR_TVL1_MS, lambda_=100.0,
+                 lambdaf=100.0, lambdams=100.0, alphaTv=3.0, alphaProj=1.0, tau=0.25,
+                 theta=0.33, nWarpIters=1, nSolverIters=100, fix_quirks=0, StrideAlignment=32):
+        self._lib = N.load()
+        p = N.RfParams()
+        N.check(self._lib.rf_params_default(ctypes.byref(p), int(method)))
+        p.width, p.height = sizes[0]
+        p.input_type = N.INPUT_F32
+        p.n_levels, p.scale, p.method = int(nLevels), float(scale), int(method)
+        p.lambda_, p.lambdaf, p.lambdams = lambda_, lambdaf, lambdams
+        p.alpha_tv, p.alpha_proj, p.tau = alphaTv, alphaProj, tau
+        p.theta = theta if method == N.METHOD_TVL1 else 1.0 / alphaTv
+        p.n_warp_iters, p.n_solver_iters = int(nWarpIters), int(nSolverIters)
+        p.stride_alignment, p.fix_quirks = StrideAlignment, int(fix_quirks)
+        self.sizes = [(int(w), int(h)) for w, h in sizes]
+        n = len(self.sizes)
+        ws = (ctypes.c_int * n)(*[w for w, _ in self.sizes])
+        hs = (ctypes.c_int * n)(*[h for _, h in self.sizes])
+        self._h = None
+        h = ctypes.c_void_p()
+        N.check(self._lib.rf_batch_create(ctypes.byref(p), n, ws, hs, ctypes.byref(h)))
+        self._h = h
+        self.n = n
+        self.params = p
+        self.strides = [self._lib.rf_batch_stride(h, i) for i in range(n)]
+
+    def close(self):
+        if self._h is not None:
+            self._lib.rf_batch_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def setCameraMatrices(self, pair, K0, K1=None):
+        K1 = K0 if K1 is None else K1
+        a, pa = _dbl(K0, 9)
+        b, pb = _dbl(K1, 9)
+        N.check(self._lib.rf_batch_set_cameras(self._h, int(pair), pa, pb))
+
+    def copyImagesToDevice(self, pair, i0, i1):
+        a = np.ascontiguousarray(i0, np.float32)
+        b = np.ascontiguousarray(i1, np.float32)
+        N.check(self._lib.rf_batch_upload_images(self._h, int(pair), _ptr(a), _ptr(b), a.shape[1]))
+
+    def solveR(self, R1s, t1s, R0s=None, t0s=None):
+        R1 = np.ascontiguousarray(np.asarray(R1s, np.float64).reshape(self.n, 9))
+        t1 = np.ascontiguousarray(np.asarray(t1s, np.float64).reshape(self.n, 3))
+        R0 = None if R0s is None else np.ascontiguousarray(np.asarray(R0s, np.float64).reshape(self.n, 9))
+        t0 = None if t0s is None else np.ascontiguousarray(np.asarray(t0s, np.float64).reshape(self.n, 3))
+        N.check(self._lib.rf_batch_solve(self._h, None if R0 is None else _ptr(R0),
+                                         None if t0 is None else _ptr(t0), _ptr(R1), _ptr(t1)))
+
+    def solveOpticalFlow(self):
+        N.check(self._lib.rf_batch_solve_flow(self._h))
+
+    def _out(self, pair):
+        w, h = self.sizes[pair]
+        return np.zeros((h, self.strides[pair]), np.float32)
+
+    def copyOpticalFlowToHost(self, pair):
+        u, v = self._out(pair), self._out(pair)
+        N.check(self._lib.rf_batch_download_flow(self._h, int(pair), _ptr(u), _ptr(v), u.shape[1]))
+        return u, v
+
+    def copy3dToHost(self, pair):
+        X, Y, Z = self._out(pair), self._out(pair), self._out(pair)
+        N.check(self._lib.rf_batch_download_points(self._h, int(pair), _ptr(X), _ptr(Y), _ptr(Z),
+                                                   X.shape[1]))
+        return X, Y, Z
+
+    def copyInverseDepthToHost(self, pair):
+        o = self._out(pair)
+        N.check(self._lib.rf_batch_download_inv_depth(self._h, int(pair), _ptr(o), o.shape[1]))
+        return o
+
+    def setStream(self, stream_ptr):
+        N.check(self._lib.rf_batch_set_stream(self._h, ctypes.c_void_p(stream_ptr or 0)))
+
+    def synchronize(self):
+        N.check(self._lib.rf_batch_synchronize(self._h))
+
+    def kernelLaunches(self):
+        return int(self._lib.rf_batch_kernel_launches(self._h))

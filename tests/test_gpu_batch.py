@@ -1,0 +1,111 @@
+"""Batched solve on the GPU: every pair of a mixed-size batch must be bit for
+bit what the single-pair solver (and the FP32 oracle) gives for that pair
+alone, whatever its neighbours in the batch."""
+import numpy as np
+import pytest
+
+from helpers import align_up, assert_bitexact, pad_rows, textured_pair
+
+pytestmark = pytest.mark.gpu
+
+SIZES = [(37, 23), (64, 48), (96, 64), (45, 90), (130, 70)]
+
+
+@pytest.fixture(scope="module", autouse=True)
+def need_gpu():
+    torch = pytest.importorskip("torch")
+    if not torch.cuda.is_available():
+        pytest.skip("no CUDA device")
+
+
+def _pose(seed):
+    rng = np.random.default_rng(seed)
+    a = rng.normal(size=3)
+    a /= np.linalg.norm(a)
+    ang = np.radians(rng.uniform(0.5, 2.0))
+    Kx = np.array([[0, -a[2], a[1]], [a[2], 0, -a[0]], [-a[1], a[0], 0]])
+    R = np.eye(3) + np.sin(ang) * Kx + (1 - np.cos(ang)) * Kx @ Kx
+    t = rng.normal(size=3)
+    return R, 0.1 * t / np.linalg.norm(t)
+
+
+def _K(w, h):
+    f = 500.0 * w / 640.0
+    return np.array([[f, 0, w / 2.0], [0, f, h / 2.0], [0, 0, 1.0]])
+
+
+def _inputs():
+    out = []
+    for i, (w, h) in enumerate(SIZES):
+        rng = np.random.default_rng(100 + i)
+        I0, I1 = textured_pair(rng, h, w, shift=(1.2 + 0.1 * i, -0.5))
+        R, t = _pose(i)
+        out.append((w, h, I0, I1, _K(w, h), R, t))
+    return out
+
+
+@pytest.mark.parametrize("fix", [0, 1])
+def test_batch_recon_matches_single_pair(oracle, rf, fix):
+    L, warps, iters = 2, 2, 4
+    data = _inputs()
+    kw = dict(lambda_=50.0, lambdaf=0.1, lambdams=100.0, alphaTv=1 / 0.33, alphaProj=60.0,
+              tau=0.25, nWarpIters=warps, nSolverIters=iters, fix_quirks=fix)
+    b = rf.ReconFlowBatch([(w, h) for w, h, *_ in data], L, method=14, **kw)
+    for i, (w, h, I0, I1, K, R, t) in enumerate(data):
+        s = b.strides[i]
+        b.setCameraMatrices(i, K, K)
+        b.copyImagesToDevice(i, pad_rows(I0, s), pad_rows(I1, s))
+    b.solveR([d[5] for d in data], [d[6] for d in data])
+    for i, (w, h, I0, I1, K, R, t) in enumerate(data):
+        s = align_up(w)
+        got_u, got_v = b.copyOpticalFlowToHost(i)
+        X, Y, Z = b.copy3dToHost(i)
+        f = rf.ReconFlow()
+        f.initializeR(w, h, 1, L, 2.0, 14, 50.0, 0.0, 0.1, 100.0, 1 / 0.33, 60.0, 0.5, 0.25, warps,
+                      iters, cvType=5, fix_quirks=fix)
+        f.setCameraMatrices(K, K)
+        f.copyImagesToDevice(pad_rows(I0, s), pad_rows(I1, s))
+        f.solveR(R, t, 5.0)
+        u1, v1 = f.copyOpticalFlowToHost()
+        X1, Y1, Z1 = f.copy3dToHost()
+        for a, c, nm in ((got_u, u1, "u"), (got_v, v1, "v"), (X, X1, "X"), (Y, Y1, "Y"), (Z, Z1, "Z")):
+            assert_bitexact(a, c, f"pair {i} {nm}", region=(h, w))
+        if i == 2:
+            p = oracle.make_params(w, h, L, lam=50.0, lambdaf=0.1, lambdams=100.0,
+                                   alpha_tv=1 / 0.33, alpha_proj=60.0, tau=0.25,
+                                   n_warp_iters=warps, n_solver_iters=iters, fix_quirks=fix)
+            ref = oracle.solve(p, pad_rows(I0, s), pad_rows(I1, s), K0=K, K1=K, R1=R, t1=t,
+                               dtype=np.float32)
+            assert_bitexact(got_u, ref["u"], "oracle u", region=(h, w))
+            assert_bitexact(Z, ref["Z"], "oracle Z", region=(h, w))
+        inv = b.copyInverseDepthToHost(i)
+        with np.errstate(divide="ignore"):
+            np.testing.assert_array_equal(inv[:, :w], np.float32(1) / Z[:, :w])
+
+
+def test_batch_plain_matches_single_pair(rf):
+    L, warps, iters = 2, 2, 5
+    data = _inputs()
+    b = rf.ReconFlowBatch([(w, h) for w, h, *_ in data], L, method=0, lambda_=50.0, theta=0.33,
+                          tau=0.25, nWarpIters=warps, nSolverIters=iters)
+    for i, (w, h, I0, I1, *_r) in enumerate(data):
+        s = b.strides[i]
+        b.copyImagesToDevice(i, pad_rows(I0, s), pad_rows(I1, s))
+    b.solveOpticalFlow()
+    for i, (w, h, I0, I1, *_r) in enumerate(data):
+        s = align_up(w)
+        u, v = b.copyOpticalFlowToHost(i)
+        f = rf.CudaFlow()
+        f.initialize(w, h, 1, 5, L, 2.0, 0, 50.0, 0.0, 0.33, 0.25, warps, iters)
+        f.copyImagesToDevice(pad_rows(I0, s), pad_rows(I1, s))
+        f.solveOpticalFlow()
+        u1, v1 = f.copyOpticalFlowToHost()
+        assert_bitexact(u, u1, f"pair {i} u", region=(h, w))
+        assert_bitexact(v, v1, f"pair {i} v", region=(h, w))
+
+
+def test_batch_rejects_unsupported(rf):
+    with pytest.raises(rf.RfError):
+        rf.ReconFlowBatch([(64, 48)], 2, method=17)
+    with pytest.raises(rf.RfError):
+        rf.ReconFlowBatch([(64, 48), (8, 4)], 4, method=14)  # 8x4 cannot make 4 levels
