@@ -45,6 +45,12 @@ WORKLOADS = {
     # profiling case: the 720p pair at its finest level only, 1 warp, 4 iterations
     # (a dozen launches, so a profiler capture ends in seconds)
     "720p-l0": dict(width=1280, height=720, levels=1, warps=1, iters=4, seed=0),
+    # batched: 64 pairs of sizes drawn uniformly from four resolutions, independent
+    # seeded scenes and poses, one launch per schedule step for all pairs
+    "batch64": dict(pairs=64, sizes=[(320, 240), (640, 480), (1280, 720), (1920, 1080)],
+                    levels=6, warps=5, iters=100, seed=0),
+    # batched: 64 pairs of 1280x720 (per-pair throughput of the batched path)
+    "batch64-720p": dict(pairs=64, sizes=[(1280, 720)], levels=6, warps=5, iters=100, seed=0),
 }
 SOLVER = dict(method=14, lam=50.0, theta=0.33, tau=0.25, alpha_proj=60.0, lambdaf=0.1,
               lambdams=100.0, fix_quirks=1)
@@ -221,6 +227,140 @@ def run_reference(args, wl, world, rank):
     print(json.dumps(line), flush=True)
 
 
+def batch_sizes(wl):
+    rng = np.random.default_rng(wl["seed"])
+    idx = rng.integers(0, len(wl["sizes"]), wl["pairs"])
+    return [wl["sizes"][i] for i in idx]
+
+
+def run_batch(args, wl, world, rank, local):
+    """Batched workloads: one step = one batched solve of all pairs."""
+    import torch
+
+    import reconflow_gb300 as R
+    from reconflow_gb300.scene import make_scene
+
+    torch.cuda.set_device(local)
+    lib = R.load()
+    sizes = batch_sizes(wl)
+    t0 = time.perf_counter()
+    scenes = [make_scene(w, h, seed=wl["seed"] + 1000 * rank + i, device="cuda")
+              for i, (w, h) in enumerate(sizes)]
+    gen_s = time.perf_counter() - t0
+    b = R.ReconFlowBatch(sizes, wl["levels"], method=SOLVER["method"], lambda_=SOLVER["lam"],
+                         lambdaf=SOLVER["lambdaf"], lambdams=SOLVER["lambdams"],
+                         alphaTv=1.0 / SOLVER["theta"], alphaProj=SOLVER["alpha_proj"],
+                         tau=SOLVER["tau"], nWarpIters=wl["warps"], nSolverIters=wl["iters"],
+                         fix_quirks=SOLVER["fix_quirks"])
+    stream = torch.cuda.Stream()
+    b.setStream(stream.cuda_stream)
+    padded = []
+    for i, sc in enumerate(scenes):
+        s_ = b.strides[i]
+        I0 = np.pad(sc["I0"], ((0, 0), (0, s_ - sc["I0"].shape[1]))).astype(np.float32)
+        I1 = np.pad(sc["I1"], ((0, 0), (0, s_ - sc["I1"].shape[1]))).astype(np.float32)
+        padded.append((I0, I1))
+        b.setCameraMatrices(i, sc["K"], sc["K"])
+        b.copyImagesToDevice(i, I0, I1)
+    Rs = [sc["R"] for sc in scenes]
+    ts = [sc["t"] for sc in scenes]
+    flush = torch.empty(L2_FLUSH_BYTES // 4, dtype=torch.float32, device="cuda")
+    with torch.cuda.stream(stream):
+        for _ in range(args.warmup):
+            b.solveR(Rs, ts)
+        torch.cuda.synchronize()
+        barrier(world)
+        l0 = b.kernelLaunches()
+        evs = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
+               for _ in range(args.steps)]
+        with ClockSampler(local) as clk:
+            torch.cuda.synchronize()
+            for a, e in evs:
+                flush.zero_()
+                a.record(stream)
+                b.solveR(Rs, ts)
+                e.record(stream)
+            torch.cuda.synchronize()
+        launches = b.kernelLaunches() - l0
+        step_ms = [a.elapsed_time(e) for a, e in evs]
+    total_s = max_over_ranks(sum(step_ms) / 1000.0, world)
+    npairs = wl["pairs"]
+    value = world * npairs * args.steps / total_s
+    # accuracy over the batch
+    epes = []
+    for i, sc in enumerate(scenes):
+        w, h = sizes[i]
+        u, v = b.copyOpticalFlowToHost(i)
+        e = np.sqrt((u[:, :w] - sc["flow"][..., 0]) ** 2 + (v[:, :w] - sc["flow"][..., 1]) ** 2)
+        epes.append(float(np.median(e[sc["valid"]])))
+    e2e = None
+    if not args.no_e2e:
+        nb = [sizes[i][1] * b.strides[i] * 4 for i in range(npairs)]
+        hosts = []
+        for i in range(npairs):
+            ptrs = []
+            for _ in range(8):
+                p_ = ctypes.c_void_p()
+                R._native.check(lib.rf_host_alloc(nb[i], ctypes.byref(p_)))
+                ptrs.append(p_)
+            h_ = sizes[i][1]
+            a0 = np.ctypeslib.as_array(ctypes.cast(ptrs[0], ctypes.POINTER(ctypes.c_float)),
+                                       shape=(h_, b.strides[i]))
+            a1 = np.ctypeslib.as_array(ctypes.cast(ptrs[1], ctypes.POINTER(ctypes.c_float)),
+                                       shape=(h_, b.strides[i]))
+            a0[:] = padded[i][0]
+            a1[:] = padded[i][1]
+            hosts.append(ptrs)
+        hb = b._h
+
+        def step():
+            for i in range(npairs):
+                R._native.check(lib.rf_batch_upload_images(hb, i, hosts[i][0], hosts[i][1],
+                                                           b.strides[i]))
+            b.solveR(Rs, ts)
+            for i in range(npairs):
+                s_ = b.strides[i]
+                R._native.check(lib.rf_batch_download_flow(hb, i, hosts[i][2], hosts[i][3], s_))
+                R._native.check(lib.rf_batch_download_inv_depth(hb, i, hosts[i][4], s_))
+                R._native.check(lib.rf_batch_download_points(hb, i, hosts[i][5], hosts[i][6],
+                                                             hosts[i][7], s_))
+
+        step()
+        times = []
+        for _ in range(args.steps):
+            flush.zero_()
+            torch.cuda.synchronize()
+            t1 = time.perf_counter()
+            step()
+            times.append(time.perf_counter() - t1)
+        e2e = {"value": world * npairs * args.steps / max_over_ranks(sum(times), world),
+               "unit": "pairs/s",
+               "h2d_bytes_per_step": sum(2 * w * h * 4 for w, h in sizes),
+               "d2h_bytes_per_step": sum(6 * w * h * 4 for w, h in sizes)}
+        for ptrs in hosts:
+            for p_ in ptrs:
+                lib.rf_host_free(p_)
+    if rank == 0:
+        counts = {}
+        for w, h in sizes:
+            counts[f"{w}x{h}"] = counts.get(f"{w}x{h}", 0) + 1
+        print(json.dumps({
+            "metric": "frame pairs/s, batched ReconFlow solve", "value": value, "unit": "pairs/s",
+            "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": 1000.0 * total_s / args.steps, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+            "data": "synthetic (seeded scene generator)",
+            "config": {"workload": args.workload, "pairs_per_step": npairs, "sizes": counts,
+                       "pyramid_levels": wl["levels"], "warps": wl["warps"],
+                       "iters": wl["iters"], "l2": "flushed between steps",
+                       "parallelism": "replicas"},
+            "e2e": e2e, "clocks": clk.summary(), "gpu_launches": int(launches),
+            "accuracy": {"epe_median_px_mean_over_pairs": float(np.mean(epes))},
+            "scene_gen_s": gen_s,
+        }), flush=True)
+    b.close()
+
+
 def config_of(wl):
     return {"workload": f"reconflow_{wl['width']}x{wl['height']}_L{wl['levels']}_w{wl['warps']}"
                         f"_i{wl['iters']}",
@@ -248,7 +388,12 @@ def main():
     wl = WORKLOADS[args.workload]
     world, rank, local = dist_setup(args)
     if args.impl == "reference":
+        if "pairs" in wl:
+            raise SystemExit("bench.py: the reference arm runs single-pair workloads")
         run_reference(args, wl, world, rank)
+        return
+    if "pairs" in wl:
+        run_batch(args, wl, world, rank, local)
         return
 
     import torch

@@ -17,6 +17,7 @@
 // All pixel-local state (duhat, p, uproj, sk) is updated in place: each is
 // read at a neighbour only by the other kernel of the pair.
 #include <cstdint>
+#include <cstdlib>
 
 #include "rf_kernels.cuh"
 #include "rf_ops.cuh"
@@ -126,10 +127,22 @@ __global__ void k_derivatives(const float* __restrict__ I0, const float* __restr
 #ifndef RF_MINB_B
 #define RF_MINB_B 6  // 40 registers: 6 blocks per SM; measured 4% faster at 720p
 #endif
+// Programmatic dependent launch: a kernel launched with the programmatic
+// stream-serialization attribute may start while its predecessor drains;
+// griddepcontrol.wait blocks until the predecessor has completed and its
+// writes are visible, and launch_dependents lets the successor be scheduled.
+// Both are no-ops for a normal launch.
+__device__ __forceinline__ void pdl_wait() { asm volatile("griddepcontrol.wait;" ::: "memory"); }
+__device__ __forceinline__ void pdl_release() {
+    asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
+}
+
 template <int PRIOR>
 __global__ void __launch_bounds__(BX* BY, RF_MINB_A) k_recon_a(ReconFields f, const LevelConsts* __restrict__ lcp,
                                                     Weights wt, LevelDims d, int first,
                                                     int uc_from_buffer) {
+    pdl_wait();
+    pdl_release();
     int ix = blockIdx.x * blockDim.x + threadIdx.x;
     int iy = blockIdx.y * blockDim.y + threadIdx.y;
     if (ix >= d.w || iy >= d.h) return;
@@ -138,6 +151,8 @@ __global__ void __launch_bounds__(BX* BY, RF_MINB_A) k_recon_a(ReconFields f, co
 
 __global__ void __launch_bounds__(BX* BY, RF_MINB_B) k_recon_b(ReconFields f, Weights wt, LevelDims d,
                                                     int first) {
+    pdl_wait();
+    pdl_release();
     int ix = blockIdx.x * blockDim.x + threadIdx.x;
     int iy = blockIdx.y * blockDim.y + threadIdx.y;
     if (ix >= d.w || iy >= d.h) return;
@@ -713,16 +728,39 @@ int launch_derivatives(const float* I0, const float* I1w, LevelDims d, float* Ix
     return check_launch();
 }
 
+bool use_pdl() {
+    static int v = -1;
+    if (v < 0) {
+        // opt-in (RF_PDL=1): measured no gain inside the captured graph on GB300
+        const char* e = std::getenv("RF_PDL");
+        v = (e && e[0] == '1') ? 1 : 0;
+    }
+    return v == 1;
+}
+
+// Launch with the programmatic stream-serialization attribute (see pdl_wait).
+template <typename... KArgs, typename... Args>
+int launch_pdl(void (*kern)(KArgs...), dim3 g, dim3 b, cudaStream_t st, Args... args) {
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = g;
+    cfg.blockDim = b;
+    cfg.dynamicSmemBytes = 0;
+    cfg.stream = st;
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+    attr[0].val.programmaticStreamSerializationAllowed = use_pdl() ? 1 : 0;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    return cudaLaunchKernelEx(&cfg, kern, args...) == cudaSuccess ? 0 : 1;
+}
+
 int launch_recon_a(const ReconFields& f, const LevelConsts* lc, const Weights& wt, LevelDims d,
                    bool first, bool uc_from_buffer, int prior, cudaStream_t st) {
     dim3 g = grid_for(d.w, d.h), b(BX, BY);
-    if (prior == 1)
-        k_recon_a<1><<<g, b, 0, st>>>(f, lc, wt, d, first, uc_from_buffer);
-    else if (prior == 2)
-        k_recon_a<2><<<g, b, 0, st>>>(f, lc, wt, d, first, uc_from_buffer);
-    else
-        k_recon_a<0><<<g, b, 0, st>>>(f, lc, wt, d, first, uc_from_buffer);
-    return check_launch();
+    int fi = first ? 1 : 0, ub = uc_from_buffer ? 1 : 0;
+    if (prior == 1) return launch_pdl(k_recon_a<1>, g, b, st, f, lc, wt, d, fi, ub);
+    if (prior == 2) return launch_pdl(k_recon_a<2>, g, b, st, f, lc, wt, d, fi, ub);
+    return launch_pdl(k_recon_a<0>, g, b, st, f, lc, wt, d, fi, ub);
 }
 
 int launch_recon_fused(const FusedFields& f, const LevelConsts* lc, const Weights& wt,
@@ -790,8 +828,7 @@ int launch_recon_persistent(const ReconFields& f, const LevelConsts* lc, const W
 
 int launch_recon_b(const ReconFields& f, const Weights& wt, LevelDims d, bool first,
                    cudaStream_t st) {
-    k_recon_b<<<grid_for(d.w, d.h), dim3(BX, BY), 0, st>>>(f, wt, d, first);
-    return check_launch();
+    return launch_pdl(k_recon_b, grid_for(d.w, d.h), dim3(BX, BY), st, f, wt, d, first ? 1 : 0);
 }
 
 int launch_plain_data(float* duhat, float* dvhat, const float* pu1, const float* pu2,

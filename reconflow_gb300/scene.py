@@ -187,17 +187,128 @@ def render_pair(width, height, K, R, t, planes, tex, rng, noise=0.01):
 
 def make_scene(width: int, height: int, seed: int = 0, K=None, n_planes: int = 8,
                n_blobs: int = 200, max_rot_deg: float = 2.0, trans: float = 0.1,
-               noise: float = 0.01) -> dict:
-    """One seeded frame pair with ground truth (see module docstring)."""
+               noise: float = 0.01, device=None) -> dict:
+    """One seeded frame pair with ground truth (see module docstring).
+
+    device=None renders with numpy; a torch CUDA device renders the same
+    scene (same seeded parameters, same formulas) on the GPU, which is much
+    faster for large or many scenes.  Returned arrays are numpy either way.
+    """
     rng = np.random.default_rng(seed)
     K = intrinsics_for(width, height) if K is None else np.asarray(K, np.float64)
     planes = _Planes(rng, width, height, K, n_planes)
     tex = _Texture(rng, width, height, n_blobs)
     # normalise the texture once, from a coarse sample of camera 0's view
     gy, gx = np.mgrid[0:height:4, 0:width:4].astype(np.float64)
-    raw = tex.raw(gx, gy)
+    raw = tex.raw(gx, gy) if device is None else _raw_torch(tex, gx, gy, device)
     tex.lo, tex.hi = float(np.percentile(raw, 0.5)), float(np.percentile(raw, 99.5))
     R, t = random_pose(rng, max_rot_deg, trans)
-    out = render_pair(width, height, K, R, t, planes, tex, rng, noise)
+    if device is None:
+        out = render_pair(width, height, K, R, t, planes, tex, rng, noise)
+    else:
+        out = _render_pair_torch(width, height, K, R, t, planes, tex, rng, noise, device)
     out.update({"K": K, "R": R, "t": t, "seed": seed})
     return out
+
+
+# ---------------------------------------------------------------------------
+# The same renderer on the GPU with torch (float64), for fast input generation
+# ---------------------------------------------------------------------------
+
+def _raw_torch(tex, x, y, device, chunk=16):
+    import torch
+
+    X = torch.as_tensor(np.asarray(x, np.float64).ravel(), device=device)
+    Y = torch.as_tensor(np.asarray(y, np.float64).ravel(), device=device)
+    out = torch.zeros_like(X)
+    cx = torch.as_tensor(tex.cx, device=device)
+    cy = torch.as_tensor(tex.cy, device=device)
+    sig = torch.as_tensor(tex.sig, device=device)
+    amp = torch.as_tensor(tex.amp, device=device)
+    for i in range(0, len(tex.amp), chunk):
+        dx = X[:, None] - cx[None, i:i + chunk]
+        dy = Y[:, None] - cy[None, i:i + chunk]
+        r = 4.0 * sig[None, i:i + chunk]
+        inside = (dx.abs() < r) & (dy.abs() < r)
+        val = amp[None, i:i + chunk] * torch.exp(-(dx * dx + dy * dy) / (2 * sig[None, i:i + chunk] ** 2))
+        out += torch.where(inside, val, torch.zeros_like(val)).sum(1)
+    kx = torch.as_tensor(tex.kx, device=device)
+    ky = torch.as_tensor(tex.ky, device=device)
+    ph = torch.as_tensor(tex.ph, device=device)
+    wa = torch.as_tensor(tex.wamp, device=device)
+    for i in range(len(tex.freq)):
+        out += wa[i] * torch.cos(kx[i] * X + ky[i] * Y + ph[i])
+    return out.cpu().numpy()
+
+
+def _render_pair_torch(width, height, K, R, t, planes, tex, rng, noise, device):
+    import torch
+
+    dev = torch.device(device)
+    T = lambda a: torch.as_tensor(np.asarray(a, np.float64), device=dev)  # noqa: E731
+    Kt, Rt, tt = T(K), T(R), T(t)
+    Kinv = torch.linalg.inv(Kt)
+    ys, xs = torch.meshgrid(torch.arange(height, device=dev, dtype=torch.float64),
+                            torch.arange(width, device=dev, dtype=torch.float64), indexing="ij")
+    xs, ys = xs.reshape(-1), ys.reshape(-1)
+    seeds = T(planes.seeds)
+    abc = T(planes.abc)
+    nrm = T(planes.n)
+
+    def label(x, y):
+        d = (x[:, None] - seeds[None, :, 0]) ** 2 + (y[:, None] - seeds[None, :, 1]) ** 2
+        return torch.argmin(d, dim=1)
+
+    def texture(x, y):
+        v = (torch.as_tensor(_raw_torch(tex, x.cpu().numpy(), y.cpu().numpy(), dev), device=dev)
+             - tex.lo) / (tex.hi - tex.lo)
+        return v.clamp(0.0, 1.0)
+
+    def raycast(px, py):
+        C = -Rt.T @ tt
+        rays = torch.stack([px, py, torch.ones_like(px)], 0)
+        d = Rt.T @ (Kinv @ rays)
+        best = torch.full_like(px, float("inf"))
+        hit = torch.zeros((3, px.numel()), dtype=torch.float64, device=dev)
+        nC = nrm @ C
+        nd = nrm @ d
+        for k in range(nrm.shape[0]):
+            lam = (1.0 - nC[k]) / nd[k]
+            X = C[:, None] + lam[None, :] * d
+            z = X[2]
+            ok = (lam > 0) & (z > 1e-6) & torch.isfinite(lam)
+            qx = torch.where(ok, Kt[0, 0] * X[0] / z + Kt[0, 2], torch.zeros_like(z))
+            qy = torch.where(ok, Kt[1, 1] * X[1] / z + Kt[1, 2], torch.zeros_like(z))
+            ok &= label(qx, qy) == k
+            better = ok & (lam < best)
+            best = torch.where(better, lam, best)
+            hit[:, better] = X[:, better]
+        return hit, torch.isfinite(best)
+
+    k = label(xs, ys)
+    inv_depth = abc[k, 0] + abc[k, 1] * xs + abc[k, 2] * ys
+    Z = 1.0 / inv_depth
+    I0 = texture(xs, ys)
+    X, found = raycast(xs, ys)
+    px = torch.where(found, Kt[0, 0] * X[0] / X[2] + Kt[0, 2], xs)
+    py = torch.where(found, Kt[1, 1] * X[1] / X[2] + Kt[1, 2], ys)
+    I1 = texture(px, py)
+    P0 = torch.stack([xs * Z, ys * Z, Z], 0)
+    X0 = Kinv @ P0
+    X1 = Rt @ X0 + tt[:, None]
+    u1 = Kt[0, 0] * X1[0] / X1[2] + Kt[0, 2]
+    v1 = Kt[1, 1] * X1[1] / X1[2] + Kt[1, 2]
+    inb = (u1 >= 0) & (u1 <= width - 1) & (v1 >= 0) & (v1 <= height - 1)
+    Xv, fv = raycast(u1, v1)
+    same = fv & (torch.linalg.norm(Xv - X0, dim=0) < 1e-3 * torch.clamp(X0[2], min=1.0))
+    valid = (inb & same).reshape(height, width)
+    sh = (height, width)
+    I0 = I0.reshape(sh).cpu().numpy() + rng.normal(0.0, noise, sh)
+    I1 = I1.reshape(sh).cpu().numpy() + rng.normal(0.0, noise, sh)
+    flow = torch.stack([(u1 - xs).reshape(sh), (v1 - ys).reshape(sh)], -1)
+    return {
+        "I0": I0.astype(np.float32), "I1": I1.astype(np.float32),
+        "flow": flow.cpu().numpy().astype(np.float32),
+        "inv_depth": inv_depth.reshape(sh).cpu().numpy().astype(np.float32),
+        "depth": Z.reshape(sh).cpu().numpy().astype(np.float32), "valid": valid.cpu().numpy(),
+    }
