@@ -146,6 +146,28 @@ RF_API rf_status rf_solve(rf_handle* h, const double R0[9], const double t0[3],
 /* CudaFlow::solveOpticalFlow (Cudaflow.cu:394-621): plain TV-L1 flow. */
 RF_API rf_status rf_solve_flow(rf_handle* h);
 
+/* Warm-started solve (no reference counterpart): the schedule begins at
+ * pyramid `level` from the given flow u, v and 3D points X, Y, Z on that
+ * level (planes of the level's size, `pitch` elements per row, host memory,
+ * or device memory when on_device != 0), with uproj = u, sk = 0 and the
+ * projection of the given points; levels `level`..0 then run `warps` warps of
+ * `iters` iterations (-1 = the handle's counts).  Method 14 only.  Used to
+ * refine a coarse estimate, e.g. a learned prediction. */
+RF_API rf_status rf_solve_warm(rf_handle* h, const double R0[9], const double t0[3],
+                               const double R1[9], const double t1[3], int level, const float* u,
+                               const float* v, const float* X, const float* Y, const float* Z,
+                               int pitch, int on_device, int warps, int iters);
+
+/* Plain TV-L1 counterpart of rf_solve_warm (flow only). */
+RF_API rf_status rf_solve_flow_warm(rf_handle* h, int level, const float* u, const float* v,
+                                    int pitch, int on_device, int warps, int iters);
+
+/* Energy of the last solution (no reference counterpart), summed in double
+ * over the level-0 pixels: lambda * |I1(x + u) - I0(x)| + |grad u| +
+ * |grad v| (+ alpha_proj / 2 * |(u, v) - uc(X)|^2 for ReconFlow, uc the
+ * projection of the solved point as SolveUc computes it).  Blocking. */
+RF_API rf_status rf_energy(rf_handle* h, double* energy);
+
 /* CudaFlow::copyOpticalFlowToHost(u, v) (Cudaflow.cu:320-325). Blocking. */
 RF_API rf_status rf_download_flow(rf_handle* h, float* u, float* v, int pitch);
 

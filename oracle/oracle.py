@@ -272,3 +272,42 @@ def solve(params: RfoParams, I0, I1, K0=None, K1=None, R0=None, t0=None, R1=None
         for k in ("X", "Y", "Z"):
             out.pop(k)
     return out
+
+
+def solve_warm(params: RfoParams, I0, I1, level, u0, v0, X0, Y0, Z0, warps, iters, K0=None,
+               K1=None, R0=None, t0=None, R1=None, t1=None):
+    """FP32 schedule started at pyramid `level` from the given flow and points
+    (planes with that level's stride).  Returns dict of (height, stride) arrays."""
+    W, H, S = pyramid_dims(params.width, params.height, params.n_levels, params.scale,
+                           params.stride_alignment)
+    s, h = S[0], H[0]
+    eye, z3 = np.eye(3), np.zeros(3)
+    K0 = np.ascontiguousarray(eye if K0 is None else K0, np.float64)
+    K1 = np.ascontiguousarray(K0 if K1 is None else K1, np.float64)
+    R0 = np.ascontiguousarray(eye if R0 is None else R0, np.float64)
+    t0 = np.ascontiguousarray(z3 if t0 is None else t0, np.float64)
+    R1 = np.ascontiguousarray(eye if R1 is None else R1, np.float64)
+    t1 = np.ascontiguousarray(z3 if t1 is None else t1, np.float64)
+    ws = [np.ascontiguousarray(a, np.float32) for a in (u0, v0, X0, Y0, Z0)]
+    out = {k: np.zeros((h, s), np.float32) for k in ("u", "v", "X", "Y", "Z")}
+    I0 = np.ascontiguousarray(I0, np.float32)
+    I1 = np.ascontiguousarray(I1, np.float32)
+    rc = lib().rfo_solve_warm_f32(ctypes.byref(params), _ptr(I0), _ptr(I1), int(s), _ptr(K0),
+                                  _ptr(K1), _ptr(R0), _ptr(t0), _ptr(R1), _ptr(t1), int(level),
+                                  *[_ptr(a) for a in ws], int(warps), int(iters),
+                                  *[_ptr(out[k]) for k in ("u", "v", "X", "Y", "Z")])
+    if rc != 0:
+        raise RuntimeError(f"oracle warm solve failed: {rc}")
+    return out
+
+
+def energy(I0, I1, u, v, X, Y, Z, w, h, s, lam, alpha_proj, R1, t1, K1, recon=True):
+    """Solution energy on level 0 (data + TV + reprojection), in double."""
+    fn = lib().rfo_energy
+    fn.restype = ctypes.c_double
+    arrs = [np.ascontiguousarray(a, np.float32) for a in (I0, I1, u, v, X, Y, Z)]
+    R1 = np.ascontiguousarray(R1, np.float64)
+    t1 = np.ascontiguousarray(t1, np.float64)
+    K1 = np.ascontiguousarray(K1, np.float64)
+    return float(fn(*[_ptr(a) for a in arrs], int(w), int(h), int(s), ctypes.c_float(lam),
+                    ctypes.c_float(alpha_proj), _ptr(R1), _ptr(t1), _ptr(K1), int(recon)))

@@ -749,11 +749,22 @@ void camera_matrix(const std::vector<double>& K, const double* R, const double* 
 // work buffers are flat level-0-sized arrays (plus one zero guard row) and
 // are exchanged by pointer swaps exactly as the reference does, because the
 // 3D buffers are re-read with the next level's stride without upscaling.
+// Warm start (no reference counterpart): begin the schedule at `level`
+// with flow u, v and 3D points X, Y, Z given on that level (planes with the
+// level's stride); uproj = u, sk = 0, uc recomputed from the points; levels
+// `level`..0 run `warps` warps of `iters` iterations each.
+struct WarmStart {
+    int level = -1;
+    const float *u = nullptr, *v = nullptr, *X = nullptr, *Y = nullptr, *Z = nullptr;
+    int warps = 0, iters = 0;
+};
+
 template <typename T>
 int solve(const rfo_params& p, const void* i0, const void* i1, int in_stride,
           const double* K0, const double* K1, const double* R0, const double* t0,
           const double* R1, const double* t1, const float* ufn, const float* vfn,
-          const float* fnmask, T* out_u, T* out_v, T* out_X, T* out_Y, T* out_Z) {
+          const float* fnmask, T* out_u, T* out_v, T* out_X, T* out_Y, T* out_Z,
+          const WarmStart* warm = nullptr) {
     const int L = p.n_levels;
     std::vector<int> W(L), H(L), S(L);
     pyramid_dims(p.width, p.height, L, p.scale, p.stride_alignment, W.data(), H.data(), S.data());
@@ -823,7 +834,30 @@ int solve(const rfo_params& p, const void* i0, const void* i1, int in_stride,
     for (int i = 0; i < 9; i++) R1f[i] = is64 ? (T)R1[i] : (T)(float)R1[i];
     for (int i = 0; i < 3; i++) t1f[i] = is64 ? (T)t1[i] : (T)(float)t1[i];
 
-    for (int level = L - 1; level >= 0; level--) {
+    const bool is_warm = warm && warm->level >= 0;
+    const int top = is_warm ? warm->level : L - 1;
+    const int n_warps = is_warm ? warm->warps : p.n_warp_iters;
+    const int n_iters = is_warm ? warm->iters : p.n_solver_iters;
+    bool uc_from_points = false;
+    if (is_warm) {
+        const int w = W[top], h = H[top], s = S[top];
+        for (int y = 0; y < h; y++)
+            for (int x = 0; x < w; x++) {
+                size_t i = x + (size_t)y * s;
+                d_u[i] = (T)warm->u[i];
+                d_v[i] = (T)warm->v[i];
+                if (recon) {
+                    d_uproj[i] = (T)warm->u[i];
+                    d_vproj[i] = (T)warm->v[i];
+                    d_X[i] = (T)warm->X[i];
+                    d_Y[i] = (T)warm->Y[i];
+                    d_Z[i] = (T)warm->Z[i];
+                }
+            }
+        uc_from_points = recon;
+    }
+
+    for (int level = top; level >= 0; level--) {
         const int w = W[level], h = H[level], s = S[level];
         T P[12], Q[12];
         T focal = 0, cxl = 0, cyl = 0;
@@ -849,12 +883,17 @@ int solve(const rfo_params& p, const void* i0, const void* i1, int in_stride,
             k_downscale(d_vfn, W[0], H[0], S[0], w, h, s, sc, true, d_vfn_l);
             k_downscale(d_mask, W[0], H[0], S[0], w, h, s, T(1), false, d_mask_l);
         }
-        for (int warp = 0; warp < p.n_warp_iters; warp++) {
+        if (uc_from_points) {
+            // warm start: uc of the supplied points at this level
+            k_solve_uc(d_X, d_Y, d_Z, R1f, t1f, focal, cxl, cyl, w, h, s, d_uc, d_vc);
+            uc_from_points = false;
+        }
+        for (int warp = 0; warp < n_warps; warp++) {
             zero(d_dumed); zero(d_dvmed); zero(d_dumeds); zero(d_dvmeds);
             zero(d_pu1); zero(d_pu2); zero(d_pv1); zero(d_pv2);
             k_warp(pI1[level], w, h, s, d_u, d_v, d_i1warp);
             k_derivatives(pI0[level], d_i1warp, w, h, s, d_Ix, d_Iy, d_Iz);
-            for (int iter = 0; iter < p.n_solver_iters; iter++) {
+            for (int iter = 0; iter < n_iters; iter++) {
                 if (recon) {
                     k_recon_data_l1(d_u, d_v, d_dumed, d_dvmed, d_uproj, d_vproj, d_ufn_l, d_vfn_l,
                                     d_mask_l, d_sku, d_skv, d_pu1, d_pu2, d_pv1, d_pv2, d_Ix, d_Iy,
@@ -929,6 +968,48 @@ int solve(const rfo_params& p, const void* i0, const void* i1, int in_stride,
         std::copy(d_Z, d_Z + m, out_Z);
     }
     return 0;
+}
+
+// Energy of a solution (no reference counterpart; defines the fallback test
+// of the warm-started solve), summed in double over the level-0 pixels:
+//   lambda * |I1(x + u) - I0(x)|                      (brightness residual,
+//                                                      I1 fetched as WarpingKernel)
+// + |grad u| + |grad v|                               (forward differences,
+//                                                      0 at the far border)
+// + alpha_proj / 2 * |(u, v) - uc(X)|^2               (reprojection of the
+//                                                      solved 3D point; recon only)
+double energy(const float* I0, const float* I1, const float* u, const float* v, const float* X,
+              const float* Y, const float* Z, int w, int h, int s, float lambda,
+              float alpha_proj, const double* R1, const double* t1, const double* K1,
+              int recon) {
+    double e = 0.0;
+    for (int iy = 0; iy < h; iy++)
+        for (int ix = 0; ix < w; ix++) {
+            int pos = ix + iy * s;
+            float x = ((float)ix + u[pos] + 0.5f) / (float)w;
+            float y = ((float)iy + v[pos] + 0.5f) / (float)h;
+            float i1w = tex2d(I1, w, h, s, x, y);
+            double data = (double)lambda * std::fabs((double)i1w - (double)I0[pos]);
+            double ux = ix + 1 < w ? (double)u[pos + 1] - u[pos] : 0.0;
+            double uy = iy + 1 < h ? (double)u[pos + s] - u[pos] : 0.0;
+            double vx = ix + 1 < w ? (double)v[pos + 1] - v[pos] : 0.0;
+            double vy = iy + 1 < h ? (double)v[pos + s] - v[pos] : 0.0;
+            double tv = std::sqrt(ux * ux + uy * uy) + std::sqrt(vx * vx + vy * vy);
+            double proj = 0.0;
+            if (recon) {
+                double Xp = X[pos], Yp = Y[pos], Zp = Z[pos];
+                double X2 = R1[0] * Xp + R1[1] * Yp + R1[2] * Zp + t1[0];
+                double Y2 = R1[3] * Xp + R1[4] * Yp + R1[5] * Zp + t1[1];
+                double Z2 = R1[6] * Xp + R1[7] * Yp + R1[8] * Zp + t1[2];
+                double uc = K1[0] * X2 / Z2 + K1[2] - ix;
+                double vc = K1[0] * Y2 / Z2 + K1[5] - iy;  // fx for both, as SolveUc
+                double du = u[pos] - uc, dv = v[pos] - vc;
+                proj = 0.5 * (double)alpha_proj * (du * du + dv * dv);
+                if (!std::isfinite(proj)) proj = 0.0;
+            }
+            e += data + tv + proj;
+        }
+    return e;
 }
 
 }  // namespace
@@ -1053,6 +1134,25 @@ void rfo_camera_matrix(const double* K, const double* R, const double* t, double
 
 RFO_KERNELS(float, f32)
 RFO_KERNELS(double, f64)
+
+int rfo_solve_warm_f32(const rfo_params* p, const float* i0, const float* i1, int in_stride,
+                       const double* K0, const double* K1, const double* R0, const double* t0,
+                       const double* R1, const double* t1, int level, const float* wu,
+                       const float* wv, const float* wX, const float* wY, const float* wZ,
+                       int warps, int iters, float* u, float* v, float* X, float* Y, float* Z) {
+    WarmStart ws;
+    ws.level = level; ws.u = wu; ws.v = wv; ws.X = wX; ws.Y = wY; ws.Z = wZ;
+    ws.warps = warps; ws.iters = iters;
+    return solve<float>(*p, i0, i1, in_stride, K0, K1, R0, t0, R1, t1, nullptr, nullptr, nullptr,
+                        u, v, X, Y, Z, &ws);
+}
+
+double rfo_energy(const float* I0, const float* I1, const float* u, const float* v,
+                  const float* X, const float* Y, const float* Z, int w, int h, int s,
+                  float lambda, float alpha_proj, const double* R1, const double* t1,
+                  const double* K1, int recon) {
+    return energy(I0, I1, u, v, X, Y, Z, w, h, s, lambda, alpha_proj, R1, t1, K1, recon);
+}
 
 void rfo_rgb_to_gray_f32(const uint8_t* rgb, int w, int h, int s, float* out) {
     k_rgb_to_gray<float>(rgb, w, h, s, out);

@@ -58,6 +58,9 @@ _SIGS = [
     ("rf_set_prior_flow", _I, [_VP, _VP, _VP, _VP, _I]),
     ("rf_solve", _I, [_VP, _D, _D, _D, _D]),
     ("rf_solve_flow", _I, [_VP]),
+    ("rf_solve_warm", _I, [_VP, _D, _D, _D, _D, _I, _VP, _VP, _VP, _VP, _VP, _I, _I, _I, _I]),
+    ("rf_solve_flow_warm", _I, [_VP, _I, _VP, _VP, _I, _I, _I, _I]),
+    ("rf_energy", _I, [_VP, ctypes.POINTER(ctypes.c_double)]),
     ("rf_download_flow", _I, [_VP, _VP, _VP, _I]),
     ("rf_download_points", _I, [_VP, _VP, _VP, _VP, _I]),
     ("rf_download_inv_depth", _I, [_VP, _VP, _I]),

@@ -694,6 +694,66 @@ __global__ void k_flow_color(const float* __restrict__ u, const float* __restric
 
 }  // namespace
 
+// Energy of a solution on level 0 (no reference counterpart; see
+// rf_energy): per-block double partial sums, then one block adds the
+// partials in a fixed order, so the result is deterministic.
+struct EnergyArgs {
+    const float *I0, *I1, *u, *v, *X, *Y, *Z;
+    double R1[9], t1[3], fx, cx, cy;
+    float lambda, alpha_proj;
+    int recon;
+};
+
+constexpr int kEnergyThreads = 256;
+
+__global__ void __launch_bounds__(kEnergyThreads) k_energy_partial(EnergyArgs a, LevelDims d,
+                                                                   double* partial) {
+    __shared__ double red[kEnergyThreads / 32];
+    double e = 0.0;
+    const int npx = d.w * d.h;
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < npx; i += gridDim.x * blockDim.x) {
+        const int ix = i % d.w, iy = i / d.w, s = d.s, pos = ix + iy * s;
+        float x = ((float)ix + a.u[pos] + 0.5f) / (float)d.w;
+        float y = ((float)iy + a.v[pos] + 0.5f) / (float)d.h;
+        float i1w = tex2d(a.I1, d.w, d.h, s, x, y);
+        double data = (double)a.lambda * fabs((double)i1w - (double)a.I0[pos]);
+        double ux = ix + 1 < d.w ? (double)a.u[pos + 1] - a.u[pos] : 0.0;
+        double uy = iy + 1 < d.h ? (double)a.u[pos + s] - a.u[pos] : 0.0;
+        double vx = ix + 1 < d.w ? (double)a.v[pos + 1] - a.v[pos] : 0.0;
+        double vy = iy + 1 < d.h ? (double)a.v[pos + s] - a.v[pos] : 0.0;
+        double tv = sqrt(ux * ux + uy * uy) + sqrt(vx * vx + vy * vy);
+        double proj = 0.0;
+        if (a.recon) {
+            double Xp = a.X[pos], Yp = a.Y[pos], Zp = a.Z[pos];
+            double X2 = a.R1[0] * Xp + a.R1[1] * Yp + a.R1[2] * Zp + a.t1[0];
+            double Y2 = a.R1[3] * Xp + a.R1[4] * Yp + a.R1[5] * Zp + a.t1[1];
+            double Z2 = a.R1[6] * Xp + a.R1[7] * Yp + a.R1[8] * Zp + a.t1[2];
+            double uc = a.fx * X2 / Z2 + a.cx - ix;
+            double vc = a.fx * Y2 / Z2 + a.cy - iy;
+            double du = a.u[pos] - uc, dv = a.v[pos] - vc;
+            proj = 0.5 * (double)a.alpha_proj * (du * du + dv * dv);
+            if (!isfinite(proj)) proj = 0.0;
+        }
+        e += data + tv + proj;
+    }
+    for (int o = 16; o > 0; o >>= 1) e += __shfl_down_sync(0xffffffffu, e, o);
+    if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = e;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        double t = 0.0;
+        for (int k = 0; k < kEnergyThreads / 32; k++) t += red[k];
+        partial[blockIdx.x] = t;
+    }
+}
+
+__global__ void k_energy_final(const double* partial, int n, double* out) {
+    if (threadIdx.x == 0 && blockIdx.x == 0) {
+        double t = 0.0;
+        for (int k = 0; k < n; k++) t += partial[k];
+        *out = t;
+    }
+}
+
 // ---------------------------------------------------------------------------
 // Launchers
 // ---------------------------------------------------------------------------
@@ -910,4 +970,25 @@ int launch_flow_color(const float* u, const float* v, LevelDims d, float flow_sc
     return check_launch();
 }
 
+}  // namespace rf
+
+namespace rf {
+int launch_energy(const float* I0, const float* I1, const float* u, const float* v,
+                  const float* X, const float* Y, const float* Z, LevelDims d, float lambda,
+                  float alpha_proj, const double* R1, const double* t1, const double* K1,
+                  int recon, double* partial, int nblocks, double* out, cudaStream_t st) {
+    EnergyArgs a;
+    a.I0 = I0; a.I1 = I1; a.u = u; a.v = v; a.X = X; a.Y = Y; a.Z = Z;
+    for (int i = 0; i < 9; i++) a.R1[i] = R1 ? R1[i] : (i % 4 == 0 ? 1.0 : 0.0);
+    for (int i = 0; i < 3; i++) a.t1[i] = t1 ? t1[i] : 0.0;
+    a.fx = K1 ? K1[0] : 1.0;
+    a.cx = K1 ? K1[2] : 0.0;
+    a.cy = K1 ? K1[5] : 0.0;
+    a.lambda = lambda;
+    a.alpha_proj = alpha_proj;
+    a.recon = recon;
+    k_energy_partial<<<nblocks, kEnergyThreads, 0, st>>>(a, d, partial);
+    k_energy_final<<<1, 32, 0, st>>>(partial, nblocks, out);
+    return check_launch();
+}
 }  // namespace rf

@@ -166,6 +166,12 @@ int launch_upscale_fields(int n, const float* const* src, float* const* dst, con
 int launch_upscale(const float* src, LevelDims coarse, LevelDims fine, float scale, float* out,
                    cudaStream_t st);
 int launch_inv_depth(const float* Z, LevelDims d, float* out, cudaStream_t st);
+// Solution energy on one level (data + TV + reprojection) into *out (device
+// double); `partial` holds `nblocks` doubles.
+int launch_energy(const float* I0, const float* I1, const float* u, const float* v,
+                  const float* X, const float* Y, const float* Z, LevelDims d, float lambda,
+                  float alpha_proj, const double* R1, const double* t1, const double* K1,
+                  int recon, double* partial, int nblocks, double* out, cudaStream_t st);
 int launch_remove_edge(const float* X, const float* Y, const float* Z, int range, float max_area,
                        LevelDims d, float* X1, float* Y1, float* Z1, cudaStream_t st);
 int launch_flow_color(const float* u, const float* v, LevelDims d, float flow_scale, float* rgb,

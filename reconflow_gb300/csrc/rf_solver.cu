@@ -6,6 +6,7 @@
 // The schedule is recorded once per handle into a CUDA graph and replayed by
 // every solve; the per-solve camera constants live in a small device block
 // that the kernels read, so one graph serves every pose.
+#include <algorithm>
 #include <cmath>
 #include <cstdio>
 #include <cstdlib>
@@ -107,6 +108,13 @@ struct rf_handle {
     float *st_uc = nullptr, *st_vc = nullptr;
     // fused path: the two state sets as left by the last solve (for the
     // profiling hook); set 0 = read, set 1 = write
+    // warm start (rf_solve_warm): staging planes and the schedule's start
+    float* warm[5] = {nullptr, nullptr, nullptr, nullptr, nullptr};
+    int warm_level = -1, warm_warps = 0, warm_iters = 0;
+    int graph_key[3] = {-1, -1, -1};
+    // energy reduction buffers and the pose of the last solve
+    double* d_energy = nullptr;  // [0] = result, [1..1024] = block partials
+    double last_R1[9], last_t1[3];
     FusedFields fz{};
     // one fused launch per iteration (RF_FUSED=1): bit-identical, but on GB300
     // it issues as many instructions as the two-kernel form at lower occupancy
@@ -250,9 +258,22 @@ rf_status enqueue_pyramid(rf_handle* h) {
 }
 
 // ReconFlow::solveReconFlow (Reconflow.cu:147-466) for methods 14 / 17 / 20.
-rf_status enqueue_recon(rf_handle* h, float** res_u, float** res_v) {
+// Copy the warm-start planes (level `lvl`) into the solver's role buffers.
+rf_status copy_warm(rf_handle* h, int lvl, float* const* dst, int n) {
+    const size_t sp = h->S[lvl] * sizeof(float);
+    for (int k = 0; k < n; k++)
+        RF_CUDA(cudaMemcpy2DAsync(dst[k], sp, h->warm[k < 2 ? k : k], sp,
+                                  h->W[lvl] * sizeof(float), h->H[lvl], cudaMemcpyDeviceToDevice,
+                                  h->stream));
+    return RF_OK;
+}
+
+rf_status enqueue_recon(rf_handle* h, float** res_u, float** res_v, bool warm = false) {
     cudaStream_t st = h->stream;
     const rf_params& p = h->p;
+    const int top = warm ? h->warm_level : h->L - 1;
+    const int n_warps = warm ? h->warm_warps : p.n_warp_iters;
+    const int n_iters = warm ? h->warm_iters : p.n_solver_iters;
     const Weights wt = make_weights(p);
     const int prior = prior_kind(p.method);
     const size_t plane_bytes = h->plane * sizeof(float);
@@ -270,8 +291,18 @@ rf_status enqueue_recon(rf_handle* h, float** res_u, float** res_v) {
     for (float* b : {u, v, uproj, vproj, uc, vc, sku, skv, h->X, h->Y, h->Z})
         RF_CUDA(cudaMemsetAsync(b, 0, plane_bytes, st));
     bool uc_in_buffer = true;
+    if (warm) {
+        // u, v and the points from the staging planes; uproj = u; uc from the points
+        float* dst[5] = {u, v, h->X, h->Y, h->Z};
+        rf_status ws = copy_warm(h, top, dst, 5);
+        if (ws != RF_OK) return ws;
+        float* dp[2] = {uproj, vproj};
+        ws = copy_warm(h, top, dp, 2);
+        if (ws != RF_OK) return ws;
+        uc_in_buffer = false;
+    }
 
-    for (int level = h->L - 1; level >= 0; level--) {
+    for (int level = top; level >= 0; level--) {
         LevelDims d{h->W[level], h->H[level], h->S[level]};
         const LevelConsts* lc = h->d_consts + level;
         ReconFields f{};
@@ -283,7 +314,7 @@ rf_status enqueue_recon(rf_handle* h, float** res_u, float** res_v) {
             RF_LAUNCH(launch_downscale(h->vfn, d0, d, sc, true, h->vfn_l, st));
             RF_LAUNCH(launch_downscale(h->mask, d0, d, 1.0f, false, h->mask_l, st));
         }
-        for (int warp = 0; warp < p.n_warp_iters; warp++) {
+        for (int warp = 0; warp < n_warps; warp++) {
             RF_LAUNCH(launch_warp(h->I1[level], u, v, d, h->i1w, st));
             RF_LAUNCH(launch_derivatives(h->I0[level], h->i1w, d, h->Ix, h->Iy, h->Iz, st));
             f.u = u; f.v = v;
@@ -294,19 +325,19 @@ rf_status enqueue_recon(rf_handle* h, float** res_u, float** res_v) {
             f.X = h->X; f.Y = h->Y; f.Z = h->Z; f.X1 = h->X1; f.Y1 = h->Y1; f.Z1 = h->Z1;
             f.uc = uc; f.vc = vc;
             f.ufn = h->ufn_l; f.vfn = h->vfn_l; f.mask = h->mask_l;
-            if (p.n_solver_iters > 0 && d.w * d.h <= h->persist_max_px) {
+            if (n_iters > 0 && d.w * d.h <= h->persist_max_px) {
                 // small level: every inner iteration of this warp in one launch
                 RF_CUDA(cudaMemsetAsync(h->d_barrier, 0, 2 * sizeof(unsigned int), st));
-                RF_LAUNCH(launch_recon_persistent(f, lc, wt, d, p.n_solver_iters, uc_in_buffer,
+                RF_LAUNCH(launch_recon_persistent(f, lc, wt, d, n_iters, uc_in_buffer,
                                                   prior, h->d_barrier, st));
                 uc_in_buffer = false;
             }
-            for (int iter = 0; iter < p.n_solver_iters && d.w * d.h > h->persist_max_px; iter++) {
+            for (int iter = 0; iter < n_iters && d.w * d.h > h->persist_max_px; iter++) {
                 RF_LAUNCH(launch_recon_a(f, lc, wt, d, iter == 0, uc_in_buffer, prior, st));
                 RF_LAUNCH(launch_recon_b(f, wt, d, iter == 0, st));
                 uc_in_buffer = false;
             }
-            if (p.n_solver_iters == 0) {
+            if (n_iters == 0) {
                 // the reference's memsets leave duhat = 0 when no iteration runs
                 RF_CUDA(cudaMemsetAsync(h->duhat, 0, plane_bytes, st));
                 RF_CUDA(cudaMemsetAsync(h->dvhat, 0, plane_bytes, st));
@@ -470,29 +501,37 @@ rf_status enqueue_recon_fused(rf_handle* h, float** res_u, float** res_v) {
 }
 
 // CudaFlow::_solveOpticalFlow (Cudaflow.cu:403-621), METHOD_TVL1.
-rf_status enqueue_plain(rf_handle* h, float** res_u, float** res_v) {
+rf_status enqueue_plain(rf_handle* h, float** res_u, float** res_v, bool warm = false) {
     cudaStream_t st = h->stream;
     const rf_params& p = h->p;
     const Weights wt = make_weights(p);
     const size_t plane_bytes = h->plane * sizeof(float);
+    const int top = warm ? h->warm_level : h->L - 1;
+    const int n_warps = warm ? h->warm_warps : p.n_warp_iters;
+    const int n_iters = warm ? h->warm_iters : p.n_solver_iters;
     float *u = h->spare[0], *v = h->spare[1];
     float *us = h->spare[2], *vs = h->spare[3];
     rf_status rs = enqueue_pyramid(h);
     if (rs != RF_OK) return rs;
     RF_CUDA(cudaMemsetAsync(u, 0, plane_bytes, st));
     RF_CUDA(cudaMemsetAsync(v, 0, plane_bytes, st));
-    for (int level = h->L - 1; level >= 0; level--) {
+    if (warm) {
+        float* dst[2] = {u, v};
+        rf_status ws = copy_warm(h, top, dst, 2);
+        if (ws != RF_OK) return ws;
+    }
+    for (int level = top; level >= 0; level--) {
         LevelDims d{h->W[level], h->H[level], h->S[level]};
-        for (int warp = 0; warp < p.n_warp_iters; warp++) {
+        for (int warp = 0; warp < n_warps; warp++) {
             RF_LAUNCH(launch_warp(h->I1[level], u, v, d, h->i1w, st));
             RF_LAUNCH(launch_derivatives(h->I0[level], h->i1w, d, h->Ix, h->Iy, h->Iz, st));
-            for (int iter = 0; iter < p.n_solver_iters; iter++) {
+            for (int iter = 0; iter < n_iters; iter++) {
                 RF_LAUNCH(launch_plain_data(h->duhat, h->dvhat, h->pu1, h->pu2, h->pv1, h->pv2,
                                             h->Ix, h->Iy, h->Iz, wt, d, iter == 0, st));
                 RF_LAUNCH(launch_plain_tv(h->duhat, h->dvhat, h->pu1, h->pu2, h->pv1, h->pv2, wt,
                                           d, iter == 0, st));
             }
-            if (p.n_solver_iters == 0) {
+            if (n_iters == 0) {
                 RF_CUDA(cudaMemsetAsync(h->duhat, 0, plane_bytes, st));
                 RF_CUDA(cudaMemsetAsync(h->dvhat, 0, plane_bytes, st));
             }
@@ -523,8 +562,18 @@ bool use_graphs() {
 rf_status run_schedule(rf_handle* h, int kind) {
     auto enqueue = [&](float** ru, float** rv) {
         if (kind == 1) return enqueue_plain(h, ru, rv);
+        if (kind == 2) return enqueue_recon(h, ru, rv, true);
+        if (kind == 3) return enqueue_plain(h, ru, rv, true);
         return h->use_fused ? enqueue_recon_fused(h, ru, rv) : enqueue_recon(h, ru, rv);
     };
+    const int key[3] = {kind >= 2 ? h->warm_level : -1, kind >= 2 ? h->warm_warps : -1,
+                        kind >= 2 ? h->warm_iters : -1};
+    if (h->graph && (key[0] != h->graph_key[0] || key[1] != h->graph_key[1] ||
+                     key[2] != h->graph_key[2])) {
+        cudaGraphExecDestroy(h->graph);
+        h->graph = nullptr;
+    }
+    std::memcpy(h->graph_key, key, sizeof key);
     if (!use_graphs()) {
         h->enqueue_launches = 0;
         rf_status rs = enqueue(&h->res_u, &h->res_v);
@@ -632,7 +681,8 @@ rf_status rf_create(const rf_params* p, rf_handle** out) {
 
     const bool recon = p->method != RF_METHOD_TVL1;
     const int prior = prior_kind(p->method);
-    int n_planes = 2 * h->L + 4 /*i1w, Ix, Iy, Iz*/ + 6 /*duhat, p*/ + 1 /*scratch*/;
+    int n_planes = 2 * h->L + 4 /*i1w, Ix, Iy, Iz*/ + 6 /*duhat, p*/ + 1 /*scratch*/ +
+                   5 /*warm-start staging*/;
     int n_spare = recon ? 31 : 4;
     if (recon) n_planes += 6; /* X, X1 */
     if (prior) n_planes += 6;
@@ -661,11 +711,13 @@ rf_status rf_create(const rf_params* p, rf_handle** out) {
     }
     for (int i = 0; i < n_spare; i++) h->spare.push_back(h->alloc_plane());
     h->scratch = h->alloc_plane();
+    for (int i = 0; i < 5; i++) h->warm[i] = h->alloc_plane();
     // zero everything once: guard rows and never-written padding read as 0
     e = cudaMemset(h->pool, 0, h->pool_floats * sizeof(float));
     if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&h->own_stream, cudaStreamNonBlocking);
     if (e == cudaSuccess) e = cudaMalloc(&h->d_consts, sizeof(LevelConsts) * h->L);
     if (e == cudaSuccess) e = cudaMalloc(&h->d_barrier, 4 * sizeof(unsigned int));
+    if (e == cudaSuccess) e = cudaMalloc(&h->d_energy, 1025 * sizeof(double));
     if (e == cudaSuccess) e = cudaMemset(h->d_barrier, 0, 4 * sizeof(unsigned int));
     if (e == cudaSuccess) e = cudaMallocHost(&h->h_consts, sizeof(LevelConsts) * h->L);
     if (e == cudaSuccess && p->input_type != RF_INPUT_F32) {
@@ -701,6 +753,7 @@ rf_status rf_destroy(rf_handle* h) {
     if (h->pool) cudaFree(h->pool);
     if (h->d_consts) cudaFree(h->d_consts);
     if (h->d_barrier) cudaFree(h->d_barrier);
+    if (h->d_energy) cudaFree(h->d_energy);
     if (h->h_consts) cudaFreeHost(h->h_consts);
     for (void* s : h->staging)
         if (s) cudaFree(s);
@@ -794,11 +847,89 @@ rf_status rf_solve(rf_handle* h, const double R0[9], const double t0[3], const d
     // the pinned block may still feed the previous solve's copy
     RF_CUDA(cudaStreamSynchronize(h->stream));
     level_consts(h, R0, t0, R1, t1, h->h_consts);
+    std::memcpy(h->last_R1, R1, sizeof h->last_R1);
+    std::memcpy(h->last_t1, t1, sizeof h->last_t1);
     RF_CUDA(cudaMemcpyAsync(h->d_consts, h->h_consts, sizeof(LevelConsts) * h->L,
                             cudaMemcpyHostToDevice, h->stream));
     rf_status rs = run_schedule(h, 0);
     h->solved = rs == RF_OK;
     return rs;
+}
+
+static rf_status stage_warm(rf_handle* h, int level, const float* const* src, int n, int pitch,
+                            int on_device, int warps, int iters) {
+    if (level < 0 || level >= h->L) return fail(RF_ERR_INVALID_ARG, "warm start: level out of range");
+    if (pitch < h->W[level]) return fail(RF_ERR_INVALID_ARG, "warm start: pitch < level width");
+    for (int k = 0; k < n; k++)
+        if (!src[k]) return fail(RF_ERR_INVALID_ARG, "warm start: null input plane");
+    const cudaMemcpyKind kind = on_device ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice;
+    for (int k = 0; k < n; k++)
+        RF_CUDA(cudaMemcpy2DAsync(h->warm[k], h->S[level] * sizeof(float), src[k],
+                                  (size_t)pitch * sizeof(float), h->W[level] * sizeof(float),
+                                  h->H[level], kind, h->stream));
+    h->warm_level = level;
+    h->warm_warps = warps < 0 ? h->p.n_warp_iters : warps;
+    h->warm_iters = iters < 0 ? h->p.n_solver_iters : iters;
+    return RF_OK;
+}
+
+rf_status rf_solve_warm(rf_handle* h, const double R0[9], const double t0[3], const double R1[9],
+                        const double t1[3], int level, const float* u, const float* v,
+                        const float* X, const float* Y, const float* Z, int pitch, int on_device,
+                        int warps, int iters) {
+    if (!h || !R1 || !t1) return fail(RF_ERR_INVALID_ARG, "rf_solve_warm: null argument");
+    if (h->p.method != RF_METHODR_TVL1_MS)
+        return fail(RF_ERR_UNSUPPORTED, "rf_solve_warm: warm start runs method 14");
+    if (!h->cams_set || !h->images_set)
+        return fail(RF_ERR_STATE, "rf_solve_warm: cameras or images missing");
+    RF_CUDA(cudaStreamSynchronize(h->stream));
+    const float* src[5] = {u, v, X, Y, Z};
+    rf_status rs = stage_warm(h, level, src, 5, pitch, on_device, warps, iters);
+    if (rs != RF_OK) return rs;
+    const double I[9] = {1, 0, 0, 0, 1, 0, 0, 0, 1};
+    const double z[3] = {0, 0, 0};
+    level_consts(h, R0 ? R0 : I, t0 ? t0 : z, R1, t1, h->h_consts);
+    std::memcpy(h->last_R1, R1, sizeof h->last_R1);
+    std::memcpy(h->last_t1, t1, sizeof h->last_t1);
+    RF_CUDA(cudaMemcpyAsync(h->d_consts, h->h_consts, sizeof(LevelConsts) * h->L,
+                            cudaMemcpyHostToDevice, h->stream));
+    rs = run_schedule(h, 2);
+    h->solved = rs == RF_OK;
+    return rs;
+}
+
+rf_status rf_solve_flow_warm(rf_handle* h, int level, const float* u, const float* v, int pitch,
+                             int on_device, int warps, int iters) {
+    if (!h) return fail(RF_ERR_INVALID_ARG, "rf_solve_flow_warm: null handle");
+    if (h->p.method != RF_METHOD_TVL1)
+        return fail(RF_ERR_STATE, "rf_solve_flow_warm: handle was created for a ReconFlow method");
+    if (!h->images_set) return fail(RF_ERR_STATE, "rf_solve_flow_warm: no images uploaded");
+    RF_CUDA(cudaStreamSynchronize(h->stream));
+    const float* src[2] = {u, v};
+    rf_status rs = stage_warm(h, level, src, 2, pitch, on_device, warps, iters);
+    if (rs != RF_OK) return rs;
+    rs = run_schedule(h, 3);
+    h->solved = rs == RF_OK;
+    return rs;
+}
+
+rf_status rf_energy(rf_handle* h, double* energy) {
+    if (!h || !energy) return fail(RF_ERR_INVALID_ARG, "rf_energy: null argument");
+    if (!h->solved) return fail(RF_ERR_STATE, "rf_energy: no solve has run");
+    const bool recon = h->p.method != RF_METHOD_TVL1;
+    LevelDims d{h->W[0], h->H[0], h->S[0]};
+    const int nb = std::min(1024, (d.w * d.h + 255) / 256);
+    if (launch_energy(h->I0[0], h->I1[0], h->res_u, h->res_v, recon ? h->X : nullptr,
+                      recon ? h->Y : nullptr, recon ? h->Z : nullptr, d, h->p.lambda,
+                      h->p.alpha_proj, recon ? h->last_R1 : nullptr, recon ? h->last_t1 : nullptr,
+                      recon ? h->K1 : nullptr, recon ? 1 : 0, h->d_energy + 1, nb, h->d_energy,
+                      h->stream) != 0)
+        return cuda_fail(cudaGetLastError(), "rf_energy: launch");
+    h->launches += 2;
+    RF_CUDA(cudaMemcpyAsync(energy, h->d_energy, sizeof(double), cudaMemcpyDeviceToHost,
+                            h->stream));
+    RF_CUDA(cudaStreamSynchronize(h->stream));
+    return RF_OK;
 }
 
 rf_status rf_solve_flow(rf_handle* h) {

@@ -162,6 +162,20 @@ class CudaFlow:
         N.check(self._lib.rf_synchronize(self._handle()))
         return 0
 
+    def energy(self) -> float:
+        """Energy of the last solution (rf_energy)."""
+        e = ctypes.c_double()
+        N.check(self._lib.rf_energy(self._handle(), ctypes.byref(e)))
+        return float(e.value)
+
+    def solveOpticalFlowWarm(self, level, u, v, nWarpIters=-1, nSolverIters=-1) -> int:
+        """Plain TV-L1 started at pyramid `level` from flow (u, v) on that level."""
+        a = np.ascontiguousarray(u, np.float32)
+        b = np.ascontiguousarray(v, np.float32)
+        N.check(self._lib.rf_solve_flow_warm(self._handle(), int(level), _ptr(a), _ptr(b),
+                                             a.shape[1], 0, int(nWarpIters), int(nSolverIters)))
+        return 0
+
     def kernelLaunches(self) -> int:
         return int(self._lib.rf_kernel_launches(self._handle()))
 
@@ -251,6 +265,26 @@ class ReconFlow(CudaFlow):
         return 0
 
     solveReconFlow = solveR
+
+    def solveWarm(self, level, u, v, X, Y, Z, R1, t1, nWarpIters=-1, nSolverIters=-1, R0=None,
+                  t0=None, on_device=False) -> int:
+        """ReconFlow started at pyramid `level` from flow and 3D points given on
+        that level (host arrays of shape (h_level, pitch), or device pointers
+        with on_device=True and an explicit pitch via arrays' shape)."""
+        planes = [np.ascontiguousarray(a, np.float32) for a in (u, v, X, Y, Z)]
+        keep = []
+        pose = []
+        for a, n in ((R0, 9), (t0, 3), (R1, 9), (t1, 3)):
+            if a is None:
+                pose.append(None)
+            else:
+                arr, p_ = _dbl(a, n)
+                keep.append(arr)
+                pose.append(p_)
+        N.check(self._lib.rf_solve_warm(self._handle(), *pose, int(level),
+                                        *[_ptr(a) for a in planes], planes[0].shape[1], 0,
+                                        int(nWarpIters), int(nSolverIters)))
+        return 0
 
     def copy3dToHost(self, X=None, Y=None, Z=None):
         """ReconFlow::copy3dToHost (Reconflow.cu:65-70); returns (X, Y, Z)."""

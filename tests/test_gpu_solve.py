@@ -268,3 +268,86 @@ def test_degenerate_baseline_nan_parity(oracle, rf, level_mode):
     got, _ = run_gpu(rf, w, h, L, 14, I0, I1, K, np.eye(3), np.array([-0.1, 0.0, 0.0]), **kw)
     want = run_oracle(oracle, w, h, L, 14, I0, I1, K, np.eye(3), np.array([-0.1, 0.0, 0.0]), **kw)
     compare(got, want, w, h)
+
+
+@pytest.mark.parametrize("level", [0, 1, 2])
+def test_warm_start_bitexact(oracle, rf, level):
+    """A solve started at `level` from a given flow and 3D state matches the
+    oracle's warm-started schedule bit for bit."""
+    w, h, L = 96, 72, 3
+    rng = np.random.default_rng(level)
+    s = align_up(w)
+    I0, I1 = textured_pair(rng, h, w)
+    I0, I1 = pad_rows(I0, s), pad_rows(I1, s)
+    K = _K(w, h)
+    R, t = _pose(7)
+    W, H, S = oracle.pyramid_dims(w, h, L)
+    hl, sl = H[level], S[level]
+    u0 = rng.normal(1.0, 0.2, (hl, sl)).astype(np.float32)
+    v0 = rng.normal(-0.5, 0.2, (hl, sl)).astype(np.float32)
+    Z0 = rng.uniform(2, 6, (hl, sl)).astype(np.float32)
+    X0 = (Z0 * rng.normal(0, 0.3, (hl, sl))).astype(np.float32)
+    Y0 = (Z0 * rng.normal(0, 0.3, (hl, sl))).astype(np.float32)
+    f = rf.ReconFlow()
+    f.initializeR(w, h, 1, L, 2.0, 14, 50.0, 0.0, 0.1, 100.0, 1 / 0.33, 60.0, 0.5, 0.25, 3, 10,
+                  cvType=5, fix_quirks=1)
+    f.setCameraMatrices(K, K)
+    f.copyImagesToDevice(I0, I1)
+    f.solveWarm(level, u0, v0, X0, Y0, Z0, R, t, 2, 4)
+    u, v = f.copyOpticalFlowToHost()
+    X, Y, Z = f.copy3dToHost()
+    p = oracle.make_params(w, h, L, lam=50.0, lambdaf=0.1, lambdams=100.0, alpha_tv=1 / 0.33,
+                           alpha_proj=60.0, tau=0.25, n_warp_iters=3, n_solver_iters=10,
+                           fix_quirks=1)
+    pad = lambda a: np.pad(a, ((0, 1), (0, 0))).ravel()  # noqa: E731  (guard row)
+    want = oracle.solve_warm(p, I0, I1, level, pad(u0), pad(v0), pad(X0), pad(Y0), pad(Z0), 2, 4,
+                             K0=K, K1=K, R1=R, t1=t)
+    compare({"u": u, "v": v, "X": X, "Y": Y, "Z": Z}, want, w, h)
+    # a full solve afterwards re-captures the normal schedule
+    f.solveR(R, t, 5.0)
+    full = run_oracle(oracle, w, h, L, 14, I0, I1, K, R, t, warps=3, iters=10, fix=1)
+    assert_bitexact(f.copyOpticalFlowToHost()[0], full["u"], "u after warm", region=(h, w))
+
+
+def test_plain_warm_start_bitexact(oracle, rf):
+    w, h, L, level = 80, 60, 3, 1
+    rng = np.random.default_rng(3)
+    s = align_up(w)
+    I0, I1 = textured_pair(rng, h, w)
+    I0, I1 = pad_rows(I0, s), pad_rows(I1, s)
+    W, H, S = oracle.pyramid_dims(w, h, L)
+    u0 = rng.normal(0.8, 0.1, (H[level], S[level])).astype(np.float32)
+    v0 = rng.normal(-0.4, 0.1, (H[level], S[level])).astype(np.float32)
+    f = rf.CudaFlow()
+    f.initialize(w, h, 1, 5, L, 2.0, 0, 50.0, 0.0, 0.33, 0.25, 2, 6)
+    f.copyImagesToDevice(I0, I1)
+    f.solveOpticalFlowWarm(level, u0, v0, 1, 5)
+    u, v = f.copyOpticalFlowToHost()
+    p = oracle.make_params(w, h, L, method=0, lam=50.0, theta=0.33, tau=0.25, n_warp_iters=2,
+                           n_solver_iters=6)
+    z = np.zeros((H[level] + 1) * S[level], np.float32)
+    pad = lambda a: np.pad(a, ((0, 1), (0, 0))).ravel()  # noqa: E731
+    want = oracle.solve_warm(p, I0, I1, level, pad(u0), pad(v0), z, z, z, 1, 5)
+    assert_bitexact(u, want["u"], "u", region=(h, w))
+    assert_bitexact(v, want["v"], "v", region=(h, w))
+
+
+@pytest.mark.parametrize("method", [14, 0])
+def test_energy_matches_oracle(oracle, rf, method):
+    w, h, L = 96, 64, 3
+    rng = np.random.default_rng(9)
+    s = align_up(w)
+    I0, I1 = textured_pair(rng, h, w)
+    I0, I1 = pad_rows(I0, s), pad_rows(I1, s)
+    K = _K(w, h)
+    R, t = _pose(8)
+    res, f = run_gpu(rf, w, h, L, method, I0, I1, K, R, t, warps=2, iters=5, fix=1)
+    e_gpu = f.energy()
+    if method == 0:
+        z = np.zeros_like(res["u"])
+        e_ref = oracle.energy(I0, I1, res["u"], res["v"], z, z, z, w, h, s, 50.0, 60.0, np.eye(3),
+                              np.zeros(3), np.eye(3), recon=False)
+    else:
+        e_ref = oracle.energy(I0, I1, res["u"], res["v"], res["X"], res["Y"], res["Z"], w, h, s,
+                              50.0, 60.0, R, t, K)
+    assert e_gpu == pytest.approx(e_ref, rel=1e-9)
