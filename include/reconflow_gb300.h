@@ -257,6 +257,39 @@ RF_API rf_status rf_batch_synchronize(rf_batch* b);
 RF_API uint64_t rf_batch_kernel_launches(const rf_batch* b);
 
 /* ------------------------------------------------------------------------
+ * Learned warm start network (no reference counterpart): a small BF16
+ * convolutional encoder-decoder run and trained with this library's own
+ * tensor-core kernels.  Tensors are float32 NHWC in device memory.  Input:
+ * 16 channels at the network's input resolution H x W (I0, I1, x and y in
+ * [-0.5, 0.5], rotation vector x 30, translation x 10, zeros).  Outputs: 8
+ * channels (u, v, inverse depth, then unused) at (H+1)/2 x (W+1)/2 ("out16")
+ * and at H x W ("out8").
+ * ---------------------------------------------------------------------- */
+typedef struct rf_cnn rf_cnn;
+
+/* Allocates for up to max_batch samples of up to height x width pixels;
+ * weights He-initialised from `seed`. */
+RF_API rf_status rf_cnn_create(int max_batch, int height, int width, unsigned long long seed,
+                               rf_cnn** out);
+RF_API rf_status rf_cnn_destroy(rf_cnn* c);
+RF_API int rf_cnn_num_params(const rf_cnn* c);
+RF_API rf_status rf_cnn_set_stream(rf_cnn* c, void* stream);
+/* FP32 master weights (host, rf_cnn_num_params floats) */
+RF_API rf_status rf_cnn_get_params(rf_cnn* c, float* host);
+RF_API rf_status rf_cnn_set_params(rf_cnn* c, const float* host);
+/* gradient of the last rf_cnn_backward (host, rf_cnn_num_params floats) */
+RF_API rf_status rf_cnn_get_grads(rf_cnn* c, float* host);
+RF_API rf_status rf_cnn_forward(rf_cnn* c, const float* input, int batch, int height, int width,
+                                float* out16, float* out8);
+/* forward + masked L1 loss (channel weights w[0..2] for u, v, inverse depth,
+ * each scale averaged over its pixels) + backward; *loss (host) may be NULL */
+RF_API rf_status rf_cnn_backward(rf_cnn* c, const float* input, const float* tgt16,
+                                 const float* mask16, const float* tgt8, const float* mask8,
+                                 int batch, int height, int width, const float* w, double* loss);
+RF_API rf_status rf_cnn_adam_step(rf_cnn* c, float lr, float beta1, float beta2, float eps);
+RF_API uint64_t rf_cnn_kernel_launches(const rf_cnn* c);
+
+/* ------------------------------------------------------------------------
  * Kernel-level entry points (device pointers, caller's stream).  Each runs
  * one reference kernel's computation on one pyramid level so it can be
  * checked against the oracle in isolation.  Arrays are stride-major planes

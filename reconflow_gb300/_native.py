@@ -90,6 +90,18 @@ _SIGS = [
     ("rf_batch_set_stream", _I, [_VP, _VP]),
     ("rf_batch_synchronize", _I, [_VP]),
     ("rf_batch_kernel_launches", ctypes.c_uint64, [_VP]),
+    ("rf_cnn_create", _I, [_I, _I, _I, ctypes.c_ulonglong, ctypes.POINTER(_VP)]),
+    ("rf_cnn_destroy", _I, [_VP]),
+    ("rf_cnn_num_params", _I, [_VP]),
+    ("rf_cnn_set_stream", _I, [_VP, _VP]),
+    ("rf_cnn_get_params", _I, [_VP, _VP]),
+    ("rf_cnn_set_params", _I, [_VP, _VP]),
+    ("rf_cnn_get_grads", _I, [_VP, _VP]),
+    ("rf_cnn_forward", _I, [_VP, _VP, _I, _I, _I, _VP, _VP]),
+    ("rf_cnn_backward", _I, [_VP, _VP, _VP, _VP, _VP, _VP, _I, _I, _I, _VP,
+                             ctypes.POINTER(ctypes.c_double)]),
+    ("rf_cnn_adam_step", _I, [_VP, _F, _F, _F, _F]),
+    ("rf_cnn_kernel_launches", ctypes.c_uint64, [_VP]),
     ("rfk_downscale", _I, [_VP, _I, _I, _I, _I, _I, _I, _F, _I, _VP, _VP]),
     ("rfk_upscale", _I, [_VP, _I, _I, _I, _I, _I, _I, _F, _VP, _VP]),
     ("rfk_warp", _I, [_VP, _I, _I, _I, _VP, _VP, _VP, _VP]),

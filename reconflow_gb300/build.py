@@ -28,6 +28,8 @@ SOURCES = {
     "rf_solver.cu": ["-fmad=false"],
     "rf_noalloc.cu": ["-fmad=false"],
     "rf_batch.cu": ["-fmad=false"],
+    # the learned warm start: BF16 tensor-core convolutions, FP32 accumulation
+    "rf_cnn.cu": [],
 }
 COMMON = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC,-ffp-contract=off,-fvisibility=hidden",
           "--expt-relaxed-constexpr", "-I" + os.path.join(ROOT, "include"), "-I" + CSRC]

@@ -1,0 +1,668 @@
+// Learned warm start: a small convolutional encoder-decoder that maps a
+// coarse image pair (+ pixel coordinates and camera pose) to flow and inverse
+// depth at two scales, trained on the GPU with hand-written forward and
+// backward kernels.  No counterpart in the reference.
+//
+// Network (NHWC, 3x3 convolutions, padding 1):
+//   in  (16 ch: I0, I1, x, y, rotation vector, translation, zeros)
+//   c1  16 -> 32, ReLU                      (input resolution, "1/8")
+//   c2  32 -> 96, stride 2, ReLU            (half resolution, "1/16")
+//   c3  96 -> 96, ReLU
+//   h16 96 -> 8 (u, v, inverse depth, 5 unused), linear   -> output at 1/16
+//   cat [nearest-upsampled c3 (96), c1 (32)] = 128 channels
+//   c4  128 -> 64, ReLU
+//   h8  64 -> 8, linear                                    -> output at 1/8
+// Weights and activations are BF16, accumulation FP32; the master weights
+// and Adam moments are FP32.
+//
+// Every convolution (forward, gradient of its input, gradient of its
+// weights) is one implicit GEMM on the tensor cores: mma.sync m16n8k16 with
+// BF16 operands and FP32 accumulators, operands gathered on the fly.  The
+// weight gradient splits the pixel (reduction) dimension into chunks with
+// partial sums reduced in a fixed order, so training is deterministic.
+#include <algorithm>
+#include <cmath>
+#include <cstdint>
+#include <cstdio>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include <cuda_bf16.h>
+#include <cuda_runtime.h>
+
+#include "../../include/reconflow_gb300.h"
+#include "rf_kernels.cuh"
+
+namespace rf_cnn_impl {
+
+typedef __nv_bfloat16 bf16;
+
+__device__ __forceinline__ uint32_t pack2(bf16 lo, bf16 hi) {
+    return (uint32_t)__bfloat16_as_ushort(lo) | ((uint32_t)__bfloat16_as_ushort(hi) << 16);
+}
+
+__device__ __forceinline__ void mma16816(float (&d)[4], uint32_t a0, uint32_t a1, uint32_t a2,
+                                         uint32_t a3, uint32_t b0, uint32_t b1) {
+    asm volatile(
+        "mma.sync.aligned.m16n8k16.row.col.f32.bf16.bf16.f32 {%0,%1,%2,%3}, {%4,%5,%6,%7}, "
+        "{%8,%9}, {%0,%1,%2,%3};\n"
+        : "+f"(d[0]), "+f"(d[1]), "+f"(d[2]), "+f"(d[3])
+        : "r"(a0), "r"(a1), "r"(a2), "r"(a3), "r"(b0), "r"(b1));
+}
+
+// C[M x N] (+)= sum_k A(m, k) B(k, n), one warp per 16x8 tile; blockIdx.y
+// selects a chunk of the K range (split-K).  Functors return 0 outside their
+// tensors, so M, N, K need no padding.
+template <class FA, class FB, class FC>
+__global__ void k_igemm(int M, int N, int K, int kchunk, FA fa, FB fb, FC fc) {
+    const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const int lane = threadIdx.x & 31;
+    const int tilesN = (N + 7) >> 3;
+    const int tm = warp / tilesN, tn = warp - tm * tilesN;
+    if (tm * 16 >= M) return;
+    const int m0 = tm * 16, n0 = tn * 8;
+    const int g = lane >> 2, q = (lane & 3) * 2;
+    const int kb = blockIdx.y * kchunk;
+    const int ke = min(K, kb + kchunk);
+    float acc[4] = {0.f, 0.f, 0.f, 0.f};
+    for (int k0 = kb; k0 < ke; k0 += 16) {
+        uint32_t a0 = pack2(fa(m0 + g, k0 + q), fa(m0 + g, k0 + q + 1));
+        uint32_t a1 = pack2(fa(m0 + g + 8, k0 + q), fa(m0 + g + 8, k0 + q + 1));
+        uint32_t a2 = pack2(fa(m0 + g, k0 + q + 8), fa(m0 + g, k0 + q + 9));
+        uint32_t a3 = pack2(fa(m0 + g + 8, k0 + q + 8), fa(m0 + g + 8, k0 + q + 9));
+        uint32_t b0 = pack2(fb(k0 + q, n0 + g), fb(k0 + q + 1, n0 + g));
+        uint32_t b1 = pack2(fb(k0 + q + 8, n0 + g), fb(k0 + q + 9, n0 + g));
+        mma16816(acc, a0, a1, a2, a3, b0, b1);
+    }
+    fc(blockIdx.y, m0 + g, n0 + q, acc[0]);
+    fc(blockIdx.y, m0 + g, n0 + q + 1, acc[1]);
+    fc(blockIdx.y, m0 + g + 8, n0 + q, acc[2]);
+    fc(blockIdx.y, m0 + g + 8, n0 + q + 1, acc[3]);
+}
+
+struct Shape {
+    int B, H, W, C;  // NHWC
+};
+
+// A for the forward conv: (output pixel, k = (ky*3 + kx)*Cin + ci)
+struct ConvIn {
+    const bf16* x;
+    Shape in;
+    int Ho, Wo, stride, K;
+    __device__ bf16 operator()(int m, int k) const {
+        if (k >= K || m >= in.B * Ho * Wo) return __float2bfloat16(0.f);
+        int ci = k % in.C, t = k / in.C, kx = t % 3, ky = t / 3;
+        int xo = m % Wo, r = m / Wo, yo = r % Ho, b = r / Ho;
+        int y = yo * stride + ky - 1, xx = xo * stride + kx - 1;
+        if (y < 0 || y >= in.H || xx < 0 || xx >= in.W) return __float2bfloat16(0.f);
+        return x[(((size_t)b * in.H + y) * in.W + xx) * in.C + ci];
+    }
+};
+
+// B for the forward conv: weights [Cout][3][3][Cin], (k, n = co)
+struct ConvW {
+    const bf16* w;
+    int K, Cout;
+    __device__ bf16 operator()(int k, int n) const {
+        if (k >= K || n >= Cout) return __float2bfloat16(0.f);
+        return w[(size_t)n * K + k];
+    }
+};
+
+// forward epilogue: + bias, optional ReLU; BF16 activation and/or FP32 copy
+struct ConvOut {
+    const float* bias;
+    bf16* y;
+    float* yf;
+    int M, Cout, relu;
+    __device__ void operator()(int, int m, int n, float v) const {
+        if (m >= M || n >= Cout) return;
+        v += bias[n];
+        if (relu) v = fmaxf(v, 0.f);
+        if (y) y[(size_t)m * Cout + n] = __float2bfloat16(v);
+        if (yf) yf[(size_t)m * Cout + n] = v;
+    }
+};
+
+// A for the input gradient: (input pixel, k = (ky*3 + kx)*Cout + co) reads the
+// output gradient at the output pixel that tap (ky, kx) of the input pixel
+// feeds.
+struct DataGradA {
+    const bf16* dy;
+    Shape in;
+    int Ho, Wo, Cout, stride, K;
+    __device__ bf16 operator()(int m, int k) const {
+        if (k >= K || m >= in.B * in.H * in.W) return __float2bfloat16(0.f);
+        int co = k % Cout, t = k / Cout, kx = t % 3, ky = t / 3;
+        int xx = m % in.W, r = m / in.W, y = r % in.H, b = r / in.H;
+        int ty = y + 1 - ky, tx = xx + 1 - kx;
+        if (ty < 0 || tx < 0 || ty % stride || tx % stride) return __float2bfloat16(0.f);
+        int yo = ty / stride, xo = tx / stride;
+        if (yo >= Ho || xo >= Wo) return __float2bfloat16(0.f);
+        return dy[(((size_t)b * Ho + yo) * Wo + xo) * Cout + co];
+    }
+};
+
+// B for the input gradient: (k = (ky*3 + kx)*Cout + co, n = ci) = W[co][ky][kx][ci]
+struct DataGradB {
+    const bf16* w;
+    int Cin, Cout, K;
+    __device__ bf16 operator()(int k, int n) const {
+        if (k >= K || n >= Cin) return __float2bfloat16(0.f);
+        int co = k % Cout, t = k / Cout;
+        return w[((size_t)co * 9 + t) * Cin + n];
+    }
+};
+
+struct StoreF32 {
+    float* out;
+    int M, N;
+    __device__ void operator()(int, int m, int n, float v) const {
+        if (m < M && n < N) out[(size_t)m * N + n] = v;
+    }
+};
+
+// A for the weight gradient: (m = co, k = output pixel) = dy[pixel][co]
+struct WGradA {
+    const bf16* dy;
+    int P, Cout;
+    __device__ bf16 operator()(int m, int k) const {
+        if (m >= Cout || k >= P) return __float2bfloat16(0.f);
+        return dy[(size_t)k * Cout + m];
+    }
+};
+
+// B for the weight gradient: (k = output pixel, n = (ky*3 + kx)*Cin + ci)
+struct WGradB {
+    const bf16* x;
+    Shape in;
+    int Ho, Wo, stride, P, N;
+    __device__ bf16 operator()(int k, int n) const {
+        if (k >= P || n >= N) return __float2bfloat16(0.f);
+        int ci = n % in.C, t = n / in.C, kx = t % 3, ky = t / 3;
+        int xo = k % Wo, r = k / Wo, yo = r % Ho, b = r / Ho;
+        int y = yo * stride + ky - 1, xx = xo * stride + kx - 1;
+        if (y < 0 || y >= in.H || xx < 0 || xx >= in.W) return __float2bfloat16(0.f);
+        return x[(((size_t)b * in.H + y) * in.W + xx) * in.C + ci];
+    }
+};
+
+struct StorePartial {
+    float* part;  // [chunk][M][N]
+    int M, N;
+    __device__ void operator()(int chunk, int m, int n, float v) const {
+        if (m < M && n < N) part[((size_t)chunk * M + m) * N + n] = v;
+    }
+};
+
+__global__ void k_reduce_partials(const float* part, int chunks, int n, float* out) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    float s = 0.f;
+    for (int c = 0; c < chunks; c++) s += part[(size_t)c * n + i];
+    out[i] = s;
+}
+
+// bias gradient: sum over pixels of dy (f32), fixed order per channel
+__global__ void k_bias_grad(const float* dy, int P, int C, float* db) {
+    int c = blockIdx.x * blockDim.x + threadIdx.x;
+    if (c >= C) return;
+    float s = 0.f;
+    for (int p = 0; p < P; p++) s += dy[(size_t)p * C + c];
+    db[c] = s;
+}
+
+__global__ void k_f32_to_bf16(const float* a, bf16* b, size_t n) {
+    size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) b[i] = __float2bfloat16(a[i]);
+}
+
+// dy = g * [activation > 0] (ReLU backward), in place on g, and a BF16 copy
+__global__ void k_relu_grad(float* g, const bf16* act, bf16* gb, size_t n) {
+    size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    float v = __bfloat162float(act[i]) > 0.f ? g[i] : 0.f;
+    g[i] = v;
+    gb[i] = __float2bfloat16(v);
+}
+
+// cat = [nearest 2x upsample of a (Ha x Wa x Ca), b (H x W x Cb)]
+__global__ void k_concat_up(const bf16* a, int Ha, int Wa, int Ca, const bf16* b, int Cb,
+                            int Bn, int H, int W, bf16* cat) {
+    size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    size_t n = (size_t)Bn * H * W * (Ca + Cb);
+    if (i >= n) return;
+    int C = Ca + Cb;
+    int c = i % C;
+    size_t p = i / C;
+    int x = p % W, r = p / W, y = r % H, bb = r / H;
+    if (c < Ca)
+        cat[i] = a[(((size_t)bb * Ha + y / 2) * Wa + x / 2) * Ca + c];
+    else
+        cat[i] = b[p * Cb + (c - Ca)];
+}
+
+// split the concat gradient: d_a (half resolution) += sum of its 2x2
+// children; d_b (+)= the rest.  accumulate != 0 adds to the existing values.
+__global__ void k_concat_up_grad(const float* dcat, int Ha, int Wa, int Ca, int Cb, int Bn,
+                                 int H, int W, float* da, float* db, int accumulate_b) {
+    size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    size_t na = (size_t)Bn * Ha * Wa * Ca;
+    size_t nb = (size_t)Bn * H * W * Cb;
+    int C = Ca + Cb;
+    if (i < na) {
+        int c = i % Ca;
+        size_t p = i / Ca;
+        int x = p % Wa, r = p / Wa, y = r % Ha, bb = r / Ha;
+        float s = 0.f;
+        for (int dy = 0; dy < 2; dy++)
+            for (int dx = 0; dx < 2; dx++) {
+                int yy = 2 * y + dy, xx = 2 * x + dx;
+                if (yy < H && xx < W) s += dcat[(((size_t)bb * H + yy) * W + xx) * C + c];
+            }
+        da[i] += s;
+    }
+    if (i < nb) {
+        int c = i % Cb;
+        size_t p = i / Cb;
+        float v = dcat[p * C + Ca + c];
+        db[i] = accumulate_b ? db[i] + v : v;
+    }
+}
+
+// L1 loss on channels 0..2 with per-channel weights, masked; writes dL/dpred
+// (already divided by the number of valid pixels) and accumulates the loss.
+__global__ void k_l1_loss(const float* pred, const float* tgt, const float* mask, int P, int C,
+                          float w0, float w1, float w2, float inv_count, float* grad,
+                          double* loss) {
+    int p = blockIdx.x * blockDim.x + threadIdx.x;
+    double l = 0.0;
+    if (p < P) {
+        float m = mask[p];
+        for (int c = 0; c < C; c++) {
+            float g = 0.f;
+            if (c < 3 && m > 0.f) {
+                float wc = c == 0 ? w0 : (c == 1 ? w1 : w2);
+                float d = pred[(size_t)p * C + c] - tgt[(size_t)p * C + c];
+                l += (double)(wc * fabsf(d)) * inv_count;
+                g = (d > 0.f ? wc : (d < 0.f ? -wc : 0.f)) * inv_count;
+            }
+            grad[(size_t)p * C + c] = g;
+        }
+    }
+    for (int o = 16; o > 0; o >>= 1) l += __shfl_down_sync(0xffffffffu, l, o);
+    if ((threadIdx.x & 31) == 0) atomicAdd(loss, l);
+}
+
+__global__ void k_adam(float* w, const float* g, float* m, float* v, size_t n, float lr, float b1,
+                       float b2, float eps, float c1, float c2) {
+    size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    float gi = g[i];
+    float mi = b1 * m[i] + (1.f - b1) * gi;
+    float vi = b2 * v[i] + (1.f - b2) * gi * gi;
+    m[i] = mi;
+    v[i] = vi;
+    float mh = mi / c1, vh = vi / c2;
+    w[i] -= lr * mh / (sqrtf(vh) + eps);
+}
+
+__global__ void k_add(float* a, const float* b, size_t n) {
+    size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) a[i] += b[i];
+}
+
+inline unsigned blocks_for(size_t n, int t = 256) { return (unsigned)((n + t - 1) / t); }
+
+struct Layer {
+    int cin, cout, stride, relu;
+    size_t woff, boff;  // offsets into the parameter vector
+};
+
+}  // namespace rf_cnn_impl
+
+using namespace rf_cnn_impl;
+
+struct rf_cnn {
+    int max_batch = 0, H = 0, W = 0;  // input resolution
+    std::vector<Layer> layers;        // c1, c2, c3, h16, c4, h8
+    size_t n_params = 0;
+    float *w = nullptr, *g = nullptr, *m = nullptr, *v = nullptr;  // FP32 master, grad, Adam
+    bf16* wb = nullptr;               // BF16 copy used by the kernels
+    int step = 0;
+    // activations (BF16) and gradients (FP32 / BF16)
+    bf16 *x = nullptr, *a1 = nullptr, *a2 = nullptr, *a3 = nullptr, *cat = nullptr, *a4 = nullptr;
+    float *o16 = nullptr, *o8 = nullptr;
+    float *g_o16 = nullptr, *g_o8 = nullptr, *g_a4 = nullptr, *g_cat = nullptr, *g_a3 = nullptr,
+          *g_a2 = nullptr, *g_a1 = nullptr;
+    bf16* gb = nullptr;   // BF16 staging of the gradient being propagated
+    float* part = nullptr;
+    size_t part_floats = 0;
+    double* d_loss = nullptr;
+    cudaStream_t stream = nullptr;
+    uint64_t launches = 0;
+};
+
+namespace rf_cnn_impl {
+
+rf_status cfail(rf_status st, const std::string& msg) {
+    return static_cast<rf_status>(rf::set_last_error(st, msg.c_str()));
+}
+
+#define CN(call)                                                                      \
+    do {                                                                              \
+        cudaError_t e__ = (call);                                                     \
+        if (e__ != cudaSuccess)                                                       \
+            return cfail(RF_ERR_CUDA, std::string(#call ": ") + cudaGetErrorString(e__)); \
+    } while (0)
+
+int Ho_of(int H, int s) { return s == 1 ? H : (H + 1) / 2; }
+
+template <class FA, class FB, class FC>
+rf_status gemm(rf_cnn* c, int M, int N, int K, int chunks, FA fa, FB fb, FC fc) {
+    int kchunk = ((K + chunks - 1) / chunks + 15) / 16 * 16;
+    chunks = (K + kchunk - 1) / kchunk;
+    long long warps = (long long)((M + 15) / 16) * ((N + 7) / 8);
+    dim3 grid((unsigned)((warps * 32 + 127) / 128), chunks);
+    k_igemm<<<grid, 128, 0, c->stream>>>(M, N, K, kchunk, fa, fb, fc);
+    c->launches++;
+    CN(cudaGetLastError());
+    return RF_OK;
+}
+
+// forward conv of layer L: x (B x H x W x cin) -> y (BF16) and/or yf (FP32)
+rf_status conv_fwd(rf_cnn* c, const Layer& L, const bf16* x, int B, int H, int W, bf16* y,
+                   float* yf) {
+    int Ho = Ho_of(H, L.stride), Wo = Ho_of(W, L.stride);
+    int M = B * Ho * Wo, K = 9 * L.cin;
+    ConvIn fa{x, Shape{B, H, W, L.cin}, Ho, Wo, L.stride, K};
+    ConvW fb{c->wb + L.woff, K, L.cout};
+    ConvOut fc{c->w + L.boff, y, yf, M, L.cout, L.relu};
+    return gemm(c, M, L.cout, K, 1, fa, fb, fc);
+}
+
+// backward of layer L given dy (FP32, already through the ReLU mask) and its
+// BF16 copy: weight and bias gradients, and the input gradient if dx != null
+rf_status conv_bwd(rf_cnn* c, const Layer& L, const bf16* x, int B, int H, int W,
+                   const float* dy, const bf16* dyb, float* dx) {
+    int Ho = Ho_of(H, L.stride), Wo = Ho_of(W, L.stride);
+    int P = B * Ho * Wo, N = 9 * L.cin;
+    int chunks = std::max(1, std::min(256, P / 2048));
+    size_t need = (size_t)chunks * L.cout * N;
+    if (need > c->part_floats) return cfail(RF_ERR_STATE, "cnn: partial buffer too small");
+    rf_status rs = gemm(c, L.cout, N, P, chunks, WGradA{dyb, P, L.cout},
+                        WGradB{x, Shape{B, H, W, L.cin}, Ho, Wo, L.stride, P, N},
+                        StorePartial{c->part, L.cout, N});
+    if (rs != RF_OK) return rs;
+    int kchunk = ((P + chunks - 1) / chunks + 15) / 16 * 16;
+    int used = (P + kchunk - 1) / kchunk;
+    k_reduce_partials<<<blocks_for((size_t)L.cout * N), 256, 0, c->stream>>>(
+        c->part, used, L.cout * N, c->g + L.woff);
+    k_bias_grad<<<blocks_for(L.cout, 64), 64, 0, c->stream>>>(dy, P, L.cout, c->g + L.boff);
+    c->launches += 2;
+    if (dx) {
+        int M = B * H * W, K = 9 * L.cout;
+        rs = gemm(c, M, L.cin, K, 1, DataGradA{dyb, Shape{B, H, W, L.cin}, Ho, Wo, L.cout, L.stride, K},
+                  DataGradB{c->wb + L.woff, L.cin, L.cout, K}, StoreF32{dx, M, L.cin});
+        if (rs != RF_OK) return rs;
+    }
+    CN(cudaGetLastError());
+    return RF_OK;
+}
+
+rf_status sync_bf16_weights(rf_cnn* c) {
+    k_f32_to_bf16<<<blocks_for(c->n_params), 256, 0, c->stream>>>(c->w, c->wb, c->n_params);
+    c->launches++;
+    CN(cudaGetLastError());
+    return RF_OK;
+}
+
+rf_status forward(rf_cnn* c, const float* input, int B, int H, int W) {
+    const Layer &c1 = c->layers[0], &c2 = c->layers[1], &c3 = c->layers[2], &h16 = c->layers[3],
+                &c4 = c->layers[4], &h8 = c->layers[5];
+    size_t nin = (size_t)B * H * W * 16;
+    k_f32_to_bf16<<<blocks_for(nin), 256, 0, c->stream>>>(input, c->x, nin);
+    c->launches++;
+    int H2 = Ho_of(H, 2), W2 = Ho_of(W, 2);
+    rf_status rs = conv_fwd(c, c1, c->x, B, H, W, c->a1, nullptr);
+    if (rs == RF_OK) rs = conv_fwd(c, c2, c->a1, B, H, W, c->a2, nullptr);
+    if (rs == RF_OK) rs = conv_fwd(c, c3, c->a2, B, H2, W2, c->a3, nullptr);
+    if (rs == RF_OK) rs = conv_fwd(c, h16, c->a3, B, H2, W2, nullptr, c->o16);
+    if (rs != RF_OK) return rs;
+    size_t ncat = (size_t)B * H * W * (c3.cout + c1.cout);
+    k_concat_up<<<blocks_for(ncat), 256, 0, c->stream>>>(c->a3, H2, W2, c3.cout, c->a1, c1.cout,
+                                                         B, H, W, c->cat);
+    c->launches++;
+    rs = conv_fwd(c, c4, c->cat, B, H, W, c->a4, nullptr);
+    if (rs == RF_OK) rs = conv_fwd(c, h8, c->a4, B, H, W, nullptr, c->o8);
+    return rs;
+}
+
+rf_status backward(rf_cnn* c, int B, int H, int W) {
+    const Layer &c1 = c->layers[0], &c2 = c->layers[1], &c3 = c->layers[2], &h16 = c->layers[3],
+                &c4 = c->layers[4], &h8 = c->layers[5];
+    int H2 = Ho_of(H, 2), W2 = Ho_of(W, 2);
+    size_t n8 = (size_t)B * H * W * 8, n16 = (size_t)B * H2 * W2 * 8;
+    // heads (linear)
+    k_f32_to_bf16<<<blocks_for(n8), 256, 0, c->stream>>>(c->g_o8, c->gb, n8);
+    rf_status rs = conv_bwd(c, h8, c->a4, B, H, W, c->g_o8, c->gb, c->g_a4);
+    if (rs != RF_OK) return rs;
+    size_t n4 = (size_t)B * H * W * c4.cout;
+    k_relu_grad<<<blocks_for(n4), 256, 0, c->stream>>>(c->g_a4, c->a4, c->gb, n4);
+    rs = conv_bwd(c, c4, c->cat, B, H, W, c->g_a4, c->gb, c->g_cat);
+    if (rs != RF_OK) return rs;
+    // split the concat gradient: g_a3 = up^T(g_cat[:96]), g_a1 = g_cat[96:]
+    size_t n3 = (size_t)B * H2 * W2 * c3.cout;
+    size_t n1 = (size_t)B * H * W * c1.cout;
+    CN(cudaMemsetAsync(c->g_a3, 0, n3 * sizeof(float), c->stream));
+    k_concat_up_grad<<<blocks_for(std::max(n3, n1)), 256, 0, c->stream>>>(
+        c->g_cat, H2, W2, c3.cout, c1.cout, B, H, W, c->g_a3, c->g_a1, 0);
+    // 1/16 head adds into g_a3
+    k_f32_to_bf16<<<blocks_for(n16), 256, 0, c->stream>>>(c->g_o16, c->gb, n16);
+    float* tmp = c->g_a2;  // scratch for the head's input gradient (same size as g_a3)
+    rs = conv_bwd(c, h16, c->a3, B, H2, W2, c->g_o16, c->gb, tmp);
+    if (rs != RF_OK) return rs;
+    // g_a3 += tmp (reuse the ReLU kernel path: add then mask)
+    k_add<<<blocks_for(n3), 256, 0, c->stream>>>(c->g_a3, tmp, n3);
+    k_relu_grad<<<blocks_for(n3), 256, 0, c->stream>>>(c->g_a3, c->a3, c->gb, n3);
+    rs = conv_bwd(c, c3, c->a2, B, H2, W2, c->g_a3, c->gb, c->g_a2);
+    if (rs != RF_OK) return rs;
+    size_t n2 = (size_t)B * H2 * W2 * c2.cout;
+    k_relu_grad<<<blocks_for(n2), 256, 0, c->stream>>>(c->g_a2, c->a2, c->gb, n2);
+    // c2's input gradient adds into g_a1 (which holds the skip part): use tmp2
+    float* tmp2 = c->g_a4;  // free now, large enough (B*H*W*64 >= B*H*W*32)
+    rs = conv_bwd(c, c2, c->a1, B, H, W, c->g_a2, c->gb, tmp2);
+    if (rs != RF_OK) return rs;
+    k_add<<<blocks_for(n1), 256, 0, c->stream>>>(c->g_a1, tmp2, n1);
+    k_relu_grad<<<blocks_for(n1), 256, 0, c->stream>>>(c->g_a1, c->a1, c->gb, n1);
+    rs = conv_bwd(c, c1, c->x, B, H, W, c->g_a1, c->gb, nullptr);
+    c->launches += 9;
+    if (rs != RF_OK) return rs;
+    CN(cudaGetLastError());
+    return RF_OK;
+}
+
+}  // namespace rf_cnn_impl
+
+extern "C" {
+
+rf_status rf_cnn_create(int max_batch, int height, int width, unsigned long long seed,
+                        rf_cnn** out) {
+    if (!out || max_batch < 1 || height < 2 || width < 2 || (long long)max_batch * height * width > (1LL << 26))
+        return cfail(RF_ERR_INVALID_ARG, "rf_cnn_create: bad size");
+    int ndev = 0;
+    if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev < 1)
+        return cfail(RF_ERR_NO_DEVICE, "rf_cnn_create: no CUDA device");
+    rf_cnn* c = new rf_cnn();
+    c->max_batch = max_batch;
+    c->H = height;
+    c->W = width;
+    const int spec[6][4] = {{16, 32, 1, 1}, {32, 96, 2, 1}, {96, 96, 1, 1},
+                            {96, 8, 1, 0},  {128, 64, 1, 1}, {64, 8, 1, 0}};
+    size_t off = 0;
+    for (auto& s : spec) {
+        Layer L{s[0], s[1], s[2], s[3], 0, 0};
+        L.woff = off;
+        off += (size_t)L.cout * 9 * L.cin;
+        L.boff = off;
+        off += L.cout;
+        c->layers.push_back(L);
+    }
+    c->n_params = off;
+    // He-normal initialization from a seeded generator (Box-Muller on a
+    // 64-bit LCG), biases zero
+    std::vector<float> hw(off, 0.0f);
+    uint64_t st = seed * 6364136223846793005ULL + 1442695040888963407ULL;
+    auto uni = [&]() {
+        st = st * 6364136223846793005ULL + 1442695040888963407ULL;
+        return ((st >> 11) + 0.5) / 9007199254740992.0;
+    };
+    for (const Layer& L : c->layers) {
+        double sd = std::sqrt(2.0 / (9.0 * L.cin)) * (L.relu ? 1.0 : 0.1);
+        for (size_t i = 0; i < (size_t)L.cout * 9 * L.cin; i++) {
+            double u1 = uni(), u2 = uni();
+            hw[L.woff + i] = (float)(sd * std::sqrt(-2.0 * std::log(u1)) * std::cos(6.283185307179586 * u2));
+        }
+    }
+    const size_t B = max_batch, P = (size_t)height * width;
+    const size_t P2 = (size_t)((height + 1) / 2) * ((width + 1) / 2);
+    cudaError_t e = cudaSuccess;
+    auto alloc = [&](auto** p, size_t bytes) {
+        if (e == cudaSuccess) e = cudaMalloc((void**)p, bytes);
+    };
+    alloc(&c->w, off * 4); alloc(&c->g, off * 4); alloc(&c->m, off * 4); alloc(&c->v, off * 4);
+    alloc(&c->wb, off * 2);
+    alloc(&c->x, B * P * 16 * 2); alloc(&c->a1, B * P * 32 * 2); alloc(&c->a2, B * P2 * 96 * 2);
+    alloc(&c->a3, B * P2 * 96 * 2); alloc(&c->cat, B * P * 128 * 2); alloc(&c->a4, B * P * 64 * 2);
+    alloc(&c->o16, B * P2 * 8 * 4); alloc(&c->o8, B * P * 8 * 4);
+    alloc(&c->g_o16, B * P2 * 8 * 4); alloc(&c->g_o8, B * P * 8 * 4);
+    alloc(&c->g_a4, B * P * 64 * 4); alloc(&c->g_cat, B * P * 128 * 4);
+    alloc(&c->g_a3, B * P2 * 96 * 4); alloc(&c->g_a2, B * P2 * 96 * 4);
+    alloc(&c->g_a1, B * P * 32 * 4); alloc(&c->gb, B * P * 128 * 2);
+    c->part_floats = (size_t)256 * 96 * 9 * 96;  // chunks x largest cout x 9 cin
+    alloc(&c->part, c->part_floats * 4);
+    alloc(&c->d_loss, sizeof(double));
+    if (e == cudaSuccess) e = cudaMemcpy(c->w, hw.data(), off * 4, cudaMemcpyHostToDevice);
+    if (e == cudaSuccess) e = cudaMemset(c->m, 0, off * 4);
+    if (e == cudaSuccess) e = cudaMemset(c->v, 0, off * 4);
+    if (e == cudaSuccess) e = cudaMemset(c->g, 0, off * 4);
+    if (e != cudaSuccess) {
+        rf_cnn_destroy(c);
+        return cfail(RF_ERR_OOM, std::string("rf_cnn_create: ") + cudaGetErrorString(e));
+    }
+    rf_status rs = sync_bf16_weights(c);
+    if (rs != RF_OK) {
+        rf_cnn_destroy(c);
+        return rs;
+    }
+    *out = c;
+    return RF_OK;
+}
+
+rf_status rf_cnn_destroy(rf_cnn* c) {
+    if (!c) return RF_OK;
+    cudaDeviceSynchronize();
+    for (void* p : {(void*)c->w, (void*)c->g, (void*)c->m, (void*)c->v, (void*)c->wb, (void*)c->x,
+                    (void*)c->a1, (void*)c->a2, (void*)c->a3, (void*)c->cat, (void*)c->a4,
+                    (void*)c->o16, (void*)c->o8, (void*)c->g_o16, (void*)c->g_o8, (void*)c->g_a4,
+                    (void*)c->g_cat, (void*)c->g_a3, (void*)c->g_a2, (void*)c->g_a1, (void*)c->gb,
+                    (void*)c->part, (void*)c->d_loss})
+        if (p) cudaFree(p);
+    delete c;
+    return RF_OK;
+}
+
+int rf_cnn_num_params(const rf_cnn* c) { return c ? (int)c->n_params : -1; }
+
+rf_status rf_cnn_set_stream(rf_cnn* c, void* stream) {
+    if (!c) return cfail(RF_ERR_INVALID_ARG, "rf_cnn_set_stream: null");
+    c->stream = static_cast<cudaStream_t>(stream);
+    return RF_OK;
+}
+
+rf_status rf_cnn_get_params(rf_cnn* c, float* host) {
+    if (!c || !host) return cfail(RF_ERR_INVALID_ARG, "rf_cnn_get_params: null");
+    CN(cudaStreamSynchronize(c->stream));
+    CN(cudaMemcpy(host, c->w, c->n_params * 4, cudaMemcpyDeviceToHost));
+    return RF_OK;
+}
+
+rf_status rf_cnn_set_params(rf_cnn* c, const float* host) {
+    if (!c || !host) return cfail(RF_ERR_INVALID_ARG, "rf_cnn_set_params: null");
+    CN(cudaStreamSynchronize(c->stream));
+    CN(cudaMemcpy(c->w, host, c->n_params * 4, cudaMemcpyHostToDevice));
+    return sync_bf16_weights(c);
+}
+
+rf_status rf_cnn_get_grads(rf_cnn* c, float* host) {
+    if (!c || !host) return cfail(RF_ERR_INVALID_ARG, "rf_cnn_get_grads: null");
+    CN(cudaStreamSynchronize(c->stream));
+    CN(cudaMemcpy(host, c->g, c->n_params * 4, cudaMemcpyDeviceToHost));
+    return RF_OK;
+}
+
+static rf_status check_batch(rf_cnn* c, int B, int H, int W) {
+    if (B < 1 || B > c->max_batch || H > c->H || W > c->W || H < 2 || W < 2)
+        return cfail(RF_ERR_INVALID_ARG, "rf_cnn: batch or size beyond the allocation");
+    return RF_OK;
+}
+
+rf_status rf_cnn_forward(rf_cnn* c, const float* input, int B, int H, int W, float* out16,
+                         float* out8) {
+    if (!c || !input) return cfail(RF_ERR_INVALID_ARG, "rf_cnn_forward: null");
+    rf_status rs = check_batch(c, B, H, W);
+    if (rs == RF_OK) rs = forward(c, input, B, H, W);
+    if (rs != RF_OK) return rs;
+    int H2 = (H + 1) / 2, W2 = (W + 1) / 2;
+    if (out16)
+        CN(cudaMemcpyAsync(out16, c->o16, (size_t)B * H2 * W2 * 8 * 4, cudaMemcpyDeviceToDevice,
+                           c->stream));
+    if (out8)
+        CN(cudaMemcpyAsync(out8, c->o8, (size_t)B * H * W * 8 * 4, cudaMemcpyDeviceToDevice,
+                           c->stream));
+    return RF_OK;
+}
+
+rf_status rf_cnn_backward(rf_cnn* c, const float* input, const float* tgt16, const float* mask16,
+                          const float* tgt8, const float* mask8, int B, int H, int W,
+                          const float* weights, double* loss) {
+    if (!c || !input || !tgt16 || !mask16 || !tgt8 || !mask8 || !weights)
+        return cfail(RF_ERR_INVALID_ARG, "rf_cnn_backward: null");
+    rf_status rs = check_batch(c, B, H, W);
+    if (rs == RF_OK) rs = forward(c, input, B, H, W);
+    if (rs != RF_OK) return rs;
+    int H2 = (H + 1) / 2, W2 = (W + 1) / 2;
+    int P8 = B * H * W, P16 = B * H2 * W2;
+    CN(cudaMemsetAsync(c->d_loss, 0, sizeof(double), c->stream));
+    k_l1_loss<<<blocks_for(P16), 256, 0, c->stream>>>(c->o16, tgt16, mask16, P16, 8, weights[0],
+                                                      weights[1], weights[2], 1.0f / P16,
+                                                      c->g_o16, c->d_loss);
+    k_l1_loss<<<blocks_for(P8), 256, 0, c->stream>>>(c->o8, tgt8, mask8, P8, 8, weights[0],
+                                                     weights[1], weights[2], 1.0f / P8, c->g_o8,
+                                                     c->d_loss);
+    c->launches += 2;
+    rs = backward(c, B, H, W);
+    if (rs != RF_OK) return rs;
+    if (loss) {
+        CN(cudaMemcpyAsync(loss, c->d_loss, sizeof(double), cudaMemcpyDeviceToHost, c->stream));
+        CN(cudaStreamSynchronize(c->stream));
+    }
+    return RF_OK;
+}
+
+rf_status rf_cnn_adam_step(rf_cnn* c, float lr, float beta1, float beta2, float eps) {
+    if (!c) return cfail(RF_ERR_INVALID_ARG, "rf_cnn_adam_step: null");
+    c->step++;
+    float c1 = 1.0f - std::pow(beta1, (float)c->step);
+    float c2 = 1.0f - std::pow(beta2, (float)c->step);
+    k_adam<<<blocks_for(c->n_params), 256, 0, c->stream>>>(c->w, c->g, c->m, c->v, c->n_params, lr,
+                                                           beta1, beta2, eps, c1, c2);
+    c->launches++;
+    CN(cudaGetLastError());
+    return sync_bf16_weights(c);
+}
+
+uint64_t rf_cnn_kernel_launches(const rf_cnn* c) { return c ? c->launches : 0; }
+
+}  // extern "C"
