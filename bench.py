@@ -49,6 +49,13 @@ WORKLOADS = {
     # seeded scenes and poses, one launch per schedule step for all pairs
     "batch64": dict(pairs=64, sizes=[(320, 240), (640, 480), (1280, 720), (1920, 1080)],
                     levels=6, warps=5, iters=100, seed=0),
+    # batched + learned warm start: 64 pairs of 1280x720; the network predicts
+    # inverse depth at 1/8, the solve refines from pyramid level 2 with the
+    # per-level schedule below (index = level, 0 = finest); plain 5 x 100
+    "720p-learned": dict(width=1280, height=720, pairs=64, levels=6, seed=2000, plain_warps=5,
+                         plain_iters=100, warm_level=2, warm_warps=[1, 3, 5],
+                         warm_iters=[30, 30, 50], fallback_margin=0.02,
+                         checkpoint="reconflow_gb300/weights/warmstart_f125.bin"),
     # batched: 64 pairs of 1280x720 (per-pair throughput of the batched path)
     "batch64-720p": dict(pairs=64, sizes=[(1280, 720)], levels=6, warps=5, iters=100, seed=0),
 }
@@ -361,6 +368,258 @@ def run_batch(args, wl, world, rank, local):
     b.close()
 
 
+def run_learned(args, wl, world, rank, local):
+    """Batched + learned warm start against the plain solver, on 720p pairs.
+
+    Untimed: the plain batched solve of the same pairs (its endpoint errors
+    and energies) and the plain single-pair solve of one pair (the drop-in
+    path's throughput).  Timed, one step = the whole batch through the
+    learned path: input features, network, warm-start state, refinement
+    from the warm level, energies, and a plain re-solve of every pair whose
+    energy exceeds its plain solve's by more than the fallback margin."""
+    import torch
+
+    import reconflow_gb300 as R
+    from reconflow_gb300.scene import make_scene
+    from reconflow_gb300.warmstart import LearnedBatchSolver, WarmStartNet
+
+    torch.cuda.set_device(local)
+    lib = R.load()
+    W, H, n = wl["width"], wl["height"], wl["pairs"]
+    t0 = time.perf_counter()
+    scenes = [make_scene(W, H, seed=wl["seed"] + 1000 * rank + i, device="cuda") for i in range(n)]
+    gen_s = time.perf_counter() - t0
+    Ks = [sc["K"] for sc in scenes]
+    Rs = [sc["R"] for sc in scenes]
+    ts = [sc["t"] for sc in scenes]
+    stream = torch.cuda.Stream()
+    flush = torch.empty(L2_FLUSH_BYTES // 4, dtype=torch.float32, device="cuda")
+
+    def new_batch(warps, iters):
+        b = R.ReconFlowBatch([(W, H)] * n, wl["levels"], method=SOLVER["method"],
+                             lambda_=SOLVER["lam"], lambdaf=SOLVER["lambdaf"],
+                             lambdams=SOLVER["lambdams"], alphaTv=1.0 / SOLVER["theta"],
+                             alphaProj=SOLVER["alpha_proj"], tau=SOLVER["tau"], nWarpIters=warps,
+                             nSolverIters=iters, fix_quirks=SOLVER["fix_quirks"])
+        b.setStream(stream.cuda_stream)
+        for i, sc in enumerate(scenes):
+            b.setCameraMatrices(i, sc["K"], sc["K"])
+            b.copyImagesToDevice(i, sc["I0"], sc["I1"])
+        return b
+
+    def epe_stats(b):
+        means, meds, allv = [], [], []
+        for i, sc in enumerate(scenes):
+            u, v = b.copyOpticalFlowToHost(i)
+            e = np.sqrt((u[:, :W] - sc["flow"][..., 0]) ** 2 + (v[:, :W] - sc["flow"][..., 1]) ** 2)
+            e = e[sc["valid"]]
+            e = np.where(np.isfinite(e), e, np.float32(1e4))
+            means.append(float(e.mean()))
+            meds.append(float(np.median(e)))
+            allv.append(e)
+        a = np.concatenate(allv)
+        return {"epe_mean_px": float(np.mean(means)), "epe_median_px": float(np.mean(meds)),
+                "frac_epe_gt_3px": float((a > 3).mean())}
+
+    def timed(fn, steps):
+        evs = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
+               for _ in range(steps)]
+        for a, e in evs:
+            flush.zero_()
+            a.record(stream)
+            fn()
+            e.record(stream)
+        torch.cuda.synchronize()
+        return [a.elapsed_time(e) for a, e in evs]
+
+    # plain, batched: reference accuracy and energies
+    plain = new_batch(wl["plain_warps"], wl["plain_iters"])
+    with torch.cuda.stream(stream):
+        plain.solveR(Rs, ts)
+        torch.cuda.synchronize()
+        plain_acc = epe_stats(plain)
+        e_plain = plain.energies()
+        plain_batch_ms = timed(lambda: plain.solveR(Rs, ts), 2)
+    plain.close()
+    # plain, one pair through the drop-in path
+    f = R.ReconFlow()
+    f.initializeR(W, H, 1, wl["levels"], 2.0, SOLVER["method"], SOLVER["lam"], 0.0,
+                  SOLVER["lambdaf"], SOLVER["lambdams"], 1.0 / SOLVER["theta"],
+                  SOLVER["alpha_proj"], 0.5, SOLVER["tau"], wl["plain_warps"], wl["plain_iters"],
+                  cvType=5, fix_quirks=SOLVER["fix_quirks"])
+    f.setStream(stream.cuda_stream)
+    f.setCameraMatrices(scenes[0]["K"], scenes[0]["K"])
+    f.copyImagesToDevice(scenes[0]["I0"], scenes[0]["I1"])
+    with torch.cuda.stream(stream):
+        for _ in range(2):
+            f.solveR(Rs[0], ts[0], 5.0)
+        single_ms = timed(lambda: f.solveR(Rs[0], ts[0], 5.0), 5)
+
+    # learned
+    net = WarmStartNet(n, (H // 8) + 1, (W // 8) + 1, seed=0)
+    net.load(os.path.join(ROOT, wl["checkpoint"]))
+    b = new_batch(wl["plain_warps"], wl["plain_iters"])
+    ls = LearnedBatchSolver(net, b, (W, H), Ks[0], warm_level=wl["warm_level"],
+                            warps=wl["warm_warps"], iters=wl["warm_iters"])
+    ls.set_stream(stream.cuda_stream)
+    margin = wl["fallback_margin"]
+    fallbacks = []
+
+    def step():
+        ls.solve(Ks, Rs, ts)
+        e = b.energies()
+        bad = [i for i in range(n) if not (e[i] <= (1.0 + margin) * e_plain[i])]
+        for i in bad:  # fall back to the plain solve, one pair at a time
+            f.setCameraMatrices(Ks[i], Ks[i])
+            f.copyImagesToDeviceFromDevice(*b.imagePlanes(i, 0), b.strides[i])
+            f.solveR(Rs[i], ts[i], 5.0)
+        fallbacks.append(len(bad))
+
+    with torch.cuda.stream(stream):
+        for _ in range(args.warmup):
+            step()
+        torch.cuda.synchronize()
+        learned_acc = epe_stats(b)
+        e_learned = b.energies()
+        barrier(world)
+        l0 = b.kernelLaunches() + net.kernel_launches() + f.kernelLaunches()
+        fallbacks.clear()
+        with ClockSampler(local) as clk:
+            torch.cuda.synchronize()
+            step_ms = timed(step, args.steps)
+        launches = b.kernelLaunches() + net.kernel_launches() + f.kernelLaunches() - l0
+    total_s = max_over_ranks(sum(step_ms) / 1000.0, world)
+    value = world * n * args.steps / total_s
+
+    # end to end: frames from pinned host memory in, flow / inverse depth /
+    # points out, every step
+    e2e = None
+    if not args.no_e2e:
+        s0 = b.strides[0]
+        nb = H * s0 * 4
+        hosts = []
+        for i in range(n):
+            ptrs = []
+            for _ in range(8):
+                p_ = ctypes.c_void_p()
+                R._native.check(lib.rf_host_alloc(nb, ctypes.byref(p_)))
+                ptrs.append(p_)
+            for k, img in ((0, scenes[i]["I0"]), (1, scenes[i]["I1"])):
+                a_ = np.ctypeslib.as_array(ctypes.cast(ptrs[k], ctypes.POINTER(ctypes.c_float)),
+                                           shape=(H, s0))
+                a_[:, :W] = img
+            hosts.append(ptrs)
+        hb = b._h
+
+        def e2e_step():
+            for i in range(n):
+                R._native.check(lib.rf_batch_upload_images(hb, i, hosts[i][0], hosts[i][1], s0))
+            step()
+            for i in range(n):
+                R._native.check(lib.rf_batch_download_flow(hb, i, hosts[i][2], hosts[i][3], s0))
+                R._native.check(lib.rf_batch_download_inv_depth(hb, i, hosts[i][4], s0))
+                R._native.check(lib.rf_batch_download_points(hb, i, hosts[i][5], hosts[i][6],
+                                                             hosts[i][7], s0))
+
+        with torch.cuda.stream(stream):
+            e2e_step()
+            times = []
+            for _ in range(args.steps):
+                flush.zero_()
+                torch.cuda.synchronize()
+                t1 = time.perf_counter()
+                e2e_step()
+                torch.cuda.synchronize()
+                times.append(time.perf_counter() - t1)
+        e2e = {"value": world * n * args.steps / max_over_ranks(sum(times), world),
+               "unit": "pairs/s", "h2d_bytes_per_step": 2 * n * W * H * 4,
+               "d2h_bytes_per_step": 6 * n * W * H * 4}
+        for ptrs in hosts:
+            for p_ in ptrs:
+                lib.rf_host_free(p_)
+
+    # roofline: the dominant stencil kernel (level-0 data / triangulation)
+    ms = (ctypes.c_float * 2)()
+    with torch.cuda.stream(stream):
+        f.setCameraMatrices(Ks[0], Ks[0])
+        f.copyImagesToDevice(scenes[0]["I0"], scenes[0]["I1"])
+        f.solveR(Rs[0], ts[0], 5.0)
+        R._native.check(lib.rf_profile_iterations(f._handle(), 0, 50, ms))
+    roofline = roofline_of(ms, W * H)
+    cpu = None
+    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+        wl1 = dict(width=W, height=H, levels=wl["levels"], warps=wl["plain_warps"],
+                   iters=wl["plain_iters"], seed=wl["seed"])
+        sc0 = scenes[0]
+        s_ = (W + 31) // 32 * 32
+        pad = lambda a: np.pad(a, ((0, 0), (0, s_ - W))).astype(np.float32)  # noqa: E731
+        run, cores = cpu_sample(wl1, sc0, pad(sc0["I0"]), pad(sc0["I1"]))
+        t1, t5 = run(1), run(5)
+        per_pair = extrapolate(t1, t5, wl["plain_iters"])
+        cpu = {"value": 1.0 / per_pair, "unit": "pairs/s", "cores": cores, "kind": "port",
+               "sample": f"plain solve of one {W}x{H} pair, full schedule at 1 and 5 inner "
+                         f"iterations ({t1:.2f} s, {t5:.2f} s), extrapolated linearly to "
+                         f"{wl['plain_iters']}"}
+    if rank == 0:
+        single_pps = 1000.0 / statistics.median(single_ms)
+        tol = 0.05
+        line = {
+            "metric": "720p frame pairs/s, batched + learned warm start (vs the plain solver at "
+                      "equal EPE)",
+            "value": value, "unit": "pairs/s", "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": 1000.0 * total_s / args.steps,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+            "data": "synthetic (seeded scene generator)",
+            "config": {"workload": args.workload, "width": W, "height": H, "pairs_per_step": n,
+                       "pyramid_levels": wl["levels"], "plain_schedule": [wl["plain_warps"],
+                                                                          wl["plain_iters"]],
+                       "warm_level": wl["warm_level"], "warm_warps_per_level": wl["warm_warps"],
+                       "warm_iters_per_level": wl["warm_iters"],
+                       "fallback": f"plain re-solve when energy > (1 + {margin}) x plain energy",
+                       "checkpoint": wl["checkpoint"], "method": "METHODR_TVL1_MS",
+                       "lambda": SOLVER["lam"], "theta": SOLVER["theta"], "tau": SOLVER["tau"],
+                       "alpha_proj": SOLVER["alpha_proj"], "lambdaf": SOLVER["lambdaf"],
+                       "lambdams": SOLVER["lambdams"], "fix_quirks": SOLVER["fix_quirks"],
+                       "scene_seeds": [wl["seed"], wl["seed"] + n - 1],
+                       "l2": "flushed between steps (512 MiB write)", "parallelism": "replicas"},
+            "plain": {"single_pair_pairs_per_s": single_pps,
+                      "batched_pairs_per_s": 1000.0 * n / statistics.median(plain_batch_ms),
+                      "accuracy": plain_acc},
+            "learned": {"accuracy": learned_acc, "fallbacks_per_step": fallbacks,
+                        "energy_ratio_median": float(np.median(e_learned / e_plain))},
+            "speedup_vs_plain_single_pair": value / single_pps,
+            "equal_epe": {"mean": learned_acc["epe_mean_px"] <= plain_acc["epe_mean_px"] + tol,
+                          "median": learned_acc["epe_median_px"] <= plain_acc["epe_median_px"] + tol,
+                          "tolerance_px": tol},
+            "e2e": e2e, "roofline": roofline, "cpu_baseline": cpu, "clocks": clk.summary(),
+            "gpu_launches": int(launches), "scene_gen_s": gen_s,
+        }
+        print(json.dumps(line), flush=True)
+    b.close()
+    f.close()
+    net.close()
+
+
+def roofline_of(ms, px):
+    """Roofline entry of the dominant level-0 kernel from per-launch times."""
+    names = ["recon_a", "recon_b"]
+    dom = 0 if ms[0] >= ms[1] else 1
+    achieved = ALG_BYTES[names[dom]] * px / (ms[dom] * 1e-3) / 1e9
+    peak, peak_kind = load_peaks()
+    traffic = None
+    tpath = os.path.join(ROOT, "profiles", "traffic_720p.json")
+    if os.path.exists(tpath):
+        with open(tpath) as fh:
+            traffic = json.load(fh).get(names[dom])
+    return {"bound": "hbm", "kernel": names[dom], "achieved": achieved, "peak": peak,
+            "peak_kind": peak_kind, "unit": "GB/s", "frac": achieved / peak, "traffic": traffic,
+            "alg_bytes_per_launch": ALG_BYTES[names[dom]] * px,
+            "launch_ms": {names[0]: ms[0], names[1]: ms[1]},
+            "frac_each": {names[k]: ALG_BYTES[names[k]] * px / (ms[k] * 1e-3) / 1e9 / peak
+                          for k in range(2)},
+            "timing": "launches of one kernel back to back in a CUDA graph, CUDA events"}
+
+
 def config_of(wl):
     return {"workload": f"reconflow_{wl['width']}x{wl['height']}_L{wl['levels']}_w{wl['warps']}"
                         f"_i{wl['iters']}",
@@ -391,6 +650,9 @@ def main():
         if "pairs" in wl:
             raise SystemExit("bench.py: the reference arm runs single-pair workloads")
         run_reference(args, wl, world, rank)
+        return
+    if "checkpoint" in wl:
+        run_learned(args, wl, world, rank, local)
         return
     if "pairs" in wl:
         run_batch(args, wl, world, rank, local)

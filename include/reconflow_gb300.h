@@ -201,13 +201,14 @@ RF_API rf_status rf_synchronize(rf_handle* h);
 RF_API rf_status rf_host_alloc(size_t bytes, void** ptr);
 RF_API rf_status rf_host_free(void* ptr);
 
-/* Timing hook (no reference counterpart): after a solve, run `n_iters` more
- * inner iterations of the fused kernels at pyramid level `level` on the
- * handle's stream, each launch bracketed by CUDA events, and return the mean
- * duration of each kernel in milliseconds (ms[0] = data/projection/
- * triangulation kernel, ms[1] = dual/median/clean-up kernel; plain TV-L1:
- * data, dual).  Changes the solver state; results of the last solve are no
- * longer valid afterwards. */
+/* Timing hook (no reference counterpart): after a solve, time each of the
+ * two inner-iteration kernels at pyramid level `level` on the handle's
+ * stream: `n_iters` launches of one kernel back to back, captured in a CUDA
+ * graph as the solve captures them, the graph replay timed with CUDA events;
+ * returns the mean time per launch in milliseconds (ms[0] = data /
+ * projection / triangulation kernel, ms[1] = dual / median / clean-up
+ * kernel; plain TV-L1: data, dual).  Changes the solver state; results of
+ * the last solve are no longer valid afterwards. */
 RF_API rf_status rf_profile_iterations(rf_handle* h, int level, int n_iters, float* ms);
 
 /* Kernel launches issued by this handle so far (count of this library's
@@ -246,6 +247,31 @@ RF_API rf_status rf_batch_upload_images_device(rf_batch* b, int pair, const floa
 RF_API rf_status rf_batch_solve(rf_batch* b, const double* R0, const double* t0, const double* R1,
                                 const double* t1);
 RF_API rf_status rf_batch_solve_flow(rf_batch* b);
+/* Warm-started batch solve (no reference counterpart): every pair starts at
+ * pyramid level `level` from the planes rf_batch_warm_planes returns (flow
+ * u, v and 3D points X, Y, Z at that level, the level's stride per row,
+ * written by the caller on the batch's stream beforehand), then runs
+ * `warps` x `iters` at that level and every finer one, like rf_solve_warm
+ * does for one pair.  Poses as in rf_batch_solve. */
+RF_API rf_status rf_batch_solve_warm(rf_batch* b, const double* R0, const double* t0,
+                                     const double* R1, const double* t1, int level, int warps,
+                                     int iters);
+/* Energy of every pair's last ReconFlow solution (as rf_energy defines it
+ * for one pair); out: n_pairs doubles on the host.  Synchronizes. */
+RF_API rf_status rf_batch_energies(rf_batch* b, double* out);
+/* rf_batch_solve_warm with its own warps / iterations at each level:
+ * warps[l], iters[l] for l = 0 .. level (level 0 = the finest). */
+RF_API rf_status rf_batch_solve_warm_levels(rf_batch* b, const double* R0, const double* t0,
+                                            const double* R1, const double* t1, int level,
+                                            const int* warps, const int* iters);
+/* Device pointers of pair `pair`'s image planes at pyramid `level` (level 0
+ * = the uploaded frames; coarser levels are filled by the next solve). */
+RF_API rf_status rf_batch_image_planes(rf_batch* b, int pair, int level, const float** I0,
+                                       const float** I1);
+/* Device pointers of pair `pair`'s warm-start input planes (level-0-sized
+ * planes; any pointer argument may be NULL). */
+RF_API rf_status rf_batch_warm_planes(rf_batch* b, int pair, float** u, float** v, float** X,
+                                      float** Y, float** Z);
 RF_API rf_status rf_batch_download_flow(rf_batch* b, int pair, float* u, float* v, int pitch);
 RF_API rf_status rf_batch_download_points(rf_batch* b, int pair, float* X, float* Y, float* Z,
                                           int pitch);
@@ -288,6 +314,31 @@ RF_API rf_status rf_cnn_backward(rf_cnn* c, const float* input, const float* tgt
                                  int batch, int height, int width, const float* w, double* loss);
 RF_API rf_status rf_cnn_adam_step(rf_cnn* c, float lr, float beta1, float beta2, float eps);
 RF_API uint64_t rf_cnn_kernel_launches(const rf_cnn* c);
+
+/* Warm-start network input (no reference counterpart): for n frame pairs
+ * (device planes of w0 x h0 float32 pixels, s0 floats per row; host arrays
+ * of n device pointers), the 16-channel NHWC features on the grid of
+ * (w0/factor) x (h0/factor) pixels, pair-major in `out` (device):
+ * channels 0, 1 = the factor x factor box averages of I0, I1 minus 0.5;
+ * 2..13 = 10 |I1(x'(rho_k)) - I0(x)| for inverse depths rho_k = 0.05 k
+ * (x'(rho) = the camera-1 image of the camera-0 pixel x at inverse depth
+ * rho, X1 = R X + t, I1 bilinear and clamped); 14, 15 = d x'/d rho at
+ * rho = 0.25 in coarse pixels per 10 1/m.  K (level-0 intrinsics), R, t:
+ * n x 9, n x 9 and n x 3 doubles on the host.  Runs on `stream`. */
+RF_API rf_status rf_ws_features(int n, const float* const* I0, const float* const* I1, int w0,
+                                int h0, int s0, int factor, const double* K, const double* R,
+                                const double* t, float* out, void* stream);
+/* Warm-start state from the network's inverse depth (channel 2 of an NHWC
+ * map of `channels` channels on a wn x hn grid per pair, device): for each
+ * pixel of a w x h pyramid level (s floats per row) the inverse depth
+ * bilinearly upsampled by `up`, clamped to [0.02, 2], the 3D point
+ * X = K_level^-1 x~ / rho and the flow to camera 1 as SolveUc forms it
+ * (solveUcSk.cu:21-33).  K_level, R, t: n x 9, n x 9, n x 3 host doubles;
+ * u, v, X, Y, Z: host arrays of n device plane pointers. */
+RF_API rf_status rf_ws_state(int n, const float* net, int channels, int wn, int hn, int w, int h,
+                             int s, float up, const double* K_level, const double* R,
+                             const double* t, float* const* u, float* const* v, float* const* X,
+                             float* const* Y, float* const* Z, void* stream);
 
 /* ------------------------------------------------------------------------
  * Kernel-level entry points (device pointers, caller's stream).  Each runs

@@ -83,6 +83,11 @@ _SIGS = [
     ("rf_batch_upload_images_device", _I, [_VP, _I, _VP, _VP, _I]),
     ("rf_batch_solve", _I, [_VP, _D, _D, _D, _D]),
     ("rf_batch_solve_flow", _I, [_VP]),
+    ("rf_batch_solve_warm", _I, [_VP, _D, _D, _D, _D, _I, _I, _I]),
+    ("rf_batch_energies", _I, [_VP, _VP]),
+    ("rf_batch_solve_warm_levels", _I, [_VP, _D, _D, _D, _D, _I, _VP, _VP]),
+    ("rf_batch_warm_planes", _I, [_VP, _I, _VP, _VP, _VP, _VP, _VP]),
+    ("rf_batch_image_planes", _I, [_VP, _I, _I, _VP, _VP]),
     ("rf_batch_download_flow", _I, [_VP, _I, _VP, _VP, _I]),
     ("rf_batch_download_points", _I, [_VP, _I, _VP, _VP, _VP, _I]),
     ("rf_batch_download_inv_depth", _I, [_VP, _I, _VP, _I]),
@@ -102,6 +107,9 @@ _SIGS = [
                              ctypes.POINTER(ctypes.c_double)]),
     ("rf_cnn_adam_step", _I, [_VP, _F, _F, _F, _F]),
     ("rf_cnn_kernel_launches", ctypes.c_uint64, [_VP]),
+    ("rf_ws_features", _I, [_I, _VP, _VP, _I, _I, _I, _I, _D, _D, _D, _VP, _VP]),
+    ("rf_ws_state", _I, [_I, _VP, _I, _I, _I, _I, _I, _I, _F, _D, _D, _D, _VP, _VP, _VP, _VP,
+                         _VP, _VP]),
     ("rfk_downscale", _I, [_VP, _I, _I, _I, _I, _I, _I, _F, _I, _VP, _VP]),
     ("rfk_upscale", _I, [_VP, _I, _I, _I, _I, _I, _I, _F, _VP, _VP]),
     ("rfk_warp", _I, [_VP, _I, _I, _I, _VP, _VP, _VP, _VP]),

@@ -28,6 +28,8 @@ SOURCES = {
     "rf_solver.cu": ["-fmad=false"],
     "rf_noalloc.cu": ["-fmad=false"],
     "rf_batch.cu": ["-fmad=false"],
+    # warm-start features and state (around the network, not on the parity path)
+    "rf_warm.cu": [],
     # the learned warm start: BF16 tensor-core convolutions, FP32 accumulation
     "rf_cnn.cu": [],
 }

@@ -235,6 +235,24 @@ struct OpInvDepth {
     }
 };
 
+// warm start (rf_batch_solve_warm): the caller's planes at the start level
+// become u, v (and uproj, vproj) and the 3D state, as rf_solve_warm stages them
+struct OpWarmInit {
+    int wu, wv, wX, wY, wZ, u, v, uproj, vproj, X, Y, Z;
+    __device__ void operator()(const BatchCtx&, const BatchPair& bp, int, int, LevelDims d, int ix,
+                               int iy) const {
+        int pos = ix + iy * d.s;
+        float a = plane_ptr(bp, wu)[pos], c = plane_ptr(bp, wv)[pos];
+        plane_ptr(bp, u)[pos] = a;
+        plane_ptr(bp, v)[pos] = c;
+        plane_ptr(bp, uproj)[pos] = a;
+        plane_ptr(bp, vproj)[pos] = c;
+        plane_ptr(bp, X)[pos] = plane_ptr(bp, wX)[pos];
+        plane_ptr(bp, Y)[pos] = plane_ptr(bp, wY)[pos];
+        plane_ptr(bp, Z)[pos] = plane_ptr(bp, wZ)[pos];
+    }
+};
+
 thread_local std::string g_batch_err;
 
 rf_status bfail(rf_status st, const std::string& msg) {
@@ -267,6 +285,12 @@ struct rf_batch {
     cudaStream_t own = nullptr, stream = nullptr;
     cudaGraphExec_t graph = nullptr;
     int graph_kind = -1;
+    // kind 2 (warm start): start level and warps / iterations per level
+    int warm_level = -1;
+    std::vector<int> warm_warps, warm_iters;
+    std::vector<int> graph_sched;  // the warm schedule the graph was captured with
+    std::vector<double> last_R1, last_t1;  // pose of the last solve, [pair][9], [pair][3]
+    double* d_energy = nullptr;            // [pair][1 + kEnergyBlocks]
     uint64_t launches = 0, graph_nodes = 0, enq = 0;
     int res_u = -1, res_v = -1;
     bool solved = false;
@@ -275,6 +299,7 @@ struct rf_batch {
     int pI0(int l) const { return l; }
     int pI1(int l) const { return L + l; }
     int base_idx() const { return 2 * L; }
+    int warm_idx(int k) const;  // warm-start input plane k (u, v, X, Y, Z)
 };
 
 namespace rf_batch_impl {
@@ -284,6 +309,14 @@ enum {
     P_Y1, P_Z1, P_SCRATCH, P_SPARE0
 };
 constexpr int kSpares = 18;
+constexpr int kWarmPlanes = 5;
+constexpr int kEnergyBlocks = 1024;
+
+}  // namespace rf_batch_impl
+
+int rf_batch::warm_idx(int k) const { return base_idx() + rf_batch_impl::P_SPARE0 + rf_batch_impl::kSpares + k; }
+
+namespace rf_batch_impl {
 
 BatchCtx ctx_of(rf_batch* b) {
     BatchCtx c;
@@ -339,7 +372,9 @@ rf_status enqueue_batch(rf_batch* b, int kind) {
     int u = sp[0], v = sp[1], uc = sp[2], vc = sp[3], uproj = sp[4], vproj = sp[5], sku = sp[6],
         skv = sp[7], tu = sp[8], tv = sp[9];
     std::vector<int> freep(sp + 10, sp + kSpares);
-    const bool recon = kind == 0;
+    const bool recon = kind == 0 || kind == 2;
+    const bool warm = kind == 2;
+    const int top = warm ? b->warm_level : b->L - 1;
     if (recon) {
         rf_status rs = memset_planes(b, {u, v, uproj, vproj, uc, vc, sku, skv, P(P_X), P(P_Y), P(P_Z)});
         if (rs != RF_OK) return rs;
@@ -348,14 +383,22 @@ rf_status enqueue_batch(rf_batch* b, int kind) {
         if (rs != RF_OK) return rs;
     }
     bool ucb = true;
-    for (int level = b->L - 1; level >= 0; level--) {
-        for (int warp = 0; warp < p.n_warp_iters; warp++) {
+    if (warm) {
+        BL(launch_op(b, top, OpWarmInit{b->warm_idx(0), b->warm_idx(1), b->warm_idx(2),
+                                        b->warm_idx(3), b->warm_idx(4), u, v, uproj, vproj,
+                                        P(P_X), P(P_Y), P(P_Z)}));
+        ucb = false;  // uc from the warm 3D state in the first iteration
+    }
+    for (int level = top; level >= 0; level--) {
+        const int n_warps = warm ? b->warm_warps[level] : p.n_warp_iters;
+        const int n_iters = warm ? b->warm_iters[level] : p.n_solver_iters;
+        for (int warp = 0; warp < n_warps; warp++) {
             BL(launch_op(b, level, OpWarp{b->pI1(level), u, v, P(P_I1W)}));
             BL(launch_op(b, level, OpDeriv{b->pI0(level), P(P_I1W), P(P_IX), P(P_IY), P(P_IZ)}));
             ReconIdx r{u, v, P(P_DUHAT), P(P_DVHAT), P(P_PU1), P(P_PU2), P(P_PV1), P(P_PV2),
                        uproj, vproj, sku, skv, P(P_IX), P(P_IY), P(P_IZ), P(P_X), P(P_Y), P(P_Z),
                        P(P_X1), P(P_Y1), P(P_Z1), uc, vc};
-            for (int iter = 0; iter < p.n_solver_iters; iter++) {
+            for (int iter = 0; iter < n_iters; iter++) {
                 const int first = iter == 0;
                 if (recon) {
                     BL(launch_op(b, level, OpReconA{r, wt, first, ucb ? 1 : 0}));
@@ -369,7 +412,7 @@ rf_status enqueue_batch(rf_batch* b, int kind) {
                                                      P(P_PV1), P(P_PV2), wt, first}));
                 }
             }
-            if (p.n_solver_iters == 0) {
+            if (n_iters == 0) {
                 rf_status rs = memset_planes(b, {P(P_DUHAT), P(P_DVHAT)});
                 if (rs != RF_OK) return rs;
             }
@@ -413,7 +456,13 @@ rf_status enqueue_batch(rf_batch* b, int kind) {
 }
 
 rf_status run_batch(rf_batch* b, int kind) {
-    if (b->graph && b->graph_kind != kind) {
+    std::vector<int> sched;
+    if (kind == 2) {
+        sched.push_back(b->warm_level);
+        sched.insert(sched.end(), b->warm_warps.begin(), b->warm_warps.end());
+        sched.insert(sched.end(), b->warm_iters.begin(), b->warm_iters.end());
+    }
+    if (b->graph && (b->graph_kind != kind || b->graph_sched != sched)) {
         cudaGraphExecDestroy(b->graph);
         b->graph = nullptr;
     }
@@ -435,6 +484,7 @@ rf_status run_batch(rf_batch* b, int kind) {
             return bfail(RF_ERR_CUDA, std::string("instantiate: ") + cudaGetErrorString(ie));
         }
         b->graph_kind = kind;
+        b->graph_sched = sched;
         b->graph_nodes = b->enq;
     }
     BC(cudaGraphLaunch(b->graph, b->stream));
@@ -467,7 +517,7 @@ rf_status rf_batch_create(const rf_params* p, int n_pairs, const int* widths, co
     b->L = p->n_levels;
     b->dims.resize(n_pairs);
     size_t total = 0;
-    b->n_planes = 2 * b->L + P_SPARE0 + kSpares;
+    b->n_planes = 2 * b->L + P_SPARE0 + kSpares + kWarmPlanes;
     for (int i = 0; i < n_pairs; i++) {
         int w = widths[i], h = heights[i];
         if (w < 1 || h < 1 || (long long)w * h > (1LL << 28)) {
@@ -541,6 +591,7 @@ rf_status rf_batch_destroy(rf_batch* b) {
     if (b->d_pairs) cudaFree(b->d_pairs);
     if (b->d_prefix) cudaFree(b->d_prefix);
     if (b->d_consts) cudaFree(b->d_consts);
+    if (b->d_energy) cudaFree(b->d_energy);
     if (b->h_consts) cudaFreeHost(b->h_consts);
     if (b->own) cudaStreamDestroy(b->own);
     delete b;
@@ -585,14 +636,14 @@ rf_status rf_batch_upload_images_device(rf_batch* b, int pair, const float* i0, 
     return batch_upload(b, pair, i0, i1, pitch, cudaMemcpyDeviceToDevice);
 }
 
-rf_status rf_batch_solve(rf_batch* b, const double* R0, const double* t0, const double* R1,
-                         const double* t1) {
-    if (!b || !R1 || !t1) return bfail(RF_ERR_INVALID_ARG, "rf_batch_solve: null argument");
+static rf_status batch_poses(rf_batch* b, const char* who, const double* R0, const double* t0,
+                             const double* R1, const double* t1) {
+    if (!b || !R1 || !t1) return bfail(RF_ERR_INVALID_ARG, std::string(who) + ": null argument");
     if (b->p.method == RF_METHOD_TVL1)
-        return bfail(RF_ERR_STATE, "rf_batch_solve: batch was created for plain TV-L1");
+        return bfail(RF_ERR_STATE, std::string(who) + ": batch was created for plain TV-L1");
     for (int i = 0; i < b->n; i++)
         if (!b->cams[i] || !b->imgs[i])
-            return bfail(RF_ERR_STATE, "rf_batch_solve: pair " + std::to_string(i) +
+            return bfail(RF_ERR_STATE, std::string(who) + ": pair " + std::to_string(i) +
                                            " has no cameras or images");
     BC(cudaStreamSynchronize(b->stream));
     const double I[9] = {1, 0, 0, 0, 1, 0, 0, 0, 1}, z[3] = {0, 0, 0};
@@ -602,9 +653,89 @@ rf_status rf_batch_solve(rf_batch* b, const double* R0, const double* t0, const 
                             t1 + 3 * i, b->h_consts + (size_t)i * b->L);
     BC(cudaMemcpyAsync(b->d_consts, b->h_consts, sizeof(LevelConsts) * b->n * b->L,
                        cudaMemcpyHostToDevice, b->stream));
-    rf_status rs = run_batch(b, 0);
+    b->last_R1.assign(R1, R1 + 9 * b->n);
+    b->last_t1.assign(t1, t1 + 3 * b->n);
+    return RF_OK;
+}
+
+rf_status rf_batch_solve(rf_batch* b, const double* R0, const double* t0, const double* R1,
+                         const double* t1) {
+    rf_status rs = batch_poses(b, "rf_batch_solve", R0, t0, R1, t1);
+    if (rs != RF_OK) return rs;
+    rs = run_batch(b, 0);
     b->solved = rs == RF_OK;
     return rs;
+}
+
+rf_status rf_batch_warm_planes(rf_batch* b, int pair, float** u, float** v, float** X, float** Y,
+                               float** Z) {
+    if (!b || pair < 0 || pair >= b->n)
+        return bfail(RF_ERR_INVALID_ARG, "rf_batch_warm_planes: bad argument");
+    float** out[5] = {u, v, X, Y, Z};
+    for (int k = 0; k < 5; k++)
+        if (out[k]) *out[k] = pair_plane(b, pair, b->warm_idx(k));
+    return RF_OK;
+}
+
+rf_status rf_batch_energies(rf_batch* b, double* out) {
+    if (!b || !out) return bfail(RF_ERR_INVALID_ARG, "rf_batch_energies: null argument");
+    if (!b->solved || b->p.method == RF_METHOD_TVL1 || b->last_R1.size() != (size_t)9 * b->n)
+        return bfail(RF_ERR_STATE, "rf_batch_energies: needs a ReconFlow solve");
+    if (!b->d_energy) BC(cudaMalloc(&b->d_energy, sizeof(double) * b->n * (1 + kEnergyBlocks)));
+    const int B0 = b->base_idx();
+    for (int i = 0; i < b->n; i++) {
+        const LevelDims& d = b->dims[i][0];
+        const int nb = std::min(kEnergyBlocks, (d.w * d.h + 255) / 256);
+        double* e = b->d_energy + (size_t)i * (1 + kEnergyBlocks);
+        if (launch_energy(pair_plane(b, i, b->pI0(0)), pair_plane(b, i, b->pI1(0)),
+                          pair_plane(b, i, b->res_u), pair_plane(b, i, b->res_v),
+                          pair_plane(b, i, B0 + P_X), pair_plane(b, i, B0 + P_Y),
+                          pair_plane(b, i, B0 + P_Z), d, b->p.lambda, b->p.alpha_proj,
+                          &b->last_R1[(size_t)9 * i], &b->last_t1[(size_t)3 * i],
+                          &b->K1[(size_t)9 * i], 1, e + 1, nb, e, b->stream) != 0)
+            return bfail(RF_ERR_CUDA, "rf_batch_energies: launch");
+        b->launches += 2;
+        BC(cudaMemcpyAsync(out + i, e, sizeof(double), cudaMemcpyDeviceToHost, b->stream));
+    }
+    BC(cudaStreamSynchronize(b->stream));
+    return RF_OK;
+}
+
+rf_status rf_batch_image_planes(rf_batch* b, int pair, int level, const float** I0,
+                                const float** I1) {
+    if (!b || pair < 0 || pair >= b->n || level < 0 || level >= b->L)
+        return bfail(RF_ERR_INVALID_ARG, "rf_batch_image_planes: bad argument");
+    if (I0) *I0 = pair_plane(b, pair, b->pI0(level));
+    if (I1) *I1 = pair_plane(b, pair, b->pI1(level));
+    return RF_OK;
+}
+
+rf_status rf_batch_solve_warm_levels(rf_batch* b, const double* R0, const double* t0,
+                                     const double* R1, const double* t1, int level,
+                                     const int* warps, const int* iters) {
+    if (!b || !warps || !iters) return bfail(RF_ERR_INVALID_ARG, "rf_batch_solve_warm: null argument");
+    if (level < 0 || level >= b->L)
+        return bfail(RF_ERR_INVALID_ARG, "rf_batch_solve_warm: level out of range");
+    for (int l = 0; l <= level; l++)
+        if (warps[l] < 0 || iters[l] < 0 || warps[l] > 1000 || iters[l] > 100000)
+            return bfail(RF_ERR_INVALID_ARG, "rf_batch_solve_warm: schedule out of range");
+    rf_status rs = batch_poses(b, "rf_batch_solve_warm", R0, t0, R1, t1);
+    if (rs != RF_OK) return rs;
+    b->warm_level = level;
+    b->warm_warps.assign(warps, warps + level + 1);
+    b->warm_iters.assign(iters, iters + level + 1);
+    rs = run_batch(b, 2);
+    b->solved = rs == RF_OK;
+    return rs;
+}
+
+rf_status rf_batch_solve_warm(rf_batch* b, const double* R0, const double* t0, const double* R1,
+                              const double* t1, int level, int warps, int iters) {
+    if (!b) return bfail(RF_ERR_INVALID_ARG, "rf_batch_solve_warm: null batch");
+    if (level < 0 || level >= b->L)
+        return bfail(RF_ERR_INVALID_ARG, "rf_batch_solve_warm: level out of range");
+    std::vector<int> w(level + 1, warps), it(level + 1, iters);
+    return rf_batch_solve_warm_levels(b, R0, t0, R1, t1, level, w.data(), it.data());
 }
 
 rf_status rf_batch_solve_flow(rf_batch* b) {

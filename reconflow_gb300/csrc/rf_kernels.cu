@@ -125,7 +125,7 @@ __global__ void k_derivatives(const float* __restrict__ I0, const float* __restr
 #define RF_MINB_A 1
 #endif
 #ifndef RF_MINB_B
-#define RF_MINB_B 6  // 40 registers: 6 blocks per SM; measured 4% faster at 720p
+#define RF_MINB_B 4  // 64 registers: 4 blocks per SM (fewer registers spill; measured slower)
 #endif
 // Programmatic dependent launch: a kernel launched with the programmatic
 // stream-serialization attribute may start while its predecessor drains;

@@ -37,7 +37,10 @@ __device__ __forceinline__ void recon_a_px(const ReconFields& f, const LevelCons
     const int s = d.s;
     const int pos = ix + iy * s;
 
-    // --- data step (solveReconDataL1.cu:24-100) ---
+    // Every load of the pixel is issued before any arithmetic or store, so a
+    // thread waits for memory once.  The kernel writes only duhat, uproj and
+    // X1 at its own pixel, and reads none of those at another pixel, so the
+    // order of loads and stores does not change any value.
     float u = f.u[pos], v = f.v[pos];
     float dix = f.Ix[pos], diy = f.Iy[pos], dit = f.Iz[pos];
     float uproj = f.uproj[pos], vproj = f.vproj[pos];
@@ -61,46 +64,13 @@ __device__ __forceinline__ void recon_a_px(const ReconFields& f, const LevelCons
             pv2d = f.pv2[pos - s];
         }
     }
-    float A, dusub, dvsub;
-    if (PRIOR == 0) {
-        A = wt.A;
-        dusub = (wt.alpha_tv * duhat + wt.alpha_proj * (uproj - u - sku)) / A;
-        dvsub = (wt.alpha_tv * dvhat + wt.alpha_proj * (vproj - v - skv)) / A;
-    } else {
-        float alphaFn = PRIOR == 2 ? wt.alpha_fn * f.mask[pos] : wt.alpha_fn;
-        float ufn = f.ufn[pos], vfn = f.vfn[pos];
-        A = wt.alpha_tv + wt.alpha_proj + alphaFn;
-        dusub = (alphaFn * (ufn - u) + wt.alpha_tv * duhat + wt.alpha_proj * (uproj - u - sku)) / A;
-        dvsub = (alphaFn * (vfn - v) + wt.alpha_tv * dvhat + wt.alpha_proj * (vproj - v - skv)) / A;
-    }
-    float du, dv;
-    l1_threshold(dusub, dvsub, dix, diy, dit, wt.lambda, A, du, dv);
-    float divpu = divergence(pu1, pu1l, pu2, pu2d, ix, iy);
-    float divpv = divergence(pv1, pv1l, pv2, pv2d, ix, iy);
-    float duhat1 = du + divpu / A;
-    float dvhat1 = dv + divpv / A;
-    f.duhat[pos] = duhat1;
-    f.dvhat[pos] = dvhat1;
-
-    // --- projection blend (solveUVProj.cu:13-21), uc from the current 3D ---
+    // X0, Y0, Z0 at: 0 = pos, 1 = x+1 (flat pos+1), 2 = y+1 (flat pos+s),
+    // 3 = x-1, 4 = y-1.  x+1 / y+1 are read at flat pos+1 / pos+s even on the
+    // last column / row (solve3dMinimalArea.cu:65,76).
     float Xn[5], Yn[5], Zn[5];
     Xn[0] = f.X[pos];
     Yn[0] = f.Y[pos];
     Zn[0] = f.Z[pos];
-    float uc, vc;
-    if (uc_from_buffer) {
-        uc = f.uc[pos];
-        vc = f.vc[pos];
-    } else {
-        project_uc(c, Xn[0], Yn[0], Zn[0], ix, iy, uc, vc);
-    }
-    float uproj1 = (wt.lambdaf * uc + wt.alpha_proj * (u + duhat1 + sku)) / wt.proj_den;
-    float vproj1 = (wt.lambdaf * vc + wt.alpha_proj * (v + dvhat1 + skv)) / wt.proj_den;
-    f.uproj[pos] = uproj1;
-    f.vproj[pos] = vproj1;
-
-    // --- triangulation with minimal-area smoothing (solve3dMinimalArea.cu:23-184) ---
-    // x+1 / y+1 are read at flat pos+1 / pos+s even on the last column / row.
     Xn[1] = f.X[pos + 1];
     Yn[1] = f.Y[pos + 1];
     Zn[1] = f.Z[pos + 1];
@@ -119,8 +89,56 @@ __device__ __forceinline__ void recon_a_px(const ReconFields& f, const LevelCons
         Yn[4] = f.Y[pos - s];
         Zn[4] = f.Z[pos - s];
     }
+    float ucb = 0.0f, vcb = 0.0f;
+    if (uc_from_buffer) {
+        ucb = f.uc[pos];
+        vcb = f.vc[pos];
+    }
+    float ufn = 0.0f, vfn = 0.0f, mk = 1.0f;
+    if (PRIOR != 0) {
+        ufn = f.ufn[pos];
+        vfn = f.vfn[pos];
+        if (PRIOR == 2) mk = f.mask[pos];
+    }
+
+    // --- data step (solveReconDataL1.cu:24-100) ---
+    float A, dusub, dvsub;
+    if (PRIOR == 0) {
+        A = wt.A;
+        dusub = (wt.alpha_tv * duhat + wt.alpha_proj * (uproj - u - sku)) / A;
+        dvsub = (wt.alpha_tv * dvhat + wt.alpha_proj * (vproj - v - skv)) / A;
+    } else {
+        float alphaFn = PRIOR == 2 ? wt.alpha_fn * mk : wt.alpha_fn;
+        A = wt.alpha_tv + wt.alpha_proj + alphaFn;
+        dusub = (alphaFn * (ufn - u) + wt.alpha_tv * duhat + wt.alpha_proj * (uproj - u - sku)) / A;
+        dvsub = (alphaFn * (vfn - v) + wt.alpha_tv * dvhat + wt.alpha_proj * (vproj - v - skv)) / A;
+    }
+    float du, dv;
+    l1_threshold(dusub, dvsub, dix, diy, dit, wt.lambda, A, du, dv);
+    float divpu = divergence(pu1, pu1l, pu2, pu2d, ix, iy);
+    float divpv = divergence(pv1, pv1l, pv2, pv2d, ix, iy);
+    float duhat1 = du + divpu / A;
+    float dvhat1 = dv + divpv / A;
+
+    // --- projection blend (solveUVProj.cu:13-21), uc from the current 3D ---
+    float uc, vc;
+    if (uc_from_buffer) {
+        uc = ucb;
+        vc = vcb;
+    } else {
+        project_uc(c, Xn[0], Yn[0], Zn[0], ix, iy, uc, vc);
+    }
+    float uproj1 = (wt.lambdaf * uc + wt.alpha_proj * (u + duhat1 + sku)) / wt.proj_den;
+    float vproj1 = (wt.lambdaf * vc + wt.alpha_proj * (v + dvhat1 + skv)) / wt.proj_den;
+
+    // --- triangulation with minimal-area smoothing (solve3dMinimalArea.cu:23-184) ---
     float Xo, Yo, Zo;
     solve3d_pixel(c, uproj1, vproj1, ix, iy, Xn, Yn, Zn, wt.lambdaf, wt.lambdams, Xo, Yo, Zo);
+
+    f.duhat[pos] = duhat1;
+    f.dvhat[pos] = dvhat1;
+    f.uproj[pos] = uproj1;
+    f.vproj[pos] = vproj1;
     f.X1[pos] = Xo;
     f.Y1[pos] = Yo;
     f.Z1[pos] = Zo;
@@ -143,22 +161,17 @@ __device__ __forceinline__ void recon_b_px(const ReconFields& f, const Weights& 
     const int s = d.s, w = d.w, h = d.h;
     const int pos = ix + iy * s;
 
-    // --- dual TV step (solveSmoothDualTVGlobal.cu:26-64) ---
+    // All loads first (see recon_a_px): the kernel writes p, X and sk only at
+    // its own pixel and reads p and sk only there, and reads no X.
     float duhat = f.duhat[pos], dvhat = f.dvhat[pos];
-    float dux, duy, dvx, dvy;
-    if ((ix + 1) >= w) {
-        dux = 0.0f;
-        dvx = 0.0f;
-    } else {
-        dux = f.duhat[pos + 1] - duhat;
-        dvx = f.dvhat[pos + 1] - dvhat;
+    float duhr = 0.0f, dvhr = 0.0f, duhd = 0.0f, dvhd = 0.0f;
+    if ((ix + 1) < w) {
+        duhr = f.duhat[pos + 1];
+        dvhr = f.dvhat[pos + 1];
     }
-    if ((iy + 1) >= h) {
-        duy = 0.0f;
-        dvy = 0.0f;
-    } else {
-        duy = f.duhat[pos + s] - duhat;
-        dvy = f.dvhat[pos + s] - dvhat;
+    if ((iy + 1) < h) {
+        duhd = f.duhat[pos + s];
+        dvhd = f.dvhat[pos + s];
     }
     float pu1 = 0.0f, pu2 = 0.0f, pv1 = 0.0f, pv2 = 0.0f;
     if (!first) {
@@ -167,16 +180,6 @@ __device__ __forceinline__ void recon_b_px(const ReconFields& f, const Weights& 
         pv1 = f.pv1[pos];
         pv2 = f.pv2[pos];
     }
-    dual_step(dux, duy, wt.fac, pu1, pu2);
-    dual_step(dvx, dvy, wt.fac, pv1, pv2);
-    f.pu1[pos] = pu1;
-    f.pu2[pos] = pu2;
-    f.pv1[pos] = pv1;
-    f.pv2[pos] = pv2;
-
-    // --- 3x3 median of the triangulated points, then clean-up ---
-    // (Solve3d outputs are finite: non-finite results fall back to the
-    // previous, finite, state; so the min/max median network applies.)
     float mX[9], mY[9], mZ[9];
     if (ix > 0 && iy > 0 && ix + 1 < w && iy + 1 < h) {
 #pragma unroll
@@ -190,6 +193,7 @@ __device__ __forceinline__ void recon_b_px(const ReconFields& f, const Weights& 
             }
         }
     } else {
+        // 3x3 taps with the reference's border rules (medianFilter.cu:181-214)
 #pragma unroll
         for (int j = 0; j < 3; j++) {
 #pragma unroll
@@ -202,19 +206,49 @@ __device__ __forceinline__ void recon_b_px(const ReconFields& f, const Weights& 
             }
         }
     }
+    const float sku = f.sku[pos], skv = f.skv[pos];
+    const float u = f.u[pos], v = f.v[pos];
+    const float uproj = f.uproj[pos], vproj = f.vproj[pos];
+
+    // --- dual TV step (solveSmoothDualTVGlobal.cu:26-64) ---
+    float dux, duy, dvx, dvy;
+    if ((ix + 1) >= w) {
+        dux = 0.0f;
+        dvx = 0.0f;
+    } else {
+        dux = duhr - duhat;
+        dvx = dvhr - dvhat;
+    }
+    if ((iy + 1) >= h) {
+        duy = 0.0f;
+        dvy = 0.0f;
+    } else {
+        duy = duhd - duhat;
+        dvy = dvhd - dvhat;
+    }
+    dual_step(dux, duy, wt.fac, pu1, pu2);
+    dual_step(dvx, dvy, wt.fac, pv1, pv2);
+
+    // --- 3x3 median of the triangulated points, then clean-up ---
+    // (Solve3d outputs are finite: non-finite results fall back to the
+    // previous, finite, state; so the min/max median network applies.)
     float X1 = mX[4], Y1 = mY[4], Z1 = mZ[4];
     float Xm = median9_finite(mX);
     float Ym = median9_finite(mY);
     float Zm = median9_finite(mZ);
     float Xo, Yo, Zo;
     cleanup_pixel(X1, Y1, Z1, Xm, Ym, Zm, Xo, Yo, Zo);
+
+    f.pu1[pos] = pu1;
+    f.pu2[pos] = pu2;
+    f.pv1[pos] = pv1;
+    f.pv2[pos] = pv2;
     f.X[pos] = Xo;
     f.Y[pos] = Yo;
     f.Z[pos] = Zo;
-
     // --- multiplier update (solveUcSk.cu:94-95) ---
-    f.sku[pos] = f.sku[pos] + f.u[pos] + duhat - f.uproj[pos];
-    f.skv[pos] = f.skv[pos] + f.v[pos] + dvhat - f.vproj[pos];
+    f.sku[pos] = sku + u + duhat - uproj;
+    f.skv[pos] = skv + v + dvhat - vproj;
 }
 
 __device__ __forceinline__ int median5_tap(int col, int row, int w, int h, int s) {

@@ -369,6 +369,68 @@ class ReconFlowBatch:
     def solveOpticalFlow(self):
         N.check(self._lib.rf_batch_solve_flow(self._h))
 
+    def _poses(self, R1s, t1s, R0s, t0s):
+        R1 = np.ascontiguousarray(np.asarray(R1s, np.float64).reshape(self.n, 9))
+        t1 = np.ascontiguousarray(np.asarray(t1s, np.float64).reshape(self.n, 3))
+        R0 = None if R0s is None else np.ascontiguousarray(np.asarray(R0s, np.float64).reshape(self.n, 9))
+        t0 = None if t0s is None else np.ascontiguousarray(np.asarray(t0s, np.float64).reshape(self.n, 3))
+        return R0, t0, R1, t1
+
+    def solveWarm(self, level, R1s, t1s, nWarpIters, nSolverIters, R0s=None, t0s=None):
+        """Warm-started solve (rf_batch_solve_warm_levels): every pair starts at
+        `level` from the planes of warmPlanes(pair).  nWarpIters and
+        nSolverIters are ints (every level) or sequences indexed by level
+        (0 = finest, level + 1 entries)."""
+        R0, t0, R1, t1 = self._poses(R1s, t1s, R0s, t0s)
+        n = int(level) + 1
+        w = [int(nWarpIters)] * n if np.isscalar(nWarpIters) else [int(x) for x in nWarpIters]
+        it = [int(nSolverIters)] * n if np.isscalar(nSolverIters) else [int(x) for x in nSolverIters]
+        if len(w) != n or len(it) != n:
+            raise ValueError("per-level schedules need level + 1 entries")
+        wa, ia = (ctypes.c_int * n)(*w), (ctypes.c_int * n)(*it)
+        N.check(self._lib.rf_batch_solve_warm_levels(self._h, None if R0 is None else _ptr(R0),
+                                                     None if t0 is None else _ptr(t0), _ptr(R1),
+                                                     _ptr(t1), int(level), wa, ia))
+
+    def energies(self):
+        """Energy of every pair's last solution (rf_batch_energies)."""
+        out = np.zeros(self.n, np.float64)
+        N.check(self._lib.rf_batch_energies(self._h, out.ctypes.data_as(ctypes.c_void_p)))
+        return out
+
+    def warmPlanes(self, pair):
+        """Device pointers (u, v, X, Y, Z) of pair's warm-start input planes."""
+        ps = [ctypes.c_void_p() for _ in range(5)]
+        N.check(self._lib.rf_batch_warm_planes(self._h, int(pair), *[ctypes.byref(p) for p in ps]))
+        return [p.value for p in ps]
+
+    def imagePlanes(self, pair, level=0):
+        a, b = ctypes.c_void_p(), ctypes.c_void_p()
+        N.check(self._lib.rf_batch_image_planes(self._h, int(pair), int(level), ctypes.byref(a),
+                                                ctypes.byref(b)))
+        return a.value, b.value
+
+    def copyImagesToDeviceFromDevice(self, pair, ptr0, ptr1, pitch):
+        N.check(self._lib.rf_batch_upload_images_device(self._h, int(pair), ctypes.c_void_p(ptr0),
+                                                        ctypes.c_void_p(ptr1), int(pitch)))
+
+    def levelDims(self, pair, level):
+        """(w, h, stride) of pair's pyramid level (Cudaflow.cu:146-171 rule)."""
+        w, h = self.sizes[pair]
+        s = self.strides[pair]
+        sc = float(self.params.scale)
+        al = int(self.params.stride_alignment)
+        for _ in range(level):
+            h = int(float(h) / sc)
+            w = int(float(w) / sc)
+            s = (w + al - 1) // al * al
+        return w, h, s
+
+    def deviceResults(self, pair):
+        ps = [ctypes.c_void_p() for _ in range(5)]
+        N.check(self._lib.rf_batch_device_results(self._h, int(pair), *[ctypes.byref(p) for p in ps]))
+        return [p.value for p in ps]
+
     def _out(self, pair):
         w, h = self.sizes[pair]
         return np.zeros((h, self.strides[pair]), np.float32)

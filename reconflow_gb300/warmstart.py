@@ -2,23 +2,28 @@
 
 A small BF16 convolutional encoder-decoder (``rf_cnn_*`` in the C ABI; all of
 its forward, backward and optimizer work runs in this library's own CUDA
-kernels) maps a coarse image pair plus the camera pose to flow and inverse
-depth.  It is trained on flow and depth fields produced by the plain solver
-itself on seeded synthetic scenes, then used to start the solve at a finer
-pyramid level (``ReconFlow.solveWarm``) with fewer iterations.  The solution
-energy (``ReconFlow.energy``) decides whether the warm-started result is kept
-or the plain solve is used instead.
+kernels) maps a coarse frame pair plus the camera pose to flow and inverse
+depth.  Its input is built on the GPU by ``rf_ws_features``: the two coarse
+frames and a plane sweep of photometric costs over inverse depth along each
+pixel's epipolar line (the pose and intrinsics enter through the sweep), so
+the network regresses inverse depth from matching evidence rather than
+learning the camera geometry.  ``rf_ws_state`` turns its inverse depth into
+the solver's state at a pyramid level (3D points and their flow, exactly as
+the solver's projection forms it), and ``ReconFlowBatch.solveWarm`` refines
+from there with fewer levels, warps and iterations than the plain solve.
+The network is trained on flow and depth fields produced by the plain
+solver itself on seeded synthetic scenes.
 
-Scale convention: the network sees images sampled at the same angular
-resolution in training and use: 640x480 pairs (f = 500) at 1/8 scale (80x60)
-in training, 1280x720 pairs (f = 1000) at 1/16 (80x45) in use.  Its finer
-output is at the input resolution, its coarser output at half of it; flow is
-in pixels of the output's own grid, inverse depth in 1/m.
+Scale convention: the network sees frames at the same angular resolution in
+training and use (focal length 125 px on its input grid): 640x480 pairs
+(f = 500) at 1/4 scale (160x120) in training, 1280x720 pairs (f = 1000) at
+1/8 (160x90) in use.  Its finer output is on its input grid (1/8 of a 720p
+frame), its coarser output at half of it (1/16); flow is in pixels of the
+output's own grid, inverse depth in 1/m.
 """
 from __future__ import annotations
 
 import ctypes
-import math
 import struct
 import zlib
 
@@ -28,33 +33,10 @@ from . import _native as N
 
 IN_CH = 16
 OUT_CH = 8
-LOSS_WEIGHTS = (1.0, 1.0, 10.0)  # u, v, inverse depth
-
-
-def rotation_vector(R) -> np.ndarray:
-    R = np.asarray(R, np.float64)
-    c = (np.trace(R) - 1.0) / 2.0
-    ang = math.acos(max(-1.0, min(1.0, c)))
-    if ang < 1e-12:
-        return np.zeros(3)
-    v = np.array([R[2, 1] - R[1, 2], R[0, 2] - R[2, 0], R[1, 0] - R[0, 1]])
-    return v * (ang / (2.0 * math.sin(ang)))
-
-
-def make_input(I0c, I1c, R, t) -> np.ndarray:
-    """(H, W) coarse frames + pose -> (H, W, 16) float32 network input."""
-    H, W = I0c.shape
-    x = np.zeros((H, W, IN_CH), np.float32)
-    x[..., 0] = I0c
-    x[..., 1] = I1c
-    x[..., 2] = (np.arange(W)[None, :] + 0.5) / W - 0.5
-    x[..., 3] = (np.arange(H)[:, None] + 0.5) / H - 0.5
-    rv = rotation_vector(R) * 30.0
-    tt = np.asarray(t, np.float64) * 10.0
-    for k in range(3):
-        x[..., 4 + k] = rv[k]
-        x[..., 7 + k] = tt[k]
-    return x
+# u, v, inverse depth: the warm start uses the inverse depth; the flow heads
+# are an auxiliary task
+LOSS_WEIGHTS = (0.1, 0.1, 10.0)
+F_NET = 125.0  # focal length (pixels) of the network's input grid
 
 
 def box_down(a: np.ndarray, f: int) -> np.ndarray:
@@ -63,6 +45,56 @@ def box_down(a: np.ndarray, f: int) -> np.ndarray:
     H, W = a.shape[0] // f * f, a.shape[1] // f * f
     a = a[:H, :W]
     return a.reshape(H // f, f, W // f, f, *a.shape[2:]).mean(axis=(1, 3))
+
+
+def _dptr_array(ptrs):
+    return (ctypes.c_void_p * len(ptrs))(*[ctypes.c_void_p(int(p)) for p in ptrs])
+
+
+def _dbl_rows(rows, k):
+    a = np.ascontiguousarray(np.asarray(rows, np.float64).reshape(-1, k))
+    return a, a.ctypes.data_as(ctypes.c_void_p)
+
+
+def features(I0_ptrs, I1_ptrs, w0, h0, s0, factor, Ks, Rs, ts, out, stream=0):
+    """rf_ws_features: network input for n pairs of device frames into the
+    (n, h0 // factor, w0 // factor, 16) float32 CUDA tensor `out`."""
+    lib = N.load()
+    n = len(I0_ptrs)
+    assert out.shape == (n, h0 // factor, w0 // factor, IN_CH) and out.is_contiguous()
+    K, pK = _dbl_rows(Ks, 9)
+    R, pR = _dbl_rows(Rs, 9)
+    t, pt = _dbl_rows(ts, 3)
+    N.check(lib.rf_ws_features(n, _dptr_array(I0_ptrs), _dptr_array(I1_ptrs), int(w0), int(h0),
+                               int(s0), int(factor), pK, pR, pt, ctypes.c_void_p(out.data_ptr()),
+                               ctypes.c_void_p(stream or 0)))
+    return out
+
+
+def state(net_out, w, h, s, up, K_level, Rs, ts, planes, stream=0):
+    """rf_ws_state: warm-start planes (u, v, X, Y, Z device pointers per
+    pair) at a w x h level from the network output tensor (n, hn, wn, C)."""
+    lib = N.load()
+    n, hn, wn, C = net_out.shape
+    K, pK = _dbl_rows(K_level, 9)
+    R, pR = _dbl_rows(Rs, 9)
+    t, pt = _dbl_rows(ts, 3)
+    cols = list(zip(*planes))
+    N.check(lib.rf_ws_state(n, ctypes.c_void_p(net_out.data_ptr()), int(C), int(wn), int(hn),
+                            int(w), int(h), int(s), ctypes.c_float(up), pK, pR, pt,
+                            *[_dptr_array(c) for c in cols], ctypes.c_void_p(stream or 0)))
+
+
+def level_intrinsics(K, level, scale=2.0):
+    """K at a pyramid level with K[2][2] = 1 (the K-pyramid fix)."""
+    Kl = np.array(K, np.float64).copy()
+    for _ in range(level):
+        Kl[0, 0] /= scale
+        Kl[0, 2] /= scale
+        Kl[1, 1] /= scale
+        Kl[1, 2] /= scale
+    Kl[2, 2] = 1.0
+    return Kl
 
 
 class WarmStartNet:
@@ -90,6 +122,9 @@ class WarmStartNet:
 
     def set_stream(self, stream_ptr):
         N.check(self._lib.rf_cnn_set_stream(self._h, ctypes.c_void_p(stream_ptr or 0)))
+
+    def kernel_launches(self) -> int:
+        return int(self._lib.rf_cnn_kernel_launches(self._h))
 
     def params(self) -> np.ndarray:
         out = np.zeros(self.n_params, np.float32)
@@ -154,23 +189,56 @@ class WarmStartNet:
 # Training data from the plain solver
 # ---------------------------------------------------------------------------
 
-SOLVER_640 = dict(levels=5, warps=3, iters=50)  # the 640x480 workload's schedule
+# the 640x480 workload's schedule and the solver weights of the benchmarks
+SOLVER_640 = dict(levels=5, warps=3, iters=50)
+SOLVER_WEIGHTS = dict(lambda_=50.0, lambdaf=0.1, lambdams=100.0, alphaTv=1 / 0.33, alphaProj=60.0,
+                      tau=0.25, fix_quirks=1)
+
+
+def _targets(u, v, Z, f):
+    """(H/f, W/f, 8) target and (H/f, W/f) mask from a level-0 solution:
+    flow / f and inverse depth box-averaged; the mask keeps blocks whose every
+    pixel has a finite flow and a depth in (0.5, 50) m."""
+    with np.errstate(divide="ignore", invalid="ignore"):
+        ok = np.isfinite(u) & np.isfinite(v) & np.isfinite(Z) & (Z > 0.5) & (Z < 50.0)
+        inv = np.where(ok, 1.0 / Z, 0.0)
+    u0 = np.where(ok, u, 0.0)
+    v0 = np.where(ok, v, 0.0)
+    okf = box_down(ok.astype(np.float32), f)
+    H, W = okf.shape
+    t = np.zeros((H, W, OUT_CH), np.float32)
+    den = np.maximum(okf, 1e-6)
+    t[..., 0] = box_down(u0, f) / den / f
+    t[..., 1] = box_down(v0, f) / den / f
+    t[..., 2] = box_down(inv, f) / den
+    m = (okf > 0.99).astype(np.float32)
+    t[m == 0] = 0.0
+    return t, m
 
 
 def training_set(n_scenes: int, seed0: int = 10_000, width: int = 640, height: int = 480,
-                 batch: int = 64, solver_params=None, device="cuda"):
-    """Render n seeded scenes, solve them with the plain (batched) solver and
-    return network inputs at 1/8 and targets at 1/8 and 1/16 (numpy)."""
+                 factor: int = 4, batch: int = 64, solver_params=None, log=None):
+    """Render n seeded scenes on the GPU, solve them with the plain batched
+    solver (the 640x480 schedule) and return numpy arrays: network inputs at
+    1/factor, targets and masks at 1/(2 factor) and 1/factor, and the
+    ground-truth inverse depth at 1/factor (for reporting only)."""
+    import time
+
+    import torch
+
     from .reconflow import ReconFlowBatch
     from .scene import make_scene
 
-    sp = dict(lambda_=50.0, lambdaf=0.1, lambdams=100.0, alphaTv=1 / 0.33, alphaProj=60.0,
-              tau=0.25, fix_quirks=1)
+    sp = dict(SOLVER_WEIGHTS)
     sp.update(solver_params or {})
-    xs, t8s, m8s, t16s, m16s = [], [], [], [], []
+    hn, wn = height // factor, width // factor
+    xs, t8s, m8s, t16s, m16s, gts = [], [], [], [], [], []
+    t_render = t_solve = 0.0
     for b0 in range(0, n_scenes, batch):
         n = min(batch, n_scenes - b0)
-        scenes = [make_scene(width, height, seed=seed0 + b0 + i, device=device) for i in range(n)]
+        ta = time.perf_counter()
+        scenes = [make_scene(width, height, seed=seed0 + b0 + i, device="cuda") for i in range(n)]
+        tb = time.perf_counter()
         bt = ReconFlowBatch([(width, height)] * n, SOLVER_640["levels"], method=14,
                             nWarpIters=SOLVER_640["warps"], nSolverIters=SOLVER_640["iters"], **sp)
         for i, sc in enumerate(scenes):
@@ -179,43 +247,49 @@ def training_set(n_scenes: int, seed0: int = 10_000, width: int = 640, height: i
             bt.setCameraMatrices(i, sc["K"], sc["K"])
             bt.copyImagesToDevice(i, pad(sc["I0"]), pad(sc["I1"]))
         bt.solveR([sc["R"] for sc in scenes], [sc["t"] for sc in scenes])
+        x = torch.empty((n, hn, wn, IN_CH), device="cuda")
+        planes = [bt.imagePlanes(i, 0) for i in range(n)]
+        features([p[0] for p in planes], [p[1] for p in planes], width, height, bt.strides[0],
+                 factor, [sc["K"] for sc in scenes], [sc["R"] for sc in scenes],
+                 [sc["t"] for sc in scenes], x)
+        xs.append(x.cpu().numpy())
         for i, sc in enumerate(scenes):
             u, v = bt.copyOpticalFlowToHost(i)
             _, _, Z = bt.copy3dToHost(i)
             u, v, Z = u[:, :width], v[:, :width], Z[:, :width]
-            with np.errstate(divide="ignore", invalid="ignore"):
-                inv = np.where((Z > 0.5) & (Z < 50.0) & np.isfinite(Z), 1.0 / Z, 0.0)
-            ok = (inv > 0).astype(np.float32)
-            for f, (tl, ml) in ((8, (t8s, m8s)), (16, (t16s, m16s))):
-                t = np.zeros((height // f, width // f, OUT_CH), np.float32)
-                t[..., 0] = box_down(u, f) / f
-                t[..., 1] = box_down(v, f) / f
-                okf = box_down(ok, f)
-                with np.errstate(invalid="ignore"):
-                    t[..., 2] = np.where(okf > 0, box_down(inv, f) / np.maximum(okf, 1e-6), 0.0)
+            for f, (tl, ml) in ((factor, (t8s, m8s)), (2 * factor, (t16s, m16s))):
+                t, m = _targets(u, v, Z, f)
                 tl.append(t)
-                ml.append((okf > 0.99).astype(np.float32))
-            xs.append(make_input(box_down(sc["I0"], 8), box_down(sc["I1"], 8), sc["R"], sc["t"]))
+                ml.append(m)
+            gts.append(box_down(sc["inv_depth"], factor))
         bt.close()
-    return (np.stack(xs), np.stack(t16s), np.stack(m16s), np.stack(t8s), np.stack(m8s))
+        t_solve += time.perf_counter() - tb
+        t_render += tb - ta
+        if log:
+            log(f"training set: {b0 + n} / {n_scenes} scenes (render {t_render:.0f} s, "
+                f"solve + features {t_solve:.0f} s)")
+    return (np.concatenate(xs), np.stack(t16s), np.stack(m16s), np.stack(t8s), np.stack(m8s),
+            np.stack(gts))
 
 
 def train(net: WarmStartNet, data, epochs: int = 20, batch: int = 64, lr: float = 1e-3,
-          seed: int = 0, log=None):
-    """Adam on shuffled mini-batches; returns the loss per epoch."""
+          seed: int = 0, log=None, lr_decay_at=None, weights=LOSS_WEIGHTS):
+    """Adam on shuffled mini-batches; returns the loss per epoch.  `data` =
+    (x, t16, m16, t8, m8[, ...]) numpy arrays or CUDA tensors."""
     import torch
 
-    x, t16, m16, t8, m8 = (torch.as_tensor(a, device="cuda") for a in data)
+    x, t16, m16, t8, m8 = (torch.as_tensor(a, device="cuda") for a in data[:5])
     n = x.shape[0]
     rng = np.random.default_rng(seed)
     hist = []
     for ep in range(epochs):
+        cur = lr * (0.1 if lr_decay_at is not None and ep >= lr_decay_at else 1.0)
         perm = rng.permutation(n)
         tot, cnt = 0.0, 0
         for b0 in range(0, n - batch + 1 if n >= batch else 1, batch):
             idx = torch.as_tensor(perm[b0:b0 + batch], device="cuda")
-            loss = net.backward(x[idx], t16[idx], m16[idx], t8[idx], m8[idx])
-            net.adam_step(lr)
+            loss = net.backward(x[idx], t16[idx], m16[idx], t8[idx], m8[idx], weights)
+            net.adam_step(cur)
             tot += loss
             cnt += 1
         hist.append(tot / max(cnt, 1))
@@ -225,49 +299,107 @@ def train(net: WarmStartNet, data, epochs: int = 20, batch: int = 64, lr: float 
 
 
 # ---------------------------------------------------------------------------
-# Warm-started solve of a 1280x720 pair
+# Warm-started batched solve
 # ---------------------------------------------------------------------------
 
-def predict(net: WarmStartNet, I0, I1, R, t, factor: int):
-    """Network prediction for one pair at 1/factor scale: (u, v, inv_depth)
-    on the input grid of the network (flow in its pixels)."""
+def net_factor(K, f_net: float = F_NET) -> int:
+    """Power-of-two downscale that brings a camera's focal length closest to
+    the network's (8 for 1280x720 at f = 1000, 4 for 640x480 at f = 500)."""
+    f = float(np.asarray(K)[0, 0])
+    k = max(0, int(round(np.log2(max(f / f_net, 1.0)))))
+    return 1 << k
+
+
+class LearnedBatchSolver:
+    """Batched ReconFlow solve started from the network's prediction.
+
+    All pairs share one size.  solve() runs, on one CUDA stream: the input
+    features at 1/factor (rf_ws_features), the network forward pass
+    (rf_cnn_forward), the warm-start state at pyramid level `warm_level`
+    from the network's finer output (rf_ws_state, written into the batch's
+    warm planes) and the refinement from that level (rf_batch_solve_warm)
+    with `warps` x `iters` per level."""
+
+    def __init__(self, net: WarmStartNet, batch, size, K, warm_level=2, warps=2, iters=20):
+        import torch
+
+        self.net, self.batch = net, batch
+        self.w, self.h = size
+        self.factor = net_factor(K)
+        self.hn, self.wn = self.h // self.factor, self.w // self.factor
+        n = batch.n
+        if n > net.max_batch or self.hn > net.height or self.wn > net.width:
+            raise ValueError("network buffers are smaller than the batch")
+        self.x = torch.empty((n, self.hn, self.wn, IN_CH), device="cuda")
+        self.o16 = torch.empty((n, (self.hn + 1) // 2, (self.wn + 1) // 2, OUT_CH), device="cuda")
+        self.o8 = torch.empty((n, self.hn, self.wn, OUT_CH), device="cuda")
+        self.warm_level, self.warps, self.iters = warm_level, warps, iters
+        lw, lh, ls = batch.levelDims(0, warm_level)
+        self.level_dims = (lw, lh, ls)
+        self.up = float(self.factor) / float(2 ** warm_level)
+        self.planes = [batch.warmPlanes(i) for i in range(n)]
+        self.images = [batch.imagePlanes(i, 0) for i in range(n)]
+        self.stream = 0
+
+    def set_stream(self, stream_ptr):
+        self.stream = stream_ptr or 0
+        self.batch.setStream(stream_ptr)
+        self.net.set_stream(stream_ptr)
+
+    def predict(self, Ks, Rs, ts):
+        features([p[0] for p in self.images], [p[1] for p in self.images], self.w, self.h,
+                 self.batch.strides[0], self.factor, Ks, Rs, ts, self.x, self.stream)
+        self.net.forward(self.x, self.o16, self.o8)
+        return self.o16, self.o8
+
+    def solve(self, Ks, Rs, ts):
+        self.predict(Ks, Rs, ts)
+        lw, lh, ls = self.level_dims
+        Kl = [level_intrinsics(K, self.warm_level) for K in Ks]
+        state(self.o8, lw, lh, ls, self.up, Kl, Rs, ts, self.planes, self.stream)
+        self.batch.solveWarm(self.warm_level, Rs, ts, self.warps, self.iters)
+
+
+# ---------------------------------------------------------------------------
+# Command line: train the network and write a checkpoint
+# ---------------------------------------------------------------------------
+
+def main(argv=None):
+    """python -m reconflow_gb300.warmstart --scenes N --epochs E --out PATH
+
+    Renders N seeded 640x480 scenes (seeds 10000 ...), solves them with the
+    plain batched solver, trains the network on its results (the last
+    N // 8 scenes held out) and writes the checkpoint."""
+    import argparse
+    import time
+
+    ap = argparse.ArgumentParser(description=main.__doc__.split("\n\n")[0])
+    ap.add_argument("--scenes", type=int, default=4096)
+    ap.add_argument("--epochs", type=int, default=30)
+    ap.add_argument("--lr", type=float, default=1e-3)
+    ap.add_argument("--seed", type=int, default=0)
+    ap.add_argument("--out", required=True)
+    a = ap.parse_args(argv)
+    t0 = time.time()
+    log = lambda m: print(f"[{time.time() - t0:7.1f} s] {m}", flush=True)  # noqa: E731
+    data = training_set(a.scenes, log=log)
+    nh = max(1, a.scenes // 8)
+    tr = tuple(d[:-nh] for d in data[:5])
+    te = tuple(d[-nh:] for d in data)
+    net = WarmStartNet(64, 120, 160, seed=a.seed)
+    train(net, tr, epochs=a.epochs, batch=64, lr=a.lr, seed=a.seed, log=log,
+          lr_decay_at=int(a.epochs * 0.75))
+    net.save(a.out)
     import torch
 
-    x = make_input(box_down(I0, factor), box_down(I1, factor), R, t)
-    _, o8 = net.forward(torch.as_tensor(x[None], device="cuda"))
-    o = o8[0].cpu().numpy()
-    return o[..., 0], o[..., 1], o[..., 2]
+    xt = torch.as_tensor(te[0], device="cuda")
+    p8 = np.concatenate([net.forward(xt[b0:b0 + 64])[1].cpu().numpy() for b0 in range(0, nh, 64)])
+    m = te[4] > 0
+    rel = (np.abs(p8[..., 2] - te[3][..., 2]) / np.maximum(te[3][..., 2], 1e-3))[m]
+    relgt = (np.abs(p8[..., 2] - te[5]) / te[5])[m]
+    log(f"held out ({nh} scenes): inverse depth relative error, median {np.median(rel):.4f} "
+        f"against the plain solver, {np.median(relgt):.4f} against ground truth; wrote {a.out}")
 
 
-def warm_state(pred, K, level_shape, level_stride, scale_up: int, level_K):
-    """Upsample a prediction to the warm-start level: flow scaled by
-    scale_up, inverse depth turned into 3D points with that level's K."""
-    import torch
-    import torch.nn.functional as F
-
-    u, v, inv = pred
-    h, w = level_shape
-    t = torch.as_tensor(np.stack([u * scale_up, v * scale_up, inv])[None], dtype=torch.float32)
-    up = F.interpolate(t, size=(h, w), mode="bilinear", align_corners=False)[0].numpy()
-    uu, vv = up[0], up[1]
-    inv = np.clip(up[2], 0.02, 2.0)
-    Z = 1.0 / inv
-    fx, fy, cx, cy = level_K[0, 0], level_K[1, 1], level_K[0, 2], level_K[1, 2]
-    xs = np.arange(w)[None, :]
-    ys = np.arange(h)[:, None]
-    X = Z * (xs - cx) / fx
-    Y = Z * (ys - cy) / fy
-    pad = lambda a: np.pad(a, ((0, 0), (0, level_stride - w))).astype(np.float32)  # noqa: E731
-    return pad(uu), pad(vv), pad(X), pad(Y), pad(Z)
-
-
-def level_intrinsics(K, level, scale=2.0):
-    """K at a pyramid level with K[2][2] = 1 (the K-pyramid fix)."""
-    Kl = np.array(K, np.float64).copy()
-    for _ in range(level):
-        Kl[0, 0] /= scale
-        Kl[0, 2] /= scale
-        Kl[1, 1] /= scale
-        Kl[1, 2] /= scale
-    Kl[2, 2] = 1.0
-    return Kl
+if __name__ == "__main__":
+    main()

@@ -83,25 +83,137 @@ def test_training_reduces_loss_and_is_deterministic(torch_cuda):
     np.testing.assert_allclose(losses[0], losses[1], rtol=1e-12)
 
 
-def test_warm_start_pipeline_runs(torch_cuda, rf):
-    """Predict at 1/8 of a 640x480 pair, start the solve at level 2 from the
-    prediction, and check the energy-based decision is available."""
-    from reconflow_gb300.scene import make_scene
-    from reconflow_gb300.warmstart import (WarmStartNet, level_intrinsics, predict,
-                                           warm_state)
+def _features_ref(I0, I1, K, R, t, factor):
+    """numpy restatement of rf_ws_features (float64)."""
+    from reconflow_gb300.warmstart import box_down
 
-    sc = make_scene(640, 480, seed=77, device="cuda")
-    net = WarmStartNet(1, 60, 80, seed=0)
-    pred = predict(net, sc["I0"], sc["I1"], sc["R"], sc["t"], 8)
-    assert pred[0].shape == (60, 80)
+    c0, c1 = box_down(I0.astype(np.float64), factor), box_down(I1.astype(np.float64), factor)
+    hn, wn = c0.shape
+    fx, fy, cx, cy = K[0, 0] / factor, K[1, 1] / factor, K[0, 2] / factor, K[1, 2] / factor
+    Kc = np.array([[fx, 0, cx], [0, fy, cy], [0, 0, 1.0]])
+    ys, xs = np.mgrid[0:hn, 0:wn].astype(np.float64)
+    a = np.stack([xs, ys, np.ones_like(xs)], -1) @ (Kc @ R @ np.linalg.inv(Kc)).T
+    b = Kc @ t
+
+    def samp(x, y):
+        x = np.clip(x, 0, wn - 1)
+        y = np.clip(y, 0, hn - 1)
+        x0 = np.minimum(x.astype(int), max(wn - 2, 0))
+        y0 = np.minimum(y.astype(int), max(hn - 2, 0))
+        x1, y1 = np.minimum(x0 + 1, wn - 1), np.minimum(y0 + 1, hn - 1)
+        ax, ay = x - x0, y - y0
+        return ((1 - ay) * ((1 - ax) * c1[y0, x0] + ax * c1[y0, x1]) +
+                ay * ((1 - ax) * c1[y1, x0] + ax * c1[y1, x1]))
+
+    out = np.zeros((hn, wn, 16))
+    out[..., 0], out[..., 1] = c0 - 0.5, c1 - 0.5
+    for k in range(12):
+        rho = 0.05 * k
+        den = a[..., 2] + rho * b[2]
+        c = np.abs(samp((a[..., 0] + rho * b[0]) / den, (a[..., 1] + rho * b[1]) / den) - c0) * 10
+        out[..., 2 + k] = np.where(den > 1e-6, c, 1.0)
+    rm = 0.25
+    den = a[..., 2] + rm * b[2]
+    out[..., 14] = (b[0] * den - (a[..., 0] + rm * b[0]) * b[2]) / den ** 2 * 0.1
+    out[..., 15] = (b[1] * den - (a[..., 1] + rm * b[1]) * b[2]) / den ** 2 * 0.1
+    return out
+
+
+def test_features_match_numpy(torch_cuda, rf):
+    from reconflow_gb300.scene import make_scene
+    from reconflow_gb300.warmstart import features
+
+    T = torch_cuda
+    w, h, s, f = 200, 120, 224, 4
+    scs = [make_scene(w, h, seed=31 + i) for i in range(3)]
+    dev = [(T.as_tensor(pad_rows(sc["I0"], s), device="cuda"),
+            T.as_tensor(pad_rows(sc["I1"], s), device="cuda")) for sc in scs]
+    out = T.empty((3, h // f, w // f, 16), device="cuda")
+    features([d[0].data_ptr() for d in dev], [d[1].data_ptr() for d in dev], w, h, s, f,
+             [sc["K"] for sc in scs], [sc["R"] for sc in scs], [sc["t"] for sc in scs], out)
+    got = out.cpu().numpy()
+    for i, sc in enumerate(scs):
+        ref = _features_ref(sc["I0"], sc["I1"], sc["K"], sc["R"], sc["t"], f)
+        # FP32 on the GPU against FP64: costs are differences of samples
+        np.testing.assert_allclose(got[i], ref, rtol=1e-4, atol=2e-4)
+
+
+def test_state_matches_numpy(torch_cuda, rf):
+    from reconflow_gb300.warmstart import level_intrinsics, state
+
+    T = torch_cuda
+    rng = np.random.default_rng(4)
+    n, hn, wn, C = 2, 9, 13, 8
+    net = rng.uniform(0.1, 0.5, (n, hn, wn, C)).astype(np.float32)
+    net[1, 2, 3, 2] = -1.0  # clamped to 0.02
+    w, h, s, up = 26, 18, 32, 2.0
+    K = np.array([[100.0, 0, 52], [0, 100.0, 36], [0, 0, 1]])
+    Kl = level_intrinsics(K, 2)
+    Rs = [np.eye(3), np.array([[0.9998, -0.02, 0], [0.02, 0.9998, 0], [0, 0, 1.0]])]
+    ts = [np.array([0.1, 0, 0]), np.array([0, 0.05, 0.08])]
+    planes = [[T.zeros((h + 1) * s, device="cuda") for _ in range(5)] for _ in range(n)]
+    state(T.as_tensor(net, device="cuda"), w, h, s, up, [Kl, Kl], Rs, ts,
+          [[p.data_ptr() for p in pl] for pl in planes])
+    fx, cx, cy = Kl[0, 0], Kl[0, 2], Kl[1, 2]
+    ys, xs = np.mgrid[0:h, 0:w].astype(np.float64)
+    for i in range(n):
+        sx = np.clip((xs + 0.5) / up - 0.5, 0, wn - 1)
+        sy = np.clip((ys + 0.5) / up - 0.5, 0, hn - 1)
+        x0, y0 = sx.astype(int), sy.astype(int)
+        x1, y1 = np.minimum(x0 + 1, wn - 1), np.minimum(y0 + 1, hn - 1)
+        ax, ay = sx - x0, sy - y0
+        r = net[i, ..., 2].astype(np.float64)
+        rho = (1 - ay) * ((1 - ax) * r[y0, x0] + ax * r[y0, x1]) + ay * ((1 - ax) * r[y1, x0] + ax * r[y1, x1])
+        rho = np.clip(rho, 0.02, 2.0)
+        Z = 1 / rho
+        P = np.stack([Z * (xs - cx) / fx, Z * (ys - cy) / Kl[1, 1], Z], -1)
+        P2 = P @ Rs[i].T + ts[i]
+        want = [fx * P2[..., 0] / P2[..., 2] + cx - xs, fx * P2[..., 1] / P2[..., 2] + cy - ys,
+                P[..., 0], P[..., 1], P[..., 2]]
+        for k in range(5):
+            got = planes[i][k].cpu().numpy().reshape(h + 1, s)[:h, :w]
+            np.testing.assert_allclose(got, want[k], rtol=2e-5, atol=2e-5)
+
+
+def test_learned_batch_pipeline_runs(torch_cuda, rf):
+    """Features -> network -> warm state -> warm-started batched solve on two
+    640x480 pairs with an untrained network: finite results, and the warm
+    solve of a pair equals the single-pair warm solve from the same state."""
+    from reconflow_gb300.reconflow import ReconFlowBatch
+    from reconflow_gb300.scene import make_scene
+    from reconflow_gb300.warmstart import (SOLVER_WEIGHTS, LearnedBatchSolver, WarmStartNet,
+                                           level_intrinsics)
+
+    scs = [make_scene(640, 480, seed=77 + i, device="cuda") for i in range(2)]
+    net = WarmStartNet(2, 120, 160, seed=0)
+    bt = ReconFlowBatch([(640, 480)] * 2, 5, method=14, nWarpIters=3, nSolverIters=50,
+                        **SOLVER_WEIGHTS)
+    for i, sc in enumerate(scs):
+        bt.setCameraMatrices(i, sc["K"], sc["K"])
+        bt.copyImagesToDevice(i, pad_rows(sc["I0"], 640), pad_rows(sc["I1"], 640))
+    ls = LearnedBatchSolver(net, bt, (640, 480), scs[0]["K"], warm_level=2, warps=1, iters=10)
+    assert ls.factor == 4 and (ls.hn, ls.wn) == (120, 160)
+    Ks, Rs, ts = [sc["K"] for sc in scs], [sc["R"] for sc in scs], [sc["t"] for sc in scs]
+    ls.solve(Ks, Rs, ts)
+    u, v = bt.copyOpticalFlowToHost(1)
+    assert np.isfinite(u[:, :640]).mean() > 0.99
+    # the same warm state through the single-pair path
+    from reconflow_gb300.warmstart import state
+
+    T = torch_cuda
+    lw, lh, lsd = bt.levelDims(1, 2)
+    Kl = level_intrinsics(scs[1]["K"], 2)
+    tens = [T.zeros((lh + 1) * lsd, device="cuda") for _ in range(5)]
+    state(ls.o8[1:2], lw, lh, lsd, ls.up, [Kl], [Rs[1]], [ts[1]], [[t.data_ptr() for t in tens]])
+    planes = [t.cpu().numpy().reshape(lh + 1, lsd)[:lh] for t in tens]
     f = rf.ReconFlow()
     f.initializeR(640, 480, 1, 5, 2.0, 14, 50.0, 0.0, 0.1, 100.0, 1 / 0.33, 60.0, 0.5, 0.25, 3,
                   50, cvType=5, fix_quirks=1)
-    f.setCameraMatrices(sc["K"], sc["K"])
-    f.copyImagesToDevice(pad_rows(sc["I0"], 640), pad_rows(sc["I1"], 640))
-    W, H, S = f.pyramid()
-    st = warm_state(pred, sc["K"], (H[2], W[2]), S[2], 2, level_intrinsics(sc["K"], 2))
-    f.solveWarm(2, *st, sc["R"], sc["t"], 2, 20)
-    e_warm = f.energy()
-    u, v = f.copyOpticalFlowToHost()
-    assert np.isfinite(e_warm) and np.isfinite(u[:, :640]).mean() > 0.99
+    f.setCameraMatrices(scs[1]["K"], scs[1]["K"])
+    f.copyImagesToDevice(pad_rows(scs[1]["I0"], 640), pad_rows(scs[1]["I1"], 640))
+    f.solveWarm(2, *planes, Rs[1], ts[1], 1, 10)
+    u1, _ = f.copyOpticalFlowToHost()
+    f.close()
+    same = (u1[:, :640].view(np.uint32) == u[:, :640].view(np.uint32)) | (
+        np.isnan(u1[:, :640]) & np.isnan(u[:, :640]))
+    assert same.all()
