@@ -4,7 +4,8 @@
 // backward kernels.  No counterpart in the reference.
 //
 // Network (NHWC, 3x3 convolutions, padding 1):
-//   in  (16 ch: I0, I1, x, y, rotation vector, translation, zeros)
+//   in  (16 ch: the features of rf_ws_features: coarse frames, plane-sweep
+//        costs, epipolar derivative)
 //   c1  16 -> 32, ReLU                      (input resolution, "1/8")
 //   c2  32 -> 96, stride 2, ReLU            (half resolution, "1/16")
 //   c3  96 -> 96, ReLU
@@ -16,10 +17,11 @@
 // and Adam moments are FP32.
 //
 // Every convolution (forward, gradient of its input, gradient of its
-// weights) is one implicit GEMM on the tensor cores: mma.sync m16n8k16 with
-// BF16 operands and FP32 accumulators, operands gathered on the fly.  The
-// weight gradient splits the pixel (reduction) dimension into chunks with
-// partial sums reduced in a fixed order, so training is deterministic.
+// weights) is one implicit GEMM on the Blackwell tensor cores (rf_tc.cuh:
+// tcgen05.mma, BF16 operands gathered into shared memory, FP32 accumulator
+// in tensor memory).  The weight gradient splits the pixel (reduction)
+// dimension into chunks whose partial sums are added in a fixed order, so
+// training is deterministic.
 #include <algorithm>
 #include <cmath>
 #include <cstdint>
@@ -33,6 +35,7 @@
 
 #include "../../include/reconflow_gb300.h"
 #include "rf_kernels.cuh"
+#include "rf_tc.cuh"
 
 namespace rf_cnn_impl {
 
@@ -42,73 +45,105 @@ __device__ __forceinline__ uint32_t pack2(bf16 lo, bf16 hi) {
     return (uint32_t)__bfloat16_as_ushort(lo) | ((uint32_t)__bfloat16_as_ushort(hi) << 16);
 }
 
-__device__ __forceinline__ void mma16816(float (&d)[4], uint32_t a0, uint32_t a1, uint32_t a2,
-                                         uint32_t a3, uint32_t b0, uint32_t b1) {
-    asm volatile(
-        "mma.sync.aligned.m16n8k16.row.col.f32.bf16.bf16.f32 {%0,%1,%2,%3}, {%4,%5,%6,%7}, "
-        "{%8,%9}, {%0,%1,%2,%3};\n"
-        : "+f"(d[0]), "+f"(d[1]), "+f"(d[2]), "+f"(d[3])
-        : "r"(a0), "r"(a1), "r"(a2), "r"(a3), "r"(b0), "r"(b1));
-}
-
-// C[M x N] (+)= sum_k A(m, k) B(k, n), one warp per 16x8 tile; blockIdx.y
-// selects a chunk of the K range (split-K).  Functors return 0 outside their
-// tensors, so M, N, K need no padding.
-template <class FA, class FB, class FC>
-__global__ void k_igemm(int M, int N, int K, int kchunk, FA fa, FB fb, FC fc) {
-    const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-    const int lane = threadIdx.x & 31;
-    const int tilesN = (N + 7) >> 3;
-    const int tm = warp / tilesN, tn = warp - tm * tilesN;
-    if (tm * 16 >= M) return;
-    const int m0 = tm * 16, n0 = tn * 8;
-    const int g = lane >> 2, q = (lane & 3) * 2;
-    const int kb = blockIdx.y * kchunk;
-    const int ke = min(K, kb + kchunk);
-    float acc[4] = {0.f, 0.f, 0.f, 0.f};
-    for (int k0 = kb; k0 < ke; k0 += 16) {
-        uint32_t a0 = pack2(fa(m0 + g, k0 + q), fa(m0 + g, k0 + q + 1));
-        uint32_t a1 = pack2(fa(m0 + g + 8, k0 + q), fa(m0 + g + 8, k0 + q + 1));
-        uint32_t a2 = pack2(fa(m0 + g, k0 + q + 8), fa(m0 + g, k0 + q + 9));
-        uint32_t a3 = pack2(fa(m0 + g + 8, k0 + q + 8), fa(m0 + g + 8, k0 + q + 9));
-        uint32_t b0 = pack2(fb(k0 + q, n0 + g), fb(k0 + q + 1, n0 + g));
-        uint32_t b1 = pack2(fb(k0 + q + 8, n0 + g), fb(k0 + q + 9, n0 + g));
-        mma16816(acc, a0, a1, a2, a3, b0, b1);
-    }
-    fc(blockIdx.y, m0 + g, n0 + q, acc[0]);
-    fc(blockIdx.y, m0 + g, n0 + q + 1, acc[1]);
-    fc(blockIdx.y, m0 + g + 8, n0 + q, acc[2]);
-    fc(blockIdx.y, m0 + g + 8, n0 + q + 1, acc[3]);
-}
-
 struct Shape {
     int B, H, W, C;  // NHWC
 };
 
-// A for the forward conv: (output pixel, k = (ky*3 + kx)*Cin + ci)
-struct ConvIn {
+// ---- tcgen05 GEMM operands: 8 consecutive K elements of one row ----------
+__device__ __forceinline__ uint4 ld16(const bf16* p) { return *reinterpret_cast<const uint4*>(p); }
+
+__device__ __forceinline__ uint4 pack8(const bf16 (&v)[8]) {
+    return make_uint4(pack2(v[0], v[1]), pack2(v[2], v[3]), pack2(v[4], v[5]), pack2(v[6], v[7]));
+}
+
+// forward A: im2col row of output pixel m, k = (ky*3 + kx)*Cin + ci (Cin % 8 == 0)
+struct TcConvIn {
     const bf16* x;
-    Shape in;
-    int Ho, Wo, stride, K;
-    __device__ bf16 operator()(int m, int k) const {
-        if (k >= K || m >= in.B * Ho * Wo) return __float2bfloat16(0.f);
-        int ci = k % in.C, t = k / in.C, kx = t % 3, ky = t / 3;
+    int B, H, W, C, Ho, Wo, stride;
+    __device__ uint4 operator()(int m, int k, int) const {
+        int ci = k % C, t = k / C, kx = t % 3, ky = t / 3;
         int xo = m % Wo, r = m / Wo, yo = r % Ho, b = r / Ho;
         int y = yo * stride + ky - 1, xx = xo * stride + kx - 1;
-        if (y < 0 || y >= in.H || xx < 0 || xx >= in.W) return __float2bfloat16(0.f);
-        return x[(((size_t)b * in.H + y) * in.W + xx) * in.C + ci];
+        if (y < 0 || y >= H || xx < 0 || xx >= W) return make_uint4(0, 0, 0, 0);
+        return ld16(x + (((size_t)b * H + y) * W + xx) * C + ci);
     }
 };
 
-// B for the forward conv: weights [Cout][3][3][Cin], (k, n = co)
-struct ConvW {
+// K-major matrix rows: w[n][k], K % 8 == 0
+struct TcRows {
     const bf16* w;
-    int K, Cout;
-    __device__ bf16 operator()(int k, int n) const {
-        if (k >= K || n >= Cout) return __float2bfloat16(0.f);
-        return w[(size_t)n * K + k];
+    int K;
+    __device__ uint4 operator()(int n, int k, int) const { return ld16(w + (size_t)n * K + k); }
+};
+
+// input-gradient A: input pixel m, k = (ky*3 + kx)*Cout + co -> dy at the
+// output pixel that tap (ky, kx) of m feeds (Cout % 8 == 0)
+struct TcDataGradA {
+    const bf16* dy;
+    int H, W, Ho, Wo, Cout, stride;
+    __device__ uint4 operator()(int m, int k, int) const {
+        int co = k % Cout, t = k / Cout, kx = t % 3, ky = t / 3;
+        int xx = m % W, r = m / W, y = r % H, b = r / H;
+        int ty = y + 1 - ky, tx = xx + 1 - kx;
+        if (ty < 0 || tx < 0 || ty % stride || tx % stride) return make_uint4(0, 0, 0, 0);
+        int yo = ty / stride, xo = tx / stride;
+        if (yo >= Ho || xo >= Wo) return make_uint4(0, 0, 0, 0);
+        return ld16(dy + (((size_t)b * Ho + yo) * Wo + xo) * Cout + co);
     }
 };
+
+// weight-gradient A: row m = (ky*3 + kx)*Cin + ci of im2col^T, k = output pixel
+struct TcWGradA {
+    const bf16* x;
+    int H, W, C, Ho, Wo, stride;
+    __device__ uint4 operator()(int m, int k, int k_end) const {
+        int ci = m % C, t = m / C, kx = t % 3, ky = t / 3;
+        bf16 v[8];
+#pragma unroll
+        for (int e = 0; e < 8; e++) {
+            int p = k + e;
+            v[e] = __float2bfloat16(0.f);
+            if (p < k_end) {
+                int xo = p % Wo, r = p / Wo, yo = r % Ho, b = r / Ho;
+                int y = yo * stride + ky - 1, xx = xo * stride + kx - 1;
+                if (y >= 0 && y < H && xx >= 0 && xx < W)
+                    v[e] = x[(((size_t)b * H + y) * W + xx) * C + ci];
+            }
+        }
+        return pack8(v);
+    }
+};
+
+// weight-gradient B: row n = co, k = output pixel -> dy[pixel][co]
+struct TcWGradB {
+    const bf16* dy;
+    int Cout;
+    __device__ uint4 operator()(int n, int k, int k_end) const {
+        bf16 v[8];
+#pragma unroll
+        for (int e = 0; e < 8; e++)
+            v[e] = k + e < k_end ? dy[(size_t)(k + e) * Cout + n] : __float2bfloat16(0.f);
+        return pack8(v);
+    }
+};
+
+// weight-gradient partial of split z: part[z][co = n][row m]
+struct TcStoreWGrad {
+    float* part;
+    int M, N;
+    __device__ void operator()(int z, int m, int n, float v) const {
+        part[((size_t)z * N + n) * M + m] = v;
+    }
+};
+
+// [co][tap][ci] -> [ci][tap][co] (the input gradient's K-major B operand)
+__global__ void k_transpose_w(const bf16* w, int cin, int cout, bf16* wt) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    int n = cout * 9 * cin;
+    if (i >= n) return;
+    int ci = i % cin, t = (i / cin) % 9, co = i / (9 * cin);
+    wt[((size_t)ci * 9 + t) * cout + co] = w[i];
+}
 
 // forward epilogue: + bias, optional ReLU; BF16 activation and/or FP32 copy
 struct ConvOut {
@@ -125,74 +160,11 @@ struct ConvOut {
     }
 };
 
-// A for the input gradient: (input pixel, k = (ky*3 + kx)*Cout + co) reads the
-// output gradient at the output pixel that tap (ky, kx) of the input pixel
-// feeds.
-struct DataGradA {
-    const bf16* dy;
-    Shape in;
-    int Ho, Wo, Cout, stride, K;
-    __device__ bf16 operator()(int m, int k) const {
-        if (k >= K || m >= in.B * in.H * in.W) return __float2bfloat16(0.f);
-        int co = k % Cout, t = k / Cout, kx = t % 3, ky = t / 3;
-        int xx = m % in.W, r = m / in.W, y = r % in.H, b = r / in.H;
-        int ty = y + 1 - ky, tx = xx + 1 - kx;
-        if (ty < 0 || tx < 0 || ty % stride || tx % stride) return __float2bfloat16(0.f);
-        int yo = ty / stride, xo = tx / stride;
-        if (yo >= Ho || xo >= Wo) return __float2bfloat16(0.f);
-        return dy[(((size_t)b * Ho + yo) * Wo + xo) * Cout + co];
-    }
-};
-
-// B for the input gradient: (k = (ky*3 + kx)*Cout + co, n = ci) = W[co][ky][kx][ci]
-struct DataGradB {
-    const bf16* w;
-    int Cin, Cout, K;
-    __device__ bf16 operator()(int k, int n) const {
-        if (k >= K || n >= Cin) return __float2bfloat16(0.f);
-        int co = k % Cout, t = k / Cout;
-        return w[((size_t)co * 9 + t) * Cin + n];
-    }
-};
-
 struct StoreF32 {
     float* out;
     int M, N;
     __device__ void operator()(int, int m, int n, float v) const {
         if (m < M && n < N) out[(size_t)m * N + n] = v;
-    }
-};
-
-// A for the weight gradient: (m = co, k = output pixel) = dy[pixel][co]
-struct WGradA {
-    const bf16* dy;
-    int P, Cout;
-    __device__ bf16 operator()(int m, int k) const {
-        if (m >= Cout || k >= P) return __float2bfloat16(0.f);
-        return dy[(size_t)k * Cout + m];
-    }
-};
-
-// B for the weight gradient: (k = output pixel, n = (ky*3 + kx)*Cin + ci)
-struct WGradB {
-    const bf16* x;
-    Shape in;
-    int Ho, Wo, stride, P, N;
-    __device__ bf16 operator()(int k, int n) const {
-        if (k >= P || n >= N) return __float2bfloat16(0.f);
-        int ci = n % in.C, t = n / in.C, kx = t % 3, ky = t / 3;
-        int xo = k % Wo, r = k / Wo, yo = r % Ho, b = r / Ho;
-        int y = yo * stride + ky - 1, xx = xo * stride + kx - 1;
-        if (y < 0 || y >= in.H || xx < 0 || xx >= in.W) return __float2bfloat16(0.f);
-        return x[(((size_t)b * in.H + y) * in.W + xx) * in.C + ci];
-    }
-};
-
-struct StorePartial {
-    float* part;  // [chunk][M][N]
-    int M, N;
-    __device__ void operator()(int chunk, int m, int n, float v) const {
-        if (m < M && n < N) part[((size_t)chunk * M + m) * N + n] = v;
     }
 };
 
@@ -204,13 +176,29 @@ __global__ void k_reduce_partials(const float* part, int chunks, int n, float* o
     out[i] = s;
 }
 
-// bias gradient: sum over pixels of dy (f32), fixed order per channel
-__global__ void k_bias_grad(const float* dy, int P, int C, float* db) {
-    int c = blockIdx.x * blockDim.x + threadIdx.x;
-    if (c >= C) return;
-    float s = 0.f;
-    for (int p = 0; p < P; p++) s += dy[(size_t)p * C + c];
-    db[c] = s;
+// bias gradient, stage 1: block b sums dy over its pixel range
+// [b * span, (b + 1) * span) for every channel; thread t takes channel t % C
+// and every R-th pixel from t / C (R = 256 / C), then the R partial sums of a
+// channel are added in a fixed order.  Stage 2 (k_reduce_partials) adds the
+// block partials in block order, so the result is deterministic.
+constexpr int kBiasThreads = 256;
+
+__global__ void __launch_bounds__(kBiasThreads) k_bias_partial(const float* dy, int P, int C,
+                                                               int span, float* part) {
+    __shared__ float red[kBiasThreads];
+    const int t = threadIdx.x, R = kBiasThreads / C;
+    const int c = t % C, r = t / C;
+    const int p0 = blockIdx.x * span, p1 = min(P, p0 + span);
+    float acc = 0.f;
+    if (r < R)
+        for (int p = p0 + r; p < p1; p += R) acc += dy[(size_t)p * C + c];
+    red[t] = acc;
+    __syncthreads();
+    if (t < C) {
+        float s = 0.f;
+        for (int k = 0; k < R; k++) s += red[t + k * C];
+        part[(size_t)blockIdx.x * C + t] = s;
+    }
 }
 
 __global__ void k_f32_to_bf16(const float* a, bf16* b, size_t n) {
@@ -330,6 +318,8 @@ struct rf_cnn {
     size_t n_params = 0;
     float *w = nullptr, *g = nullptr, *m = nullptr, *v = nullptr;  // FP32 master, grad, Adam
     bf16* wb = nullptr;               // BF16 copy used by the kernels
+    bf16* wt = nullptr;               // BF16 weights per layer as [ci][tap][co]
+    int* d_status = nullptr;          // set by a tensor-core launch whose wait gave up
     int step = 0;
     // activations (BF16) and gradients (FP32 / BF16)
     bf16 *x = nullptr, *a1 = nullptr, *a2 = nullptr, *a3 = nullptr, *cat = nullptr, *a4 = nullptr;
@@ -359,16 +349,39 @@ rf_status cfail(rf_status st, const std::string& msg) {
 
 int Ho_of(int H, int s) { return s == 1 ? H : (H + 1) / 2; }
 
-template <class FA, class FB, class FC>
-rf_status gemm(rf_cnn* c, int M, int N, int K, int chunks, FA fa, FB fb, FC fc) {
-    int kchunk = ((K + chunks - 1) / chunks + 15) / 16 * 16;
-    chunks = (K + kchunk - 1) / kchunk;
-    long long warps = (long long)((M + 15) / 16) * ((N + 7) / 8);
-    dim3 grid((unsigned)((warps * 32 + 127) / 128), chunks);
-    k_igemm<<<grid, 128, 0, c->stream>>>(M, N, K, kchunk, fa, fb, fc);
+template <int NT, class LA, class LB, class EP>
+rf_status tc_launch(rf_cnn* c, int M, int N, int K, int splits, LA la, LB lb, EP ep) {
+    using S = rf_tc::TcSmem<NT>;
+    static bool attr_set = false;
+    if (!attr_set) {
+        CN(cudaFuncSetAttribute(rf_tc::k_tc_gemm<NT, LA, LB, EP>,
+                                cudaFuncAttributeMaxDynamicSharedMemorySize, S::kBytes));
+        attr_set = true;
+    }
+    int kspan = ((K + splits - 1) / splits + rf_tc::kTK - 1) / rf_tc::kTK * rf_tc::kTK;
+    splits = (K + kspan - 1) / kspan;
+    dim3 grid((M + rf_tc::kTM - 1) / rf_tc::kTM, (N + NT - 1) / NT, splits);
+    rf_tc::k_tc_gemm<NT, LA, LB, EP><<<grid, rf_tc::kThreads, S::kBytes, c->stream>>>(
+        M, N, K, kspan, la, lb, ep, c->d_status);
     c->launches++;
     CN(cudaGetLastError());
     return RF_OK;
+}
+
+// D[M x N] = A[M x K] B[N x K]^T on the tensor cores; returns the number of
+// K splits actually used through *used (if not null)
+template <class LA, class LB, class EP>
+rf_status tc_gemm(rf_cnn* c, int M, int N, int K, int splits, LA la, LB lb, EP ep,
+                  int* used = nullptr) {
+    if (used) {
+        int kspan = ((K + splits - 1) / splits + rf_tc::kTK - 1) / rf_tc::kTK * rf_tc::kTK;
+        *used = (K + kspan - 1) / kspan;
+    }
+    if (N <= 16) return tc_launch<16>(c, M, N, K, splits, la, lb, ep);
+    if (N <= 32) return tc_launch<32>(c, M, N, K, splits, la, lb, ep);
+    if (N <= 64) return tc_launch<64>(c, M, N, K, splits, la, lb, ep);
+    if (N <= 96) return tc_launch<96>(c, M, N, K, splits, la, lb, ep);
+    return tc_launch<128>(c, M, N, K, splits, la, lb, ep);
 }
 
 // forward conv of layer L: x (B x H x W x cin) -> y (BF16) and/or yf (FP32)
@@ -376,10 +389,10 @@ rf_status conv_fwd(rf_cnn* c, const Layer& L, const bf16* x, int B, int H, int W
                    float* yf) {
     int Ho = Ho_of(H, L.stride), Wo = Ho_of(W, L.stride);
     int M = B * Ho * Wo, K = 9 * L.cin;
-    ConvIn fa{x, Shape{B, H, W, L.cin}, Ho, Wo, L.stride, K};
-    ConvW fb{c->wb + L.woff, K, L.cout};
-    ConvOut fc{c->w + L.boff, y, yf, M, L.cout, L.relu};
-    return gemm(c, M, L.cout, K, 1, fa, fb, fc);
+    TcConvIn la{x, B, H, W, L.cin, Ho, Wo, L.stride};
+    TcRows lb{c->wb + L.woff, K};
+    ConvOut ep{c->w + L.boff, y, yf, M, L.cout, L.relu};
+    return tc_gemm(c, M, L.cout, K, 1, la, lb, ep);
 }
 
 // backward of layer L given dy (FP32, already through the ReLU mask) and its
@@ -387,24 +400,29 @@ rf_status conv_fwd(rf_cnn* c, const Layer& L, const bf16* x, int B, int H, int W
 rf_status conv_bwd(rf_cnn* c, const Layer& L, const bf16* x, int B, int H, int W,
                    const float* dy, const bf16* dyb, float* dx) {
     int Ho = Ho_of(H, L.stride), Wo = Ho_of(W, L.stride);
-    int P = B * Ho * Wo, N = 9 * L.cin;
-    int chunks = std::max(1, std::min(256, P / 2048));
-    size_t need = (size_t)chunks * L.cout * N;
+    int P = B * Ho * Wo, Mw = 9 * L.cin;
+    // weight gradient: [tap*cin + ci] x [co] over the pixels, split over K
+    int splits = std::max(1, std::min(128, P / 4096));
+    int used = 1;
+    size_t need = (size_t)splits * L.cout * Mw;
     if (need > c->part_floats) return cfail(RF_ERR_STATE, "cnn: partial buffer too small");
-    rf_status rs = gemm(c, L.cout, N, P, chunks, WGradA{dyb, P, L.cout},
-                        WGradB{x, Shape{B, H, W, L.cin}, Ho, Wo, L.stride, P, N},
-                        StorePartial{c->part, L.cout, N});
+    rf_status rs = tc_gemm(c, Mw, L.cout, P, splits, TcWGradA{x, H, W, L.cin, Ho, Wo, L.stride},
+                           TcWGradB{dyb, L.cout}, TcStoreWGrad{c->part, Mw, L.cout}, &used);
     if (rs != RF_OK) return rs;
-    int kchunk = ((P + chunks - 1) / chunks + 15) / 16 * 16;
-    int used = (P + kchunk - 1) / kchunk;
-    k_reduce_partials<<<blocks_for((size_t)L.cout * N), 256, 0, c->stream>>>(
-        c->part, used, L.cout * N, c->g + L.woff);
-    k_bias_grad<<<blocks_for(L.cout, 64), 64, 0, c->stream>>>(dy, P, L.cout, c->g + L.boff);
-    c->launches += 2;
+    k_reduce_partials<<<blocks_for((size_t)L.cout * Mw), 256, 0, c->stream>>>(
+        c->part, used, L.cout * Mw, c->g + L.woff);
+    // bias: the weight-gradient partials are consumed above, so their buffer is free
+    const int span = 2048, nblk = (P + span - 1) / span;
+    if ((size_t)nblk * L.cout > c->part_floats || L.cout > kBiasThreads)
+        return cfail(RF_ERR_STATE, "cnn: partial buffer too small for the bias gradient");
+    k_bias_partial<<<nblk, kBiasThreads, 0, c->stream>>>(dy, P, L.cout, span, c->part);
+    k_reduce_partials<<<blocks_for(L.cout, 64), 64, 0, c->stream>>>(c->part, nblk, L.cout,
+                                                                   c->g + L.boff);
+    c->launches += 3;
     if (dx) {
         int M = B * H * W, K = 9 * L.cout;
-        rs = gemm(c, M, L.cin, K, 1, DataGradA{dyb, Shape{B, H, W, L.cin}, Ho, Wo, L.cout, L.stride, K},
-                  DataGradB{c->wb + L.woff, L.cin, L.cout, K}, StoreF32{dx, M, L.cin});
+        rs = tc_gemm(c, M, L.cin, K, 1, TcDataGradA{dyb, H, W, Ho, Wo, L.cout, L.stride},
+                     TcRows{c->wt + L.woff, K}, StoreF32{dx, M, L.cin});
         if (rs != RF_OK) return rs;
     }
     CN(cudaGetLastError());
@@ -414,6 +432,11 @@ rf_status conv_bwd(rf_cnn* c, const Layer& L, const bf16* x, int B, int H, int W
 rf_status sync_bf16_weights(rf_cnn* c) {
     k_f32_to_bf16<<<blocks_for(c->n_params), 256, 0, c->stream>>>(c->w, c->wb, c->n_params);
     c->launches++;
+    for (const Layer& L : c->layers) {
+        k_transpose_w<<<blocks_for((size_t)L.cout * 9 * L.cin), 256, 0, c->stream>>>(
+            c->wb + L.woff, L.cin, L.cout, c->wt + L.woff);
+        c->launches++;
+    }
     CN(cudaGetLastError());
     return RF_OK;
 }
@@ -533,6 +556,8 @@ rf_status rf_cnn_create(int max_batch, int height, int width, unsigned long long
     };
     alloc(&c->w, off * 4); alloc(&c->g, off * 4); alloc(&c->m, off * 4); alloc(&c->v, off * 4);
     alloc(&c->wb, off * 2);
+    alloc(&c->wt, off * 2);
+    alloc(&c->d_status, sizeof(int));
     alloc(&c->x, B * P * 16 * 2); alloc(&c->a1, B * P * 32 * 2); alloc(&c->a2, B * P2 * 96 * 2);
     alloc(&c->a3, B * P2 * 96 * 2); alloc(&c->cat, B * P * 128 * 2); alloc(&c->a4, B * P * 64 * 2);
     alloc(&c->o16, B * P2 * 8 * 4); alloc(&c->o8, B * P * 8 * 4);
@@ -551,6 +576,10 @@ rf_status rf_cnn_create(int max_batch, int height, int width, unsigned long long
         rf_cnn_destroy(c);
         return cfail(RF_ERR_OOM, std::string("rf_cnn_create: ") + cudaGetErrorString(e));
     }
+    if (cudaMemset(c->d_status, 0, sizeof(int)) != cudaSuccess) {
+        rf_cnn_destroy(c);
+        return cfail(RF_ERR_CUDA, "rf_cnn_create: status init");
+    }
     rf_status rs = sync_bf16_weights(c);
     if (rs != RF_OK) {
         rf_cnn_destroy(c);
@@ -563,6 +592,7 @@ rf_status rf_cnn_create(int max_batch, int height, int width, unsigned long long
 rf_status rf_cnn_destroy(rf_cnn* c) {
     if (!c) return RF_OK;
     cudaDeviceSynchronize();
+    for (void* p : {(void*)c->wt, (void*)c->d_status}) if (p) cudaFree(p);
     for (void* p : {(void*)c->w, (void*)c->g, (void*)c->m, (void*)c->v, (void*)c->wb, (void*)c->x,
                     (void*)c->a1, (void*)c->a2, (void*)c->a3, (void*)c->cat, (void*)c->a4,
                     (void*)c->o16, (void*)c->o8, (void*)c->g_o16, (void*)c->g_o8, (void*)c->g_a4,

@@ -12,6 +12,8 @@
 #include <cuda_runtime.h>
 #include <math.h>
 
+#include <utility>
+
 namespace rf {
 
 // Half-sample-symmetric extension of a tap index (period 2n): -1 -> 0,
@@ -342,6 +344,56 @@ __device__ __forceinline__ float median25_exchange(float (&m)[25]) {
         }
     }
     return m[12];
+}
+
+// Comparators of Batcher's odd-even merge sort of 32 keys (K. E. Batcher,
+// "Sorting networks and their applications", AFIPS SJCC 1968), keeping only
+// those whose both keys are among the first 25: a comparator against a key
+// >= 25 would meet +inf padding and change nothing.  The 140 comparators
+// sort 25 keys; the median needs the 113 of them that reach key 12, and the
+// compiler drops the rest once the loop below is unrolled.
+constexpr int sortnet25_count_or_pair(int want, int which) {
+    int n = 0;
+    for (int p = 1; p < 32; p <<= 1)
+        for (int k = p; k >= 1; k >>= 1)
+            for (int j = k % p; j + k < 32; j += 2 * k)
+                for (int i = 0; i < k && i < 32 - j - k; i++)
+                    if ((i + j) / (2 * p) == (i + j + k) / (2 * p) && i + j + k < 25) {
+                        if (n == want) return which == 0 ? i + j : i + j + k;
+                        n++;
+                    }
+    return n;  // want < 0: the comparator count
+}
+constexpr int kSortNet25 = sortnet25_count_or_pair(-1, 0);
+
+template <int A, int B>
+__device__ __forceinline__ void cmp_exchange(float (&s)[25]) {
+    const float lo = fminf(s[A], s[B]);
+    s[B] = fmaxf(s[A], s[B]);
+    s[A] = lo;
+}
+
+template <int... C>
+__device__ __forceinline__ void sortnet25(float (&s)[25], std::integer_sequence<int, C...>) {
+    (cmp_exchange<sortnet25_count_or_pair(C, 0), sortnet25_count_or_pair(C, 1)>(s), ...);
+}
+
+// Median of 25 with the min/max network above.  For inputs without NaN its
+// value equals the exchange selection's except possibly the sign of a zero
+// result, so a NaN input or a zero result is recomputed with the reference's
+// exchange order (median25_exchange), and the result is bit-identical.
+__device__ __forceinline__ float median25(float (&m)[25]) {
+    bool nan_in = false;
+#pragma unroll
+    for (int k = 0; k < 25; k++) nan_in |= isnan(m[k]);
+    if (!nan_in) {
+        float s[25];
+#pragma unroll
+        for (int k = 0; k < 25; k++) s[k] = m[k];
+        sortnet25(s, std::make_integer_sequence<int, kSortNet25>{});
+        if (s[12] != 0.0f) return s[12];
+    }
+    return median25_exchange(m);
 }
 
 // CleanUp3DKernel body (solve3dMinimalArea.cu:259-295).

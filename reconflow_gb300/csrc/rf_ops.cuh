@@ -274,8 +274,8 @@ __device__ __forceinline__ void median5_pair(const float* __restrict__ a,
             mv[j * 5 + i] = at >= 0 ? b[at] : 0.0f;
         }
     }
-    ma = median25_exchange(mu);
-    mb = median25_exchange(mv);
+    ma = median25(mu);
+    mb = median25(mv);
 }
 
 

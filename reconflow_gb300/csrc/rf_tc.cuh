@@ -1,0 +1,248 @@
+// Blackwell (sm_100 family) tensor-core GEMM for the warm-start network's
+// convolutions: tcgen05.mma with BF16 operands staged in shared memory and
+// the FP32 accumulator in tensor memory (TMEM).
+//
+//   D[M x N] = sum_k A(m, k) B(n, k)      (both operands K-major)
+//
+// One CTA of 128 threads computes a 128 x NT tile of D (NT = 16 .. 256, a
+// multiple of 16) over a range of K (split-K over gridDim.z).  For each
+// K-chunk of 64 the 128 threads gather the A tile (128 x 64) and the B tile
+// (NT x 64) into shared memory in the canonical no-swizzle K-major layout
+// (8 x 16-byte core matrices: rows of a core matrix 16 bytes apart, core
+// matrices 128 bytes apart along K and 1024 bytes apart along M / N), make
+// the writes visible to the tensor core (fence.proxy.async), and one thread
+// issues four 128 x NT x 16 MMAs and commits them to an mbarrier.  Two
+// chunk buffers alternate, so the gather of chunk c+1 overlaps the MMAs of
+// chunk c.  The epilogue reads the accumulator with tcgen05.ld: warp w owns
+// TMEM lanes (= rows of D) 32w .. 32w + 31.
+//
+// The loaders are functors returning 8 consecutive K elements of one row as
+// a uint4 (zeros outside the operand); the epilogue functor receives
+// (split, m, n, value).
+#pragma once
+
+#include <cstdint>
+
+#include <cuda_bf16.h>
+#include <cuda_runtime.h>
+
+namespace rf_tc {
+
+constexpr int kTM = 128;      // rows of D per CTA (the MMA's M)
+constexpr int kTK = 64;       // K per chunk (four MMAs of K = 16)
+constexpr int kThreads = 128;
+// bounded waits: an mbarrier that does not complete in this many polls
+// marks the launch as failed (see k_tc_gemm)
+constexpr unsigned kSpinLimit = 1u << 26;
+
+__device__ __forceinline__ uint32_t smem_u32(const void* p) {
+    return static_cast<uint32_t>(__cvta_generic_to_shared(p));
+}
+
+// shared-memory matrix descriptor (tcgen05): start address, leading (K)
+// and stride (M / N) byte offsets in 16-byte units, descriptor version 1 at
+// bit 46, no swizzle (layout type 0 in bits 61..63)
+__device__ __forceinline__ uint64_t smem_desc(uint32_t addr, uint32_t lbo, uint32_t sbo) {
+    uint64_t d = 0;
+    d |= (uint64_t)((addr >> 4) & 0x3FFFu);
+    d |= (uint64_t)((lbo >> 4) & 0x3FFFu) << 16;
+    d |= (uint64_t)((sbo >> 4) & 0x3FFFu) << 32;
+    d |= (uint64_t)1 << 46;
+    return d;
+}
+
+// instruction descriptor, kind::f16: D = F32 (bits 4..5 = 1), A = B = BF16
+// (bits 7..9 and 10..12 = 1), both K-major (bits 15, 16 = 0), N >> 3 in
+// bits 17..22, M >> 4 in bits 24..28
+__host__ __device__ constexpr uint32_t idesc_bf16(int M, int N) {
+    return (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(N >> 3) << 17) |
+           ((uint32_t)(M >> 4) << 24);
+}
+
+__device__ __forceinline__ void mbar_init(uint64_t* bar, unsigned count) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(count)
+                 : "memory");
+}
+
+// bounded wait on an mbarrier phase; false if it did not complete
+__device__ __forceinline__ bool mbar_wait(uint64_t* bar, unsigned parity) {
+    const uint32_t a = smem_u32(bar);
+    for (unsigned i = 0; i < kSpinLimit; i++) {
+        uint32_t done;
+        asm volatile(
+            "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n"
+            " selp.u32 %0, 1, 0, p;\n}\n"
+            : "=r"(done)
+            : "r"(a), "r"(parity)
+            : "memory");
+        if (done) return true;
+    }
+    return false;
+}
+
+__device__ __forceinline__ void fence_async_smem() {
+    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+}
+__device__ __forceinline__ void tc_fence_before() {
+    asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+}
+__device__ __forceinline__ void tc_fence_after() {
+    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+}
+
+__device__ __forceinline__ void tmem_alloc(uint32_t* dst_smem, uint32_t ncols) {
+    asm volatile(
+        "tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;\n"
+        "tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;\n" ::"r"(smem_u32(dst_smem)),
+        "r"(ncols)
+        : "memory");
+}
+__device__ __forceinline__ void tmem_dealloc(uint32_t taddr, uint32_t ncols) {
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(taddr), "r"(ncols)
+                 : "memory");
+}
+
+__device__ __forceinline__ void mma_bf16(uint32_t d_tmem, uint64_t a, uint64_t b, uint32_t idesc,
+                                         uint32_t accumulate) {
+    asm volatile(
+        "{\n .reg .pred p;\n setp.ne.u32 p, %4, 0;\n"
+        " tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}\n" ::"r"(d_tmem),
+        "l"(a), "l"(b), "r"(idesc), "r"(accumulate)
+        : "memory");
+}
+
+__device__ __forceinline__ void mma_commit(uint64_t* bar) {
+    asm volatile(
+        "tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(
+            smem_u32(bar))
+        : "memory");
+}
+
+// 8 consecutive 32-bit TMEM columns of this thread's lane
+__device__ __forceinline__ void tmem_ld8(uint32_t taddr, float (&v)[8]) {
+    uint32_t r[8];
+    asm volatile(
+        "tcgen05.ld.sync.aligned.32x32b.x8.b32 {%0, %1, %2, %3, %4, %5, %6, %7}, [%8];\n"
+        "tcgen05.wait::ld.sync.aligned;\n"
+        : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]),
+          "=r"(r[7])
+        : "r"(taddr)
+        : "memory");
+#pragma unroll
+    for (int i = 0; i < 8; i++) v[i] = __uint_as_float(r[i]);
+}
+
+// byte offset of element row r, k-group g (8 elements) in a chunk tile
+__device__ __forceinline__ uint32_t tile_off(int r, int g) {
+    return (uint32_t)(((r >> 3) * (kTK / 8) + g) * 128 + (r & 7) * 16);
+}
+
+template <int NT>
+struct TcSmem {
+    static_assert(NT % 16 == 0 && NT >= 16 && NT <= 256, "N tile");
+    static constexpr int kA = kTM * kTK * 2;  // bytes of one A chunk
+    static constexpr int kB = NT * kTK * 2;
+    static constexpr int kBytes = 2 * (kA + kB) + 2048;  // two chunk buffers, barriers, alignment slack
+    static constexpr uint32_t kCols = NT <= 32 ? 32 : (NT <= 64 ? 64 : (NT <= 128 ? 128 : 256));
+};
+
+// grid: x = M tiles, y = N tiles, z = K splits (each `kspan` long, a multiple
+// of kTK).  `status` (device int) is set to 1 if a wait gave up.
+template <int NT, class LA, class LB, class EP>
+__global__ void __launch_bounds__(kThreads) k_tc_gemm(int M, int N, int K, int kspan, LA la,
+                                                     LB lb, EP ep, int* status) {
+    extern __shared__ __align__(1024) unsigned char smem_raw[];
+    using S = TcSmem<NT>;
+    unsigned char* base = (unsigned char*)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
+    uint64_t* bars = (uint64_t*)(base + 2 * (S::kA + S::kB));  // [2] chunk barriers
+    uint32_t* tslot = (uint32_t*)(bars + 2);
+    int* fail = (int*)(tslot + 1);
+
+    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+    const int m0 = blockIdx.x * kTM, n0 = blockIdx.y * NT;
+    const int k_begin = blockIdx.z * kspan;
+    const int k_end = min(K, k_begin + kspan);
+    const int nchunks = (k_end - k_begin + kTK - 1) / kTK;
+
+    if (tid == 0) {
+        mbar_init(&bars[0], 1);
+        mbar_init(&bars[1], 1);
+        *fail = 0;
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
+    if (warp == 0) tmem_alloc(tslot, S::kCols);
+    tc_fence_before();
+    __syncthreads();
+    tc_fence_after();
+    const uint32_t tmem = *tslot;
+    constexpr uint32_t idesc = idesc_bf16(kTM, NT);
+
+    unsigned phases = 0u;  // bit b: parity of the next completion of barrier b
+    for (int c = 0; c < nchunks; c++) {
+        const int b = c & 1;
+        unsigned char* tA = base + b * S::kA;
+        unsigned char* tB = base + 2 * S::kA + b * S::kB;
+        // before refilling buffer b, the MMAs that read it (chunk c - 2) must be done
+        if (c >= 2) {
+            if (!mbar_wait(&bars[b], (phases >> b) & 1u)) *fail = 1;
+            phases ^= 1u << b;
+        }
+        const int kc = k_begin + c * kTK;
+        // gather: A 128 rows x 8 groups, B NT rows x 8 groups, 16 bytes each
+        for (int i = tid; i < kTM * (kTK / 8); i += kThreads) {
+            const int r = i >> 3, g = i & 7;
+            const int k = kc + g * 8;
+            uint4 v = make_uint4(0, 0, 0, 0);
+            if (m0 + r < M && k < k_end) v = la(m0 + r, k, k_end);
+            *(uint4*)(tA + tile_off(r, g)) = v;
+        }
+        for (int i = tid; i < NT * (kTK / 8); i += kThreads) {
+            const int r = i >> 3, g = i & 7;
+            const int k = kc + g * 8;
+            uint4 v = make_uint4(0, 0, 0, 0);
+            if (n0 + r < N && k < k_end) v = lb(n0 + r, k, k_end);
+            *(uint4*)(tB + tile_off(r, g)) = v;
+        }
+        fence_async_smem();
+        __syncthreads();
+        if (tid == 0) {
+            tc_fence_after();
+            const uint32_t a0 = smem_u32(tA), b0 = smem_u32(tB);
+#pragma unroll
+            for (int kk = 0; kk < kTK / 16; kk++) {
+                const uint64_t da = smem_desc(a0 + kk * 256, 128, 1024);
+                const uint64_t db = smem_desc(b0 + kk * 256, 128, 1024);
+                mma_bf16(tmem, da, db, idesc, (c > 0 || kk > 0) ? 1u : 0u);
+            }
+            mma_commit(&bars[b]);
+        }
+        __syncthreads();
+    }
+    // the last commit covers every earlier MMA of this CTA
+    if (nchunks > 0) {
+        const int b = (nchunks - 1) & 1;
+        if (!mbar_wait(&bars[b], (phases >> b) & 1u)) *fail = 1;
+    }
+    tc_fence_after();
+    __syncthreads();
+    if (*fail) {
+        if (tid == 0) atomicExch(status, 1);
+    } else if (nchunks > 0) {
+        const int m = m0 + warp * 32 + lane;
+        const uint32_t lane_addr = tmem + ((uint32_t)(warp * 32) << 16);
+#pragma unroll 1
+        for (int j = 0; j < NT; j += 8) {
+            float v[8];
+            tmem_ld8(lane_addr + (uint32_t)j, v);
+            if (m < M)
+#pragma unroll
+                for (int e = 0; e < 8; e++)
+                    if (n0 + j + e < N) ep(blockIdx.z, m, n0 + j + e, v[e]);
+        }
+    }
+    tc_fence_before();
+    __syncthreads();
+    if (warp == 0) tmem_dealloc(tmem, S::kCols);
+}
+
+}  // namespace rf_tc

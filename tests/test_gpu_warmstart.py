@@ -37,10 +37,11 @@ def test_gradients_match_fp64_oracle(torch_cuda):
     params = net.params()
     x, t16, m16, t8, m8 = _rand_case(rng, B, H, W)
     T = lambda a: torch_cuda.as_tensor(a, device="cuda")  # noqa: E731
-    loss = net.backward(T(x), T(t16), T(m16), T(t8), T(m8))
+    w = (1.0, 1.0, 10.0)
+    loss = net.backward(T(x), T(t16), T(m16), T(t8), T(m8), w)
     g = net.grads()
     o16, o8 = net.forward(T(x))
-    gref, lref, f = CO.backward(params.astype(np.float64), x, t16, m16, t8, m8)
+    gref, lref, f = CO.backward(params.astype(np.float64), x, t16, m16, t8, m8, w)
     # forward outputs (FP32 accumulation of BF16 products vs FP64)
     np.testing.assert_allclose(o8.cpu().numpy(), f["o8"], rtol=0, atol=2e-2 * np.abs(f["o8"]).max())
     np.testing.assert_allclose(o16.cpu().numpy(), f["o16"], rtol=0,
