@@ -164,8 +164,10 @@ RF_API rf_status rf_solve_flow_warm(rf_handle* h, int level, const float* u, con
 
 /* Energy of the last solution (no reference counterpart), summed in double
  * over the level-0 pixels: lambda * |I1(x + u) - I0(x)| + |grad u| +
- * |grad v| (+ alpha_proj / 2 * |(u, v) - uc(X)|^2 for ReconFlow, uc the
- * projection of the solved point as SolveUc computes it).  Blocking. */
+ * |grad v| (+ alpha_proj / 2 * min(|(u, v) - uc(X)|^2, 1) for ReconFlow, uc
+ * the projection of the solved point as SolveUc computes it; the
+ * reprojection residual is truncated at 1 px^2, so a few pixels whose point
+ * projects near infinity cannot dominate the sum).  Blocking. */
 RF_API rf_status rf_energy(rf_handle* h, double* energy);
 
 /* CudaFlow::copyOpticalFlowToHost(u, v) (Cudaflow.cu:320-325). Blocking. */

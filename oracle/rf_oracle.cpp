@@ -976,8 +976,9 @@ int solve(const rfo_params& p, const void* i0, const void* i1, int in_stride,
 //                                                      I1 fetched as WarpingKernel)
 // + |grad u| + |grad v|                               (forward differences,
 //                                                      0 at the far border)
-// + alpha_proj / 2 * |(u, v) - uc(X)|^2               (reprojection of the
-//                                                      solved 3D point; recon only)
+// + alpha_proj / 2 * min(|(u, v) - uc(X)|^2, 1)       (reprojection of the
+//                                                      solved 3D point, truncated
+//                                                      at 1 px^2; recon only)
 double energy(const float* I0, const float* I1, const float* u, const float* v, const float* X,
               const float* Y, const float* Z, int w, int h, int s, float lambda,
               float alpha_proj, const double* R1, const double* t1, const double* K1,
@@ -1004,8 +1005,9 @@ double energy(const float* I0, const float* I1, const float* u, const float* v, 
                 double uc = K1[0] * X2 / Z2 + K1[2] - ix;
                 double vc = K1[0] * Y2 / Z2 + K1[5] - iy;  // fx for both, as SolveUc
                 double du = u[pos] - uc, dv = v[pos] - vc;
-                proj = 0.5 * (double)alpha_proj * (du * du + dv * dv);
-                if (!std::isfinite(proj)) proj = 0.0;
+                double r2 = du * du + dv * dv;
+                if (!(r2 < 1.0)) r2 = 1.0;  // truncated at 1 px^2 (NaN included)
+                proj = 0.5 * (double)alpha_proj * r2;
             }
             e += data + tv + proj;
         }

@@ -731,8 +731,9 @@ __global__ void __launch_bounds__(kEnergyThreads) k_energy_partial(EnergyArgs a,
             double uc = a.fx * X2 / Z2 + a.cx - ix;
             double vc = a.fx * Y2 / Z2 + a.cy - iy;
             double du = a.u[pos] - uc, dv = a.v[pos] - vc;
-            proj = 0.5 * (double)a.alpha_proj * (du * du + dv * dv);
-            if (!isfinite(proj)) proj = 0.0;
+            double r2 = du * du + dv * dv;
+            if (!(r2 < 1.0)) r2 = 1.0;  // truncated at 1 px^2 (NaN included)
+            proj = 0.5 * (double)a.alpha_proj * r2;
         }
         e += data + tv + proj;
     }
