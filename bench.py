@@ -1,13 +1,19 @@
 #!/usr/bin/env python
 """Benchmark of the GB300 Reconflow solver: 720p frame pairs per second.
 
-Workload (default ``720p``): one 1280x720 float32 gray frame pair from the
-seeded synthetic scene generator (8 planes, depth 2-10 m, blob + 1/f
-texture, pose <= 2 deg / 0.1 m, N(0, 0.01) noise), 6 pyramid levels (x0.5),
-5 warps, 100 primal-dual iterations per warp, lambda = 50, theta = 0.33
-(alpha_tv = 1/theta), tau = 0.25, with the reference demo's projection weights
-(alpha_proj = 60, lambdaf = 0.1, lambdams = 100) and the K-pyramid fix.  One
-step = one full ReconFlow solve (flow, 3D points; inverse depth derived).
+Default workload ``720p-learned`` (the headline: batched + learned warm start
+against the plain solver at equal endpoint error): 64 1280x720 float32 gray
+frame pairs from the seeded synthetic scene generator (8 planes, depth 2-10
+m, blob + 1/f texture, pose <= 2 deg / 0.1 m, N(0, 0.01) noise), lambda = 50,
+theta = 0.33 (alpha_tv = 1/theta), tau = 0.25, with the reference demo's
+projection weights (alpha_proj = 60, lambdaf = 0.1, lambdams = 100) and the
+K-pyramid fix.  One step = the whole batch through the learned path:
+plane-sweep features, the network, the warm-start state at pyramid level 2,
+the refinement from there, the energies, and a plain re-solve of every pair
+whose energy exceeds its plain solve's by more than 2%.  The line also
+carries the plain solver's single-pair and batched throughput (6 levels,
+5 warps x 100 iterations) and both solvers' endpoint errors on the same
+pairs.  Workload ``720p`` is the plain drop-in solve of one pair.
 
 ``value``: pairs/s with the frames already in HBM (CUDA events on the solve
 stream, L2 flushed between steps).  ``e2e``: the same through the C ABI with
@@ -16,9 +22,11 @@ depth and 3D points, every step.  ``roofline``: the dominant kernel at level
 0, timed live with CUDA events on its stream.  ``cpu_baseline``: the oracle's
 FP32 reference-semantics path on this host's cores, on a bounded sample.
 
-``--impl reference`` times the reference semantics on the host CPU (the FP32
-oracle; the reference itself cannot be built: it needs OpenCV and the texture
-reference API that CUDA 12 removed).  Several GPUs run independent replicas.
+``--impl reference`` times the reference semantics of the plain solve of one
+pair of the workload's size on the host CPU (the FP32 oracle; the reference
+itself cannot be built: it needs OpenCV and the texture reference API that
+CUDA 12 removed, and it has no batched or learned path).  Several GPUs run
+independent replicas.
 """
 from __future__ import annotations
 
@@ -51,10 +59,11 @@ WORKLOADS = {
                     levels=6, warps=5, iters=100, seed=0),
     # batched + learned warm start: 64 pairs of 1280x720; the network predicts
     # inverse depth at 1/8, the solve refines from pyramid level 2 with the
-    # per-level schedule below (index = level, 0 = finest); plain 5 x 100
+    # per-level schedule below (index = level, 0 = finest: 1 x 20, 2 x 30,
+    # 3 x 50); plain 5 x 100
     "720p-learned": dict(width=1280, height=720, pairs=64, levels=6, seed=2000, plain_warps=5,
-                         plain_iters=100, warm_level=2, warm_warps=[1, 3, 5],
-                         warm_iters=[30, 30, 50], fallback_margin=0.02,
+                         plain_iters=100, warm_level=2, warm_warps=[1, 2, 3],
+                         warm_iters=[20, 30, 50], fallback_margin=0.02,
                          checkpoint="reconflow_gb300/weights/warmstart_f125.bin"),
     # batched: 64 pairs of 1280x720 (per-pair throughput of the batched path)
     "batch64-720p": dict(pairs=64, sizes=[(1280, 720)], levels=6, warps=5, iters=100, seed=0),
@@ -67,6 +76,9 @@ SOLVER = dict(method=14, lam=50.0, theta=0.33, tau=0.25, alpha_proj=60.0, lambda
 # = 15, writes p(4),X,Y,Z,sk(2) = 9.
 ALG_BYTES = {"recon_a": 25 * 4, "recon_b": 24 * 4}
 L2_FLUSH_BYTES = 512 << 20
+LEARNED_METRIC = ("720p frame pairs/s, batched + learned warm start (vs the plain solver at "
+                  "equal EPE)")
+PLAIN_METRIC = "720p frame pairs/s (ReconFlow flow + depth)"
 
 
 def load_peaks():
@@ -220,12 +232,15 @@ def run_reference(args, wl, world, rank):
     value = args.steps / total
     sample = (f"{wl['width']}x{wl['height']} pair, full {wl['levels']}-level x {wl['warps']}-warp "
               f"schedule at 1 and 5 inner iterations, extrapolated linearly to {wl['iters']}")
+    cfg = config_of(wl)
+    if "workload" in wl:
+        cfg["workload"] = wl["workload"]
     line = {
-        "impl": "reference", "metric": "720p frame pairs/s (ReconFlow flow + depth)",
+        "impl": "reference", "metric": wl.get("metric", PLAIN_METRIC),
         "value": value, "unit": "pairs/s", "n_gpus": args.gpus, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": 1000.0 * total / args.steps,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
-        "data": "synthetic (seeded scene generator)", "config": config_of(wl),
+        "data": "synthetic (seeded scene generator)", "config": cfg,
         "cpu_baseline": {"value": value, "unit": "pairs/s", "cores": cores, "kind": "port",
                          "sample": sample},
         "e2e": {"value": value, "unit": "pairs/s", "h2d_bytes_per_step": 0,
@@ -488,6 +503,7 @@ def run_learned(args, wl, world, rank, local):
             torch.cuda.synchronize()
             step_ms = timed(step, args.steps)
         launches = b.kernelLaunches() + net.kernel_launches() + f.kernelLaunches() - l0
+    timed_fallbacks = list(fallbacks)
     total_s = max_over_ranks(sum(step_ms) / 1000.0, world)
     value = world * n * args.steps / total_s
 
@@ -564,8 +580,7 @@ def run_learned(args, wl, world, rank, local):
         single_pps = 1000.0 / statistics.median(single_ms)
         tol = 0.05
         line = {
-            "metric": "720p frame pairs/s, batched + learned warm start (vs the plain solver at "
-                      "equal EPE)",
+            "metric": LEARNED_METRIC,
             "value": value, "unit": "pairs/s", "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": 1000.0 * total_s / args.steps,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
@@ -585,7 +600,7 @@ def run_learned(args, wl, world, rank, local):
             "plain": {"single_pair_pairs_per_s": single_pps,
                       "batched_pairs_per_s": 1000.0 * n / statistics.median(plain_batch_ms),
                       "accuracy": plain_acc},
-            "learned": {"accuracy": learned_acc, "fallbacks_per_step": fallbacks,
+            "learned": {"accuracy": learned_acc, "fallbacks_per_step": timed_fallbacks,
                         "energy_ratio_median": float(np.median(e_learned / e_plain))},
             "speedup_vs_plain_single_pair": value / single_pps,
             "equal_epe": {"mean": learned_acc["epe_mean_px"] <= plain_acc["epe_mean_px"] + tol,
@@ -638,7 +653,7 @@ def main():
     ap.add_argument("--steps", type=int, default=10)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--workload", default="720p", choices=sorted(WORKLOADS))
+    ap.add_argument("--workload", default="720p-learned", choices=sorted(WORKLOADS))
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--solve-only", action="store_true",
@@ -647,7 +662,12 @@ def main():
     wl = WORKLOADS[args.workload]
     world, rank, local = dist_setup(args)
     if args.impl == "reference":
-        if "pairs" in wl:
+        if "checkpoint" in wl:
+            # the reference's counterpart of a learned batch: its plain solve, one pair
+            wl = dict(width=wl["width"], height=wl["height"], levels=wl["levels"],
+                      warps=wl["plain_warps"], iters=wl["plain_iters"], seed=wl["seed"],
+                      metric=LEARNED_METRIC, workload=args.workload)
+        elif "pairs" in wl:
             raise SystemExit("bench.py: the reference arm runs single-pair workloads")
         run_reference(args, wl, world, rank)
         return
@@ -791,7 +811,7 @@ def main():
 
     if rank == 0:
         line = {
-            "metric": "720p frame pairs/s (ReconFlow flow + depth)", "value": value,
+            "metric": PLAIN_METRIC, "value": value,
             "unit": "pairs/s", "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
             "ms_per_step": 1000.0 * total_s / args.steps, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f32",

@@ -143,8 +143,9 @@ __device__ __forceinline__ void dual_step(float dx, float dy, float fac, float& 
 }
 
 // Per-level camera constants (float copies, as the reference passes them:
-// solve3dMinimalArea.cu:204-228, solveUcSk.cu:42-56).
-struct LevelConsts {
+// solve3dMinimalArea.cu:204-228, solveUcSk.cu:42-56).  16-byte aligned (52
+// floats = 13 x 16 bytes) so a thread reads them with 128-bit loads.
+struct __align__(16) LevelConsts {
     float P[12];
     float Q[12];
     float R1[9];
