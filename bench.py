@@ -59,12 +59,13 @@ WORKLOADS = {
                     levels=6, warps=5, iters=100, seed=0),
     # batched + learned warm start: 64 pairs of 1280x720; the network predicts
     # inverse depth at 1/8, the solve refines from pyramid level 2 with the
-    # per-level schedule below (index = level, 0 = finest: 1 x 20, 2 x 30,
-    # 3 x 50); plain 5 x 100
+    # per-level schedule below (index = level, 0 = finest: 1 x 20, 1 x 30,
+    # 2 x 40); plain 5 x 100
     "720p-learned": dict(width=1280, height=720, pairs=64, levels=6, seed=2000, plain_warps=5,
-                         plain_iters=100, warm_level=2, warm_warps=[1, 2, 3],
-                         warm_iters=[20, 30, 50], fallback_margin=0.02,
-                         checkpoint="reconflow_gb300/weights/warmstart_f125.bin"),
+                         plain_iters=100, warm_level=2, warm_warps=[1, 1, 2],
+                         warm_iters=[20, 30, 40], fallback_margin=0.02,
+                         checkpoint="reconflow_gb300/weights/warmstart_f125.bin",
+                         tiles="reconflow_gb300/tuning/gb300_720p_x64.json"),
     # batched: 64 pairs of 1280x720 (per-pair throughput of the batched path)
     "batch64-720p": dict(pairs=64, sizes=[(1280, 720)], levels=6, warps=5, iters=100, seed=0),
 }
@@ -410,6 +411,14 @@ def run_learned(args, wl, world, rank, local):
     stream = torch.cuda.Stream()
     flush = torch.empty(L2_FLUSH_BYTES // 4, dtype=torch.float32, device="cuda")
 
+    from reconflow_gb300 import autotune
+
+    tiles = None
+    tpath = os.path.join(ROOT, wl.get("tiles", ""))
+    if wl.get("tiles") and os.path.exists(tpath):
+        with open(tpath) as fh:
+            tiles = json.load(fh)
+
     def new_batch(warps, iters):
         b = R.ReconFlowBatch([(W, H)] * n, wl["levels"], method=SOLVER["method"],
                              lambda_=SOLVER["lam"], lambdaf=SOLVER["lambdaf"],
@@ -420,6 +429,8 @@ def run_learned(args, wl, world, rank, local):
         for i, sc in enumerate(scenes):
             b.setCameraMatrices(i, sc["K"], sc["K"])
             b.copyImagesToDevice(i, sc["I0"], sc["I1"])
+        if tiles is not None:
+            autotune.apply(b, tiles["levels"])
         return b
 
     def epe_stats(b):
@@ -591,7 +602,9 @@ def run_learned(args, wl, world, rank, local):
                        "warm_level": wl["warm_level"], "warm_warps_per_level": wl["warm_warps"],
                        "warm_iters_per_level": wl["warm_iters"],
                        "fallback": f"plain re-solve when energy > (1 + {margin}) x plain energy",
-                       "checkpoint": wl["checkpoint"], "method": "METHODR_TVL1_MS",
+                       "checkpoint": wl["checkpoint"],
+                       "tiles": wl.get("tiles") if tiles is not None else "default 32x8",
+                       "method": "METHODR_TVL1_MS",
                        "lambda": SOLVER["lam"], "theta": SOLVER["theta"], "tau": SOLVER["tau"],
                        "alpha_proj": SOLVER["alpha_proj"], "lambdaf": SOLVER["lambdaf"],
                        "lambdams": SOLVER["lambdams"], "fix_quirks": SOLVER["fix_quirks"],
@@ -625,7 +638,9 @@ def roofline_of(ms, px):
     tpath = os.path.join(ROOT, "profiles", "traffic_720p.json")
     if os.path.exists(tpath):
         with open(tpath) as fh:
-            traffic = json.load(fh).get(names[dom])
+            t720 = json.load(fh).get(names[dom])
+        # the capture is of a 1280x720 launch; other sizes scale by their pixels
+        traffic = None if t720 is None else t720 * px / (1280 * 720)
     return {"bound": "hbm", "kernel": names[dom], "achieved": achieved, "peak": peak,
             "peak_kind": peak_kind, "unit": "GB/s", "frac": achieved / peak, "traffic": traffic,
             "alg_bytes_per_launch": ALG_BYTES[names[dom]] * px,
@@ -783,21 +798,8 @@ def main():
     # roofline of the dominant kernel: level-0 inner iterations, CUDA events
     ms = (ctypes.c_float * 2)()
     f.solveR(sc["R"], sc["t"], 5.0)
-    R._native.check(lib.rf_profile_iterations(f._handle(), 0, 20, ms))
-    names = ["recon_a", "recon_b"]
-    dom = 0 if ms[0] >= ms[1] else 1
-    px = w * h
-    achieved = ALG_BYTES[names[dom]] * px / (ms[dom] * 1e-3) / 1e9
-    peak, peak_kind = load_peaks()
-    traffic = None
-    tpath = os.path.join(ROOT, "profiles", "traffic_720p.json")
-    if os.path.exists(tpath):
-        with open(tpath) as fh:
-            traffic = json.load(fh).get(names[dom])
-    roofline = {"bound": "hbm", "kernel": names[dom], "achieved": achieved, "peak": peak,
-                "peak_kind": peak_kind, "unit": "GB/s", "frac": achieved / peak,
-                "traffic": traffic, "alg_bytes_per_launch": ALG_BYTES[names[dom]] * px,
-                "launch_ms": {names[0]: ms[0], names[1]: ms[1]}}
+    R._native.check(lib.rf_profile_iterations(f._handle(), 0, 50, ms))
+    roofline = roofline_of(ms, w * h)
 
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
@@ -811,7 +813,8 @@ def main():
 
     if rank == 0:
         line = {
-            "metric": PLAIN_METRIC, "value": value,
+            "metric": PLAIN_METRIC if (w, h) == (1280, 720) else
+                      f"{w}x{h} frame pairs/s (ReconFlow flow + depth)", "value": value,
             "unit": "pairs/s", "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
             "ms_per_step": 1000.0 * total_s / args.steps, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f32",

@@ -167,7 +167,8 @@ RF_API rf_status rf_solve_flow_warm(rf_handle* h, int level, const float* u, con
  * |grad v| (+ alpha_proj / 2 * min(|(u, v) - uc(X)|^2, 1) for ReconFlow, uc
  * the projection of the solved point as SolveUc computes it; the
  * reprojection residual is truncated at 1 px^2, so a few pixels whose point
- * projects near infinity cannot dominate the sum).  Blocking. */
+ * projects near infinity cannot dominate the sum).  Per-pixel terms in FP32,
+ * the sum in double.  Blocking. */
 RF_API rf_status rf_energy(rf_handle* h, double* energy);
 
 /* CudaFlow::copyOpticalFlowToHost(u, v) (Cudaflow.cu:320-325). Blocking. */
@@ -266,6 +267,16 @@ RF_API rf_status rf_batch_energies(rf_batch* b, double* out);
 RF_API rf_status rf_batch_solve_warm_levels(rf_batch* b, const double* R0, const double* t0,
                                             const double* R1, const double* t1, int level,
                                             const int* warps, const int* iters);
+/* Tile shape of each pyramid level (tile_w[l] x tile_h[l] pixels, one
+ * thread each; 32 .. 256 threads, a multiple of 32; default 32 x 8), as
+ * reconflow_gb300/autotune.py picks them.  Results do not depend on it. */
+RF_API rf_status rf_batch_set_tiles(rf_batch* b, const int* tile_w, const int* tile_h);
+/* Timing hook (no reference counterpart): after a ReconFlow solve, the mean
+ * time in milliseconds of one launch of each inner-iteration kernel over
+ * every pair at `level` with the current tiles (ms[0] data / projection /
+ * triangulation, ms[1] dual / median / clean-up; n_iters launches back to
+ * back in a CUDA graph, CUDA events).  Invalidates the last solve. */
+RF_API rf_status rf_batch_profile_level(rf_batch* b, int level, int n_iters, float* ms);
 /* Device pointers of pair `pair`'s image planes at pyramid `level` (level 0
  * = the uploaded frames; coarser levels are filled by the next solve). */
 RF_API rf_status rf_batch_image_planes(rf_batch* b, int pair, int level, const float** I0,

@@ -88,6 +88,8 @@ _SIGS = [
     ("rf_batch_solve_warm_levels", _I, [_VP, _D, _D, _D, _D, _I, _VP, _VP]),
     ("rf_batch_warm_planes", _I, [_VP, _I, _VP, _VP, _VP, _VP, _VP]),
     ("rf_batch_image_planes", _I, [_VP, _I, _I, _VP, _VP]),
+    ("rf_batch_set_tiles", _I, [_VP, _VP, _VP]),
+    ("rf_batch_profile_level", _I, [_VP, _I, _I, _VP]),
     ("rf_batch_download_flow", _I, [_VP, _I, _VP, _VP, _I]),
     ("rf_batch_download_points", _I, [_VP, _I, _VP, _VP, _VP, _I]),
     ("rf_batch_download_inv_depth", _I, [_VP, _I, _VP, _I]),

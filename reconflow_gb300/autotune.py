@@ -1,0 +1,100 @@
+"""Tile-shape autotuner for the batched solver.
+
+Every step of a batched solve is one launch over the tiles of every pair at
+one pyramid level (``rf_batch.cu``); the tile shape decides how pixels map
+to blocks (and so the wave count, the tail of the last wave and how well
+neighbouring pixels share cache lines), never the arithmetic, so results are
+identical for every shape.  ``autotune`` times the two inner-iteration
+kernels of each level (``rf_batch_profile_level``: launches back to back in a
+CUDA graph, CUDA events) for every candidate shape and keeps the fastest per
+level.  ``tiles_for`` turns a saved table into per-level shapes for a batch
+of any size by the pixel count of the level (summed over pairs).
+
+    python -m reconflow_gb300.autotune --size 1280x720 --pairs 64 --out table.json
+"""
+from __future__ import annotations
+
+import json
+
+CANDIDATES = [(32, 8), (64, 4), (128, 2), (32, 4), (64, 2), (16, 16), (32, 2), (16, 8)]
+
+
+def autotune(batch, R1s, t1s, candidates=CANDIDATES, iters=20, log=None):
+    """Pick the fastest tile per level of `batch` (images and cameras set).
+    Returns [{"level", "pixels", "tile", "ms": {shape: ms}}] and leaves the
+    batch set to the chosen tiles."""
+    L = int(batch.params.n_levels)
+    best = [(32, 8)] * L
+    table = []
+    for level in range(L):
+        px = sum(batch.levelDims(i, level)[0] * batch.levelDims(i, level)[1]
+                 for i in range(batch.n))
+        times = {}
+        for shape in candidates:
+            trial = list(best)
+            trial[level] = shape
+            batch.setTiles([s[0] for s in trial], [s[1] for s in trial])
+            batch.solveR(R1s, t1s)
+            a, b = batch.profileLevel(level, iters)
+            times[f"{shape[0]}x{shape[1]}"] = a + b
+        pick = min(times, key=times.get)
+        best[level] = tuple(int(x) for x in pick.split("x"))
+        table.append({"level": level, "pixels": px, "tile": list(best[level]), "ms": times})
+        if log:
+            log(f"level {level} ({px} px): {pick}  " +
+                " ".join(f"{k} {v * 1e3:.1f}us" for k, v in sorted(times.items(), key=lambda x: x[1])))
+    batch.setTiles([s[0] for s in best], [s[1] for s in best])
+    return table
+
+
+def tiles_for(batch, table):
+    """Per-level shapes for `batch` from a saved table: each level takes the
+    tile of the table entry whose pixel count is closest (in ratio)."""
+    import math
+
+    L = int(batch.params.n_levels)
+    tw, th = [], []
+    for level in range(L):
+        px = sum(batch.levelDims(i, level)[0] * batch.levelDims(i, level)[1]
+                 for i in range(batch.n))
+        e = min(table, key=lambda r: abs(math.log(max(px, 1) / max(r["pixels"], 1))))
+        tw.append(e["tile"][0])
+        th.append(e["tile"][1])
+    return tw, th
+
+
+def apply(batch, table):
+    tw, th = tiles_for(batch, table)
+    batch.setTiles(tw, th)
+
+
+def main(argv=None):
+    import argparse
+
+    from .reconflow import ReconFlowBatch
+    from .scene import make_scene
+    from .warmstart import SOLVER_WEIGHTS
+
+    ap = argparse.ArgumentParser(description="tile-shape autotuner for the batched solver")
+    ap.add_argument("--size", default="1280x720")
+    ap.add_argument("--pairs", type=int, default=64)
+    ap.add_argument("--levels", type=int, default=6)
+    ap.add_argument("--iters", type=int, default=20)
+    ap.add_argument("--out", required=True)
+    a = ap.parse_args(argv)
+    w, h = (int(x) for x in a.size.split("x"))
+    scs = [make_scene(w, h, seed=7000 + i, device="cuda") for i in range(a.pairs)]
+    b = ReconFlowBatch([(w, h)] * a.pairs, a.levels, method=14, nWarpIters=1, nSolverIters=5,
+                       **SOLVER_WEIGHTS)
+    for i, sc in enumerate(scs):
+        b.setCameraMatrices(i, sc["K"], sc["K"])
+        b.copyImagesToDevice(i, sc["I0"], sc["I1"])
+    table = autotune(b, [s["R"] for s in scs], [s["t"] for s in scs], iters=a.iters, log=print)
+    with open(a.out, "w") as f:
+        json.dump({"device": "GB300", "size": a.size, "pairs": a.pairs, "levels": table}, f,
+                  indent=1)
+    b.close()
+
+
+if __name__ == "__main__":
+    main()

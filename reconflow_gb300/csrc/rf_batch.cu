@@ -29,8 +29,11 @@ using namespace rf;
 
 namespace rf_batch_impl {
 
+// default tile of a level: 32 x 8 pixels = 256 threads (rf_batch_set_tiles
+// chooses another shape per level; every tile has at most kMaxTile threads)
 constexpr int BX = 32;
 constexpr int BY = 8;
+constexpr int kMaxTile = 256;
 constexpr int kMaxLevels = 16;
 
 struct BatchPair {
@@ -53,7 +56,7 @@ __device__ __forceinline__ float* plane_ptr(const BatchPair& bp, int k) {
 
 // One block = one 32x8 tile of one pair at `level`.
 template <class Op>
-__global__ void __launch_bounds__(BX* BY) k_batch(BatchCtx ctx, int level, Op op) {
+__global__ void __launch_bounds__(kMaxTile) k_batch(BatchCtx ctx, int level, Op op) {
     const int* pre = ctx.prefix + level * (ctx.n + 1);
     const int b = blockIdx.x;
     int lo = 0, hi = ctx.n - 1;
@@ -67,8 +70,9 @@ __global__ void __launch_bounds__(BX* BY) k_batch(BatchCtx ctx, int level, Op op
     const BatchPair& bp = ctx.pairs[lo];
     const LevelDims d = bp.dims[level];
     const int t = b - pre[lo];
-    const int tw = (d.w + BX - 1) / BX;
-    const int ix = (t % tw) * BX + threadIdx.x, iy = (t / tw) * BY + threadIdx.y;
+    const int bx = blockDim.x, by = blockDim.y;  // this level's tile shape
+    const int tw = (d.w + bx - 1) / bx;
+    const int ix = (t % tw) * bx + threadIdx.x, iy = (t / tw) * by + threadIdx.y;
     if (ix >= d.w || iy >= d.h) return;
     op(ctx, bp, lo, level, d, ix, iy);
 }
@@ -277,6 +281,7 @@ struct rf_batch {
     BatchPair* d_pairs = nullptr;
     int* d_prefix = nullptr;
     std::vector<int> prefix;  // host copy: [level][n + 1]
+    std::vector<int> tile_w, tile_h;  // tile shape of each level
     LevelConsts* d_consts = nullptr;
     LevelConsts* h_consts = nullptr;
     std::vector<double> K0, K1;  // [pair][9]
@@ -318,6 +323,18 @@ int rf_batch::warm_idx(int k) const { return base_idx() + rf_batch_impl::P_SPARE
 
 namespace rf_batch_impl {
 
+// per-level prefix sums of tile counts (host copy) for the current tiles
+void fill_prefix(rf_batch* b) {
+    b->prefix.assign((size_t)b->L * (b->n + 1), 0);
+    for (int l = 0; l < b->L; l++)
+        for (int i = 0; i < b->n; i++) {
+            const LevelDims& d = b->dims[i][l];
+            int tiles = ((d.w + b->tile_w[l] - 1) / b->tile_w[l]) *
+                        ((d.h + b->tile_h[l] - 1) / b->tile_h[l]);
+            b->prefix[l * (b->n + 1) + i + 1] = b->prefix[l * (b->n + 1) + i] + tiles;
+        }
+}
+
 BatchCtx ctx_of(rf_batch* b) {
     BatchCtx c;
     c.pairs = b->d_pairs;
@@ -332,7 +349,8 @@ template <class Op>
 int launch_op(rf_batch* b, int level, const Op& op) {
     int tiles = b->prefix[level * (b->n + 1) + b->n];
     if (tiles <= 0) return 0;
-    k_batch<Op><<<tiles, dim3(BX, BY), 0, b->stream>>>(ctx_of(b), level, op);
+    k_batch<Op><<<tiles, dim3(b->tile_w[level], b->tile_h[level]), 0, b->stream>>>(ctx_of(b),
+                                                                                  level, op);
     b->enq++;
     return cudaGetLastError() == cudaSuccess ? 0 : 1;
 }
@@ -553,13 +571,9 @@ rf_status rf_batch_create(const rf_params* p, int n_pairs, const int* widths, co
         hp[i].plane = b->plane[i];
         for (int l = 0; l < b->L; l++) hp[i].dims[l] = b->dims[i][l];
     }
-    b->prefix.assign((size_t)b->L * (n_pairs + 1), 0);
-    for (int l = 0; l < b->L; l++)
-        for (int i = 0; i < n_pairs; i++) {
-            const LevelDims& d = b->dims[i][l];
-            int tiles = ((d.w + BX - 1) / BX) * ((d.h + BY - 1) / BY);
-            b->prefix[l * (n_pairs + 1) + i + 1] = b->prefix[l * (n_pairs + 1) + i] + tiles;
-        }
+    b->tile_w.assign(b->L, BX);
+    b->tile_h.assign(b->L, BY);
+    fill_prefix(b);
     if (e == cudaSuccess) e = cudaMalloc(&b->d_pairs, sizeof(BatchPair) * n_pairs);
     if (e == cudaSuccess)
         e = cudaMemcpy(b->d_pairs, hp.data(), sizeof(BatchPair) * n_pairs, cudaMemcpyHostToDevice);
@@ -698,6 +712,78 @@ rf_status rf_batch_energies(rf_batch* b, double* out) {
         BC(cudaMemcpyAsync(out + i, e, sizeof(double), cudaMemcpyDeviceToHost, b->stream));
     }
     BC(cudaStreamSynchronize(b->stream));
+    return RF_OK;
+}
+
+rf_status rf_batch_set_tiles(rf_batch* b, const int* tile_w, const int* tile_h) {
+    if (!b || !tile_w || !tile_h) return bfail(RF_ERR_INVALID_ARG, "rf_batch_set_tiles: null argument");
+    for (int l = 0; l < b->L; l++) {
+        const int w = tile_w[l], h = tile_h[l];
+        if (w < 1 || h < 1 || w * h > kMaxTile || (w * h) % 32 != 0)
+            return bfail(RF_ERR_INVALID_ARG, "rf_batch_set_tiles: a tile needs 32..256 threads, a "
+                                             "multiple of 32");
+    }
+    BC(cudaStreamSynchronize(b->stream));
+    b->tile_w.assign(tile_w, tile_w + b->L);
+    b->tile_h.assign(tile_h, tile_h + b->L);
+    fill_prefix(b);
+    BC(cudaMemcpy(b->d_prefix, b->prefix.data(), sizeof(int) * b->prefix.size(),
+                  cudaMemcpyHostToDevice));
+    if (b->graph) {
+        cudaGraphExecDestroy(b->graph);
+        b->graph = nullptr;
+        b->graph_kind = -1;
+    }
+    return RF_OK;
+}
+
+rf_status rf_batch_profile_level(rf_batch* b, int level, int n_iters, float* ms) {
+    if (!b || !ms || n_iters < 1 || level < 0 || level >= b->L)
+        return bfail(RF_ERR_INVALID_ARG, "rf_batch_profile_level: bad argument");
+    if (!b->solved || b->p.method == RF_METHOD_TVL1)
+        return bfail(RF_ERR_STATE, "rf_batch_profile_level: needs a ReconFlow solve");
+    const Weights wt = solver_weights(&b->p);
+    const int B0 = b->base_idx();
+    auto P = [&](int k) { return B0 + k; };
+    const int u = b->res_u, v = b->res_v;
+    // the role planes of the last solve's finest level (values only matter for timing)
+    ReconIdx r{u, v, P(P_DUHAT), P(P_DVHAT), P(P_PU1), P(P_PU2), P(P_PV1), P(P_PV2),
+               P(P_SPARE0 + 4), P(P_SPARE0 + 5), P(P_SPARE0 + 6), P(P_SPARE0 + 7), P(P_IX),
+               P(P_IY), P(P_IZ), P(P_X), P(P_Y), P(P_Z), P(P_X1), P(P_Y1), P(P_Z1),
+               P(P_SPARE0 + 2), P(P_SPARE0 + 3)};
+    for (int k = 0; k < 2; k++) {
+        cudaGraph_t g = nullptr;
+        cudaGraphExec_t ge = nullptr;
+        BC(cudaStreamBeginCapture(b->stream, cudaStreamCaptureModeThreadLocal));
+        int bad = 0;
+        for (int i = 0; i < n_iters && !bad; i++)
+            bad = k == 0 ? launch_op(b, level, OpReconA{r, wt, 0, 0})
+                         : launch_op(b, level, OpReconB{r, wt, 0});
+        cudaError_t ce = cudaStreamEndCapture(b->stream, &g);
+        if (bad || ce != cudaSuccess) {
+            if (g) cudaGraphDestroy(g);
+            return bfail(RF_ERR_CUDA, "rf_batch_profile_level: capture");
+        }
+        ce = cudaGraphInstantiate(&ge, g, 0);
+        cudaGraphDestroy(g);
+        if (ce != cudaSuccess) return bfail(RF_ERR_CUDA, "rf_batch_profile_level: instantiate");
+        cudaEvent_t e0, e1;
+        BC(cudaEventCreate(&e0));
+        BC(cudaEventCreate(&e1));
+        BC(cudaGraphLaunch(ge, b->stream));
+        BC(cudaEventRecord(e0, b->stream));
+        BC(cudaGraphLaunch(ge, b->stream));
+        BC(cudaEventRecord(e1, b->stream));
+        BC(cudaEventSynchronize(e1));
+        float t = 0;
+        cudaEventElapsedTime(&t, e0, e1);
+        cudaEventDestroy(e0);
+        cudaEventDestroy(e1);
+        cudaGraphExecDestroy(ge);
+        ms[k] = t / (float)n_iters;
+        b->launches += 2 * (uint64_t)n_iters;
+    }
+    b->solved = false;
     return RF_OK;
 }
 

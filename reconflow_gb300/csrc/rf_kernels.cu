@@ -699,7 +699,7 @@ __global__ void k_flow_color(const float* __restrict__ u, const float* __restric
 // partials in a fixed order, so the result is deterministic.
 struct EnergyArgs {
     const float *I0, *I1, *u, *v, *X, *Y, *Z;
-    double R1[9], t1[3], fx, cx, cy;
+    float R1f[9], t1f[3], fxf, cxf, cyf;
     float lambda, alpha_proj;
     int recon;
 };
@@ -716,26 +716,29 @@ __global__ void __launch_bounds__(kEnergyThreads) k_energy_partial(EnergyArgs a,
         float x = ((float)ix + a.u[pos] + 0.5f) / (float)d.w;
         float y = ((float)iy + a.v[pos] + 0.5f) / (float)d.h;
         float i1w = tex2d(a.I1, d.w, d.h, s, x, y);
-        double data = (double)a.lambda * fabs((double)i1w - (double)a.I0[pos]);
-        double ux = ix + 1 < d.w ? (double)a.u[pos + 1] - a.u[pos] : 0.0;
-        double uy = iy + 1 < d.h ? (double)a.u[pos + s] - a.u[pos] : 0.0;
-        double vx = ix + 1 < d.w ? (double)a.v[pos + 1] - a.v[pos] : 0.0;
-        double vy = iy + 1 < d.h ? (double)a.v[pos + s] - a.v[pos] : 0.0;
-        double tv = sqrt(ux * ux + uy * uy) + sqrt(vx * vx + vy * vy);
-        double proj = 0.0;
+        // per-pixel terms in FP32 (GB300's FP64 division and square root
+        // would bound the kernel), summed in double
+        const float u0 = a.u[pos], v0 = a.v[pos];
+        const float data = a.lambda * fabsf(i1w - a.I0[pos]);
+        const float ux = ix + 1 < d.w ? a.u[pos + 1] - u0 : 0.0f;
+        const float uy = iy + 1 < d.h ? a.u[pos + s] - u0 : 0.0f;
+        const float vx = ix + 1 < d.w ? a.v[pos + 1] - v0 : 0.0f;
+        const float vy = iy + 1 < d.h ? a.v[pos + s] - v0 : 0.0f;
+        const float tv = sqrtf(ux * ux + uy * uy) + sqrtf(vx * vx + vy * vy);
+        float proj = 0.0f;
         if (a.recon) {
-            double Xp = a.X[pos], Yp = a.Y[pos], Zp = a.Z[pos];
-            double X2 = a.R1[0] * Xp + a.R1[1] * Yp + a.R1[2] * Zp + a.t1[0];
-            double Y2 = a.R1[3] * Xp + a.R1[4] * Yp + a.R1[5] * Zp + a.t1[1];
-            double Z2 = a.R1[6] * Xp + a.R1[7] * Yp + a.R1[8] * Zp + a.t1[2];
-            double uc = a.fx * X2 / Z2 + a.cx - ix;
-            double vc = a.fx * Y2 / Z2 + a.cy - iy;
-            double du = a.u[pos] - uc, dv = a.v[pos] - vc;
-            double r2 = du * du + dv * dv;
-            if (!(r2 < 1.0)) r2 = 1.0;  // truncated at 1 px^2 (NaN included)
-            proj = 0.5 * (double)a.alpha_proj * r2;
+            const float Xp = a.X[pos], Yp = a.Y[pos], Zp = a.Z[pos];
+            const float X2 = a.R1f[0] * Xp + a.R1f[1] * Yp + a.R1f[2] * Zp + a.t1f[0];
+            const float Y2 = a.R1f[3] * Xp + a.R1f[4] * Yp + a.R1f[5] * Zp + a.t1f[1];
+            const float Z2 = a.R1f[6] * Xp + a.R1f[7] * Yp + a.R1f[8] * Zp + a.t1f[2];
+            const float uc = a.fxf * X2 / Z2 + a.cxf - (float)ix;
+            const float vc = a.fxf * Y2 / Z2 + a.cyf - (float)iy;
+            const float du = u0 - uc, dv = v0 - vc;
+            float r2 = du * du + dv * dv;
+            if (!(r2 < 1.0f)) r2 = 1.0f;  // truncated at 1 px^2 (NaN included)
+            proj = 0.5f * a.alpha_proj * r2;
         }
-        e += data + tv + proj;
+        e += (double)data + (double)tv + (double)proj;
     }
     for (int o = 16; o > 0; o >>= 1) e += __shfl_down_sync(0xffffffffu, e, o);
     if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = e;
@@ -980,11 +983,11 @@ int launch_energy(const float* I0, const float* I1, const float* u, const float*
                   int recon, double* partial, int nblocks, double* out, cudaStream_t st) {
     EnergyArgs a;
     a.I0 = I0; a.I1 = I1; a.u = u; a.v = v; a.X = X; a.Y = Y; a.Z = Z;
-    for (int i = 0; i < 9; i++) a.R1[i] = R1 ? R1[i] : (i % 4 == 0 ? 1.0 : 0.0);
-    for (int i = 0; i < 3; i++) a.t1[i] = t1 ? t1[i] : 0.0;
-    a.fx = K1 ? K1[0] : 1.0;
-    a.cx = K1 ? K1[2] : 0.0;
-    a.cy = K1 ? K1[5] : 0.0;
+    for (int i = 0; i < 9; i++) a.R1f[i] = (float)(R1 ? R1[i] : (i % 4 == 0 ? 1.0 : 0.0));
+    for (int i = 0; i < 3; i++) a.t1f[i] = (float)(t1 ? t1[i] : 0.0);
+    a.fxf = (float)(K1 ? K1[0] : 1.0);
+    a.cxf = (float)(K1 ? K1[2] : 0.0);
+    a.cyf = (float)(K1 ? K1[5] : 0.0);
     a.lambda = lambda;
     a.alpha_proj = alpha_proj;
     a.recon = recon;

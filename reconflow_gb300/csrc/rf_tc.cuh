@@ -140,6 +140,7 @@ __device__ __forceinline__ uint32_t tile_off(int r, int g) {
 template <int NT>
 struct TcSmem {
     static_assert(NT % 16 == 0 && NT >= 16 && NT <= 256, "N tile");
+    static_assert((NT * 8) % 128 == 0, "B tile rows split evenly over the CTA's threads");
     static constexpr int kA = kTM * kTK * 2;  // bytes of one A chunk
     static constexpr int kB = NT * kTK * 2;
     static constexpr int kBytes = 2 * (kA + kB) + 2048;  // two chunk buffers, barriers, alignment slack
@@ -188,20 +189,34 @@ __global__ void __launch_bounds__(kThreads) k_tc_gemm(int M, int N, int K, int k
             phases ^= 1u << b;
         }
         const int kc = k_begin + c * kTK;
-        // gather: A 128 rows x 8 groups, B NT rows x 8 groups, 16 bytes each
-        for (int i = tid; i < kTM * (kTK / 8); i += kThreads) {
-            const int r = i >> 3, g = i & 7;
-            const int k = kc + g * 8;
-            uint4 v = make_uint4(0, 0, 0, 0);
-            if (m0 + r < M && k < k_end) v = la(m0 + r, k, k_end);
-            *(uint4*)(tA + tile_off(r, g)) = v;
+        // gather: A 128 rows x 8 groups, B NT rows x 8 groups, 16 bytes each.
+        // All of a thread's global loads are issued before its shared-memory
+        // stores, so they are in flight together (the stores go through a
+        // generic pointer the compiler cannot tell apart from global memory).
+        constexpr int kPerA = kTM * (kTK / 8) / kThreads;  // 8
+        constexpr int kPerB = NT * (kTK / 8) / kThreads;   // NT / 16
+        uint4 va[kPerA], vb[kPerB];
+#pragma unroll
+        for (int j = 0; j < kPerA; j++) {
+            const int i = tid + j * kThreads, r = i >> 3, g = i & 7, k = kc + g * 8;
+            va[j] = make_uint4(0, 0, 0, 0);
+            if (m0 + r < M && k < k_end) va[j] = la(m0 + r, k, k_end);
         }
-        for (int i = tid; i < NT * (kTK / 8); i += kThreads) {
-            const int r = i >> 3, g = i & 7;
-            const int k = kc + g * 8;
-            uint4 v = make_uint4(0, 0, 0, 0);
-            if (n0 + r < N && k < k_end) v = lb(n0 + r, k, k_end);
-            *(uint4*)(tB + tile_off(r, g)) = v;
+#pragma unroll
+        for (int j = 0; j < kPerB; j++) {
+            const int i = tid + j * kThreads, r = i >> 3, g = i & 7, k = kc + g * 8;
+            vb[j] = make_uint4(0, 0, 0, 0);
+            if (n0 + r < N && k < k_end) vb[j] = lb(n0 + r, k, k_end);
+        }
+#pragma unroll
+        for (int j = 0; j < kPerA; j++) {
+            const int i = tid + j * kThreads;
+            *(uint4*)(tA + tile_off(i >> 3, i & 7)) = va[j];
+        }
+#pragma unroll
+        for (int j = 0; j < kPerB; j++) {
+            const int i = tid + j * kThreads;
+            *(uint4*)(tB + tile_off(i >> 3, i & 7)) = vb[j];
         }
         fence_async_smem();
         __syncthreads();

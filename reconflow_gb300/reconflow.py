@@ -414,6 +414,21 @@ class ReconFlowBatch:
         N.check(self._lib.rf_batch_upload_images_device(self._h, int(pair), ctypes.c_void_p(ptr0),
                                                         ctypes.c_void_p(ptr1), int(pitch)))
 
+    def setTiles(self, tile_w, tile_h):
+        """Tile shape per pyramid level (rf_batch_set_tiles)."""
+        n = int(self.params.n_levels)
+        if len(tile_w) != n or len(tile_h) != n:
+            raise ValueError("one tile shape per level")
+        N.check(self._lib.rf_batch_set_tiles(self._h, (ctypes.c_int * n)(*map(int, tile_w)),
+                                             (ctypes.c_int * n)(*map(int, tile_h))))
+
+    def profileLevel(self, level, nIters=20):
+        """Mean ms per launch of the two inner-iteration kernels at `level`
+        (rf_batch_profile_level); needs a prior solve and invalidates it."""
+        ms = (ctypes.c_float * 2)()
+        N.check(self._lib.rf_batch_profile_level(self._h, int(level), int(nIters), ms))
+        return float(ms[0]), float(ms[1])
+
     def levelDims(self, pair, level):
         """(w, h, stride) of pair's pyramid level (Cudaflow.cu:146-171 rule)."""
         w, h = self.sizes[pair]

@@ -247,7 +247,7 @@ def _render_pair_torch(width, height, K, R, t, planes, tex, rng, noise, device):
     dev = torch.device(device)
     T = lambda a: torch.as_tensor(np.asarray(a, np.float64), device=dev)  # noqa: E731
     Kt, Rt, tt = T(K), T(R), T(t)
-    Kinv = torch.linalg.inv(Kt)
+    Kinv = T(np.linalg.inv(np.asarray(K, np.float64)))  # host inverse: no GPU LAPACK needed
     ys, xs = torch.meshgrid(torch.arange(height, device=dev, dtype=torch.float64),
                             torch.arange(width, device=dev, dtype=torch.float64), indexing="ij")
     xs, ys = xs.reshape(-1), ys.reshape(-1)
@@ -300,7 +300,7 @@ def _render_pair_torch(width, height, K, R, t, planes, tex, rng, noise, device):
     v1 = Kt[1, 1] * X1[1] / X1[2] + Kt[1, 2]
     inb = (u1 >= 0) & (u1 <= width - 1) & (v1 >= 0) & (v1 <= height - 1)
     Xv, fv = raycast(u1, v1)
-    same = fv & (torch.linalg.norm(Xv - X0, dim=0) < 1e-3 * torch.clamp(X0[2], min=1.0))
+    same = fv & (torch.sqrt(((Xv - X0) ** 2).sum(0)) < 1e-3 * torch.clamp(X0[2], min=1.0))
     valid = (inb & same).reshape(height, width)
     sh = (height, width)
     I0 = I0.reshape(sh).cpu().numpy() + rng.normal(0.0, noise, sh)

@@ -109,3 +109,38 @@ def test_batch_rejects_unsupported(rf):
         rf.ReconFlowBatch([(64, 48)], 2, method=17)
     with pytest.raises(rf.RfError):
         rf.ReconFlowBatch([(64, 48), (8, 4)], 4, method=14)  # 8x4 cannot make 4 levels
+
+
+def test_tile_shapes_do_not_change_results(rf):
+    """rf_batch_set_tiles changes how pixels map to blocks, never a value;
+    bad shapes are rejected; the autotuner leaves a valid choice."""
+    from reconflow_gb300 import autotune
+    from reconflow_gb300._native import RfError
+
+    L = 3
+    data = _inputs()
+    kw = dict(lambda_=50.0, lambdaf=0.1, lambdams=100.0, alphaTv=1 / 0.33, alphaProj=60.0,
+              tau=0.25, nWarpIters=2, nSolverIters=4, fix_quirks=1)
+    b = rf.ReconFlowBatch([(w, h) for w, h, *_ in data], L, method=14, **kw)
+    for i, (w, h, I0, I1, K, R, t) in enumerate(data):
+        s = b.strides[i]
+        b.setCameraMatrices(i, K, K)
+        b.copyImagesToDevice(i, pad_rows(I0, s), pad_rows(I1, s))
+    Rs, ts = [d[5] for d in data], [d[6] for d in data]
+    b.solveR(Rs, ts)
+    ref = [b.copyOpticalFlowToHost(i) + b.copy3dToHost(i) for i in range(len(data))]
+    for tw, th in (([64, 16, 128], [4, 16, 2]), ([16, 32, 32], [8, 2, 4]), ([128, 64, 16], [2, 2, 2])):
+        b.setTiles(tw, th)
+        b.solveR(Rs, ts)
+        for i in range(len(data)):
+            got = b.copyOpticalFlowToHost(i) + b.copy3dToHost(i)
+            for a, r, nm in zip(got, ref[i], "uvXYZ"):
+                assert_bitexact(a, r, f"pair {i} {nm} tiles {tw}x{th}")
+    for bad in (([0, 32, 32], [8, 8, 8]), ([32, 32, 33], [8, 8, 1]), ([64, 32, 32], [8, 8, 8])):
+        with pytest.raises(RfError):
+            b.setTiles(*bad)
+    table = autotune.autotune(b, Rs, ts, iters=2)
+    assert len(table) == L and all(tuple(e["tile"]) in autotune.CANDIDATES for e in table)
+    tw, th = autotune.tiles_for(b, table)
+    assert [tuple(x) for x in zip(tw, th)] == [tuple(e["tile"]) for e in table]
+    b.close()

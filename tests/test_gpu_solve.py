@@ -350,4 +350,5 @@ def test_energy_matches_oracle(oracle, rf, method):
     else:
         e_ref = oracle.energy(I0, I1, res["u"], res["v"], res["X"], res["Y"], res["Z"], w, h, s,
                               50.0, 60.0, R, t, K)
-    assert e_gpu == pytest.approx(e_ref, rel=1e-9)
+    # per-pixel terms in FP32 on the GPU, FP64 in the oracle; both sum in double
+    assert e_gpu == pytest.approx(e_ref, rel=1e-5)
