@@ -208,4 +208,64 @@ public:
 #endif
 };
 
+// Many frame pairs solved together (rf_batch_*; no reference counterpart):
+// pairs may differ in size, cameras and pose and share the solver
+// parameters; a pair's results are bit-identical to solving it alone.
+class ReconFlowBatch {
+public:
+    // p: parameters as rf_params_default(RF_METHODR_TVL1_MS) plus the
+    // caller's weights and schedule; widths / heights: n_pairs sizes
+    ReconFlowBatch(const rf_params& p, int n_pairs, const int* widths, const int* heights) {
+        check(rf_batch_create(&p, n_pairs, widths, heights, &b_));
+    }
+    ~ReconFlowBatch() { rf_batch_destroy(b_); }
+    ReconFlowBatch(const ReconFlowBatch&) = delete;
+    ReconFlowBatch& operator=(const ReconFlowBatch&) = delete;
+
+    int stride(int pair) const { return rf_batch_stride(b_, pair); }
+    int setCameraMatrices(int pair, const double* K0, const double* K1) {
+        check(rf_batch_set_cameras(b_, pair, K0, K1));
+        return 0;
+    }
+    int copyImagesToDevice(int pair, const float* i0, const float* i1, int pitch) {
+        check(rf_batch_upload_images(b_, pair, i0, i1, pitch));
+        return 0;
+    }
+    // R1s, t1s: n_pairs x 9 and n_pairs x 3 doubles (camera 0 = identity)
+    int solveR(const double* R1s, const double* t1s) {
+        check(rf_batch_solve(b_, nullptr, nullptr, R1s, t1s));
+        return 0;
+    }
+    // warm start at `level` from the planes of warmPlanes (filled beforehand)
+    int solveWarm(int level, const int* warps, const int* iters, const double* R1s,
+                  const double* t1s) {
+        check(rf_batch_solve_warm_levels(b_, nullptr, nullptr, R1s, t1s, level, warps, iters));
+        return 0;
+    }
+    int warmPlanes(int pair, float** u, float** v, float** X, float** Y, float** Z) {
+        check(rf_batch_warm_planes(b_, pair, u, v, X, Y, Z));
+        return 0;
+    }
+    int setTiles(const int* tile_w, const int* tile_h) {
+        check(rf_batch_set_tiles(b_, tile_w, tile_h));
+        return 0;
+    }
+    int copyOpticalFlowToHost(int pair, float* u, float* v, int pitch) {
+        check(rf_batch_download_flow(b_, pair, u, v, pitch));
+        return 0;
+    }
+    int copy3dToHost(int pair, float* X, float* Y, float* Z, int pitch) {
+        check(rf_batch_download_points(b_, pair, X, Y, Z, pitch));
+        return 0;
+    }
+    int energies(double* out) {
+        check(rf_batch_energies(b_, out));
+        return 0;
+    }
+    rf_batch* handle() { return b_; }
+
+private:
+    rf_batch* b_ = nullptr;
+};
+
 }  // namespace reconflow_gb300

@@ -750,12 +750,14 @@ __global__ void __launch_bounds__(kEnergyThreads) k_energy_partial(EnergyArgs a,
     }
 }
 
+// One warp: lane l adds partials l, l + 32, ... in order, then a fixed
+// shuffle tree adds the 32 lane sums, so the result is deterministic.
 __global__ void k_energy_final(const double* partial, int n, double* out) {
-    if (threadIdx.x == 0 && blockIdx.x == 0) {
-        double t = 0.0;
-        for (int k = 0; k < n; k++) t += partial[k];
-        *out = t;
-    }
+    const int lane = threadIdx.x;
+    double t = 0.0;
+    for (int k = lane; k < n; k += 32) t += partial[k];
+    for (int o = 16; o > 0; o >>= 1) t += __shfl_down_sync(0xffffffffu, t, o);
+    if (lane == 0) *out = t;
 }
 
 // ---------------------------------------------------------------------------

@@ -374,8 +374,8 @@ def main(argv=None):
     import time
 
     ap = argparse.ArgumentParser(description=main.__doc__.split("\n\n")[0])
-    ap.add_argument("--scenes", type=int, default=4096)
-    ap.add_argument("--epochs", type=int, default=30)
+    ap.add_argument("--scenes", type=int, default=8192)
+    ap.add_argument("--epochs", type=int, default=60)
     ap.add_argument("--lr", type=float, default=1e-3)
     ap.add_argument("--seed", type=int, default=0)
     ap.add_argument("--out", required=True)

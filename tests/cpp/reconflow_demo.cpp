@@ -47,6 +47,47 @@ int main() {
             }
         std::nth_element(uu.begin(), uu.begin() + uu.size() / 2, uu.end());
         std::nth_element(zz.begin(), zz.begin() + zz.size() / 2, zz.end());
+        // the same pair twice through the batch class: bit-identical to the
+        // single-pair solve
+        rf_params p;
+        rf_params_default(&p, RF_METHODR_TVL1_MS);
+        p.width = width;
+        p.height = height;
+        p.input_type = RF_INPUT_F32;
+        p.n_levels = nLevels;
+        p.lambda = 50.0f;
+        p.lambdaf = 0.1f;
+        p.lambdams = 100.0f;
+        p.alpha_tv = 1.0f / 0.33f;
+        p.alpha_proj = 60.0f;
+        p.tau = 0.25f;
+        p.theta = 0.33f;
+        p.n_warp_iters = 2;
+        p.n_solver_iters = 20;
+        p.fix_quirks = RF_FIX_K_PYRAMID;
+        const int ws[2] = {width, width}, hs[2] = {height, height};
+        reconflow_gb300::ReconFlowBatch batch(p, 2, ws, hs);
+        double Rs[18], ts[6];
+        for (int k = 0; k < 2; k++) {
+            batch.setCameraMatrices(k, K, K);
+            batch.copyImagesToDevice(k, i0.data(), i1.data(), stride);
+            for (int i = 0; i < 9; i++) Rs[9 * k + i] = R[i];
+            for (int i = 0; i < 3; i++) ts[3 * k + i] = t[i];
+        }
+        batch.solveR(Rs, ts);
+        std::vector<float> bu(stride * height), bv(stride * height);
+        int same = 1;
+        for (int k = 0; k < 2; k++) {
+            batch.copyOpticalFlowToHost(k, bu.data(), bv.data(), stride);
+            for (int y = 0; y < height; y++)
+                for (int x = 0; x < width; x++)
+                    same &= bu[x + y * stride] == u[x + y * stride] ||
+                            (std::isnan(bu[x + y * stride]) && std::isnan(u[x + y * stride]));
+        }
+        if (!same) {
+            std::printf("error 0 batch differs from the single-pair solve\n");
+            return 1;
+        }
         std::printf("ok %.4f %.4f\n", uu[uu.size() / 2], zz[zz.size() / 2]);
     } catch (const reconflow_gb300::Error& e) {
         std::printf("error %d %s\n", (int)e.status, e.what());
