@@ -82,6 +82,21 @@ LEARNED_METRIC = ("720p frame pairs/s, batched + learned warm start (vs the plai
 PLAIN_METRIC = "720p frame pairs/s (ReconFlow flow + depth)"
 
 
+# tile table of the single-pair (drop-in) solver at 1280x720 on GB300
+SINGLE_TILES = "reconflow_gb300/tuning/gb300_720p_single.json"
+
+
+def load_tiles(rel):
+    """A committed autotuner table (reconflow_gb300/autotune.py), or None."""
+    if not rel:
+        return None
+    path = os.path.join(ROOT, rel)
+    if not os.path.exists(path):
+        return None
+    with open(path) as fh:
+        return json.load(fh)
+
+
 def load_peaks():
     p = os.path.join(ROOT, "MEASURED_PEAKS.json")
     if os.path.exists(p):
@@ -413,11 +428,7 @@ def run_learned(args, wl, world, rank, local):
 
     from reconflow_gb300 import autotune
 
-    tiles = None
-    tpath = os.path.join(ROOT, wl.get("tiles", ""))
-    if wl.get("tiles") and os.path.exists(tpath):
-        with open(tpath) as fh:
-            tiles = json.load(fh)
+    tiles = load_tiles(wl.get("tiles"))
 
     def new_batch(warps, iters):
         b = R.ReconFlowBatch([(W, H)] * n, wl["levels"], method=SOLVER["method"],
@@ -474,6 +485,9 @@ def run_learned(args, wl, world, rank, local):
                   SOLVER["alpha_proj"], 0.5, SOLVER["tau"], wl["plain_warps"], wl["plain_iters"],
                   cvType=5, fix_quirks=SOLVER["fix_quirks"])
     f.setStream(stream.cuda_stream)
+    single_tiles = load_tiles(SINGLE_TILES)
+    if single_tiles is not None:
+        autotune.apply_single(f, single_tiles["levels"], wl["levels"])
     f.setCameraMatrices(scenes[0]["K"], scenes[0]["K"])
     f.copyImagesToDevice(scenes[0]["I0"], scenes[0]["I1"])
     with torch.cuda.stream(stream):
@@ -604,6 +618,8 @@ def run_learned(args, wl, world, rank, local):
                        "fallback": f"plain re-solve when energy > (1 + {margin}) x plain energy",
                        "checkpoint": wl["checkpoint"],
                        "tiles": wl.get("tiles") if tiles is not None else "default 32x8",
+                       "single_pair_tiles": SINGLE_TILES if single_tiles is not None
+                       else "default 32x8",
                        "method": "METHODR_TVL1_MS",
                        "lambda": SOLVER["lam"], "theta": SOLVER["theta"], "tau": SOLVER["tau"],
                        "alpha_proj": SOLVER["alpha_proj"], "lambdaf": SOLVER["lambdaf"],
@@ -709,6 +725,11 @@ def main():
                   fix_quirks=SOLVER["fix_quirks"])
     stream = torch.cuda.Stream()
     f.setStream(stream.cuda_stream)
+    single_tiles = load_tiles(SINGLE_TILES) if (wl["width"], wl["height"]) == (1280, 720) else None
+    if single_tiles is not None:
+        from reconflow_gb300 import autotune
+
+        autotune.apply_single(f, single_tiles["levels"], wl["levels"])
     f.setCameraMatrices(sc["K"], sc["K"])
     f.copyImagesToDevice(I0, I1)
     flush = torch.empty(L2_FLUSH_BYTES // 4, dtype=torch.float32, device="cuda")
@@ -818,7 +839,9 @@ def main():
             "unit": "pairs/s", "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
             "ms_per_step": 1000.0 * total_s / args.steps, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f32",
-            "data": "synthetic (seeded scene generator)", "config": config_of(wl),
+            "data": "synthetic (seeded scene generator)",
+            "config": dict(config_of(wl), tiles=SINGLE_TILES if single_tiles is not None
+                           else "default 32x8"),
             "e2e": e2e, "roofline": roofline, "cpu_baseline": cpu,
             "clocks": clk.summary(), "gpu_launches": int(launches),
             "wall_s_timed": wall, "accuracy": accuracy,

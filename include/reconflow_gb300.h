@@ -195,6 +195,14 @@ RF_API rf_status rf_remove_edge_artifacts(rf_handle* h, int surface_width, float
 RF_API rf_status rf_device_results(rf_handle* h, const float** u, const float** v,
                                    const float** X, const float** Y, const float** Z);
 
+/* Tile shape of the inner-iteration kernels at each pyramid level
+ * (tile_w[l] x tile_h[l] pixels, one thread each; 32 .. 256 threads, a
+ * multiple of 32; default 32 x 8), as reconflow_gb300/autotune.py picks
+ * them.  No reference counterpart (the reference's BlockWidth / BlockHeight
+ * constructor arguments, Reconflow.h:12, play this role for all kernels).
+ * Results do not depend on it. */
+RF_API rf_status rf_set_tiles(rf_handle* h, const int* tile_w, const int* tile_h);
+
 /* Use a caller's CUDA stream (cudaStream_t passed as void*; NULL = the
  * handle's own stream). */
 RF_API rf_status rf_set_stream(rf_handle* h, void* stream);

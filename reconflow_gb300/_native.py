@@ -67,6 +67,7 @@ _SIGS = [
     ("rf_download_flow_color", _I, [_VP, _F, _VP, _I]),
     ("rf_remove_edge_artifacts", _I, [_VP, _I, _F]),
     ("rf_device_results", _I, [_VP, _VP, _VP, _VP, _VP, _VP]),
+    ("rf_set_tiles", _I, [_VP, _VP, _VP]),
     ("rf_set_stream", _I, [_VP, _VP]),
     ("rf_synchronize", _I, [_VP]),
     ("rf_host_alloc", _I, [ctypes.c_size_t, ctypes.POINTER(_VP)]),

@@ -47,6 +47,30 @@ def autotune(batch, R1s, t1s, candidates=CANDIDATES, iters=20, log=None):
     return table
 
 
+def autotune_single(flow, R1, t1, n_levels, candidates=CANDIDATES, iters=20, log=None):
+    """The same search for one ReconFlow handle (rf_set_tiles,
+    rf_profile_iterations); images and cameras must be set."""
+    best = [(32, 8)] * n_levels
+    table = []
+    for level in range(n_levels):
+        times = {}
+        for shape in candidates:
+            trial = list(best)
+            trial[level] = shape
+            flow.setTiles([x[0] for x in trial], [x[1] for x in trial])
+            flow.solveR(R1, t1, 5.0)
+            a, b = flow.profileLevel(level, iters)
+            times[f"{shape[0]}x{shape[1]}"] = a + b
+        pick = min(times, key=times.get)
+        best[level] = tuple(int(x) for x in pick.split("x"))
+        table.append({"level": level, "tile": list(best[level]), "ms": times})
+        if log:
+            log(f"level {level}: {pick}  " +
+                " ".join(f"{k} {v * 1e3:.1f}us" for k, v in sorted(times.items(), key=lambda x: x[1])))
+    flow.setTiles([x[0] for x in best], [x[1] for x in best])
+    return table
+
+
 def tiles_for(batch, table):
     """Per-level shapes for `batch` from a saved table: each level takes the
     tile of the table entry whose pixel count is closest (in ratio)."""
@@ -68,6 +92,13 @@ def apply(batch, table):
     batch.setTiles(tw, th)
 
 
+def apply_single(flow, table, n_levels):
+    """Per-level shapes of a single-pair table (by level index; levels past
+    the table take its last entry) on a ReconFlow handle."""
+    ent = [table[min(l, len(table) - 1)]["tile"] for l in range(n_levels)]
+    flow.setTiles([e[0] for e in ent], [e[1] for e in ent])
+
+
 def main(argv=None):
     import argparse
 
@@ -81,8 +112,26 @@ def main(argv=None):
     ap.add_argument("--levels", type=int, default=6)
     ap.add_argument("--iters", type=int, default=20)
     ap.add_argument("--out", required=True)
+    ap.add_argument("--single", action="store_true",
+                    help="tune one ReconFlow handle (the drop-in path) instead of a batch")
     a = ap.parse_args(argv)
     w, h = (int(x) for x in a.size.split("x"))
+    if a.single:
+        from .reconflow import ReconFlow
+
+        sc = make_scene(w, h, seed=7000, device="cuda")
+        f = ReconFlow()
+        sw = SOLVER_WEIGHTS
+        f.initializeR(w, h, 1, a.levels, 2.0, 14, sw["lambda_"], 0.0, sw["lambdaf"], sw["lambdams"],
+                      sw["alphaTv"], sw["alphaProj"], 0.5, sw["tau"], 1, 5, cvType=5,
+                      fix_quirks=sw["fix_quirks"])
+        f.setCameraMatrices(sc["K"], sc["K"])
+        f.copyImagesToDevice(sc["I0"], sc["I1"])
+        table = autotune_single(f, sc["R"], sc["t"], a.levels, iters=a.iters, log=print)
+        with open(a.out, "w") as fh:
+            json.dump({"device": "GB300", "size": a.size, "pairs": 1, "levels": table}, fh, indent=1)
+        f.close()
+        return
     scs = [make_scene(w, h, seed=7000 + i, device="cuda") for i in range(a.pairs)]
     b = ReconFlowBatch([(w, h)] * a.pairs, a.levels, method=14, nWarpIters=1, nSolverIters=5,
                        **SOLVER_WEIGHTS)

@@ -821,8 +821,8 @@ int launch_pdl(void (*kern)(KArgs...), dim3 g, dim3 b, cudaStream_t st, Args... 
 }
 
 int launch_recon_a(const ReconFields& f, const LevelConsts* lc, const Weights& wt, LevelDims d,
-                   bool first, bool uc_from_buffer, int prior, cudaStream_t st) {
-    dim3 g = grid_for(d.w, d.h), b(BX, BY);
+                   bool first, bool uc_from_buffer, int prior, cudaStream_t st, dim3 b) {
+    dim3 g((d.w + b.x - 1) / b.x, (d.h + b.y - 1) / b.y);
     int fi = first ? 1 : 0, ub = uc_from_buffer ? 1 : 0;
     if (prior == 1) return launch_pdl(k_recon_a<1>, g, b, st, f, lc, wt, d, fi, ub);
     if (prior == 2) return launch_pdl(k_recon_a<2>, g, b, st, f, lc, wt, d, fi, ub);
@@ -893,8 +893,9 @@ int launch_recon_persistent(const ReconFields& f, const LevelConsts* lc, const W
 }
 
 int launch_recon_b(const ReconFields& f, const Weights& wt, LevelDims d, bool first,
-                   cudaStream_t st) {
-    return launch_pdl(k_recon_b, grid_for(d.w, d.h), dim3(BX, BY), st, f, wt, d, first ? 1 : 0);
+                   cudaStream_t st, dim3 b) {
+    dim3 g((d.w + b.x - 1) / b.x, (d.h + b.y - 1) / b.y);
+    return launch_pdl(k_recon_b, g, b, st, f, wt, d, first ? 1 : 0);
 }
 
 int launch_plain_data(float* duhat, float* dvhat, const float* pu1, const float* pu2,

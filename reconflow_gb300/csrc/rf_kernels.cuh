@@ -126,10 +126,12 @@ int launch_warp(const float* I1, const float* u, const float* v, LevelDims d, fl
                 cudaStream_t st);
 int launch_derivatives(const float* I0, const float* I1w, LevelDims d, float* Ix, float* Iy,
                        float* Iz, cudaStream_t st);
+// `block` = the level's tile (default 32 x 8; at most 256 threads)
 int launch_recon_a(const ReconFields& f, const LevelConsts* lc, const Weights& wt, LevelDims d,
-                   bool first, bool uc_from_buffer, int prior, cudaStream_t st);
+                   bool first, bool uc_from_buffer, int prior, cudaStream_t st,
+                   dim3 block = dim3(32, 8));
 int launch_recon_b(const ReconFields& f, const Weights& wt, LevelDims d, bool first,
-                   cudaStream_t st);
+                   cudaStream_t st, dim3 block = dim3(32, 8));
 // All `iters` inner iterations of one warp in one cooperative launch (small
 // levels); bar = 3 zeroed words (count, generation, timeout flag).
 int launch_recon_persistent(const ReconFields& f, const LevelConsts* lc, const Weights& wt,

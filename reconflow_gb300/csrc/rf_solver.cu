@@ -112,6 +112,8 @@ struct rf_handle {
     float* warm[5] = {nullptr, nullptr, nullptr, nullptr, nullptr};
     int warm_level = -1, warm_warps = 0, warm_iters = 0;
     int graph_key[3] = {-1, -1, -1};
+    // tile shape of the inner-iteration kernels at each level (rf_set_tiles)
+    std::vector<int> tile_w, tile_h;
     // energy reduction buffers and the pose of the last solve
     double* d_energy = nullptr;  // [0] = result, [1..1024] = block partials
     double last_R1[9], last_t1[3];
@@ -333,8 +335,9 @@ rf_status enqueue_recon(rf_handle* h, float** res_u, float** res_v, bool warm = 
                 uc_in_buffer = false;
             }
             for (int iter = 0; iter < n_iters && d.w * d.h > h->persist_max_px; iter++) {
-                RF_LAUNCH(launch_recon_a(f, lc, wt, d, iter == 0, uc_in_buffer, prior, st));
-                RF_LAUNCH(launch_recon_b(f, wt, d, iter == 0, st));
+                const dim3 tile(h->tile_w[level], h->tile_h[level]);
+                RF_LAUNCH(launch_recon_a(f, lc, wt, d, iter == 0, uc_in_buffer, prior, st, tile));
+                RF_LAUNCH(launch_recon_b(f, wt, d, iter == 0, st, tile));
                 uc_in_buffer = false;
             }
             if (n_iters == 0) {
@@ -657,6 +660,8 @@ rf_status rf_create(const rf_params* p, rf_handle** out) {
     h->p = *p;
     h->L = p->n_levels;
     h->W.resize(h->L); h->H.resize(h->L); h->S.resize(h->L);
+    h->tile_w.assign(h->L, 32);
+    h->tile_h.assign(h->L, 8);
     // Cudaflow.cu:146-171
     int nh = p->height, nw = p->width, ns = align_up(p->width, p->stride_alignment);
     for (int l = 0; l < h->L; l++) {
@@ -1048,6 +1053,25 @@ rf_status rf_device_results(rf_handle* h, const float** u, const float** v, cons
     return RF_OK;
 }
 
+rf_status rf_set_tiles(rf_handle* h, const int* tile_w, const int* tile_h) {
+    if (!h || !tile_w || !tile_h) return fail(RF_ERR_INVALID_ARG, "rf_set_tiles: null argument");
+    for (int l = 0; l < h->L; l++) {
+        const int w = tile_w[l], t = tile_h[l];
+        if (w < 1 || t < 1 || w * t > 256 || (w * t) % 32 != 0)
+            return fail(RF_ERR_INVALID_ARG,
+                        "rf_set_tiles: a tile needs 32..256 threads, a multiple of 32");
+    }
+    RF_CUDA(cudaStreamSynchronize(h->stream));
+    h->tile_w.assign(tile_w, tile_w + h->L);
+    h->tile_h.assign(tile_h, tile_h + h->L);
+    if (h->graph) {  // the captured schedule has the old launch shapes
+        cudaGraphExecDestroy(h->graph);
+        h->graph = nullptr;
+        h->graph_kind = -1;
+    }
+    return RF_OK;
+}
+
 rf_status rf_set_stream(rf_handle* h, void* stream) {
     if (!h) return fail(RF_ERR_INVALID_ARG, "rf_set_stream: null handle");
     RF_CUDA(cudaStreamSynchronize(h->stream));
@@ -1142,8 +1166,10 @@ rf_status rf_profile_iterations(rf_handle* h, int level, int n_iters, float* ms)
         int bad = 0;
         for (int i = 0; i < n_iters && !bad; i++) {
             if (recon)
-                bad = k == 0 ? launch_recon_a(f, h->d_consts + level, wt, d, false, false, prior, st)
-                             : launch_recon_b(f, wt, d, false, st);
+                bad = k == 0 ? launch_recon_a(f, h->d_consts + level, wt, d, false, false, prior, st,
+                                              dim3(h->tile_w[level], h->tile_h[level]))
+                             : launch_recon_b(f, wt, d, false, st,
+                                              dim3(h->tile_w[level], h->tile_h[level]));
             else
                 bad = k == 0 ? launch_plain_data(h->duhat, h->dvhat, h->pu1, h->pu2, h->pv1,
                                                  h->pv2, h->Ix, h->Iy, h->Iz, wt, d, false, st)

@@ -185,6 +185,21 @@ class CudaFlow:
         N.check(self._lib.rf_device_results(self._handle(), *[ctypes.byref(p) for p in ptrs]))
         return [p.value or 0 for p in ptrs]
 
+    def setTiles(self, tile_w, tile_h) -> int:
+        """Tile shape of the inner-iteration kernels per pyramid level
+        (rf_set_tiles); results do not depend on it."""
+        n = len(tile_w)
+        N.check(self._lib.rf_set_tiles(self._handle(), (ctypes.c_int * n)(*map(int, tile_w)),
+                                       (ctypes.c_int * n)(*map(int, tile_h))))
+        return 0
+
+    def profileLevel(self, level, nIters=20):
+        """Mean ms per launch of the two inner-iteration kernels at `level`
+        (rf_profile_iterations); needs a prior solve and invalidates it."""
+        ms = (ctypes.c_float * 2)()
+        N.check(self._lib.rf_profile_iterations(self._handle(), int(level), int(nIters), ms))
+        return float(ms[0]), float(ms[1])
+
     def setStream(self, stream_ptr: int | None) -> int:
         N.check(self._lib.rf_set_stream(self._handle(), ctypes.c_void_p(stream_ptr or 0)))
         return 0

@@ -352,3 +352,31 @@ def test_energy_matches_oracle(oracle, rf, method):
                               50.0, 60.0, R, t, K)
     # per-pixel terms in FP32 on the GPU, FP64 in the oracle; both sum in double
     assert e_gpu == pytest.approx(e_ref, rel=1e-5)
+
+
+def test_tiles_do_not_change_single_pair_results(rf):
+    """rf_set_tiles changes only the launch shape of the inner iterations."""
+    from reconflow_gb300._native import RfError
+
+    w, h, L = 150, 100, 3
+    rng = np.random.default_rng(12)
+    s = align_up(w)
+    I0, I1 = textured_pair(rng, h, w)
+    I0, I1 = pad_rows(I0, s), pad_rows(I1, s)
+    K, (R, t) = _K(w, h), _pose(3)
+    f = rf.ReconFlow()
+    f.initializeR(w, h, 1, L, 2.0, 14, 50.0, 0.0, 0.1, 100.0, 1 / 0.33, 60.0, 0.5, 0.25, 2, 6,
+                  cvType=5, fix_quirks=1)
+    f.setCameraMatrices(K, K)
+    f.copyImagesToDevice(I0, I1)
+    f.solveR(R, t, 5.0)
+    ref = f.copyOpticalFlowToHost() + f.copy3dToHost()
+    for tw, th in (([32, 16, 64], [2, 8, 4]), ([128, 32, 16], [2, 4, 16])):
+        f.setTiles(tw, th)
+        f.solveR(R, t, 5.0)
+        got = f.copyOpticalFlowToHost() + f.copy3dToHost()
+        for a, b, nm in zip(got, ref, "uvXYZ"):
+            assert_bitexact(a, b, f"{nm} tiles {tw}x{th}")
+    with pytest.raises(RfError):
+        f.setTiles([32, 32, 32], [8, 8, 9])
+    f.close()
