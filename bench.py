@@ -59,11 +59,11 @@ WORKLOADS = {
                     levels=6, warps=5, iters=100, seed=0),
     # batched + learned warm start: 64 pairs of 1280x720; the network predicts
     # inverse depth at 1/8, the solve refines from pyramid level 2 with the
-    # per-level schedule below (index = level, 0 = finest: 1 x 20, 1 x 30,
-    # 2 x 40); plain 5 x 100
+    # per-level schedule below (index = level, 0 = finest: 1 x 15, 1 x 30,
+    # 1 x 50); plain 5 x 100
     "720p-learned": dict(width=1280, height=720, pairs=64, levels=6, seed=2000, plain_warps=5,
-                         plain_iters=100, warm_level=2, warm_warps=[1, 1, 2],
-                         warm_iters=[20, 30, 40], fallback_margin=0.02,
+                         plain_iters=100, warm_level=2, warm_warps=[1, 1, 1],
+                         warm_iters=[15, 30, 50], fallback_margin=0.02,
                          checkpoint="reconflow_gb300/weights/warmstart_f125.bin",
                          tiles="reconflow_gb300/tuning/gb300_720p_x64.json"),
     # batched: 64 pairs of 1280x720 (per-pair throughput of the batched path)
