@@ -160,363 +160,6 @@ __global__ void __launch_bounds__(BX* BY, RF_MINB_B) k_recon_b(ReconFields f, We
 }
 
 // ---------------------------------------------------------------------------
-// Fused inner iteration: one launch per iteration.  The kernel boundary sits
-// after the triangulation, so a launch (1) settles iteration i-1's
-// triangulation (3x3 median + clean-up, recomputed on a one-pixel ring
-// around the tile), (2) runs the data step of iteration i on the tile plus
-// its right column and bottom row, then (3) the dual step, projection blend,
-// triangulation and multiplier update of iteration i on the tile.
-// ---------------------------------------------------------------------------
-#ifndef RF_FUSED_FY
-#define RF_FUSED_FY 16
-#endif
-constexpr int FX = 32;
-constexpr int FY = RF_FUSED_FY;
-
-// Settled 3D state (X after the median and clean-up of i-1) at one pixel.
-__device__ __forceinline__ void settle_px(const float* __restrict__ X1,
-                                          const float* __restrict__ Y1,
-                                          const float* __restrict__ Z1, LevelDims d, int ix,
-                                          int iy, float& Xo, float& Yo, float& Zo) {
-    const int w = d.w, h = d.h, s = d.s, pos = ix + iy * s;
-    float mX[9], mY[9], mZ[9];
-    if (ix > 0 && iy > 0 && ix + 1 < w && iy + 1 < h) {
-#pragma unroll
-        for (int j = 0; j < 3; j++)
-#pragma unroll
-            for (int i = 0; i < 3; i++) {
-                int at = pos + (j - 1) * s + (i - 1);
-                mX[j * 3 + i] = X1[at];
-                mY[j * 3 + i] = Y1[at];
-                mZ[j * 3 + i] = Z1[at];
-            }
-    } else {
-#pragma unroll
-        for (int j = 0; j < 3; j++)
-#pragma unroll
-            for (int i = 0; i < 3; i++) {
-                int at = median3_tap(ix + i - 1, iy + j - 1, w, h, s);
-                int k = j * 3 + i;
-                mX[k] = at >= 0 ? X1[at] : 0.0f;
-                mY[k] = at >= 0 ? Y1[at] : 0.0f;
-                mZ[k] = at >= 0 ? Z1[at] : 0.0f;
-            }
-    }
-    float Xc = mX[4], Yc = mY[4], Zc = mZ[4];
-    float Xm = median9_finite(mX), Ym = median9_finite(mY), Zm = median9_finite(mZ);
-    cleanup_pixel(Xc, Yc, Zc, Xm, Ym, Zm, Xo, Yo, Zo);
-}
-
-// Settled 3D value at image position (x, y) in [0, w] x [0, h] as the
-// triangulation reads it through the flat buffer: pixels are settled from
-// the pending triangulation; column w is the padding cell (stride > w) or
-// the next row's first pixel (stride == w); row h is the zero row below.
-__device__ __forceinline__ void settled_at(const FusedFields& f, LevelDims d, int x, int y,
-                                           bool x_from_A, float& X, float& Y, float& Z) {
-    const int flat = y * d.s + x;
-    int px = -1, py = -1;
-    if (!x_from_A) {
-        if (x < d.w && y < d.h) {
-            px = x;
-            py = y;
-        } else if (x == d.w && d.s == d.w && y + 1 < d.h) {
-            px = 0;
-            py = y + 1;
-        }
-    }
-    if (px >= 0) {
-        settle_px(f.X1, f.Y1, f.Z1, d, px, py, X, Y, Z);
-    } else {
-        X = f.XA[flat];
-        Y = f.YA[flat];
-        Z = f.ZA[flat];
-    }
-}
-
-__device__ __forceinline__ bool slot_needed(int x, int y, LevelDims d) {
-    return x >= 0 && y >= 0 && ((x < d.w && y <= d.h) || (x == d.w && y < d.h));
-}
-
-// Data step of the ReconFlow iteration at one pixel (solveReconDataL1.cu:24-100).
-template <int PRIOR>
-__device__ __forceinline__ void fused_data_px(const FusedFields& f, const Weights& wt, LevelDims d,
-                                              int ix, int iy, int first, float& hu, float& hv) {
-    const int s = d.s, pos = ix + iy * s;
-    float u = f.u[pos], v = f.v[pos];
-    float dix = f.Ix[pos], diy = f.Iy[pos], dit = f.Iz[pos];
-    float uproj = f.uproj[pos], vproj = f.vproj[pos];
-    float sku = f.sku[pos], skv = f.skv[pos];
-    float duhat = 0.0f, dvhat = 0.0f;
-    float pu1 = 0.0f, pu2 = 0.0f, pv1 = 0.0f, pv2 = 0.0f;
-    float pu1l = 0.0f, pv1l = 0.0f, pu2d = 0.0f, pv2d = 0.0f;
-    if (!first) {
-        duhat = f.duhat[pos];
-        dvhat = f.dvhat[pos];
-        pu1 = f.pu1[pos];
-        pu2 = f.pu2[pos];
-        pv1 = f.pv1[pos];
-        pv2 = f.pv2[pos];
-        if (ix > 0) {
-            pu1l = f.pu1[pos - 1];
-            pv1l = f.pv1[pos - 1];
-        }
-        if (iy > 0) {
-            pu2d = f.pu2[pos - s];
-            pv2d = f.pv2[pos - s];
-        }
-    }
-    float A, dusub, dvsub;
-    if (PRIOR == 0) {
-        A = wt.A;
-        dusub = (wt.alpha_tv * duhat + wt.alpha_proj * (uproj - u - sku)) / A;
-        dvsub = (wt.alpha_tv * dvhat + wt.alpha_proj * (vproj - v - skv)) / A;
-    } else {
-        float alphaFn = PRIOR == 2 ? wt.alpha_fn * f.mask[pos] : wt.alpha_fn;
-        float ufn = f.ufn[pos], vfn = f.vfn[pos];
-        A = wt.alpha_tv + wt.alpha_proj + alphaFn;
-        dusub = (alphaFn * (ufn - u) + wt.alpha_tv * duhat + wt.alpha_proj * (uproj - u - sku)) / A;
-        dvsub = (alphaFn * (vfn - v) + wt.alpha_tv * dvhat + wt.alpha_proj * (vproj - v - skv)) / A;
-    }
-    float du, dv;
-    l1_threshold(dusub, dvsub, dix, diy, dit, wt.lambda, A, du, dv);
-    float divpu = divergence(pu1, pu1l, pu2, pu2d, ix, iy);
-    float divpv = divergence(pv1, pv1l, pv2, pv2d, ix, iy);
-    hu = du + divpu / A;
-    hv = dv + divpv / A;
-}
-
-template <int PRIOR>
-__global__ void __launch_bounds__(FX* FY) k_recon_fused(FusedFields f,
-                                                        const LevelConsts* __restrict__ lcp,
-                                                        Weights wt, LevelDims d, int first,
-                                                        int x_from_A, int uc_from_buffer) {
-    // settled 3D state on the tile plus a one-pixel ring (corners unused)
-    __shared__ float xs[3][FY + 2][FX + 2];
-    // data step of this iteration on the tile plus right column / bottom row
-    __shared__ float hs[2][FY + 1][FX + 1];
-    const int tx = threadIdx.x, ty = threadIdx.y, tid = ty * FX + tx;
-    const int x0 = blockIdx.x * FX, y0 = blockIdx.y * FY;
-    const int w = d.w, h = d.h, s = d.s;
-    const int x = x0 + tx, y = y0 + ty;
-    const bool fromA = x_from_A != 0;
-
-    // (1) settle iteration i-1 on the tile and the ring
-    if (slot_needed(x, y, d)) {
-        float a, b, c;
-        settled_at(f, d, x, y, fromA, a, b, c);
-        xs[0][ty + 1][tx + 1] = a;
-        xs[1][ty + 1][tx + 1] = b;
-        xs[2][ty + 1][tx + 1] = c;
-    }
-    constexpr int NRX = 2 * (FX + FY);
-    if (tid < NRX) {
-        int rx, ry;
-        if (tid < FY) {
-            rx = -1; ry = tid;
-        } else if (tid < 2 * FY) {
-            rx = FX; ry = tid - FY;
-        } else if (tid < 2 * FY + FX) {
-            rx = tid - 2 * FY; ry = -1;
-        } else {
-            rx = tid - 2 * FY - FX; ry = FY;
-        }
-        if (slot_needed(x0 + rx, y0 + ry, d)) {
-            float a, b, c;
-            settled_at(f, d, x0 + rx, y0 + ry, fromA, a, b, c);
-            xs[0][ry + 1][rx + 1] = a;
-            xs[1][ry + 1][rx + 1] = b;
-            xs[2][ry + 1][rx + 1] = c;
-        }
-    }
-    // (2) data step of iteration i on the tile and right column / bottom row
-    const bool active = x < w && y < h;
-    float hu = 0.0f, hv = 0.0f;
-    if (active) {
-        fused_data_px<PRIOR>(f, wt, d, x, y, first, hu, hv);
-        hs[0][ty][tx] = hu;
-        hs[1][ty][tx] = hv;
-    }
-    if (tid >= NRX && tid < NRX + FX + FY) {
-        int k = tid - NRX, rx, ry;
-        if (k < FY) {
-            rx = FX; ry = k;
-        } else {
-            rx = k - FY; ry = FY;
-        }
-        if (x0 + rx < w && y0 + ry < h) {
-            float a, b;
-            fused_data_px<PRIOR>(f, wt, d, x0 + rx, y0 + ry, first, a, b);
-            hs[0][ry][rx] = a;
-            hs[1][ry][rx] = b;
-        }
-    }
-    __syncthreads();
-    if (!active) return;
-    const int pos = x + y * s;
-    const LevelConsts& c = *lcp;
-    f.duhat_o[pos] = hu;
-    f.dvhat_o[pos] = hv;
-
-    // (3a) dual TV step (solveSmoothDualTVGlobal.cu:26-64)
-    float dux = 0.0f, dvx = 0.0f, duy = 0.0f, dvy = 0.0f;
-    if (x + 1 < w) {
-        dux = hs[0][ty][tx + 1] - hu;
-        dvx = hs[1][ty][tx + 1] - hv;
-    }
-    if (y + 1 < h) {
-        duy = hs[0][ty + 1][tx] - hu;
-        dvy = hs[1][ty + 1][tx] - hv;
-    }
-    float pu1 = 0.0f, pu2 = 0.0f, pv1 = 0.0f, pv2 = 0.0f;
-    if (!first) {
-        pu1 = f.pu1[pos];
-        pu2 = f.pu2[pos];
-        pv1 = f.pv1[pos];
-        pv2 = f.pv2[pos];
-    }
-    dual_step(dux, duy, wt.fac, pu1, pu2);
-    dual_step(dvx, dvy, wt.fac, pv1, pv2);
-    f.pu1_o[pos] = pu1;
-    f.pu2_o[pos] = pu2;
-    f.pv1_o[pos] = pv1;
-    f.pv2_o[pos] = pv2;
-
-    // (3b) projection blend with uc from the settled state (solveUVProj.cu:13-21)
-    float Xn[5], Yn[5], Zn[5];
-    Xn[0] = xs[0][ty + 1][tx + 1];
-    Yn[0] = xs[1][ty + 1][tx + 1];
-    Zn[0] = xs[2][ty + 1][tx + 1];
-    float uc, vc;
-    if (uc_from_buffer) {
-        uc = f.uc[pos];
-        vc = f.vc[pos];
-    } else {
-        project_uc(c, Xn[0], Yn[0], Zn[0], x, y, uc, vc);
-    }
-    const float u = f.u[pos], v = f.v[pos];
-    const float sku = f.sku[pos], skv = f.skv[pos];
-    float uproj1 = (wt.lambdaf * uc + wt.alpha_proj * (u + hu + sku)) / wt.proj_den;
-    float vproj1 = (wt.lambdaf * vc + wt.alpha_proj * (v + hv + skv)) / wt.proj_den;
-    f.uproj_o[pos] = uproj1;
-    f.vproj_o[pos] = vproj1;
-
-    // (3c) triangulation (solve3dMinimalArea.cu:23-184) from the settled ring
-    Xn[1] = xs[0][ty + 1][tx + 2];
-    Yn[1] = xs[1][ty + 1][tx + 2];
-    Zn[1] = xs[2][ty + 1][tx + 2];
-    Xn[2] = xs[0][ty + 2][tx + 1];
-    Yn[2] = xs[1][ty + 2][tx + 1];
-    Zn[2] = xs[2][ty + 2][tx + 1];
-    Xn[3] = Yn[3] = Zn[3] = 0.0f;
-    Xn[4] = Yn[4] = Zn[4] = 0.0f;
-    if (x > 0) {
-        Xn[3] = xs[0][ty + 1][tx];
-        Yn[3] = xs[1][ty + 1][tx];
-        Zn[3] = xs[2][ty + 1][tx];
-    }
-    if (y > 0) {
-        Xn[4] = xs[0][ty][tx + 1];
-        Yn[4] = xs[1][ty][tx + 1];
-        Zn[4] = xs[2][ty][tx + 1];
-    }
-    float Xo, Yo, Zo;
-    solve3d_pixel(c, uproj1, vproj1, x, y, Xn, Yn, Zn, wt.lambdaf, wt.lambdams, Xo, Yo, Zo);
-    f.X1_o[pos] = Xo;
-    f.Y1_o[pos] = Yo;
-    f.Z1_o[pos] = Zo;
-
-    // (3d) multiplier update (solveUcSk.cu:94-95)
-    f.sku_o[pos] = sku + u + hu - uproj1;
-    f.skv_o[pos] = skv + v + hv - vproj1;
-}
-
-__global__ void k_recon_settle(const float* __restrict__ X1, const float* __restrict__ Y1,
-                               const float* __restrict__ Z1, float* __restrict__ X,
-                               float* __restrict__ Y, float* __restrict__ Z, LevelDims d) {
-    int ix = blockIdx.x * blockDim.x + threadIdx.x;
-    int iy = blockIdx.y * blockDim.y + threadIdx.y;
-    if (ix >= d.w || iy >= d.h) return;
-    float a, b, c;
-    settle_px(X1, Y1, Z1, d, ix, iy, a, b, c);
-    int pos = ix + iy * d.s;
-    X[pos] = a;
-    Y[pos] = b;
-    Z[pos] = c;
-}
-
-// ---------------------------------------------------------------------------
-// Persistent form for small levels: all inner iterations of one warp in one
-// cooperative launch (every block resident), the two halves of an iteration
-// separated by a grid-wide barrier instead of a kernel boundary.
-// ---------------------------------------------------------------------------
-__device__ __forceinline__ unsigned int ld_acquire_gpu(const unsigned int* p) {
-    unsigned int v;
-    asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
-    return v;
-}
-
-// Grid barrier on a {count, generation, timeout flag} word triple.  The wait
-// is bounded (kBarrierSpins polls, about a second): a block that gives up, or
-// that finds the flag already set by another block, sets the flag and the
-// barrier returns false so the kernel exits; the host reports the solve as
-// failed.  Cooperative launch keeps every block resident, so a wait ends.
-constexpr unsigned int kBarrierSpins = 1u << 22;
-
-__device__ __forceinline__ bool grid_barrier(unsigned int* bar, unsigned int nblocks,
-                                             unsigned int& gen) {
-    __shared__ int s_fail;
-    __syncthreads();
-    if (threadIdx.x == 0 && threadIdx.y == 0) {
-        int fail = 0;
-        __threadfence();
-        unsigned int arrived = atomicAdd(&bar[0], 1u) + 1u;
-        if (arrived == nblocks) {
-            bar[0] = 0u;
-            __threadfence();
-            atomicExch(&bar[1], gen + 1u);
-        } else {
-            unsigned int spins = 0;
-            while (ld_acquire_gpu(&bar[1]) == gen) {
-                if (++spins > kBarrierSpins || ld_acquire_gpu(&bar[2]) != 0u) {
-                    atomicOr(&bar[2], 1u);
-                    fail = 1;
-                    break;
-                }
-                __nanosleep(64);
-            }
-        }
-        __threadfence();
-        gen += 1u;
-        s_fail = fail;
-    }
-    __syncthreads();
-    return s_fail == 0;
-}
-
-template <int PRIOR>
-__global__ void __launch_bounds__(BX* BY) k_recon_persistent(ReconFields f,
-                                                             const LevelConsts* __restrict__ lcp,
-                                                             Weights wt, LevelDims d, int iters,
-                                                             int uc_from_buffer,
-                                                             unsigned int* bar) {
-    const unsigned int nblocks = gridDim.x;
-    unsigned int gen = 0;
-    if (threadIdx.x == 0 && threadIdx.y == 0) gen = ld_acquire_gpu(&bar[1]);
-    const int npx = d.w * d.h;
-    const int tid = blockIdx.x * (BX * BY) + threadIdx.y * BX + threadIdx.x;
-    const int nthreads = nblocks * (BX * BY);
-    const LevelConsts& c = *lcp;
-    for (int it = 0; it < iters; it++) {
-        const int first = it == 0;
-        for (int i = tid; i < npx; i += nthreads)
-            recon_a_px<PRIOR>(f, c, wt, d, i % d.w, i / d.w, first, first && uc_from_buffer);
-        if (!grid_barrier(bar, nblocks, gen)) return;
-        for (int i = tid; i < npx; i += nthreads) recon_b_px(f, wt, d, i % d.w, i / d.w, first);
-        if (!grid_barrier(bar, nblocks, gen)) return;
-    }
-}
-
-// ---------------------------------------------------------------------------
 // Plain TV-L1 (solveDataL1.cu:4-91 + solveSmoothDualTVGlobal.cu:4-65)
 // ---------------------------------------------------------------------------
 __global__ void k_plain_data(float* __restrict__ duhat0, float* __restrict__ dvhat0,
@@ -829,68 +472,9 @@ int launch_recon_a(const ReconFields& f, const LevelConsts* lc, const Weights& w
     return launch_pdl(k_recon_a<0>, g, b, st, f, lc, wt, d, fi, ub);
 }
 
-int launch_recon_fused(const FusedFields& f, const LevelConsts* lc, const Weights& wt,
-                       LevelDims d, bool first, bool x_from_A, bool uc_from_buffer, int prior,
-                       cudaStream_t st) {
-    dim3 g((d.w + FX - 1) / FX, (d.h + FY - 1) / FY), b(FX, FY);
-    int fi = first ? 1 : 0, xa = x_from_A ? 1 : 0, ub = uc_from_buffer ? 1 : 0;
-    if (prior == 1)
-        k_recon_fused<1><<<g, b, 0, st>>>(f, lc, wt, d, fi, xa, ub);
-    else if (prior == 2)
-        k_recon_fused<2><<<g, b, 0, st>>>(f, lc, wt, d, fi, xa, ub);
-    else
-        k_recon_fused<0><<<g, b, 0, st>>>(f, lc, wt, d, fi, xa, ub);
-    return check_launch();
-}
 
-int launch_recon_settle(const float* X1, const float* Y1, const float* Z1, float* X, float* Y,
-                        float* Z, LevelDims d, cudaStream_t st) {
-    k_recon_settle<<<grid_for(d.w, d.h), dim3(BX, BY), 0, st>>>(X1, Y1, Z1, X, Y, Z, d);
-    return check_launch();
-}
 
-int persistent_grid(int npx) {
-    static int max_blocks = 0;
-    if (max_blocks == 0) {
-        int dev = 0, sms = 0, per_sm = 0;
-        cudaGetDevice(&dev);
-        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_recon_persistent<0>, BX * BY, 0);
-        int per_sm1 = 0, per_sm2 = 0;
-        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm1, k_recon_persistent<1>, BX * BY, 0);
-        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm2, k_recon_persistent<2>, BX * BY, 0);
-        per_sm = per_sm < per_sm1 ? per_sm : per_sm1;
-        per_sm = per_sm < per_sm2 ? per_sm : per_sm2;
-        max_blocks = sms * (per_sm > 0 ? per_sm : 1);
-    }
-    int need = (npx + BX * BY - 1) / (BX * BY);
-    return need < max_blocks ? need : max_blocks;
-}
 
-int launch_recon_persistent(const ReconFields& f, const LevelConsts* lc, const Weights& wt,
-                            LevelDims d, int iters, bool uc_from_buffer, int prior,
-                            unsigned int* bar, cudaStream_t st) {
-    if (iters <= 0) return 0;
-    cudaLaunchConfig_t cfg = {};
-    cfg.gridDim = dim3(persistent_grid(d.w * d.h));
-    cfg.blockDim = dim3(BX, BY);
-    cfg.dynamicSmemBytes = 0;
-    cfg.stream = st;
-    cudaLaunchAttribute attr[1];
-    attr[0].id = cudaLaunchAttributeCooperative;
-    attr[0].val.cooperative = 1;
-    cfg.attrs = attr;
-    cfg.numAttrs = 1;
-    int ucb = uc_from_buffer ? 1 : 0;
-    cudaError_t e;
-    if (prior == 1)
-        e = cudaLaunchKernelEx(&cfg, k_recon_persistent<1>, f, lc, wt, d, iters, ucb, bar);
-    else if (prior == 2)
-        e = cudaLaunchKernelEx(&cfg, k_recon_persistent<2>, f, lc, wt, d, iters, ucb, bar);
-    else
-        e = cudaLaunchKernelEx(&cfg, k_recon_persistent<0>, f, lc, wt, d, iters, ucb, bar);
-    return e == cudaSuccess ? 0 : 1;
-}
 
 int launch_recon_b(const ReconFields& f, const Weights& wt, LevelDims d, bool first,
                    cudaStream_t st, dim3 b) {

@@ -57,53 +57,6 @@ struct ReconFields {
     const float* mask;
 };
 
-// Fields of the fused inner iteration: the state of iteration i-1 is read
-// from one buffer set and iteration i is written to the other (neighbouring
-// tiles read the old state on their halo while this tile writes).
-struct FusedFields {
-    const float* u;
-    const float* v;
-    const float* Ix;
-    const float* Iy;
-    const float* Iz;
-    // iteration i-1
-    const float* duhat;
-    const float* dvhat;
-    const float* pu1;
-    const float* pu2;
-    const float* pv1;
-    const float* pv2;
-    const float* uproj;
-    const float* vproj;
-    const float* sku;
-    const float* skv;
-    const float* X1;  // triangulation of i-1, before its 3x3 median and clean-up
-    const float* Y1;
-    const float* Z1;
-    const float* XA;  // settled 3D state (flat level-0 buffer)
-    const float* YA;
-    const float* ZA;
-    const float* uc;  // read only when uc_from_buffer
-    const float* vc;
-    const float* ufn;
-    const float* vfn;
-    const float* mask;
-    // iteration i
-    float* duhat_o;
-    float* dvhat_o;
-    float* pu1_o;
-    float* pu2_o;
-    float* pv1_o;
-    float* pv2_o;
-    float* uproj_o;
-    float* vproj_o;
-    float* sku_o;
-    float* skv_o;
-    float* X1_o;
-    float* Y1_o;
-    float* Z1_o;
-};
-
 // Per-level camera constants of one pair (K pyramid, P = K0 [R0|t0],
 // Q = K1 [R1|t1], float copies), fix_quirks as rf_params.
 void camera_level_consts(const double* K0, const double* K1, int L, float scale, int fix_quirks,
@@ -132,21 +85,6 @@ int launch_recon_a(const ReconFields& f, const LevelConsts* lc, const Weights& w
                    dim3 block = dim3(32, 8));
 int launch_recon_b(const ReconFields& f, const Weights& wt, LevelDims d, bool first,
                    cudaStream_t st, dim3 block = dim3(32, 8));
-// All `iters` inner iterations of one warp in one cooperative launch (small
-// levels); bar = 3 zeroed words (count, generation, timeout flag).
-int launch_recon_persistent(const ReconFields& f, const LevelConsts* lc, const Weights& wt,
-                            LevelDims d, int iters, bool uc_from_buffer, int prior,
-                            unsigned int* bar, cudaStream_t st);
-// One whole inner iteration in one launch.  x_from_A: the 3D state of i-1 is
-// the settled buffer (first launch of a level) instead of the pending
-// triangulation.
-int launch_recon_fused(const FusedFields& f, const LevelConsts* lc, const Weights& wt,
-                       LevelDims d, bool first, bool x_from_A, bool uc_from_buffer, int prior,
-                       cudaStream_t st);
-// Settle the pending triangulation into the flat 3D state:
-// X = cleanup(X1, median3(X1)) on the level (end of a level).
-int launch_recon_settle(const float* X1, const float* Y1, const float* Z1, float* X, float* Y,
-                        float* Z, LevelDims d, cudaStream_t st);
 int launch_plain_data(float* duhat, float* dvhat, const float* pu1, const float* pu2,
                       const float* pv1, const float* pv2, const float* Ix, const float* Iy,
                       const float* Iz, const Weights& wt, LevelDims d, bool first,

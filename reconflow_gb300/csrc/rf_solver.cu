@@ -88,10 +88,6 @@ struct rf_handle {
 
     LevelConsts* d_consts = nullptr;
     LevelConsts* h_consts = nullptr;  // pinned
-    // grid barrier of the persistent small-level kernel: {count, generation,
-    // timeout flag, pad}; the host reads the flag back with the results
-    unsigned int* d_barrier = nullptr;
-    int persist_max_px = 0;  // opt-in (RF_PERSIST_MAX_PX): slower than graph launches on GB300
 
     double K0[9], K1[9];
     bool cams_set = false, images_set = false, prior_set = false;
@@ -106,8 +102,6 @@ struct rf_handle {
     float *res_u = nullptr, *res_v = nullptr;
     float *st_uproj = nullptr, *st_vproj = nullptr, *st_sku = nullptr, *st_skv = nullptr;
     float *st_uc = nullptr, *st_vc = nullptr;
-    // fused path: the two state sets as left by the last solve (for the
-    // profiling hook); set 0 = read, set 1 = write
     // warm start (rf_solve_warm): staging planes and the schedule's start
     float* warm[5] = {nullptr, nullptr, nullptr, nullptr, nullptr};
     int warm_level = -1, warm_warps = 0, warm_iters = 0;
@@ -117,10 +111,6 @@ struct rf_handle {
     // energy reduction buffers and the pose of the last solve
     double* d_energy = nullptr;  // [0] = result, [1..1024] = block partials
     double last_R1[9], last_t1[3];
-    FusedFields fz{};
-    // one fused launch per iteration (RF_FUSED=1): bit-identical, but on GB300
-    // it issues as many instructions as the two-kernel form at lower occupancy
-    bool use_fused = false;
     bool solved = false;
 
     float* alloc_plane() {
@@ -288,7 +278,6 @@ rf_status enqueue_recon(rf_handle* h, float** res_u, float** res_v, bool warm = 
 
     rf_status rs = enqueue_pyramid(h);
     if (rs != RF_OK) return rs;
-    RF_CUDA(cudaMemsetAsync(h->d_barrier, 0, 4 * sizeof(unsigned int), st));
     // Reconflow.cu:209-220
     for (float* b : {u, v, uproj, vproj, uc, vc, sku, skv, h->X, h->Y, h->Z})
         RF_CUDA(cudaMemsetAsync(b, 0, plane_bytes, st));
@@ -327,14 +316,7 @@ rf_status enqueue_recon(rf_handle* h, float** res_u, float** res_v, bool warm = 
             f.X = h->X; f.Y = h->Y; f.Z = h->Z; f.X1 = h->X1; f.Y1 = h->Y1; f.Z1 = h->Z1;
             f.uc = uc; f.vc = vc;
             f.ufn = h->ufn_l; f.vfn = h->vfn_l; f.mask = h->mask_l;
-            if (n_iters > 0 && d.w * d.h <= h->persist_max_px) {
-                // small level: every inner iteration of this warp in one launch
-                RF_CUDA(cudaMemsetAsync(h->d_barrier, 0, 2 * sizeof(unsigned int), st));
-                RF_LAUNCH(launch_recon_persistent(f, lc, wt, d, n_iters, uc_in_buffer,
-                                                  prior, h->d_barrier, st));
-                uc_in_buffer = false;
-            }
-            for (int iter = 0; iter < n_iters && d.w * d.h > h->persist_max_px; iter++) {
+            for (int iter = 0; iter < n_iters; iter++) {
                 const dim3 tile(h->tile_w[level], h->tile_h[level]);
                 RF_LAUNCH(launch_recon_a(f, lc, wt, d, iter == 0, uc_in_buffer, prior, st, tile));
                 RF_LAUNCH(launch_recon_b(f, wt, d, iter == 0, st, tile));
@@ -385,123 +367,6 @@ rf_status enqueue_recon(rf_handle* h, float** res_u, float** res_v, bool warm = 
     return RF_OK;
 }
 
-// ReconFlow schedule with one fused launch per inner iteration.  The state
-// read by iteration i (set `cur`) and written by it (set `cur ^ 1`) swap
-// after every launch; the triangulation of the last iteration of a level is
-// settled into the flat 3D buffer (median + clean-up) when the level ends.
-rf_status enqueue_recon_fused(rf_handle* h, float** res_u, float** res_v) {
-    cudaStream_t st = h->stream;
-    const rf_params& p = h->p;
-    const Weights wt = make_weights(p);
-    const int prior = prior_kind(p.method);
-    const size_t plane_bytes = h->plane * sizeof(float);
-
-    std::vector<float*> pl(h->spare.begin(), h->spare.end());
-    size_t k = 0;
-    float *u = pl[k++], *v = pl[k++], *uc = pl[k++], *vc = pl[k++];
-    float *tu = pl[k++], *tv = pl[k++];
-    float *uproj[2], *vproj[2], *sku[2], *skv[2], *hu[2], *hv[2], *P[2][4], *X1[2][3];
-    for (int b = 0; b < 2; b++) {
-        uproj[b] = pl[k++]; vproj[b] = pl[k++]; sku[b] = pl[k++]; skv[b] = pl[k++];
-    }
-    hu[0] = h->duhat; hv[0] = h->dvhat; hu[1] = pl[k++]; hv[1] = pl[k++];
-    P[0][0] = h->pu1; P[0][1] = h->pu2; P[0][2] = h->pv1; P[0][3] = h->pv2;
-    for (int c = 0; c < 4; c++) P[1][c] = pl[k++];
-    X1[0][0] = h->X1; X1[0][1] = h->Y1; X1[0][2] = h->Z1;
-    for (int c = 0; c < 3; c++) X1[1][c] = pl[k++];
-    std::vector<float*> free_planes(pl.begin() + k, pl.end());  // >= 8 upscale targets
-
-    rf_status rs = enqueue_pyramid(h);
-    if (rs != RF_OK) return rs;
-    RF_CUDA(cudaMemsetAsync(h->d_barrier, 0, 4 * sizeof(unsigned int), st));
-    int cur = 0;
-    // Reconflow.cu:209-220
-    for (float* b : {u, v, uproj[cur], vproj[cur], uc, vc, sku[cur], skv[cur], h->X, h->Y, h->Z})
-        RF_CUDA(cudaMemsetAsync(b, 0, plane_bytes, st));
-    bool uc_in_buffer = true;
-
-    for (int level = h->L - 1; level >= 0; level--) {
-        LevelDims d{h->W[level], h->H[level], h->S[level]};
-        const LevelConsts* lc = h->d_consts + level;
-        if (prior) {
-            LevelDims d0{h->W[0], h->H[0], h->S[0]};
-            float sc = (float)h->W[level] / (float)h->W[0];
-            RF_LAUNCH(launch_downscale(h->ufn, d0, d, sc, true, h->ufn_l, st));
-            RF_LAUNCH(launch_downscale(h->vfn, d0, d, sc, true, h->vfn_l, st));
-            RF_LAUNCH(launch_downscale(h->mask, d0, d, 1.0f, false, h->mask_l, st));
-        }
-        bool x_settled = true;  // the flat buffer holds this level's starting 3D state
-        for (int warp = 0; warp < p.n_warp_iters; warp++) {
-            RF_LAUNCH(launch_warp(h->I1[level], u, v, d, h->i1w, st));
-            RF_LAUNCH(launch_derivatives(h->I0[level], h->i1w, d, h->Ix, h->Iy, h->Iz, st));
-            for (int iter = 0; iter < p.n_solver_iters; iter++) {
-                const int nx = cur ^ 1;
-                FusedFields f{};
-                f.u = u; f.v = v; f.Ix = h->Ix; f.Iy = h->Iy; f.Iz = h->Iz;
-                f.duhat = hu[cur]; f.dvhat = hv[cur];
-                f.pu1 = P[cur][0]; f.pu2 = P[cur][1]; f.pv1 = P[cur][2]; f.pv2 = P[cur][3];
-                f.uproj = uproj[cur]; f.vproj = vproj[cur]; f.sku = sku[cur]; f.skv = skv[cur];
-                f.X1 = X1[cur][0]; f.Y1 = X1[cur][1]; f.Z1 = X1[cur][2];
-                f.XA = h->X; f.YA = h->Y; f.ZA = h->Z;
-                f.uc = uc; f.vc = vc;
-                f.ufn = h->ufn_l; f.vfn = h->vfn_l; f.mask = h->mask_l;
-                f.duhat_o = hu[nx]; f.dvhat_o = hv[nx];
-                f.pu1_o = P[nx][0]; f.pu2_o = P[nx][1]; f.pv1_o = P[nx][2]; f.pv2_o = P[nx][3];
-                f.uproj_o = uproj[nx]; f.vproj_o = vproj[nx]; f.sku_o = sku[nx]; f.skv_o = skv[nx];
-                f.X1_o = X1[nx][0]; f.Y1_o = X1[nx][1]; f.Z1_o = X1[nx][2];
-                RF_LAUNCH(launch_recon_fused(f, lc, wt, d, iter == 0, x_settled, uc_in_buffer,
-                                             prior, st));
-                cur = nx;
-                h->fz = f;
-                x_settled = false;
-                uc_in_buffer = false;
-            }
-            if (p.n_solver_iters == 0) {
-                RF_CUDA(cudaMemsetAsync(hu[cur], 0, plane_bytes, st));
-                RF_CUDA(cudaMemsetAsync(hv[cur], 0, plane_bytes, st));
-            }
-            // Reconflow.cu:410-420: median of duhat, u += it, median of u
-            RF_LAUNCH(launch_median_add(hu[cur], hv[cur], u, v, tu, tv, d, st));
-            RF_LAUNCH(launch_median5(tu, tv, u, v, d, st));
-        }
-        if (!x_settled)
-            RF_LAUNCH(launch_recon_settle(X1[cur][0], X1[cur][1], X1[cur][2], h->X, h->Y, h->Z, d,
-                                          st));
-        if (level > 0) {
-            LevelDims fd{h->W[level - 1], h->H[level - 1], h->S[level - 1]};
-            if (!uc_in_buffer) RF_LAUNCH(launch_solve_uc(h->X, h->Y, h->Z, lc, d, uc, vc, st));
-            // Reconflow.cu:424-458: u, v, uc, vc, uproj, vproj, sku, skv scaled by fScale
-            float* src[8] = {u, v, uc, vc, uproj[cur], vproj[cur], sku[cur], skv[cur]};
-            float* dst[8];
-            float sc[8];
-            for (int i = 0; i < 8; i++) {
-                dst[i] = free_planes[i];
-                sc[i] = p.scale;
-            }
-            RF_LAUNCH(launch_upscale_fields(8, src, dst, sc, d, fd, st));
-            for (int i = 0; i < 8; i++) free_planes[i] = src[i];
-            u = dst[0]; v = dst[1]; uc = dst[2]; vc = dst[3];
-            uproj[cur] = dst[4]; vproj[cur] = dst[5]; sku[cur] = dst[6]; skv[cur] = dst[7];
-            uc_in_buffer = true;
-            if (p.fix_quirks & RF_FIX_XYZ_UPSCALE) {
-                const float* xs[3] = {h->X, h->Y, h->Z};
-                float* xd[3] = {X1[cur][0], X1[cur][1], X1[cur][2]};
-                float one[3] = {1.0f, 1.0f, 1.0f};
-                RF_LAUNCH(launch_upscale_fields(3, xs, xd, one, d, fd, st));
-                float* xt[3] = {h->X, h->Y, h->Z};
-                for (int c = 0; c < 3; c++)
-                    RF_CUDA(cudaMemcpy2DAsync(xt[c], fd.s * sizeof(float), xd[c],
-                                              fd.s * sizeof(float), fd.w * sizeof(float), fd.h,
-                                              cudaMemcpyDeviceToDevice, st));
-            }
-        }
-    }
-    *res_u = u;
-    *res_v = v;
-    h->st_uproj = uproj[cur]; h->st_vproj = vproj[cur]; h->st_sku = sku[cur]; h->st_skv = skv[cur];
-    h->st_uc = uc; h->st_vc = vc;
-    return RF_OK;
-}
 
 // CudaFlow::_solveOpticalFlow (Cudaflow.cu:403-621), METHOD_TVL1.
 rf_status enqueue_plain(rf_handle* h, float** res_u, float** res_v, bool warm = false) {
@@ -567,7 +432,7 @@ rf_status run_schedule(rf_handle* h, int kind) {
         if (kind == 1) return enqueue_plain(h, ru, rv);
         if (kind == 2) return enqueue_recon(h, ru, rv, true);
         if (kind == 3) return enqueue_plain(h, ru, rv, true);
-        return h->use_fused ? enqueue_recon_fused(h, ru, rv) : enqueue_recon(h, ru, rv);
+        return enqueue_recon(h, ru, rv);
     };
     const int key[3] = {kind >= 2 ? h->warm_level : -1, kind >= 2 ? h->warm_warps : -1,
                         kind >= 2 ? h->warm_iters : -1};
@@ -721,9 +586,7 @@ rf_status rf_create(const rf_params* p, rf_handle** out) {
     e = cudaMemset(h->pool, 0, h->pool_floats * sizeof(float));
     if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&h->own_stream, cudaStreamNonBlocking);
     if (e == cudaSuccess) e = cudaMalloc(&h->d_consts, sizeof(LevelConsts) * h->L);
-    if (e == cudaSuccess) e = cudaMalloc(&h->d_barrier, 4 * sizeof(unsigned int));
     if (e == cudaSuccess) e = cudaMalloc(&h->d_energy, 1025 * sizeof(double));
-    if (e == cudaSuccess) e = cudaMemset(h->d_barrier, 0, 4 * sizeof(unsigned int));
     if (e == cudaSuccess) e = cudaMallocHost(&h->h_consts, sizeof(LevelConsts) * h->L);
     if (e == cudaSuccess && p->input_type != RF_INPUT_F32) {
         h->staging_bytes = (size_t)h->stride * h->height * input_elem_bytes(p->input_type);
@@ -735,9 +598,6 @@ rf_status rf_create(const rf_params* p, rf_handle** out) {
         return fail(RF_ERR_OOM, std::string("rf_create: ") + cudaGetErrorString(e));
     }
     h->stream = h->own_stream;
-    if (const char* env = std::getenv("RF_PERSIST_MAX_PX")) h->persist_max_px = std::atoi(env);
-    if (const char* env = std::getenv("RF_FUSED")) h->use_fused = env[0] != '0';
-    if (h->persist_max_px > 0) h->use_fused = false;
     if (prior) {
         // the mask defaults to ones (Cudaflow.cu:327-331)
         std::vector<float> ones((size_t)h->stride * h->height, 1.0f);
@@ -757,7 +617,6 @@ rf_status rf_destroy(rf_handle* h) {
     if (h->graph) cudaGraphExecDestroy(h->graph);
     if (h->pool) cudaFree(h->pool);
     if (h->d_consts) cudaFree(h->d_consts);
-    if (h->d_barrier) cudaFree(h->d_barrier);
     if (h->d_energy) cudaFree(h->d_energy);
     if (h->h_consts) cudaFreeHost(h->h_consts);
     for (void* s : h->staging)
@@ -947,16 +806,6 @@ rf_status rf_solve_flow(rf_handle* h) {
     return rs;
 }
 
-// A persistent-kernel barrier that gave up waiting leaves a flag; the
-// results of that solve are invalid.
-static rf_status check_barrier(rf_handle* h) {
-    unsigned int flag = 0;
-    RF_CUDA(cudaMemcpyAsync(&flag, h->d_barrier + 2, sizeof flag, cudaMemcpyDeviceToHost,
-                            h->stream));
-    RF_CUDA(cudaStreamSynchronize(h->stream));
-    if (flag) return fail(RF_ERR_CUDA, "solve: a grid barrier timed out; results are invalid");
-    return RF_OK;
-}
 
 static rf_status download(rf_handle* h, const float* src, float* dst, int pitch) {
     RF_CUDA(cudaMemcpy2DAsync(dst, (size_t)pitch * sizeof(float), src, h->stride * sizeof(float),
@@ -969,8 +818,7 @@ rf_status rf_download_flow(rf_handle* h, float* u, float* v, int pitch) {
     if (!h || !u || !v) return fail(RF_ERR_INVALID_ARG, "rf_download_flow: null argument");
     if (!h->solved) return fail(RF_ERR_STATE, "rf_download_flow: no solve has run");
     if (pitch < h->p.width) return fail(RF_ERR_INVALID_ARG, "rf_download_flow: pitch < width");
-    rf_status rs = check_barrier(h);
-    if (rs == RF_OK) rs = download(h, h->res_u, u, pitch);
+    rf_status rs = download(h, h->res_u, u, pitch);
     if (rs == RF_OK) rs = download(h, h->res_v, v, pitch);
     if (rs == RF_OK) RF_CUDA(cudaStreamSynchronize(h->stream));
     return rs;
@@ -982,8 +830,7 @@ rf_status rf_download_points(rf_handle* h, float* X, float* Y, float* Z, int pit
         return fail(RF_ERR_STATE, "rf_download_points: plain TV-L1 has no 3D output");
     if (!h->solved) return fail(RF_ERR_STATE, "rf_download_points: no solve has run");
     if (pitch < h->p.width) return fail(RF_ERR_INVALID_ARG, "rf_download_points: pitch < width");
-    rf_status rs = check_barrier(h);
-    if (rs == RF_OK) rs = download(h, h->X, X, pitch);
+    rf_status rs = download(h, h->X, X, pitch);
     if (rs == RF_OK) rs = download(h, h->Y, Y, pitch);
     if (rs == RF_OK) rs = download(h, h->Z, Z, pitch);
     if (rs == RF_OK) RF_CUDA(cudaStreamSynchronize(h->stream));
@@ -1082,7 +929,7 @@ rf_status rf_set_stream(rf_handle* h, void* stream) {
 rf_status rf_synchronize(rf_handle* h) {
     if (!h) return fail(RF_ERR_INVALID_ARG, "rf_synchronize: null handle");
     RF_CUDA(cudaStreamSynchronize(h->stream));
-    return h->d_barrier ? check_barrier(h) : RF_OK;
+    return RF_OK;
 }
 
 rf_status rf_host_alloc(size_t bytes, void** ptr) {
@@ -1104,8 +951,6 @@ rf_status rf_profile_iterations(rf_handle* h, int level, int n_iters, float* ms)
     cudaStream_t st = h->stream;
     const Weights wt = make_weights(h->p);
     LevelDims d{h->W[level], h->H[level], h->S[level]};
-    std::vector<cudaEvent_t> ev(2 * n_iters + 1);
-    for (auto& e : ev) RF_CUDA(cudaEventCreate(&e));
     const bool recon = h->p.method != RF_METHOD_TVL1;
     ReconFields f{};
     if (recon) {
@@ -1119,43 +964,6 @@ rf_status rf_profile_iterations(rf_handle* h, int level, int n_iters, float* ms)
         f.ufn = h->ufn_l; f.vfn = h->vfn_l; f.mask = h->mask_l;
     }
     const int prior = prior_kind(h->p.method);
-    if (recon && h->use_fused) {
-        // ms[0] = one fused iteration launch; ms[1] = 0 (no second kernel)
-        FusedFields a = h->fz, b = h->fz;
-        // b reads what a writes and writes what a reads
-        b.duhat = a.duhat_o; b.dvhat = a.dvhat_o; b.duhat_o = const_cast<float*>(a.duhat);
-        b.dvhat_o = const_cast<float*>(a.dvhat);
-        b.pu1 = a.pu1_o; b.pu2 = a.pu2_o; b.pv1 = a.pv1_o; b.pv2 = a.pv2_o;
-        b.pu1_o = const_cast<float*>(a.pu1); b.pu2_o = const_cast<float*>(a.pu2);
-        b.pv1_o = const_cast<float*>(a.pv1); b.pv2_o = const_cast<float*>(a.pv2);
-        b.uproj = a.uproj_o; b.vproj = a.vproj_o; b.uproj_o = const_cast<float*>(a.uproj);
-        b.vproj_o = const_cast<float*>(a.vproj);
-        b.sku = a.sku_o; b.skv = a.skv_o; b.sku_o = const_cast<float*>(a.sku);
-        b.skv_o = const_cast<float*>(a.skv);
-        b.X1 = a.X1_o; b.Y1 = a.Y1_o; b.Z1 = a.Z1_o; b.X1_o = const_cast<float*>(a.X1);
-        b.Y1_o = const_cast<float*>(a.Y1); b.Z1_o = const_cast<float*>(a.Z1);
-        RF_CUDA(cudaEventRecord(ev[0], st));
-        for (int i = 0; i < n_iters; i++) {
-            if (launch_recon_fused(i % 2 ? b : a, h->d_consts + level, wt, d, false, false, false,
-                                   prior, st))
-                return cuda_fail(cudaGetLastError(), "rf_profile_iterations: launch");
-            RF_CUDA(cudaEventRecord(ev[i + 1], st));
-            h->launches += 1;
-        }
-        RF_CUDA(cudaEventSynchronize(ev[n_iters]));
-        double sa = 0;
-        for (int i = 0; i < n_iters; i++) {
-            float t = 0;
-            cudaEventElapsedTime(&t, ev[i], ev[i + 1]);
-            sa += t;
-        }
-        for (auto& e : ev) cudaEventDestroy(e);
-        ms[0] = (float)(sa / n_iters);
-        ms[1] = 0.0f;
-        h->solved = false;
-        return RF_OK;
-    }
-    for (auto& e : ev) cudaEventDestroy(e);
     // Each kernel alone: n_iters launches back to back captured in one CUDA
     // graph (the form the solve uses), the graph launch timed with events;
     // ms = graph time / n_iters.  The first replay warms the graph up.

@@ -96,26 +96,9 @@ CASES = [
 ]
 
 
-@pytest.fixture(params=["fused", "two-kernel", "persistent"])
-def level_mode(request, monkeypatch):
-    """The inner iterations run as one fused launch per iteration (default),
-    as two launches per iteration, or as one persistent cooperative launch
-    per warp; all three must give the same bits."""
-    if request.param == "fused":
-        monkeypatch.setenv("RF_FUSED", "1")
-        monkeypatch.setenv("RF_PERSIST_MAX_PX", "0")
-    elif request.param == "two-kernel":
-        monkeypatch.setenv("RF_FUSED", "0")
-        monkeypatch.setenv("RF_PERSIST_MAX_PX", "0")
-    else:
-        monkeypatch.setenv("RF_FUSED", "0")
-        monkeypatch.setenv("RF_PERSIST_MAX_PX", "1000000000")
-    return request.param
-
-
 @pytest.mark.parametrize("w,h,L,warps,iters", CASES)
 @pytest.mark.parametrize("fix", [0, 1, 3])
-def test_recon_bitexact(oracle, rf, w, h, L, warps, iters, fix, level_mode):
+def test_recon_bitexact(oracle, rf, w, h, L, warps, iters, fix):
     rng = np.random.default_rng(w + h + fix)
     s = align_up(w)
     I0, I1 = textured_pair(rng, h, w)
@@ -129,7 +112,7 @@ def test_recon_bitexact(oracle, rf, w, h, L, warps, iters, fix, level_mode):
 
 
 @pytest.mark.parametrize("method", [17, 20])
-def test_prior_methods_bitexact(oracle, rf, method, level_mode):
+def test_prior_methods_bitexact(oracle, rf, method):
     w, h, L = 70, 50, 3
     rng = np.random.default_rng(method)
     s = align_up(w)
@@ -160,7 +143,7 @@ def test_plain_tvl1_bitexact(oracle, rf, w, h, L, warps, iters):
 
 
 @pytest.mark.parametrize("input_type", [1, 2, 3])
-def test_input_types_bitexact(oracle, rf, input_type, level_mode):
+def test_input_types_bitexact(oracle, rf, input_type):
     w, h, L = 50, 40, 2
     rng = np.random.default_rng(input_type)
     s = align_up(w)
@@ -254,7 +237,7 @@ def test_device_results_and_inverse_depth(rf):
     assert all(p != 0 for p in ptrs)
 
 
-def test_degenerate_baseline_nan_parity(oracle, rf, level_mode):
+def test_degenerate_baseline_nan_parity(oracle, rf):
     """Pure sideways baseline (t_z = 0, R = I): the reference's projection
     divides 0/0 wherever a point is reset to the origin, so NaNs appear; the
     GPU must still match the oracle everywhere (NaN for NaN)."""
