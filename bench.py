@@ -66,6 +66,16 @@ WORKLOADS = {
                          warm_iters=[15, 30, 50], fallback_margin=0.02,
                          checkpoint="reconflow_gb300/weights/warmstart_f125.bin",
                          tiles="reconflow_gb300/tuning/gb300_720p_x64.json"),
+    # batched + learned on mixed sizes (config 5 at a reduced count: 16 pairs
+    # of 3840x2160 and 16 of 1920x1080, independent scenes); 4K starts the
+    # refinement at pyramid level 3 (its network grid is 1/32)
+    "mixed-4k-1080p-learned": dict(
+        levels=6, plain_warps=5, plain_iters=100, fallback_margin=0.02,
+        checkpoint="reconflow_gb300/weights/warmstart_f125.bin",
+        groups=[dict(width=3840, height=2160, pairs=16, seed=6000, warm_level=3,
+                     warm_warps=[1, 1, 1, 1], warm_iters=[15, 30, 50, 50]),
+                dict(width=1920, height=1080, pairs=16, seed=6500, warm_level=2,
+                     warm_warps=[1, 1, 2], warm_iters=[20, 40, 60])]),
     # batched: 64 pairs of 1280x720 (per-pair throughput of the batched path)
     "batch64-720p": dict(pairs=64, sizes=[(1280, 720)], levels=6, warps=5, iters=100, seed=0),
 }
@@ -644,6 +654,210 @@ def run_learned(args, wl, world, rank, local):
     net.close()
 
 
+def run_learned_mixed(args, wl, world, rank, local):
+    """Batched + learned warm start on a mix of frame sizes (one batch, one
+    network pass and one refinement per size group; BASELINE config 5 at a
+    reduced count, with independent seeded scenes instead of sequences).
+    One step = every group through the learned path with its fallback; the
+    plain solver's batched and single-pair times are measured per group."""
+    import torch
+
+    import reconflow_gb300 as R
+    from reconflow_gb300.scene import make_scene
+    from reconflow_gb300.warmstart import LearnedBatchSolver, WarmStartNet, net_factor
+
+    torch.cuda.set_device(local)
+    lib = R.load()
+    stream = torch.cuda.Stream()
+    flush = torch.empty(L2_FLUSH_BYTES // 4, dtype=torch.float32, device="cuda")
+    groups = []
+    t0 = time.perf_counter()
+    for gi, g in enumerate(wl["groups"]):
+        W, H, n = g["width"], g["height"], g["pairs"]
+        scenes = [make_scene(W, H, seed=g["seed"] + 1000 * rank + i, device="cuda")
+                  for i in range(n)]
+        groups.append(dict(g=g, W=W, H=H, n=n, scenes=scenes, Ks=[s_["K"] for s_ in scenes],
+                           Rs=[s_["R"] for s_ in scenes], ts=[s_["t"] for s_ in scenes]))
+    gen_s = time.perf_counter() - t0
+
+    def new_batch(G):
+        b = R.ReconFlowBatch([(G["W"], G["H"])] * G["n"], wl["levels"], method=SOLVER["method"],
+                             lambda_=SOLVER["lam"], lambdaf=SOLVER["lambdaf"],
+                             lambdams=SOLVER["lambdams"], alphaTv=1.0 / SOLVER["theta"],
+                             alphaProj=SOLVER["alpha_proj"], tau=SOLVER["tau"],
+                             nWarpIters=wl["plain_warps"], nSolverIters=wl["plain_iters"],
+                             fix_quirks=SOLVER["fix_quirks"])
+        b.setStream(stream.cuda_stream)
+        for i, sc in enumerate(G["scenes"]):
+            b.setCameraMatrices(i, sc["K"], sc["K"])
+            b.copyImagesToDevice(i, sc["I0"], sc["I1"])
+        return b
+
+    def epe_stats(G, b):
+        means, meds = [], []
+        for i, sc in enumerate(G["scenes"]):
+            u, v = b.copyOpticalFlowToHost(i)
+            W = G["W"]
+            e = np.sqrt((u[:, :W] - sc["flow"][..., 0]) ** 2 + (v[:, :W] - sc["flow"][..., 1]) ** 2)
+            e = e[sc["valid"]]
+            e = np.where(np.isfinite(e), e, np.float32(1e4))
+            means.append(float(e.mean()))
+            meds.append(float(np.median(e)))
+        return {"epe_mean_px": float(np.mean(means)), "epe_median_px": float(np.mean(meds))}
+
+    def timed(fn, steps):
+        evs = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
+               for _ in range(steps)]
+        for a, e in evs:
+            flush.zero_()
+            a.record(stream)
+            fn()
+            e.record(stream)
+        torch.cuda.synchronize()
+        return [a.elapsed_time(e) for a, e in evs]
+
+    with torch.cuda.stream(stream):
+        for G in groups:
+            plain = new_batch(G)
+            plain.solveR(G["Rs"], G["ts"])
+            torch.cuda.synchronize()
+            G["plain_acc"] = epe_stats(G, plain)
+            G["e_plain"] = plain.energies()
+            G["plain_batch_ms"] = statistics.median(timed(lambda: plain.solveR(G["Rs"], G["ts"]), 1))
+            plain.close()
+            f = R.ReconFlow()
+            f.initializeR(G["W"], G["H"], 1, wl["levels"], 2.0, SOLVER["method"], SOLVER["lam"],
+                          0.0, SOLVER["lambdaf"], SOLVER["lambdams"], 1.0 / SOLVER["theta"],
+                          SOLVER["alpha_proj"], 0.5, SOLVER["tau"], wl["plain_warps"],
+                          wl["plain_iters"], cvType=5, fix_quirks=SOLVER["fix_quirks"])
+            f.setStream(stream.cuda_stream)
+            f.setCameraMatrices(G["Ks"][0], G["Ks"][0])
+            f.copyImagesToDevice(G["scenes"][0]["I0"], G["scenes"][0]["I1"])
+            f.solveR(G["Rs"][0], G["ts"][0], 5.0)
+            G["single_ms"] = statistics.median(timed(lambda: f.solveR(G["Rs"][0], G["ts"][0], 5.0), 2))
+            G["f"] = f
+            fct = net_factor(G["Ks"][0])
+            net = WarmStartNet(G["n"], G["H"] // fct + 1, G["W"] // fct + 1, seed=0)
+            net.load(os.path.join(ROOT, wl["checkpoint"]))
+            b = new_batch(G)
+            G["net"], G["b"] = net, b
+            G["ls"] = LearnedBatchSolver(net, b, (G["W"], G["H"]), G["Ks"][0],
+                                         warm_level=G["g"]["warm_level"],
+                                         warps=G["g"]["warm_warps"], iters=G["g"]["warm_iters"])
+            G["ls"].set_stream(stream.cuda_stream)
+    margin = wl["fallback_margin"]
+    fallbacks = []
+
+    def step():
+        nbad = 0
+        for G in groups:
+            G["ls"].solve(G["Ks"], G["Rs"], G["ts"])
+            e = G["b"].energies()
+            bad = [i for i in range(G["n"]) if not (e[i] <= (1.0 + margin) * G["e_plain"][i])]
+            for i in bad:
+                f = G["f"]
+                f.setCameraMatrices(G["Ks"][i], G["Ks"][i])
+                f.copyImagesToDeviceFromDevice(*G["b"].imagePlanes(i, 0), G["b"].strides[i])
+                f.solveR(G["Rs"][i], G["ts"][i], 5.0)
+            nbad += len(bad)
+        fallbacks.append(nbad)
+
+    with torch.cuda.stream(stream):
+        for _ in range(args.warmup):
+            step()
+        torch.cuda.synchronize()
+        for G in groups:
+            G["learned_acc"] = epe_stats(G, G["b"])
+        barrier(world)
+        fallbacks.clear()
+        with ClockSampler(local) as clk:
+            torch.cuda.synchronize()
+            step_ms = timed(step, args.steps)
+    timed_fallbacks = list(fallbacks)
+    npairs = sum(G["n"] for G in groups)
+    total_s = max_over_ranks(sum(step_ms) / 1000.0, world)
+    value = world * npairs * args.steps / total_s
+    single_step_ms = sum(G["single_ms"] * G["n"] for G in groups)
+    e2e = None
+    if not args.no_e2e:
+        hosts = []
+        for G in groups:
+            s0, H = G["b"].strides[0], G["H"]
+            for i in range(G["n"]):
+                ptrs = []
+                for _ in range(8):
+                    p_ = ctypes.c_void_p()
+                    R._native.check(lib.rf_host_alloc(H * s0 * 4, ctypes.byref(p_)))
+                    ptrs.append(p_)
+                for k, img in ((0, G["scenes"][i]["I0"]), (1, G["scenes"][i]["I1"])):
+                    a_ = np.ctypeslib.as_array(ctypes.cast(ptrs[k], ctypes.POINTER(ctypes.c_float)),
+                                               shape=(H, s0))
+                    a_[:, :G["W"]] = img
+                hosts.append((G, i, ptrs))
+
+        def e2e_step():
+            for G, i, ptrs in hosts:
+                R._native.check(lib.rf_batch_upload_images(G["b"]._h, i, ptrs[0], ptrs[1],
+                                                           G["b"].strides[0]))
+            step()
+            for G, i, ptrs in hosts:
+                hb, s0 = G["b"]._h, G["b"].strides[0]
+                R._native.check(lib.rf_batch_download_flow(hb, i, ptrs[2], ptrs[3], s0))
+                R._native.check(lib.rf_batch_download_inv_depth(hb, i, ptrs[4], s0))
+                R._native.check(lib.rf_batch_download_points(hb, i, ptrs[5], ptrs[6], ptrs[7], s0))
+
+        with torch.cuda.stream(stream):
+            e2e_step()
+            times = []
+            for _ in range(args.steps):
+                flush.zero_()
+                torch.cuda.synchronize()
+                t1 = time.perf_counter()
+                e2e_step()
+                torch.cuda.synchronize()
+                times.append(time.perf_counter() - t1)
+        px = sum(G["n"] * G["W"] * G["H"] for G in groups)
+        e2e = {"value": world * npairs * args.steps / max_over_ranks(sum(times), world),
+               "unit": "pairs/s", "h2d_bytes_per_step": 2 * px * 4, "d2h_bytes_per_step": 6 * px * 4}
+        for _, _, ptrs in hosts:
+            for p_ in ptrs:
+                lib.rf_host_free(p_)
+    if rank == 0:
+        tol = 0.05
+        per = {}
+        for G in groups:
+            key = f"{G['W']}x{G['H']}"
+            per[key] = {"pairs": G["n"], "warm_level": G["g"]["warm_level"],
+                        "warm_warps_per_level": G["g"]["warm_warps"],
+                        "warm_iters_per_level": G["g"]["warm_iters"],
+                        "plain_accuracy": G["plain_acc"], "learned_accuracy": G["learned_acc"],
+                        "plain_single_pair_ms": G["single_ms"],
+                        "plain_batched_ms_per_pair": G["plain_batch_ms"] / G["n"],
+                        "equal_epe_median": G["learned_acc"]["epe_median_px"]
+                        <= G["plain_acc"]["epe_median_px"] + tol,
+                        "equal_epe_mean": G["learned_acc"]["epe_mean_px"]
+                        <= G["plain_acc"]["epe_mean_px"] + tol}
+        print(json.dumps({
+            "metric": "frame pairs/s, batched + learned warm start on mixed 4K / 1080p pairs",
+            "value": value, "unit": "pairs/s", "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": 1000.0 * total_s / args.steps,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+            "data": "synthetic (seeded scene generator, independent scenes, not sequences)",
+            "config": {"workload": args.workload, "groups": per, "pyramid_levels": wl["levels"],
+                       "plain_schedule": [wl["plain_warps"], wl["plain_iters"]],
+                       "fallback": f"plain re-solve when energy > (1 + {margin}) x plain energy",
+                       "checkpoint": wl["checkpoint"], "l2": "flushed between steps",
+                       "parallelism": "replicas"},
+            "speedup_vs_plain_single_pair": single_step_ms / (1000.0 * total_s / args.steps),
+            "fallbacks_per_step": timed_fallbacks, "e2e": e2e, "clocks": clk.summary(),
+            "scene_gen_s": gen_s,
+        }), flush=True)
+    for G in groups:
+        G["b"].close()
+        G["net"].close()
+        G["f"].close()
+
+
 def roofline_of(ms, px):
     """Roofline entry of the dominant level-0 kernel from per-launch times."""
     names = ["recon_a", "recon_b"]
@@ -693,6 +907,8 @@ def main():
     wl = WORKLOADS[args.workload]
     world, rank, local = dist_setup(args)
     if args.impl == "reference":
+        if "groups" in wl:
+            raise SystemExit("bench.py: the reference arm runs single-size workloads")
         if "checkpoint" in wl:
             # the reference's counterpart of a learned batch: its plain solve, one pair
             wl = dict(width=wl["width"], height=wl["height"], levels=wl["levels"],
@@ -701,6 +917,9 @@ def main():
         elif "pairs" in wl:
             raise SystemExit("bench.py: the reference arm runs single-pair workloads")
         run_reference(args, wl, world, rank)
+        return
+    if "groups" in wl:
+        run_learned_mixed(args, wl, world, rank, local)
         return
     if "checkpoint" in wl:
         run_learned(args, wl, world, rank, local)

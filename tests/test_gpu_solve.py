@@ -218,6 +218,41 @@ def test_scene_640x480_matches_fp32_oracle_and_ground_truth(oracle, rf):
     assert e32 < 0.5 and abs(e32 - e64) < 0.05, (e32, e64)
 
 
+@pytest.mark.slow
+def test_scene_720p_headline_workload_matches_fp32_oracle(oracle, rf):
+    """The benchmark's 1280x720 workload (6 levels, 5 warps, 100 iterations,
+    the bench's weights and tuned tiles): bit-exact with the FP32 oracle at
+    full size, and inverse depth = 1 / Z exactly."""
+    import json
+    import os
+
+    from reconflow_gb300 import autotune
+    from reconflow_gb300.scene import make_scene
+
+    sc = make_scene(1280, 720, seed=0)
+    w, h, L = 1280, 720, 6
+    s = align_up(w)
+    I0, I1 = pad_rows(sc["I0"], s), pad_rows(sc["I1"], s)
+    f = rf.ReconFlow()
+    f.initializeR(w, h, 1, L, 2.0, 14, 50.0, 0.0, 0.1, 100.0, 1 / 0.33, 60.0, 0.5, 0.25, 5, 100,
+                  cvType=5, fix_quirks=1)
+    root = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+    with open(os.path.join(root, "reconflow_gb300", "tuning", "gb300_720p_single.json")) as fh:
+        autotune.apply_single(f, json.load(fh)["levels"], L)
+    f.setCameraMatrices(sc["K"], sc["K"])
+    f.copyImagesToDevice(I0, I1)
+    f.solveR(sc["R"], sc["t"], 5.0)
+    u, v = f.copyOpticalFlowToHost()
+    X, Y, Z = f.copy3dToHost()
+    inv = f.copyInverseDepthToHost()
+    f.close()
+    want = run_oracle(oracle, w, h, L, 14, I0, I1, sc["K"], sc["R"], sc["t"], warps=5, iters=100,
+                      fix=1)
+    compare({"u": u, "v": v, "X": X, "Y": Y, "Z": Z}, want, w, h)
+    with np.errstate(divide="ignore"):
+        assert_bitexact(inv, np.float32(1) / Z, "inverse depth", region=(h, w))
+
+
 def test_device_results_and_inverse_depth(rf):
     w, h = 64, 48
     rng = np.random.default_rng(4)
