@@ -560,17 +560,13 @@ def run_learned(args, wl, world, rank, local):
                                            shape=(H, s0))
                 a_[:, :W] = img
             hosts.append(ptrs)
-        hb = b._h
+        col = [[hosts[i][k].value for i in range(n)] for k in range(8)]
 
         def e2e_step():
-            for i in range(n):
-                R._native.check(lib.rf_batch_upload_images(hb, i, hosts[i][0], hosts[i][1], s0))
+            b.uploadAll(col[0], col[1], s0)  # rf_batch_upload_all
             step()
-            for i in range(n):
-                R._native.check(lib.rf_batch_download_flow(hb, i, hosts[i][2], hosts[i][3], s0))
-                R._native.check(lib.rf_batch_download_inv_depth(hb, i, hosts[i][4], s0))
-                R._native.check(lib.rf_batch_download_points(hb, i, hosts[i][5], hosts[i][6],
-                                                             hosts[i][7], s0))
+            b.downloadAll(s0, u=col[2], v=col[3], inv_depth=col[4], X=col[5], Y=col[6],
+                          Z=col[7])  # rf_batch_download_all
 
         with torch.cuda.stream(stream):
             e2e_step()
@@ -795,16 +791,19 @@ def run_learned_mixed(args, wl, world, rank, local):
                     a_[:, :G["W"]] = img
                 hosts.append((G, i, ptrs))
 
+        cols = {}
+        for G, i, ptrs in hosts:
+            cols.setdefault(id(G), (G, [[] for _ in range(8)]))
+            for k in range(8):
+                cols[id(G)][1][k].append(ptrs[k].value)
+
         def e2e_step():
-            for G, i, ptrs in hosts:
-                R._native.check(lib.rf_batch_upload_images(G["b"]._h, i, ptrs[0], ptrs[1],
-                                                           G["b"].strides[0]))
+            for G, c in cols.values():
+                G["b"].uploadAll(c[0], c[1], G["b"].strides[0])
             step()
-            for G, i, ptrs in hosts:
-                hb, s0 = G["b"]._h, G["b"].strides[0]
-                R._native.check(lib.rf_batch_download_flow(hb, i, ptrs[2], ptrs[3], s0))
-                R._native.check(lib.rf_batch_download_inv_depth(hb, i, ptrs[4], s0))
-                R._native.check(lib.rf_batch_download_points(hb, i, ptrs[5], ptrs[6], ptrs[7], s0))
+            for G, c in cols.values():
+                G["b"].downloadAll(G["b"].strides[0], u=c[2], v=c[3], inv_depth=c[4], X=c[5],
+                                   Y=c[6], Z=c[7])
 
         with torch.cuda.stream(stream):
             e2e_step()

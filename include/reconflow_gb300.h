@@ -297,6 +297,16 @@ RF_API rf_status rf_batch_download_flow(rf_batch* b, int pair, float* u, float* 
 RF_API rf_status rf_batch_download_points(rf_batch* b, int pair, float* X, float* Y, float* Z,
                                           int pitch);
 RF_API rf_status rf_batch_download_inv_depth(rf_batch* b, int pair, float* inv_depth, int pitch);
+/* Every pair's frames at once (host arrays of n_pairs host pointers, one
+ * pitch); asynchronous on the batch's stream like rf_batch_upload_images. */
+RF_API rf_status rf_batch_upload_all(rf_batch* b, const float* const* i0, const float* const* i1,
+                                     int pitch);
+/* Every pair's results at once: host arrays of n_pairs host pointers per
+ * output (an array, or an entry, may be NULL to skip it), one pitch; the
+ * copies are queued together and the call synchronizes once.  Blocking. */
+RF_API rf_status rf_batch_download_all(rf_batch* b, float* const* u, float* const* v,
+                                       float* const* inv_depth, float* const* X,
+                                       float* const* Y, float* const* Z, int pitch);
 RF_API rf_status rf_batch_device_results(rf_batch* b, int pair, const float** u, const float** v,
                                          const float** X, const float** Y, const float** Z);
 RF_API rf_status rf_batch_set_stream(rf_batch* b, void* stream);

@@ -94,6 +94,8 @@ _SIGS = [
     ("rf_batch_download_flow", _I, [_VP, _I, _VP, _VP, _I]),
     ("rf_batch_download_points", _I, [_VP, _I, _VP, _VP, _VP, _I]),
     ("rf_batch_download_inv_depth", _I, [_VP, _I, _VP, _I]),
+    ("rf_batch_upload_all", _I, [_VP, _VP, _VP, _I]),
+    ("rf_batch_download_all", _I, [_VP, _VP, _VP, _VP, _VP, _VP, _VP, _I]),
     ("rf_batch_device_results", _I, [_VP, _I, _VP, _VP, _VP, _VP, _VP]),
     ("rf_batch_set_stream", _I, [_VP, _VP]),
     ("rf_batch_synchronize", _I, [_VP]),

@@ -883,6 +883,49 @@ rf_status rf_batch_download_inv_depth(rf_batch* b, int pair, float* inv, int pit
     return rs;
 }
 
+rf_status rf_batch_upload_all(rf_batch* b, const float* const* i0, const float* const* i1,
+                              int pitch) {
+    if (!b || !i0 || !i1) return bfail(RF_ERR_INVALID_ARG, "rf_batch_upload_all: null argument");
+    for (int i = 0; i < b->n; i++) {
+        if (!i0[i] || !i1[i]) return bfail(RF_ERR_INVALID_ARG, "rf_batch_upload_all: null image");
+        rf_status rs = batch_upload(b, i, i0[i], i1[i], pitch, cudaMemcpyHostToDevice);
+        if (rs != RF_OK) return rs;
+    }
+    return RF_OK;
+}
+
+rf_status rf_batch_download_all(rf_batch* b, float* const* u, float* const* v,
+                                float* const* inv_depth, float* const* X, float* const* Y,
+                                float* const* Z, int pitch) {
+    if (!b) return bfail(RF_ERR_INVALID_ARG, "rf_batch_download_all: null batch");
+    if (!b->solved) return bfail(RF_ERR_STATE, "rf_batch_download_all: no solve has run");
+    const bool recon = b->p.method != RF_METHOD_TVL1;
+    if (!recon && (inv_depth || X || Y || Z))
+        return bfail(RF_ERR_STATE, "rf_batch_download_all: plain TV-L1 has no 3D output");
+    for (int i = 0; i < b->n; i++)
+        if (pitch < b->dims[i][0].w) return bfail(RF_ERR_INVALID_ARG, "pitch < width");
+    const int B0 = b->base_idx();
+    if (inv_depth) {
+        BL(launch_op(b, 0, OpInvDepth{B0 + P_Z, B0 + P_SCRATCH}));
+        b->launches++;
+    }
+    struct Out {
+        float* const* dst;
+        int plane;
+    } outs[6] = {{u, b->res_u}, {v, b->res_v}, {inv_depth, B0 + P_SCRATCH},
+                 {X, B0 + P_X}, {Y, B0 + P_Y}, {Z, B0 + P_Z}};
+    for (const Out& o : outs) {
+        if (!o.dst) continue;
+        for (int i = 0; i < b->n; i++) {
+            if (!o.dst[i]) continue;
+            rf_status rs = batch_down(b, i, o.plane, o.dst[i], pitch);
+            if (rs != RF_OK) return rs;
+        }
+    }
+    BC(cudaStreamSynchronize(b->stream));
+    return RF_OK;
+}
+
 rf_status rf_batch_device_results(rf_batch* b, int pair, const float** u, const float** v,
                                   const float** X, const float** Y, const float** Z) {
     if (!b || pair < 0 || pair >= b->n)

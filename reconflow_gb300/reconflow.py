@@ -407,6 +407,22 @@ class ReconFlowBatch:
                                                      None if t0 is None else _ptr(t0), _ptr(R1),
                                                      _ptr(t1), int(level), wa, ia))
 
+    def uploadAll(self, ptrs0, ptrs1, pitch):
+        """rf_batch_upload_all: every pair's frames from host pointers."""
+        a = (ctypes.c_void_p * self.n)(*[ctypes.c_void_p(int(p)) for p in ptrs0])
+        b = (ctypes.c_void_p * self.n)(*[ctypes.c_void_p(int(p)) for p in ptrs1])
+        N.check(self._lib.rf_batch_upload_all(self._h, a, b, int(pitch)))
+
+    def downloadAll(self, pitch, u=None, v=None, inv_depth=None, X=None, Y=None, Z=None):
+        """rf_batch_download_all: each argument a list of n host pointers (or
+        None to skip that output); blocking."""
+        def arr(lst):
+            if lst is None:
+                return None
+            return (ctypes.c_void_p * self.n)(*[ctypes.c_void_p(int(p)) for p in lst])
+        N.check(self._lib.rf_batch_download_all(self._h, arr(u), arr(v), arr(inv_depth), arr(X),
+                                                arr(Y), arr(Z), int(pitch)))
+
     def energies(self):
         """Energy of every pair's last solution (rf_batch_energies)."""
         out = np.zeros(self.n, np.float64)

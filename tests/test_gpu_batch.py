@@ -144,3 +144,49 @@ def test_tile_shapes_do_not_change_results(rf):
     tw, th = autotune.tiles_for(b, table)
     assert [tuple(x) for x in zip(tw, th)] == [tuple(e["tile"]) for e in table]
     b.close()
+
+
+def test_bulk_transfers_match_per_pair_calls(rf):
+    """rf_batch_upload_all / rf_batch_download_all move the same bytes as the
+    per-pair calls (one pitch for every pair)."""
+    import ctypes
+
+    from reconflow_gb300 import _native
+
+    lib = _native.load()
+    sizes = [(64, 48), (50, 40), (64, 30)]
+    pitch = 64
+    kw = dict(lambda_=50.0, lambdaf=0.1, lambdams=100.0, alphaTv=1 / 0.33, alphaProj=60.0,
+              tau=0.25, nWarpIters=1, nSolverIters=3, fix_quirks=1)
+    b = rf.ReconFlowBatch(sizes, 2, method=14, **kw)
+    imgs = []
+    for i, (w, h) in enumerate(sizes):
+        rng = np.random.default_rng(50 + i)
+        I0, I1 = textured_pair(rng, h, w)
+        imgs.append((pad_rows(I0, pitch), pad_rows(I1, pitch)))
+        b.setCameraMatrices(i, _K(w, h), _K(w, h))
+    b.uploadAll([a.ctypes.data for a, _ in imgs], [c.ctypes.data for _, c in imgs], pitch)
+    R_, t_ = zip(*[_pose(i) for i in range(len(sizes))])
+    b.solveR(list(R_), list(t_))
+    outs = [[np.full((h, pitch), 7.0, np.float32) for _ in range(6)] for (w, h) in sizes]
+    cols = [[outs[i][k].ctypes.data for i in range(len(sizes))] for k in range(6)]
+    b.downloadAll(pitch, u=cols[0], v=cols[1], inv_depth=cols[2], X=cols[3], Y=cols[4],
+                  Z=cols[5])
+    for i, (w, h) in enumerate(sizes):
+        u, v = b.copyOpticalFlowToHost(i)
+        X, Y, Z = b.copy3dToHost(i)
+        inv = b.copyInverseDepthToHost(i)
+        for got, want, nm in zip(outs[i], (u, v, inv, X, Y, Z), ("u", "v", "inv", "X", "Y", "Z")):
+            assert_bitexact(got[:, :w], want[:, :w], f"pair {i} {nm}")
+    # a pair uploaded one at a time gives the same solve
+    b2 = rf.ReconFlowBatch(sizes, 2, method=14, **kw)
+    for i, (w, h) in enumerate(sizes):
+        b2.setCameraMatrices(i, _K(w, h), _K(w, h))
+        s = b2.strides[i]
+        b2.copyImagesToDevice(i, imgs[i][0][:, :s] if s <= pitch else pad_rows(imgs[i][0], s),
+                              imgs[i][1][:, :s] if s <= pitch else pad_rows(imgs[i][1], s))
+    b2.solveR(list(R_), list(t_))
+    for i, (w, h) in enumerate(sizes):
+        assert_bitexact(b2.copyOpticalFlowToHost(i)[0][:, :w], outs[i][0][:, :w], f"pair {i}")
+    b.close()
+    b2.close()
