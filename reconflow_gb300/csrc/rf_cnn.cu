@@ -50,50 +50,55 @@ struct Shape {
 };
 
 // ---- tcgen05 GEMM operands: 8 consecutive K elements of one row ----------
-__device__ __forceinline__ uint4 ld16(const bf16* p) { return *reinterpret_cast<const uint4*>(p); }
-
 __device__ __forceinline__ uint4 pack8(const bf16 (&v)[8]) {
     return make_uint4(pack2(v[0], v[1]), pack2(v[2], v[3]), pack2(v[4], v[5]), pack2(v[6], v[7]));
 }
 
 // forward A: im2col row of output pixel m, k = (ky*3 + kx)*Cin + ci (Cin % 8 == 0)
 struct TcConvIn {
+    static constexpr bool kAsync = true;
     const bf16* x;
     int B, H, W, C, Ho, Wo, stride;
-    __device__ uint4 operator()(int m, int k, int) const {
+    __device__ const void* base() const { return x; }
+    __device__ const void* src(int m, int k) const {
         int ci = k % C, t = k / C, kx = t % 3, ky = t / 3;
         int xo = m % Wo, r = m / Wo, yo = r % Ho, b = r / Ho;
         int y = yo * stride + ky - 1, xx = xo * stride + kx - 1;
-        if (y < 0 || y >= H || xx < 0 || xx >= W) return make_uint4(0, 0, 0, 0);
-        return ld16(x + (((size_t)b * H + y) * W + xx) * C + ci);
+        if (y < 0 || y >= H || xx < 0 || xx >= W) return nullptr;
+        return x + (((size_t)b * H + y) * W + xx) * C + ci;
     }
 };
 
 // K-major matrix rows: w[n][k], K % 8 == 0
 struct TcRows {
+    static constexpr bool kAsync = true;
     const bf16* w;
     int K;
-    __device__ uint4 operator()(int n, int k, int) const { return ld16(w + (size_t)n * K + k); }
+    __device__ const void* base() const { return w; }
+    __device__ const void* src(int n, int k) const { return w + (size_t)n * K + k; }
 };
 
 // input-gradient A: input pixel m, k = (ky*3 + kx)*Cout + co -> dy at the
 // output pixel that tap (ky, kx) of m feeds (Cout % 8 == 0)
 struct TcDataGradA {
+    static constexpr bool kAsync = true;
     const bf16* dy;
     int H, W, Ho, Wo, Cout, stride;
-    __device__ uint4 operator()(int m, int k, int) const {
+    __device__ const void* base() const { return dy; }
+    __device__ const void* src(int m, int k) const {
         int co = k % Cout, t = k / Cout, kx = t % 3, ky = t / 3;
         int xx = m % W, r = m / W, y = r % H, b = r / H;
         int ty = y + 1 - ky, tx = xx + 1 - kx;
-        if (ty < 0 || tx < 0 || ty % stride || tx % stride) return make_uint4(0, 0, 0, 0);
+        if (ty < 0 || tx < 0 || ty % stride || tx % stride) return nullptr;
         int yo = ty / stride, xo = tx / stride;
-        if (yo >= Ho || xo >= Wo) return make_uint4(0, 0, 0, 0);
-        return ld16(dy + (((size_t)b * Ho + yo) * Wo + xo) * Cout + co);
+        if (yo >= Ho || xo >= Wo) return nullptr;
+        return dy + (((size_t)b * Ho + yo) * Wo + xo) * Cout + co;
     }
 };
 
 // weight-gradient A: row m = (ky*3 + kx)*Cin + ci of im2col^T, k = output pixel
 struct TcWGradA {
+    static constexpr bool kAsync = false;
     const bf16* x;
     int H, W, C, Ho, Wo, stride;
     __device__ uint4 operator()(int m, int k, int k_end) const {
@@ -116,6 +121,7 @@ struct TcWGradA {
 
 // weight-gradient B: row n = co, k = output pixel -> dy[pixel][co]
 struct TcWGradB {
+    static constexpr bool kAsync = false;
     const bf16* dy;
     int Cout;
     __device__ uint4 operator()(int n, int k, int k_end) const {
@@ -351,7 +357,7 @@ int Ho_of(int H, int s) { return s == 1 ? H : (H + 1) / 2; }
 
 template <int NT, class LA, class LB, class EP>
 rf_status tc_launch(rf_cnn* c, int M, int N, int K, int splits, LA la, LB lb, EP ep) {
-    using S = rf_tc::TcSmem<NT>;
+    using S = rf_tc::TcSmem<NT, rf_tc::stages_for<LA, LB>()>;
     static bool attr_set = false;
     if (!attr_set) {
         CN(cudaFuncSetAttribute(rf_tc::k_tc_gemm<NT, LA, LB, EP>,

@@ -11,14 +11,18 @@
 // (8 x 16-byte core matrices: rows of a core matrix 16 bytes apart, core
 // matrices 128 bytes apart along K and 1024 bytes apart along M / N), make
 // the writes visible to the tensor core (fence.proxy.async), and one thread
-// issues four 128 x NT x 16 MMAs and commits them to an mbarrier.  Two
-// chunk buffers alternate, so the gather of chunk c+1 overlaps the MMAs of
-// chunk c.  The epilogue reads the accumulator with tcgen05.ld: warp w owns
-// TMEM lanes (= rows of D) 32w .. 32w + 31.
+// issues four 128 x NT x 16 MMAs and commits them to an mbarrier.  kStages
+// chunk buffers form a ring: the copies of chunks c+1 .. c+kStages-1 are in
+// flight (cp.async, 16 bytes each, zero-filled outside the operand) while
+// the MMAs of chunk c run.  The epilogue reads the accumulator with
+// tcgen05.ld: warp w owns TMEM lanes (= rows of D) 32w .. 32w + 31.
 //
-// The loaders are functors returning 8 consecutive K elements of one row as
-// a uint4 (zeros outside the operand); the epilogue functor receives
-// (split, m, n, value).
+// A loader functor gives the 8 consecutive K elements of one row: an
+// asynchronous loader (kAsync = true) their 16-byte-aligned global address
+// (src(), null for zeros), a gathering loader (kAsync = false) their value as
+// a uint4 (operator(), zeros outside the operand), which the threads store
+// into the ring themselves.  The epilogue functor receives (split, m, n,
+// value).
 #pragma once
 
 #include <cstdint>
@@ -137,13 +141,36 @@ __device__ __forceinline__ uint32_t tile_off(int r, int g) {
     return (uint32_t)(((r >> 3) * (kTK / 8) + g) * 128 + (r & 7) * 16);
 }
 
-template <int NT>
+__device__ __forceinline__ void cp_async16(void* smem_dst, const void* gsrc, int src_bytes) {
+    asm volatile("cp.async.cg.shared.global [%0], [%1], 16, %2;" ::"r"(smem_u32(smem_dst)),
+                 "l"(gsrc), "r"(src_bytes)
+                 : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() {
+    asm volatile("cp.async.commit_group;" ::: "memory");
+}
+template <int N>
+__device__ __forceinline__ void cp_async_wait() {
+    asm volatile("cp.async.wait_group %0;" ::"n"(N) : "memory");
+}
+
+// chunk buffers in the ring: three when a loader copies asynchronously (two
+// chunks in flight during an MMA), two when both gather through registers
+// (their stores finish before the chunk's barrier anyway; less shared
+// memory keeps more CTAs resident)
+template <class LA, class LB>
+constexpr int stages_for() {
+    return (LA::kAsync || LB::kAsync) ? 3 : 2;
+}
+
+template <int NT, int kStages>
 struct TcSmem {
     static_assert(NT % 16 == 0 && NT >= 16 && NT <= 256, "N tile");
     static_assert((NT * 8) % 128 == 0, "B tile rows split evenly over the CTA's threads");
     static constexpr int kA = kTM * kTK * 2;  // bytes of one A chunk
     static constexpr int kB = NT * kTK * 2;
-    static constexpr int kBytes = 2 * (kA + kB) + 2048;  // two chunk buffers, barriers, alignment slack
+    // the chunk ring, barriers, alignment slack
+    static constexpr int kBytes = kStages * (kA + kB) + 2048;
     static constexpr uint32_t kCols = NT <= 32 ? 32 : (NT <= 64 ? 64 : (NT <= 128 ? 128 : 256));
 };
 
@@ -153,10 +180,11 @@ template <int NT, class LA, class LB, class EP>
 __global__ void __launch_bounds__(kThreads) k_tc_gemm(int M, int N, int K, int kspan, LA la,
                                                      LB lb, EP ep, int* status) {
     extern __shared__ __align__(1024) unsigned char smem_raw[];
-    using S = TcSmem<NT>;
+    constexpr int kStages = stages_for<LA, LB>();
+    using S = TcSmem<NT, kStages>;
     unsigned char* base = (unsigned char*)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
-    uint64_t* bars = (uint64_t*)(base + 2 * (S::kA + S::kB));  // [2] chunk barriers
-    uint32_t* tslot = (uint32_t*)(bars + 2);
+    uint64_t* bars = (uint64_t*)(base + kStages * (S::kA + S::kB));  // one per ring slot
+    uint32_t* tslot = (uint32_t*)(bars + kStages);
     int* fail = (int*)(tslot + 1);
 
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
@@ -166,8 +194,7 @@ __global__ void __launch_bounds__(kThreads) k_tc_gemm(int M, int N, int K, int k
     const int nchunks = (k_end - k_begin + kTK - 1) / kTK;
 
     if (tid == 0) {
-        mbar_init(&bars[0], 1);
-        mbar_init(&bars[1], 1);
+        for (int q = 0; q < kStages; q++) mbar_init(&bars[q], 1);
         *fail = 0;
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
     }
@@ -178,65 +205,99 @@ __global__ void __launch_bounds__(kThreads) k_tc_gemm(int M, int N, int K, int k
     const uint32_t tmem = *tslot;
     constexpr uint32_t idesc = idesc_bf16(kTM, NT);
 
-    unsigned phases = 0u;  // bit b: parity of the next completion of barrier b
-    for (int c = 0; c < nchunks; c++) {
-        const int b = c & 1;
-        unsigned char* tA = base + b * S::kA;
-        unsigned char* tB = base + 2 * S::kA + b * S::kB;
-        // before refilling buffer b, the MMAs that read it (chunk c - 2) must be done
-        if (c >= 2) {
-            if (!mbar_wait(&bars[b], (phases >> b) & 1u)) *fail = 1;
-            phases ^= 1u << b;
-        }
+    // queue the copies (or do the gathers) of chunk c into ring slot c % kStages
+    auto issue = [&](int c) {
+        const int q = c % kStages;
+        unsigned char* tA = base + q * S::kA;
+        unsigned char* tB = base + kStages * S::kA + q * S::kB;
         const int kc = k_begin + c * kTK;
-        // gather: A 128 rows x 8 groups, B NT rows x 8 groups, 16 bytes each.
-        // All of a thread's global loads are issued before its shared-memory
-        // stores, so they are in flight together (the stores go through a
-        // generic pointer the compiler cannot tell apart from global memory).
         constexpr int kPerA = kTM * (kTK / 8) / kThreads;  // 8
         constexpr int kPerB = NT * (kTK / 8) / kThreads;   // NT / 16
-        uint4 va[kPerA], vb[kPerB];
+        if constexpr (LA::kAsync) {
 #pragma unroll
-        for (int j = 0; j < kPerA; j++) {
-            const int i = tid + j * kThreads, r = i >> 3, g = i & 7, k = kc + g * 8;
-            va[j] = make_uint4(0, 0, 0, 0);
-            if (m0 + r < M && k < k_end) va[j] = la(m0 + r, k, k_end);
-        }
+            for (int j = 0; j < kPerA; j++) {
+                const int i = tid + j * kThreads, r = i >> 3, g = i & 7, k = kc + g * 8;
+                const void* src = (m0 + r < M && k < k_end) ? la.src(m0 + r, k) : nullptr;
+                cp_async16(tA + tile_off(r, g), src ? src : la.base(), src ? 16 : 0);
+            }
+        } else {
+            // all of a thread's loads are issued before its stores (the stores go
+            // through a generic pointer the compiler cannot tell from global memory)
+            uint4 va[kPerA];
 #pragma unroll
-        for (int j = 0; j < kPerB; j++) {
-            const int i = tid + j * kThreads, r = i >> 3, g = i & 7, k = kc + g * 8;
-            vb[j] = make_uint4(0, 0, 0, 0);
-            if (n0 + r < N && k < k_end) vb[j] = lb(n0 + r, k, k_end);
-        }
+            for (int j = 0; j < kPerA; j++) {
+                const int i = tid + j * kThreads, r = i >> 3, g = i & 7, k = kc + g * 8;
+                va[j] = make_uint4(0, 0, 0, 0);
+                if (m0 + r < M && k < k_end) va[j] = la(m0 + r, k, k_end);
+            }
 #pragma unroll
-        for (int j = 0; j < kPerA; j++) {
-            const int i = tid + j * kThreads;
-            *(uint4*)(tA + tile_off(i >> 3, i & 7)) = va[j];
+            for (int j = 0; j < kPerA; j++) {
+                const int i = tid + j * kThreads;
+                *(uint4*)(tA + tile_off(i >> 3, i & 7)) = va[j];
+            }
         }
+        if constexpr (LB::kAsync) {
 #pragma unroll
-        for (int j = 0; j < kPerB; j++) {
-            const int i = tid + j * kThreads;
-            *(uint4*)(tB + tile_off(i >> 3, i & 7)) = vb[j];
+            for (int j = 0; j < kPerB; j++) {
+                const int i = tid + j * kThreads, r = i >> 3, g = i & 7, k = kc + g * 8;
+                const void* src = (n0 + r < N && k < k_end) ? lb.src(n0 + r, k) : nullptr;
+                cp_async16(tB + tile_off(r, g), src ? src : lb.base(), src ? 16 : 0);
+            }
+        } else {
+            uint4 vb[kPerB];
+#pragma unroll
+            for (int j = 0; j < kPerB; j++) {
+                const int i = tid + j * kThreads, r = i >> 3, g = i & 7, k = kc + g * 8;
+                vb[j] = make_uint4(0, 0, 0, 0);
+                if (n0 + r < N && k < k_end) vb[j] = lb(n0 + r, k, k_end);
+            }
+#pragma unroll
+            for (int j = 0; j < kPerB; j++) {
+                const int i = tid + j * kThreads;
+                *(uint4*)(tB + tile_off(i >> 3, i & 7)) = vb[j];
+            }
         }
+    };
+
+    // prologue: chunks 0 .. kStages-2 in flight; one commit group per chunk
+    // (empty past the end) keeps the group count uniform
+    for (int c = 0; c < kStages - 1; c++) {
+        if (c < nchunks) issue(c);
+        cp_async_commit();
+    }
+    for (int c = 0; c < nchunks; c++) {
+        const int q = c % kStages;
+        cp_async_wait<kStages - 2>();  // chunk c has landed
         fence_async_smem();
         __syncthreads();
         if (tid == 0) {
             tc_fence_after();
-            const uint32_t a0 = smem_u32(tA), b0 = smem_u32(tB);
+            const uint32_t a0 = smem_u32(base + q * S::kA);
+            const uint32_t b0 = smem_u32(base + kStages * S::kA + q * S::kB);
 #pragma unroll
             for (int kk = 0; kk < kTK / 16; kk++) {
                 const uint64_t da = smem_desc(a0 + kk * 256, 128, 1024);
                 const uint64_t db = smem_desc(b0 + kk * 256, 128, 1024);
                 mma_bf16(tmem, da, db, idesc, (c > 0 || kk > 0) ? 1u : 0u);
             }
-            mma_commit(&bars[b]);
+            mma_commit(&bars[q]);
         }
-        __syncthreads();
+        // refill the slot chunk c - 1 used once its MMAs are done
+        const int nc = c + kStages - 1;
+        if (nc < nchunks) {
+            if (c >= 1) {
+                const int pc = c - 1;
+                if (!mbar_wait(&bars[pc % kStages], (unsigned)(pc / kStages) & 1u)) *fail = 1;
+            }
+            issue(nc);
+        }
+        cp_async_commit();
     }
     // the last commit covers every earlier MMA of this CTA
+    cp_async_wait<0>();
     if (nchunks > 0) {
-        const int b = (nchunks - 1) & 1;
-        if (!mbar_wait(&bars[b], (phases >> b) & 1u)) *fail = 1;
+        const int lc = nchunks - 1;
+        if (!mbar_wait(&bars[lc % kStages], (unsigned)(lc / kStages) & 1u)) *fail = 1;
     }
     tc_fence_after();
     __syncthreads();
