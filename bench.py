@@ -78,6 +78,11 @@ WORKLOADS = {
                      warm_warps=[1, 1, 2], warm_iters=[20, 40, 60])]),
     # batched: 64 pairs of 1280x720 (per-pair throughput of the batched path)
     "batch64-720p": dict(pairs=64, sizes=[(1280, 720)], levels=6, warps=5, iters=100, seed=0),
+    # profiling case of the batched kernels: 4 pairs of 1280x720 at their finest
+    # level only, 1 warp, 4 iterations, the 64-pair tile table (a dozen launches;
+    # 3.7 M pixels per launch, above the L2 size)
+    "720p-x4-l0": dict(pairs=4, sizes=[(1280, 720)], levels=1, warps=1, iters=4, seed=2000,
+                       tiles="reconflow_gb300/tuning/gb300_720p_x64.json"),
 }
 SOLVER = dict(method=14, lam=50.0, theta=0.33, tau=0.25, alpha_proj=60.0, lambdaf=0.1,
               lambdams=100.0, fix_quirks=1)
@@ -310,6 +315,11 @@ def run_batch(args, wl, world, rank, local):
         padded.append((I0, I1))
         b.setCameraMatrices(i, sc["K"], sc["K"])
         b.copyImagesToDevice(i, I0, I1)
+    tiles = load_tiles(wl.get("tiles"))
+    if tiles is not None:
+        from reconflow_gb300 import autotune
+
+        autotune.apply(b, tiles["levels"])
     Rs = [sc["R"] for sc in scenes]
     ts = [sc["t"] for sc in scenes]
     flush = torch.empty(L2_FLUSH_BYTES // 4, dtype=torch.float32, device="cuda")
@@ -334,6 +344,12 @@ def run_batch(args, wl, world, rank, local):
     total_s = max_over_ranks(sum(step_ms) / 1000.0, world)
     npairs = wl["pairs"]
     value = world * npairs * args.steps / total_s
+    if args.solve_only:
+        if rank == 0:
+            print(json.dumps({"metric": "frame pairs/s, batched ReconFlow solve", "value": value,
+                              "unit": "pairs/s", "note": "solve-only run"}), flush=True)
+        b.close()
+        return
     # accuracy over the batch
     epes = []
     for i, sc in enumerate(scenes):
@@ -360,8 +376,16 @@ def run_batch(args, wl, world, rank, local):
             a1[:] = padded[i][1]
             hosts.append(ptrs)
         hb = b._h
+        uniform = len(set(b.strides)) == 1
+        col = [[hosts[i][k].value for i in range(npairs)] for k in range(8)]
 
         def step():
+            if uniform:  # one pitch: whole-batch transfers, one sync each way
+                b.uploadAll(col[0], col[1], b.strides[0])
+                b.solveR(Rs, ts)
+                b.downloadAll(b.strides[0], u=col[2], v=col[3], inv_depth=col[4], X=col[5],
+                              Y=col[6], Z=col[7])
+                return
             for i in range(npairs):
                 R._native.check(lib.rf_batch_upload_images(hb, i, hosts[i][0], hosts[i][1],
                                                            b.strides[i]))
@@ -426,7 +450,7 @@ def run_learned(args, wl, world, rank, local):
 
     torch.cuda.set_device(local)
     lib = R.load()
-    W, H, n = wl["width"], wl["height"], wl["pairs"]
+    W, H, n = wl["width"], wl["height"], args.pairs or wl["pairs"]
     t0 = time.perf_counter()
     scenes = [make_scene(W, H, seed=wl["seed"] + 1000 * rank + i, device="cuda") for i in range(n)]
     gen_s = time.perf_counter() - t0
@@ -479,15 +503,19 @@ def run_learned(args, wl, world, rank, local):
         torch.cuda.synchronize()
         return [a.elapsed_time(e) for a, e in evs]
 
-    # plain, batched: reference accuracy and energies
-    plain = new_batch(wl["plain_warps"], wl["plain_iters"])
-    with torch.cuda.stream(stream):
-        plain.solveR(Rs, ts)
-        torch.cuda.synchronize()
-        plain_acc = epe_stats(plain)
-        e_plain = plain.energies()
-        plain_batch_ms = timed(lambda: plain.solveR(Rs, ts), 2)
-    plain.close()
+    # plain, batched: reference accuracy and energies (a solve-only run, for
+    # profiler launch lists, skips it and so never falls back)
+    if args.solve_only:
+        e_plain = np.full(n, np.inf)
+    else:
+        plain = new_batch(wl["plain_warps"], wl["plain_iters"])
+        with torch.cuda.stream(stream):
+            plain.solveR(Rs, ts)
+            torch.cuda.synchronize()
+            plain_acc = epe_stats(plain)
+            e_plain = plain.energies()
+            plain_batch_ms = timed(lambda: plain.solveR(Rs, ts), 2)
+        plain.close()
     # plain, one pair through the drop-in path
     f = R.ReconFlow()
     f.initializeR(W, H, 1, wl["levels"], 2.0, SOLVER["method"], SOLVER["lam"], 0.0,
@@ -500,10 +528,11 @@ def run_learned(args, wl, world, rank, local):
         autotune.apply_single(f, single_tiles["levels"], wl["levels"])
     f.setCameraMatrices(scenes[0]["K"], scenes[0]["K"])
     f.copyImagesToDevice(scenes[0]["I0"], scenes[0]["I1"])
-    with torch.cuda.stream(stream):
-        for _ in range(2):
-            f.solveR(Rs[0], ts[0], 5.0)
-        single_ms = timed(lambda: f.solveR(Rs[0], ts[0], 5.0), 5)
+    if not args.solve_only:
+        with torch.cuda.stream(stream):
+            for _ in range(2):
+                f.solveR(Rs[0], ts[0], 5.0)
+            single_ms = timed(lambda: f.solveR(Rs[0], ts[0], 5.0), 5)
 
     # learned
     net = WarmStartNet(n, (H // 8) + 1, (W // 8) + 1, seed=0)
@@ -529,8 +558,9 @@ def run_learned(args, wl, world, rank, local):
         for _ in range(args.warmup):
             step()
         torch.cuda.synchronize()
-        learned_acc = epe_stats(b)
-        e_learned = b.energies()
+        if not args.solve_only:
+            learned_acc = epe_stats(b)
+            e_learned = b.energies()
         barrier(world)
         l0 = b.kernelLaunches() + net.kernel_launches() + f.kernelLaunches()
         fallbacks.clear()
@@ -541,6 +571,12 @@ def run_learned(args, wl, world, rank, local):
     timed_fallbacks = list(fallbacks)
     total_s = max_over_ranks(sum(step_ms) / 1000.0, world)
     value = world * n * args.steps / total_s
+    if args.solve_only:
+        if rank == 0:
+            print(json.dumps({"metric": LEARNED_METRIC, "value": value, "unit": "pairs/s",
+                              "pairs_per_step": n, "note": "solve-only run (no plain reference "
+                              "solve, no fallbacks)"}), flush=True)
+        return
 
     # end to end: frames from pinned host memory in, flow / inverse depth /
     # points out, every step
@@ -585,14 +621,19 @@ def run_learned(args, wl, world, rank, local):
             for p_ in ptrs:
                 lib.rf_host_free(p_)
 
-    # roofline: the dominant stencil kernel (level-0 data / triangulation)
+    # roofline: the dominant kernel of the step, the batched level-0 data /
+    # triangulation kernel over all pairs (rf_batch_profile_level); the
+    # single-pair kernels of the drop-in path beside it
+    with torch.cuda.stream(stream):
+        ms_b = b.profileLevel(0, 20)
+    roofline = roofline_of(ms_b, W * H * n, batched=True)
     ms = (ctypes.c_float * 2)()
     with torch.cuda.stream(stream):
         f.setCameraMatrices(Ks[0], Ks[0])
         f.copyImagesToDevice(scenes[0]["I0"], scenes[0]["I1"])
         f.solveR(Rs[0], ts[0], 5.0)
         R._native.check(lib.rf_profile_iterations(f._handle(), 0, 50, ms))
-    roofline = roofline_of(ms, W * H)
+    roofline["single_pair"] = roofline_of(ms, W * H)
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         wl1 = dict(width=W, height=H, levels=wl["levels"], warps=wl["plain_warps"],
@@ -857,20 +898,26 @@ def run_learned_mixed(args, wl, world, rank, local):
         G["f"].close()
 
 
-def roofline_of(ms, px):
-    """Roofline entry of the dominant level-0 kernel from per-launch times."""
+def roofline_of(ms, px, batched=False):
+    """Roofline entry of the dominant level-0 kernel from per-launch times
+    (`px` pixels per launch; `batched`: the batched solver's kernels)."""
     names = ["recon_a", "recon_b"]
     dom = 0 if ms[0] >= ms[1] else 1
     achieved = ALG_BYTES[names[dom]] * px / (ms[dom] * 1e-3) / 1e9
     peak, peak_kind = load_peaks()
     traffic = None
-    tpath = os.path.join(ROOT, "profiles", "traffic_720p.json")
+    tpath = os.path.join(ROOT, "profiles",
+                         "traffic_720p_batch.json" if batched else "traffic_720p.json")
     if os.path.exists(tpath):
         with open(tpath) as fh:
-            t720 = json.load(fh).get(names[dom])
-        # the capture is of a 1280x720 launch; other sizes scale by their pixels
-        traffic = None if t720 is None else t720 * px / (1280 * 720)
-    return {"bound": "hbm", "kernel": names[dom], "achieved": achieved, "peak": peak,
+            tr = json.load(fh)
+        per = tr.get(names[dom])
+        # the capture's DRAM bytes per launch scaled by pixels (traffic grows
+        # with the pixel count: one pass over every field per launch)
+        traffic = None if per is None else per * px / tr["pixels"]
+    return {"bound": "hbm", "kernel": ("k_batch<OpReconA>" if dom == 0 else "k_batch<OpReconB>")
+            if batched else ("k_recon_a" if dom == 0 else "k_recon_b"),
+            "achieved": achieved, "peak": peak,
             "peak_kind": peak_kind, "unit": "GB/s", "frac": achieved / peak, "traffic": traffic,
             "alg_bytes_per_launch": ALG_BYTES[names[dom]] * px,
             "launch_ms": {names[0]: ms[0], names[1]: ms[1]},
@@ -902,6 +949,9 @@ def main():
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--solve-only", action="store_true",
                     help="only warm-up + timed solves (for profiler launch lists)")
+    ap.add_argument("--pairs", type=int, default=0,
+                    help="pairs per step of the 720p learned workload (profiling; default: the "
+                         "workload's)")
     args = ap.parse_args()
     wl = WORKLOADS[args.workload]
     world, rank, local = dist_setup(args)

@@ -5,16 +5,20 @@
 // per-launch cost is paid once per step instead of once per pair.  The whole
 // batch schedule is captured into one CUDA graph.
 //
-// Layout: each pair owns a run of level-0-sized planes (its stride x (height
-// + 1) floats, aligned to 64 floats) in one pool; plane k of pair i starts at
-// base_i + k * plane_i, and all pairs use the same plane indices for the same
-// role, so a launch names its fields by plane index.  Blocks map to pairs
-// through a per-level prefix sum of tile counts (32x8 tiles).
+// Layout: plane-major.  Plane k (one role: u, duhat, X, ...) is one array
+// holding every pair's level-0-sized region (its stride x (height + 1)
+// floats, aligned to 64 floats) at the pair's offset off_i, the same offset
+// in every plane; all pairs use the same plane index for the same role.  A
+// pixel of pair i is therefore element off_i + x + y * stride of each of its
+// planes, and the hot operations carry plain plane base pointers, so their
+// per-field address arithmetic is the single-pair kernels'.  Blocks map to
+// (pair, tile) through a per-level tile table.
 //
 // Per-pixel arithmetic is the shared code of the single-pair kernels
 // (rf_ops.cuh), so a pair solved in a batch is bit-identical to the same pair
 // solved alone.
 #include <algorithm>
+#include <climits>
 #include <cstring>
 #include <string>
 #include <vector>
@@ -37,71 +41,66 @@ constexpr int kMaxTile = 256;
 constexpr int kMaxLevels = 16;
 
 struct BatchPair {
-    float* base;
-    size_t plane;  // floats per plane
     LevelDims dims[kMaxLevels];
+};
+
+// One block of a level: the tile whose first pixel is (x0, y0) in pair
+// `pair`, whose region starts `off` floats into every plane.
+struct __align__(16) TileEntry {
+    int pair, x0, y0, off;
 };
 
 struct BatchCtx {
     const BatchPair* pairs;
-    const int* prefix;          // [level][n + 1] tile prefix sums
+    const TileEntry* tiles;     // this launch's level: one entry per block
     const LevelConsts* consts;  // [pair][level]
+    float* pool;
+    size_t total;               // floats per plane
     int n;
     int L;
 };
 
-__device__ __forceinline__ float* plane_ptr(const BatchPair& bp, int k) {
-    return bp.base + (size_t)k * bp.plane;
+// plane k of the tile's pair
+__device__ __forceinline__ float* plane_ptr(const BatchCtx& c, const TileEntry& t, int k) {
+    return c.pool + (size_t)k * c.total + t.off;
 }
 
-// One block = one 32x8 tile of one pair at `level`.
+// One block = one tile of one pair at `level` (the level's tile shape is
+// the block shape; the tile table gives the pair and the tile's origin).
 template <class Op>
 __global__ void __launch_bounds__(kMaxTile) k_batch(BatchCtx ctx, int level, Op op) {
-    const int* pre = ctx.prefix + level * (ctx.n + 1);
-    const int b = blockIdx.x;
-    int lo = 0, hi = ctx.n - 1;
-    while (lo < hi) {
-        int mid = (lo + hi + 1) >> 1;
-        if (pre[mid] <= b)
-            lo = mid;
-        else
-            hi = mid - 1;
-    }
-    const BatchPair& bp = ctx.pairs[lo];
-    const LevelDims d = bp.dims[level];
-    const int t = b - pre[lo];
-    const int bx = blockDim.x, by = blockDim.y;  // this level's tile shape
-    const int tw = (d.w + bx - 1) / bx;
-    const int ix = (t % tw) * bx + threadIdx.x, iy = (t / tw) * by + threadIdx.y;
+    const TileEntry t = ctx.tiles[blockIdx.x];
+    const LevelDims d = ctx.pairs[t.pair].dims[level];
+    const int ix = t.x0 + (int)threadIdx.x, iy = t.y0 + (int)threadIdx.y;
     if (ix >= d.w || iy >= d.h) return;
-    op(ctx, bp, lo, level, d, ix, iy);
+    op(ctx, t, level, d, ix, iy);
 }
 
 // ---- per-step operations (plane indices resolved per pair) ----------------
 struct OpDownscale2 {
     int a, b, oa, ob;  // fine planes (level-1) -> coarse planes (level)
-    __device__ void operator()(const BatchCtx&, const BatchPair& bp, int, int level, LevelDims c,
+    __device__ void operator()(const BatchCtx& ctx, const TileEntry& t, int level, LevelDims c,
                                int ix, int iy) const {
-        LevelDims f = bp.dims[level - 1];
-        plane_ptr(bp, oa)[ix + iy * c.s] = 0.25f * downscale_px(plane_ptr(bp, a), f, c.w, c.h, ix, iy);
-        plane_ptr(bp, ob)[ix + iy * c.s] = 0.25f * downscale_px(plane_ptr(bp, b), f, c.w, c.h, ix, iy);
+        LevelDims f = ctx.pairs[t.pair].dims[level - 1];
+        plane_ptr(ctx, t, oa)[ix + iy * c.s] = 0.25f * downscale_px(plane_ptr(ctx, t, a), f, c.w, c.h, ix, iy);
+        plane_ptr(ctx, t, ob)[ix + iy * c.s] = 0.25f * downscale_px(plane_ptr(ctx, t, b), f, c.w, c.h, ix, iy);
     }
 };
 
 struct OpWarp {
     int I1, u, v, out;
-    __device__ void operator()(const BatchCtx&, const BatchPair& bp, int, int, LevelDims d, int ix,
+    __device__ void operator()(const BatchCtx& ctx, const TileEntry& t, int, LevelDims d, int ix,
                                int iy) const {
-        warp_px(plane_ptr(bp, I1), plane_ptr(bp, u), plane_ptr(bp, v), d, plane_ptr(bp, out), ix, iy);
+        warp_px(plane_ptr(ctx, t, I1), plane_ptr(ctx, t, u), plane_ptr(ctx, t, v), d, plane_ptr(ctx, t, out), ix, iy);
     }
 };
 
 struct OpDeriv {
     int I0, I1w, Ix, Iy, Iz;
-    __device__ void operator()(const BatchCtx&, const BatchPair& bp, int, int, LevelDims d, int ix,
+    __device__ void operator()(const BatchCtx& ctx, const TileEntry& t, int, LevelDims d, int ix,
                                int iy) const {
-        derivatives_px(plane_ptr(bp, I0), plane_ptr(bp, I1w), d, plane_ptr(bp, Ix), plane_ptr(bp, Iy),
-                       plane_ptr(bp, Iz), ix, iy);
+        derivatives_px(plane_ptr(ctx, t, I0), plane_ptr(ctx, t, I1w), d, plane_ptr(ctx, t, Ix), plane_ptr(ctx, t, Iy),
+                       plane_ptr(ctx, t, Iz), ix, iy);
     }
 };
 
@@ -110,40 +109,26 @@ struct ReconIdx {
         Y1, Z1, uc, vc;
 };
 
-__device__ __forceinline__ ReconFields resolve(const BatchPair& bp, const ReconIdx& r) {
-    ReconFields f{};
-    f.u = plane_ptr(bp, r.u); f.v = plane_ptr(bp, r.v);
-    f.duhat = plane_ptr(bp, r.duhat); f.dvhat = plane_ptr(bp, r.dvhat);
-    f.pu1 = plane_ptr(bp, r.pu1); f.pu2 = plane_ptr(bp, r.pu2);
-    f.pv1 = plane_ptr(bp, r.pv1); f.pv2 = plane_ptr(bp, r.pv2);
-    f.uproj = plane_ptr(bp, r.uproj); f.vproj = plane_ptr(bp, r.vproj);
-    f.sku = plane_ptr(bp, r.sku); f.skv = plane_ptr(bp, r.skv);
-    f.Ix = plane_ptr(bp, r.Ix); f.Iy = plane_ptr(bp, r.Iy); f.Iz = plane_ptr(bp, r.Iz);
-    f.X = plane_ptr(bp, r.X); f.Y = plane_ptr(bp, r.Y); f.Z = plane_ptr(bp, r.Z);
-    f.X1 = plane_ptr(bp, r.X1); f.Y1 = plane_ptr(bp, r.Y1); f.Z1 = plane_ptr(bp, r.Z1);
-    f.uc = plane_ptr(bp, r.uc); f.vc = plane_ptr(bp, r.vc);
-    return f;
-}
-
+// The inner-iteration operations carry the planes' base pointers
+// (ReconFields, resolved on the host from plane indices); a pixel's element
+// is the tile's pair offset plus its position in the level.
 struct OpReconA {
-    ReconIdx r;
+    ReconFields f;
     Weights wt;
     int first, ucb;
-    __device__ void operator()(const BatchCtx& ctx, const BatchPair& bp, int pair, int level,
-                               LevelDims d, int ix, int iy) const {
-        ReconFields f = resolve(bp, r);
-        recon_a_px<0>(f, ctx.consts[pair * ctx.L + level], wt, d, ix, iy, first, ucb);
+    __device__ void operator()(const BatchCtx& ctx, const TileEntry& t, int level, LevelDims d,
+                               int ix, int iy) const {
+        recon_a_px<0>(f, ctx.consts[t.pair * ctx.L + level], wt, d, ix, iy, first, ucb, t.off);
     }
 };
 
 struct OpReconB {
-    ReconIdx r;
+    ReconFields f;
     Weights wt;
     int first;
-    __device__ void operator()(const BatchCtx&, const BatchPair& bp, int, int, LevelDims d, int ix,
+    __device__ void operator()(const BatchCtx&, const TileEntry& t, int, LevelDims d, int ix,
                                int iy) const {
-        ReconFields f = resolve(bp, r);
-        recon_b_px(f, wt, d, ix, iy, first);
+        recon_b_px(f, wt, d, ix, iy, first, t.off);
     }
 };
 
@@ -151,11 +136,11 @@ struct OpPlainData {
     int duhat, dvhat, pu1, pu2, pv1, pv2, Ix, Iy, Iz;
     Weights wt;
     int first;
-    __device__ void operator()(const BatchCtx&, const BatchPair& bp, int, int, LevelDims d, int ix,
+    __device__ void operator()(const BatchCtx& ctx, const TileEntry& t, int, LevelDims d, int ix,
                                int iy) const {
-        plain_data_px(plane_ptr(bp, duhat), plane_ptr(bp, dvhat), plane_ptr(bp, pu1),
-                      plane_ptr(bp, pu2), plane_ptr(bp, pv1), plane_ptr(bp, pv2), plane_ptr(bp, Ix),
-                      plane_ptr(bp, Iy), plane_ptr(bp, Iz), wt, d, first, ix, iy);
+        plain_data_px(plane_ptr(ctx, t, duhat), plane_ptr(ctx, t, dvhat), plane_ptr(ctx, t, pu1),
+                      plane_ptr(ctx, t, pu2), plane_ptr(ctx, t, pv1), plane_ptr(ctx, t, pv2), plane_ptr(ctx, t, Ix),
+                      plane_ptr(ctx, t, Iy), plane_ptr(ctx, t, Iz), wt, d, first, ix, iy);
     }
 };
 
@@ -163,50 +148,58 @@ struct OpPlainTV {
     int duhat, dvhat, pu1, pu2, pv1, pv2;
     Weights wt;
     int first;
-    __device__ void operator()(const BatchCtx&, const BatchPair& bp, int, int, LevelDims d, int ix,
+    __device__ void operator()(const BatchCtx& ctx, const TileEntry& t, int, LevelDims d, int ix,
                                int iy) const {
-        plain_tv_px(plane_ptr(bp, duhat), plane_ptr(bp, dvhat), plane_ptr(bp, pu1),
-                    plane_ptr(bp, pu2), plane_ptr(bp, pv1), plane_ptr(bp, pv2), wt, d, first, ix,
+        plain_tv_px(plane_ptr(ctx, t, duhat), plane_ptr(ctx, t, dvhat), plane_ptr(ctx, t, pu1),
+                    plane_ptr(ctx, t, pu2), plane_ptr(ctx, t, pv1), plane_ptr(ctx, t, pv2), wt, d, first, ix,
                     iy);
     }
 };
 
 // u + median5(duhat) (Reconflow.cu:410-416); out may be u itself
 struct OpMedianAdd {
-    int duhat, dvhat, u, v, ou, ov;
-    __device__ void operator()(const BatchCtx&, const BatchPair& bp, int, int, LevelDims d, int ix,
+    const float* duhat;  // plane base pointers
+    const float* dvhat;
+    const float* u;
+    const float* v;
+    float* ou;
+    float* ov;
+    __device__ void operator()(const BatchCtx&, const TileEntry& t, int, LevelDims d, int ix,
                                int iy) const {
         float mu, mv;
-        median5_pair(plane_ptr(bp, duhat), plane_ptr(bp, dvhat), ix, iy, d, mu, mv);
-        int pos = ix + iy * d.s;
-        float a = plane_ptr(bp, u)[pos] + mu;
-        float b = plane_ptr(bp, v)[pos] + mv;
-        plane_ptr(bp, ou)[pos] = a;
-        plane_ptr(bp, ov)[pos] = b;
+        median5_pair(duhat, dvhat, ix, iy, d, mu, mv, t.off);
+        int pos = t.off + ix + iy * d.s;
+        float a = u[pos] + mu;
+        float b = v[pos] + mv;
+        ou[pos] = a;
+        ov[pos] = b;
     }
 };
 
 struct OpMedian5 {
-    int u, v, ou, ov;
-    __device__ void operator()(const BatchCtx&, const BatchPair& bp, int, int, LevelDims d, int ix,
+    const float* u;  // plane base pointers
+    const float* v;
+    float* ou;
+    float* ov;
+    __device__ void operator()(const BatchCtx&, const TileEntry& t, int, LevelDims d, int ix,
                                int iy) const {
         float mu, mv;
-        median5_pair(plane_ptr(bp, u), plane_ptr(bp, v), ix, iy, d, mu, mv);
-        plane_ptr(bp, ou)[ix + iy * d.s] = mu;
-        plane_ptr(bp, ov)[ix + iy * d.s] = mv;
+        median5_pair(u, v, ix, iy, d, mu, mv, t.off);
+        ou[t.off + ix + iy * d.s] = mu;
+        ov[t.off + ix + iy * d.s] = mv;
     }
 };
 
 struct OpSolveUc {
     int X, Y, Z, uc, vc;
-    __device__ void operator()(const BatchCtx& ctx, const BatchPair& bp, int pair, int level,
-                               LevelDims d, int ix, int iy) const {
+    __device__ void operator()(const BatchCtx& ctx, const TileEntry& t, int level, LevelDims d,
+                               int ix, int iy) const {
         int pos = ix + iy * d.s;
         float a, b;
-        project_uc(ctx.consts[pair * ctx.L + level], plane_ptr(bp, X)[pos], plane_ptr(bp, Y)[pos],
-                   plane_ptr(bp, Z)[pos], ix, iy, a, b);
-        plane_ptr(bp, uc)[pos] = a;
-        plane_ptr(bp, vc)[pos] = b;
+        project_uc(ctx.consts[t.pair * ctx.L + level], plane_ptr(ctx, t, X)[pos], plane_ptr(ctx, t, Y)[pos],
+                   plane_ptr(ctx, t, Z)[pos], ix, iy, a, b);
+        plane_ptr(ctx, t, uc)[pos] = a;
+        plane_ptr(ctx, t, vc)[pos] = b;
     }
 };
 
@@ -216,26 +209,28 @@ struct OpUpscale {
     int n;
     int src[8], dst[8];
     float scale;
-    __device__ void operator()(const BatchCtx&, const BatchPair& bp, int, int level, LevelDims f,
+    __device__ void operator()(const BatchCtx& ctx, const TileEntry& t, int level, LevelDims f,
                                int ix, int iy) const {
-        LevelDims c = bp.dims[level + 1];
+        LevelDims c = ctx.pairs[t.pair].dims[level + 1];
         float x = ((float)ix + 0.5f) / (float)f.w;
         float y = ((float)iy + 0.5f) / (float)f.h;
         Taps tx = taps_of(x, c.w);
         Taps ty = taps_of(y, c.h);
         int pos = ix + iy * f.s;
-#pragma unroll 1
-        for (int i = 0; i < n; i++)
-            plane_ptr(bp, dst[i])[pos] = bilerp(plane_ptr(bp, src[i]), c.s, tx, ty) * scale;
+        // fixed trip count: the field indices stay in the parameter bank
+#pragma unroll
+        for (int i = 0; i < 8; i++)
+            if (i < n)
+                plane_ptr(ctx, t, dst[i])[pos] = bilerp(plane_ptr(ctx, t, src[i]), c.s, tx, ty) * scale;
     }
 };
 
 struct OpInvDepth {
     int Z, out;
-    __device__ void operator()(const BatchCtx&, const BatchPair& bp, int, int, LevelDims d, int ix,
+    __device__ void operator()(const BatchCtx& ctx, const TileEntry& t, int, LevelDims d, int ix,
                                int iy) const {
         int pos = ix + iy * d.s;
-        plane_ptr(bp, out)[pos] = 1.0f / plane_ptr(bp, Z)[pos];
+        plane_ptr(ctx, t, out)[pos] = 1.0f / plane_ptr(ctx, t, Z)[pos];
     }
 };
 
@@ -243,17 +238,17 @@ struct OpInvDepth {
 // become u, v (and uproj, vproj) and the 3D state, as rf_solve_warm stages them
 struct OpWarmInit {
     int wu, wv, wX, wY, wZ, u, v, uproj, vproj, X, Y, Z;
-    __device__ void operator()(const BatchCtx&, const BatchPair& bp, int, int, LevelDims d, int ix,
+    __device__ void operator()(const BatchCtx& ctx, const TileEntry& t, int, LevelDims d, int ix,
                                int iy) const {
         int pos = ix + iy * d.s;
-        float a = plane_ptr(bp, wu)[pos], c = plane_ptr(bp, wv)[pos];
-        plane_ptr(bp, u)[pos] = a;
-        plane_ptr(bp, v)[pos] = c;
-        plane_ptr(bp, uproj)[pos] = a;
-        plane_ptr(bp, vproj)[pos] = c;
-        plane_ptr(bp, X)[pos] = plane_ptr(bp, wX)[pos];
-        plane_ptr(bp, Y)[pos] = plane_ptr(bp, wY)[pos];
-        plane_ptr(bp, Z)[pos] = plane_ptr(bp, wZ)[pos];
+        float a = plane_ptr(ctx, t, wu)[pos], c = plane_ptr(ctx, t, wv)[pos];
+        plane_ptr(ctx, t, u)[pos] = a;
+        plane_ptr(ctx, t, v)[pos] = c;
+        plane_ptr(ctx, t, uproj)[pos] = a;
+        plane_ptr(ctx, t, vproj)[pos] = c;
+        plane_ptr(ctx, t, X)[pos] = plane_ptr(ctx, t, wX)[pos];
+        plane_ptr(ctx, t, Y)[pos] = plane_ptr(ctx, t, wY)[pos];
+        plane_ptr(ctx, t, Z)[pos] = plane_ptr(ctx, t, wZ)[pos];
     }
 };
 
@@ -276,11 +271,14 @@ struct rf_batch {
     rf_params p{};
     int n = 0, L = 0;
     std::vector<std::vector<LevelDims>> dims;  // [pair][level]
-    std::vector<size_t> plane, base_off;
-    float* pool = nullptr;
+    std::vector<size_t> plane, base_off;  // per pair: region size and offset in a plane
+    size_t total = 0;                     // floats per plane (every pair's region)
+    float* pool = nullptr;                // n_planes x total floats
     BatchPair* d_pairs = nullptr;
-    int* d_prefix = nullptr;
-    std::vector<int> prefix;  // host copy: [level][n + 1]
+    TileEntry* d_tiles = nullptr;         // every level's tile table, level after level
+    size_t tiles_cap = 0;                 // entries allocated at d_tiles
+    std::vector<size_t> tile_start;       // first entry of each level
+    std::vector<int> prefix;  // [level][n + 1] tile prefix sums
     std::vector<int> tile_w, tile_h;  // tile shape of each level
     LevelConsts* d_consts = nullptr;
     LevelConsts* h_consts = nullptr;
@@ -323,34 +321,73 @@ int rf_batch::warm_idx(int k) const { return base_idx() + rf_batch_impl::P_SPARE
 
 namespace rf_batch_impl {
 
-// per-level prefix sums of tile counts (host copy) for the current tiles
-void fill_prefix(rf_batch* b) {
+// Per-level prefix sums of tile counts and the tile tables for the current
+// tile shapes (row-major tiles of each pair, pairs in order), copied to the
+// device; the caller makes sure no launch is in flight.
+cudaError_t fill_tiles(rf_batch* b) {
     b->prefix.assign((size_t)b->L * (b->n + 1), 0);
-    for (int l = 0; l < b->L; l++)
+    b->tile_start.assign(b->L, 0);
+    std::vector<TileEntry> tab;
+    for (int l = 0; l < b->L; l++) {
+        b->tile_start[l] = tab.size();
+        const int tw = b->tile_w[l], th = b->tile_h[l];
         for (int i = 0; i < b->n; i++) {
             const LevelDims& d = b->dims[i][l];
-            int tiles = ((d.w + b->tile_w[l] - 1) / b->tile_w[l]) *
-                        ((d.h + b->tile_h[l] - 1) / b->tile_h[l]);
-            b->prefix[l * (b->n + 1) + i + 1] = b->prefix[l * (b->n + 1) + i] + tiles;
+            const int nx = (d.w + tw - 1) / tw, ny = (d.h + th - 1) / th;
+            for (int y = 0; y < ny; y++)
+                for (int x = 0; x < nx; x++)
+                    tab.push_back(TileEntry{i, x * tw, y * th, (int)b->base_off[i]});
+            b->prefix[l * (b->n + 1) + i + 1] = b->prefix[l * (b->n + 1) + i] + nx * ny;
         }
+    }
+    if (tab.size() > b->tiles_cap) {
+        if (b->d_tiles) cudaFree(b->d_tiles);
+        b->d_tiles = nullptr;
+        b->tiles_cap = 0;
+        cudaError_t e = cudaMalloc(&b->d_tiles, sizeof(TileEntry) * tab.size());
+        if (e != cudaSuccess) return e;
+        b->tiles_cap = tab.size();
+    }
+    return cudaMemcpy(b->d_tiles, tab.data(), sizeof(TileEntry) * tab.size(),
+                      cudaMemcpyHostToDevice);
 }
 
-BatchCtx ctx_of(rf_batch* b) {
+BatchCtx ctx_of(rf_batch* b, int level) {
     BatchCtx c;
     c.pairs = b->d_pairs;
-    c.prefix = b->d_prefix;
+    c.tiles = b->d_tiles + b->tile_start[level];
     c.consts = b->d_consts;
+    c.pool = b->pool;
+    c.total = b->total;
     c.n = b->n;
     c.L = b->L;
     return c;
+}
+
+// base pointer of plane k (every pair's region of it)
+float* plane_base(rf_batch* b, int k) { return b->pool + (size_t)k * b->total; }
+
+ReconFields fields_of(rf_batch* b, const ReconIdx& r) {
+    ReconFields f{};
+    f.u = plane_base(b, r.u); f.v = plane_base(b, r.v);
+    f.duhat = plane_base(b, r.duhat); f.dvhat = plane_base(b, r.dvhat);
+    f.pu1 = plane_base(b, r.pu1); f.pu2 = plane_base(b, r.pu2);
+    f.pv1 = plane_base(b, r.pv1); f.pv2 = plane_base(b, r.pv2);
+    f.uproj = plane_base(b, r.uproj); f.vproj = plane_base(b, r.vproj);
+    f.sku = plane_base(b, r.sku); f.skv = plane_base(b, r.skv);
+    f.Ix = plane_base(b, r.Ix); f.Iy = plane_base(b, r.Iy); f.Iz = plane_base(b, r.Iz);
+    f.X = plane_base(b, r.X); f.Y = plane_base(b, r.Y); f.Z = plane_base(b, r.Z);
+    f.X1 = plane_base(b, r.X1); f.Y1 = plane_base(b, r.Y1); f.Z1 = plane_base(b, r.Z1);
+    f.uc = plane_base(b, r.uc); f.vc = plane_base(b, r.vc);
+    return f;
 }
 
 template <class Op>
 int launch_op(rf_batch* b, int level, const Op& op) {
     int tiles = b->prefix[level * (b->n + 1) + b->n];
     if (tiles <= 0) return 0;
-    k_batch<Op><<<tiles, dim3(b->tile_w[level], b->tile_h[level]), 0, b->stream>>>(ctx_of(b),
-                                                                                  level, op);
+    const dim3 block(b->tile_w[level], b->tile_h[level]);
+    k_batch<Op><<<tiles, block, 0, b->stream>>>(ctx_of(b, level), level, op);
     b->enq++;
     return cudaGetLastError() == cudaSuccess ? 0 : 1;
 }
@@ -370,10 +407,8 @@ int launch_op(rf_batch* b, int level, const Op& op) {
 
 // zero `count` planes starting at index k for every pair
 rf_status memset_planes(rf_batch* b, std::initializer_list<int> ks) {
-    for (int i = 0; i < b->n; i++)
-        for (int k : ks)
-            BC(cudaMemsetAsync(b->pool + b->base_off[i] + (size_t)k * b->plane[i], 0,
-                               b->plane[i] * sizeof(float), b->stream));
+    for (int k : ks)
+        BC(cudaMemsetAsync(plane_base(b, k), 0, b->total * sizeof(float), b->stream));
     return RF_OK;
 }
 
@@ -382,6 +417,7 @@ rf_status enqueue_batch(rf_batch* b, int kind) {
     const Weights wt = solver_weights(&p);
     const int B0 = b->base_idx();
     auto P = [&](int k) { return B0 + k; };
+    auto PB = [&](int k) { return plane_base(b, k); };
     // pyramid
     for (int l = 1; l < b->L; l++)
         BL(launch_op(b, l, OpDownscale2{b->pI0(l - 1), b->pI1(l - 1), b->pI0(l), b->pI1(l)}));
@@ -413,9 +449,10 @@ rf_status enqueue_batch(rf_batch* b, int kind) {
         for (int warp = 0; warp < n_warps; warp++) {
             BL(launch_op(b, level, OpWarp{b->pI1(level), u, v, P(P_I1W)}));
             BL(launch_op(b, level, OpDeriv{b->pI0(level), P(P_I1W), P(P_IX), P(P_IY), P(P_IZ)}));
-            ReconIdx r{u, v, P(P_DUHAT), P(P_DVHAT), P(P_PU1), P(P_PU2), P(P_PV1), P(P_PV2),
-                       uproj, vproj, sku, skv, P(P_IX), P(P_IY), P(P_IZ), P(P_X), P(P_Y), P(P_Z),
-                       P(P_X1), P(P_Y1), P(P_Z1), uc, vc};
+            const ReconFields r = fields_of(
+                b, ReconIdx{u, v, P(P_DUHAT), P(P_DVHAT), P(P_PU1), P(P_PU2), P(P_PV1), P(P_PV2),
+                            uproj, vproj, sku, skv, P(P_IX), P(P_IY), P(P_IZ), P(P_X), P(P_Y),
+                            P(P_Z), P(P_X1), P(P_Y1), P(P_Z1), uc, vc});
             for (int iter = 0; iter < n_iters; iter++) {
                 const int first = iter == 0;
                 if (recon) {
@@ -435,10 +472,12 @@ rf_status enqueue_batch(rf_batch* b, int kind) {
                 if (rs != RF_OK) return rs;
             }
             if (recon) {
-                BL(launch_op(b, level, OpMedianAdd{P(P_DUHAT), P(P_DVHAT), u, v, tu, tv}));
-                BL(launch_op(b, level, OpMedian5{tu, tv, u, v}));
+                BL(launch_op(b, level, OpMedianAdd{PB(P(P_DUHAT)), PB(P(P_DVHAT)), PB(u), PB(v),
+                                                   PB(tu), PB(tv)}));
+                BL(launch_op(b, level, OpMedian5{PB(tu), PB(tv), PB(u), PB(v)}));
             } else {
-                BL(launch_op(b, level, OpMedianAdd{P(P_DUHAT), P(P_DVHAT), u, v, u, v}));
+                BL(launch_op(b, level, OpMedianAdd{PB(P(P_DUHAT)), PB(P(P_DVHAT)), PB(u), PB(v),
+                                                   PB(u), PB(v)}));
             }
         }
         if (level > 0) {
@@ -510,7 +549,7 @@ rf_status run_batch(rf_batch* b, int kind) {
     return RF_OK;
 }
 
-float* pair_plane(rf_batch* b, int i, int k) { return b->pool + b->base_off[i] + (size_t)k * b->plane[i]; }
+float* pair_plane(rf_batch* b, int i, int k) { return plane_base(b, k) + b->base_off[i]; }
 
 }  // namespace rf_batch_impl
 
@@ -556,31 +595,32 @@ rf_status rf_batch_create(const rf_params* p, int n_pairs, const int* widths, co
         size_t pl = ((size_t)b->dims[i][0].s * (h + 1) + 63) / 64 * 64;
         b->plane.push_back(pl);
         b->base_off.push_back(total);
-        total += pl * b->n_planes;
+        total += pl;
     }
+    // a pixel's element in a plane (pair offset + position) is a 32-bit int
+    if (total > (size_t)INT_MAX) {
+        delete b;
+        return bfail(RF_ERR_INVALID_ARG, "rf_batch_create: batch too large (over 2^31 - 1 "
+                                         "floats per plane)");
+    }
+    b->total = total;
     int ndev = 0;
     if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev < 1) {
         delete b;
         return bfail(RF_ERR_NO_DEVICE, "rf_batch_create: no CUDA device");
     }
-    cudaError_t e = cudaMalloc(&b->pool, total * sizeof(float));
-    if (e == cudaSuccess) e = cudaMemset(b->pool, 0, total * sizeof(float));
+    const size_t pool_floats = total * (size_t)b->n_planes;
+    cudaError_t e = cudaMalloc(&b->pool, pool_floats * sizeof(float));
+    if (e == cudaSuccess) e = cudaMemset(b->pool, 0, pool_floats * sizeof(float));
     std::vector<BatchPair> hp(n_pairs);
-    for (int i = 0; i < n_pairs && e == cudaSuccess; i++) {
-        hp[i].base = b->pool + b->base_off[i];
-        hp[i].plane = b->plane[i];
+    for (int i = 0; i < n_pairs; i++)
         for (int l = 0; l < b->L; l++) hp[i].dims[l] = b->dims[i][l];
-    }
     b->tile_w.assign(b->L, BX);
     b->tile_h.assign(b->L, BY);
-    fill_prefix(b);
+    if (e == cudaSuccess) e = fill_tiles(b);
     if (e == cudaSuccess) e = cudaMalloc(&b->d_pairs, sizeof(BatchPair) * n_pairs);
     if (e == cudaSuccess)
         e = cudaMemcpy(b->d_pairs, hp.data(), sizeof(BatchPair) * n_pairs, cudaMemcpyHostToDevice);
-    if (e == cudaSuccess) e = cudaMalloc(&b->d_prefix, sizeof(int) * b->prefix.size());
-    if (e == cudaSuccess)
-        e = cudaMemcpy(b->d_prefix, b->prefix.data(), sizeof(int) * b->prefix.size(),
-                       cudaMemcpyHostToDevice);
     if (e == cudaSuccess) e = cudaMalloc(&b->d_consts, sizeof(LevelConsts) * n_pairs * b->L);
     if (e == cudaSuccess) e = cudaMallocHost(&b->h_consts, sizeof(LevelConsts) * n_pairs * b->L);
     if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&b->own, cudaStreamNonBlocking);
@@ -603,7 +643,7 @@ rf_status rf_batch_destroy(rf_batch* b) {
     if (b->graph) cudaGraphExecDestroy(b->graph);
     if (b->pool) cudaFree(b->pool);
     if (b->d_pairs) cudaFree(b->d_pairs);
-    if (b->d_prefix) cudaFree(b->d_prefix);
+    if (b->d_tiles) cudaFree(b->d_tiles);
     if (b->d_consts) cudaFree(b->d_consts);
     if (b->d_energy) cudaFree(b->d_energy);
     if (b->h_consts) cudaFreeHost(b->h_consts);
@@ -726,9 +766,7 @@ rf_status rf_batch_set_tiles(rf_batch* b, const int* tile_w, const int* tile_h) 
     BC(cudaStreamSynchronize(b->stream));
     b->tile_w.assign(tile_w, tile_w + b->L);
     b->tile_h.assign(tile_h, tile_h + b->L);
-    fill_prefix(b);
-    BC(cudaMemcpy(b->d_prefix, b->prefix.data(), sizeof(int) * b->prefix.size(),
-                  cudaMemcpyHostToDevice));
+    BC(fill_tiles(b));
     if (b->graph) {
         cudaGraphExecDestroy(b->graph);
         b->graph = nullptr;
@@ -747,10 +785,11 @@ rf_status rf_batch_profile_level(rf_batch* b, int level, int n_iters, float* ms)
     auto P = [&](int k) { return B0 + k; };
     const int u = b->res_u, v = b->res_v;
     // the role planes of the last solve's finest level (values only matter for timing)
-    ReconIdx r{u, v, P(P_DUHAT), P(P_DVHAT), P(P_PU1), P(P_PU2), P(P_PV1), P(P_PV2),
-               P(P_SPARE0 + 4), P(P_SPARE0 + 5), P(P_SPARE0 + 6), P(P_SPARE0 + 7), P(P_IX),
-               P(P_IY), P(P_IZ), P(P_X), P(P_Y), P(P_Z), P(P_X1), P(P_Y1), P(P_Z1),
-               P(P_SPARE0 + 2), P(P_SPARE0 + 3)};
+    const ReconFields r = fields_of(
+        b, ReconIdx{u, v, P(P_DUHAT), P(P_DVHAT), P(P_PU1), P(P_PU2), P(P_PV1), P(P_PV2),
+                    P(P_SPARE0 + 4), P(P_SPARE0 + 5), P(P_SPARE0 + 6), P(P_SPARE0 + 7), P(P_IX),
+                    P(P_IY), P(P_IZ), P(P_X), P(P_Y), P(P_Z), P(P_X1), P(P_Y1), P(P_Z1),
+                    P(P_SPARE0 + 2), P(P_SPARE0 + 3)});
     for (int k = 0; k < 2; k++) {
         cudaGraph_t g = nullptr;
         cudaGraphExec_t ge = nullptr;

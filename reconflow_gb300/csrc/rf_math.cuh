@@ -93,21 +93,21 @@ __device__ __forceinline__ void l1_threshold(float dusub, float dvsub, float dix
     float rho = (dix * dusub + diy * dvsub + dit);
     float upper = lambda * (dix * dix + diy * diy) / A;
     float lower = -upper;  // == -lambda*g/A exactly (negation is exact)
-    du = dusub;
-    dv = dvsub;
-    if ((rho <= upper) && (rho >= lower)) {
-        float magi = dix * dix + diy * diy;
-        if (magi != 0) {
-            du = dusub - rho * dix / magi;
-            dv = dvsub - rho * diy / magi;
-        }
-    } else if (rho < lower) {
-        du = dusub + lambda * dix / A;
-        dv = dvsub + lambda * diy / A;
-    } else if (rho > upper) {
-        du = dusub - lambda * dix / A;
-        dv = dvsub - lambda * diy / A;
-    }
+    // The three branches differ only in the numerator factor, the divisor and
+    // the sign of the step, so each component takes one division whichever
+    // branch its pixel is in (a warp whose pixels diverge would otherwise run
+    // the divisions of every branch); every value is formed exactly as the
+    // branch formulas form it.
+    const bool inside = (rho <= upper) && (rho >= lower);
+    const float magi = dix * dix + diy * diy;
+    const bool step = inside ? (magi != 0) : (rho < lower || rho > upper);  // NaN rho: no step
+    const float fac = inside ? rho : lambda;
+    const float den = inside ? magi : A;
+    const float qu = fac * dix / (step ? den : 1.0f);
+    const float qv = fac * diy / (step ? den : 1.0f);
+    const bool plus = !inside && (rho < lower);
+    du = !step ? dusub : (plus ? dusub + qu : dusub - qu);
+    dv = !step ? dvsub : (plus ? dvsub + qv : dvsub - qv);
 }
 
 // Plain TV-L1 threshold step (solveDataL1.cu:27-51); lt = lambda*theta.

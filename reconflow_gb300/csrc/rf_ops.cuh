@@ -30,12 +30,14 @@ __device__ __forceinline__ float deriv5(float m2, float m1, float p1, float p2) 
     return t;
 }
 
+// `base`: element of the level's pixel (0, 0) in every field (0 for a
+// single pair; a pair's offset in the batched solver's planes).
 template <int PRIOR>
 __device__ __forceinline__ void recon_a_px(const ReconFields& f, const LevelConsts& c,
                                            const Weights& wt, LevelDims d, int ix, int iy,
-                                           int first, int uc_from_buffer) {
+                                           int first, int uc_from_buffer, int base = 0) {
     const int s = d.s;
-    const int pos = ix + iy * s;
+    const int pos = base + ix + iy * s;
 
     // Every load of the pixel is issued before any arithmetic or store, so a
     // thread waits for memory once.  The kernel writes only duhat, uproj and
@@ -157,9 +159,9 @@ __device__ __forceinline__ int median3_tap(int col, int row, int w, int h, int s
 // ReconFlow inner iteration, part B: dual step, 3D median, clean-up, sk
 // ---------------------------------------------------------------------------
 __device__ __forceinline__ void recon_b_px(const ReconFields& f, const Weights& wt, LevelDims d,
-                                           int ix, int iy, int first) {
+                                           int ix, int iy, int first, int base = 0) {
     const int s = d.s, w = d.w, h = d.h;
-    const int pos = ix + iy * s;
+    const int pos = base + ix + iy * s;
 
     // All loads first (see recon_a_px): the kernel writes p, X and sk only at
     // its own pixel and reads p and sk only there, and reads no X.
@@ -200,9 +202,9 @@ __device__ __forceinline__ void recon_b_px(const ReconFields& f, const Weights& 
             for (int i = 0; i < 3; i++) {
                 int at = median3_tap(ix + i - 1, iy + j - 1, w, h, s);
                 int k = j * 3 + i;
-                mX[k] = at >= 0 ? f.X1[at] : 0.0f;
-                mY[k] = at >= 0 ? f.Y1[at] : 0.0f;
-                mZ[k] = at >= 0 ? f.Z1[at] : 0.0f;
+                mX[k] = at >= 0 ? f.X1[base + at] : 0.0f;
+                mY[k] = at >= 0 ? f.Y1[base + at] : 0.0f;
+                mZ[k] = at >= 0 ? f.Z1[base + at] : 0.0f;
             }
         }
     }
@@ -261,17 +263,18 @@ __device__ __forceinline__ int median5_tap(int col, int row, int w, int h, int s
     return -1;
 }
 
+// `base` as recon_a_px
 __device__ __forceinline__ void median5_pair(const float* __restrict__ a,
                                              const float* __restrict__ b, int ix, int iy,
-                                             LevelDims d, float& ma, float& mb) {
+                                             LevelDims d, float& ma, float& mb, int base = 0) {
     float mu[25], mv[25];
 #pragma unroll
     for (int j = 0; j < 5; j++) {
 #pragma unroll
         for (int i = 0; i < 5; i++) {
             int at = median5_tap(ix + i - 2, iy + j - 2, d.w, d.h, d.s);
-            mu[j * 5 + i] = at >= 0 ? a[at] : 0.0f;
-            mv[j * 5 + i] = at >= 0 ? b[at] : 0.0f;
+            mu[j * 5 + i] = at >= 0 ? a[base + at] : 0.0f;
+            mv[j * 5 + i] = at >= 0 ? b[base + at] : 0.0f;
         }
     }
     ma = median25(mu);
