@@ -293,7 +293,9 @@ struct rf_batch {
     std::vector<int> warm_warps, warm_iters;
     std::vector<int> graph_sched;  // the warm schedule the graph was captured with
     std::vector<double> last_R1, last_t1;  // pose of the last solve, [pair][9], [pair][3]
-    double* d_energy = nullptr;            // [pair][1 + kEnergyBlocks]
+    double* d_energy = nullptr;            // [pair][kEnergyMaxBlocks] partials, then [pair] sums
+    EnergyJob* d_ejobs = nullptr;          // [pair]
+    EnergyJob* h_ejobs = nullptr;          // pinned staging of d_ejobs
     uint64_t launches = 0, graph_nodes = 0, enq = 0;
     int res_u = -1, res_v = -1;
     bool solved = false;
@@ -313,7 +315,6 @@ enum {
 };
 constexpr int kSpares = 18;
 constexpr int kWarmPlanes = 5;
-constexpr int kEnergyBlocks = 1024;
 
 }  // namespace rf_batch_impl
 
@@ -646,6 +647,8 @@ rf_status rf_batch_destroy(rf_batch* b) {
     if (b->d_tiles) cudaFree(b->d_tiles);
     if (b->d_consts) cudaFree(b->d_consts);
     if (b->d_energy) cudaFree(b->d_energy);
+    if (b->d_ejobs) cudaFree(b->d_ejobs);
+    if (b->h_ejobs) cudaFreeHost(b->h_ejobs);
     if (b->h_consts) cudaFreeHost(b->h_consts);
     if (b->own) cudaStreamDestroy(b->own);
     delete b;
@@ -735,22 +738,36 @@ rf_status rf_batch_energies(rf_batch* b, double* out) {
     if (!b || !out) return bfail(RF_ERR_INVALID_ARG, "rf_batch_energies: null argument");
     if (!b->solved || b->p.method == RF_METHOD_TVL1 || b->last_R1.size() != (size_t)9 * b->n)
         return bfail(RF_ERR_STATE, "rf_batch_energies: needs a ReconFlow solve");
-    if (!b->d_energy) BC(cudaMalloc(&b->d_energy, sizeof(double) * b->n * (1 + kEnergyBlocks)));
+    if (!b->d_energy) BC(cudaMalloc(&b->d_energy, sizeof(double) * b->n * (kEnergyMaxBlocks + 1)));
+    if (!b->d_ejobs) BC(cudaMalloc(&b->d_ejobs, sizeof(EnergyJob) * b->n));
+    if (!b->h_ejobs) BC(cudaMallocHost(&b->h_ejobs, sizeof(EnergyJob) * b->n));
+    BC(cudaStreamSynchronize(b->stream));  // the staging buffer is free to refill
     const int B0 = b->base_idx();
+    double* sums = b->d_energy + (size_t)b->n * kEnergyMaxBlocks;
+    int blocks = 0;
+    // every pair's evaluation in one launch (blocks in pair order) and the
+    // sums in a second; each pair's value is its single-pair evaluation's
     for (int i = 0; i < b->n; i++) {
-        const LevelDims& d = b->dims[i][0];
-        const int nb = std::min(kEnergyBlocks, (d.w * d.h + 255) / 256);
-        double* e = b->d_energy + (size_t)i * (1 + kEnergyBlocks);
-        if (launch_energy(pair_plane(b, i, b->pI0(0)), pair_plane(b, i, b->pI1(0)),
+        EnergyJob& j = b->h_ejobs[i];
+        j.a = energy_args(pair_plane(b, i, b->pI0(0)), pair_plane(b, i, b->pI1(0)),
                           pair_plane(b, i, b->res_u), pair_plane(b, i, b->res_v),
                           pair_plane(b, i, B0 + P_X), pair_plane(b, i, B0 + P_Y),
-                          pair_plane(b, i, B0 + P_Z), d, b->p.lambda, b->p.alpha_proj,
+                          pair_plane(b, i, B0 + P_Z), b->p.lambda, b->p.alpha_proj,
                           &b->last_R1[(size_t)9 * i], &b->last_t1[(size_t)3 * i],
-                          &b->K1[(size_t)9 * i], 1, e + 1, nb, e, b->stream) != 0)
-            return bfail(RF_ERR_CUDA, "rf_batch_energies: launch");
-        b->launches += 2;
-        BC(cudaMemcpyAsync(out + i, e, sizeof(double), cudaMemcpyDeviceToHost, b->stream));
+                          &b->K1[(size_t)9 * i], 1);
+        j.d = b->dims[i][0];
+        j.nblocks = energy_blocks(j.d);
+        j.first_block = blocks;
+        j.partial = b->d_energy + (size_t)i * kEnergyMaxBlocks;
+        j.out = sums + i;
+        blocks += j.nblocks;
     }
+    BC(cudaMemcpyAsync(b->d_ejobs, b->h_ejobs, sizeof(EnergyJob) * b->n, cudaMemcpyHostToDevice,
+                       b->stream));
+    if (launch_energy_jobs(b->d_ejobs, b->n, blocks, b->stream) != 0)
+        return bfail(RF_ERR_CUDA, "rf_batch_energies: launch");
+    b->launches += 2;
+    BC(cudaMemcpyAsync(out, sums, sizeof(double) * b->n, cudaMemcpyDeviceToHost, b->stream));
     BC(cudaStreamSynchronize(b->stream));
     return RF_OK;
 }

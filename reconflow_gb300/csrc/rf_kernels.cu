@@ -340,21 +340,16 @@ __global__ void k_flow_color(const float* __restrict__ u, const float* __restric
 // Energy of a solution on level 0 (no reference counterpart; see
 // rf_energy): per-block double partial sums, then one block adds the
 // partials in a fixed order, so the result is deterministic.
-struct EnergyArgs {
-    const float *I0, *I1, *u, *v, *X, *Y, *Z;
-    float R1f[9], t1f[3], fxf, cxf, cyf;
-    float lambda, alpha_proj;
-    int recon;
-};
-
 constexpr int kEnergyThreads = 256;
 
-__global__ void __launch_bounds__(kEnergyThreads) k_energy_partial(EnergyArgs a, LevelDims d,
-                                                                   double* partial) {
+// Block `blk` of `nblk` of one energy evaluation: its grid-stride share of
+// the pixels, summed in double in a fixed order, into partial[blk].
+__device__ __forceinline__ void energy_block(const EnergyArgs& a, LevelDims d, int blk, int nblk,
+                                             double* partial) {
     __shared__ double red[kEnergyThreads / 32];
     double e = 0.0;
     const int npx = d.w * d.h;
-    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < npx; i += gridDim.x * blockDim.x) {
+    for (int i = blk * kEnergyThreads + threadIdx.x; i < npx; i += nblk * kEnergyThreads) {
         const int ix = i % d.w, iy = i / d.w, s = d.s, pos = ix + iy * s;
         float x = ((float)ix + a.u[pos] + 0.5f) / (float)d.w;
         float y = ((float)iy + a.v[pos] + 0.5f) / (float)d.h;
@@ -389,18 +384,50 @@ __global__ void __launch_bounds__(kEnergyThreads) k_energy_partial(EnergyArgs a,
     if (threadIdx.x == 0) {
         double t = 0.0;
         for (int k = 0; k < kEnergyThreads / 32; k++) t += red[k];
-        partial[blockIdx.x] = t;
+        partial[blk] = t;
     }
+}
+
+__global__ void __launch_bounds__(kEnergyThreads) k_energy_partial(EnergyArgs a, LevelDims d,
+                                                                   double* partial) {
+    energy_block(a, d, blockIdx.x, gridDim.x, partial);
 }
 
 // One warp: lane l adds partials l, l + 32, ... in order, then a fixed
 // shuffle tree adds the 32 lane sums, so the result is deterministic.
-__global__ void k_energy_final(const double* partial, int n, double* out) {
+__device__ __forceinline__ void energy_final(const double* partial, int n, double* out) {
     const int lane = threadIdx.x;
     double t = 0.0;
     for (int k = lane; k < n; k += 32) t += partial[k];
     for (int o = 16; o > 0; o >>= 1) t += __shfl_down_sync(0xffffffffu, t, o);
     if (lane == 0) *out = t;
+}
+
+__global__ void k_energy_final(const double* partial, int n, double* out) {
+    energy_final(partial, n, out);
+}
+
+// Many evaluations in one launch: block b belongs to the job whose block
+// range holds it and does that job's block b - first_block, so every job's
+// partials and sum are the ones its own two launches would make.
+__global__ void __launch_bounds__(kEnergyThreads) k_energy_partial_jobs(const EnergyJob* jobs,
+                                                                        int n) {
+    const int b = blockIdx.x;
+    int lo = 0, hi = n - 1;
+    while (lo < hi) {
+        const int mid = (lo + hi + 1) >> 1;
+        if (jobs[mid].first_block <= b)
+            lo = mid;
+        else
+            hi = mid - 1;
+    }
+    const EnergyJob& j = jobs[lo];
+    energy_block(j.a, j.d, b - j.first_block, j.nblocks, j.partial);
+}
+
+__global__ void k_energy_final_jobs(const EnergyJob* jobs) {
+    const EnergyJob& j = jobs[blockIdx.x];
+    energy_final(j.partial, j.nblocks, j.out);
 }
 
 // ---------------------------------------------------------------------------
@@ -564,10 +591,10 @@ int launch_flow_color(const float* u, const float* v, LevelDims d, float flow_sc
 }  // namespace rf
 
 namespace rf {
-int launch_energy(const float* I0, const float* I1, const float* u, const float* v,
-                  const float* X, const float* Y, const float* Z, LevelDims d, float lambda,
-                  float alpha_proj, const double* R1, const double* t1, const double* K1,
-                  int recon, double* partial, int nblocks, double* out, cudaStream_t st) {
+EnergyArgs energy_args(const float* I0, const float* I1, const float* u, const float* v,
+                       const float* X, const float* Y, const float* Z, float lambda,
+                       float alpha_proj, const double* R1, const double* t1, const double* K1,
+                       int recon) {
     EnergyArgs a;
     a.I0 = I0; a.I1 = I1; a.u = u; a.v = v; a.X = X; a.Y = Y; a.Z = Z;
     for (int i = 0; i < 9; i++) a.R1f[i] = (float)(R1 ? R1[i] : (i % 4 == 0 ? 1.0 : 0.0));
@@ -578,8 +605,28 @@ int launch_energy(const float* I0, const float* I1, const float* u, const float*
     a.lambda = lambda;
     a.alpha_proj = alpha_proj;
     a.recon = recon;
+    return a;
+}
+
+int launch_energy(const float* I0, const float* I1, const float* u, const float* v,
+                  const float* X, const float* Y, const float* Z, LevelDims d, float lambda,
+                  float alpha_proj, const double* R1, const double* t1, const double* K1,
+                  int recon, double* partial, int nblocks, double* out, cudaStream_t st) {
+    const EnergyArgs a = energy_args(I0, I1, u, v, X, Y, Z, lambda, alpha_proj, R1, t1, K1, recon);
     k_energy_partial<<<nblocks, kEnergyThreads, 0, st>>>(a, d, partial);
     k_energy_final<<<1, 32, 0, st>>>(partial, nblocks, out);
+    return check_launch();
+}
+
+int energy_blocks(LevelDims d) {
+    const int nb = (d.w * d.h + kEnergyThreads - 1) / kEnergyThreads;
+    return nb < kEnergyMaxBlocks ? nb : kEnergyMaxBlocks;
+}
+
+int launch_energy_jobs(const EnergyJob* jobs, int n, int total_blocks, cudaStream_t st) {
+    if (n <= 0 || total_blocks <= 0) return 0;
+    k_energy_partial_jobs<<<total_blocks, kEnergyThreads, 0, st>>>(jobs, n);
+    k_energy_final_jobs<<<n, 32, 0, st>>>(jobs);
     return check_launch();
 }
 }  // namespace rf

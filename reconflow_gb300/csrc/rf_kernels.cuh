@@ -106,6 +106,36 @@ int launch_upscale_fields(int n, const float* const* src, float* const* dst, con
 int launch_upscale(const float* src, LevelDims coarse, LevelDims fine, float scale, float* out,
                    cudaStream_t st);
 int launch_inv_depth(const float* Z, LevelDims d, float* out, cudaStream_t st);
+// Arguments of one solution-energy evaluation (float copies of the pose
+// and intrinsics, as the per-pixel terms use them).
+struct EnergyArgs {
+    const float *I0, *I1, *u, *v, *X, *Y, *Z;
+    float R1f[9], t1f[3], fxf, cxf, cyf;
+    float lambda, alpha_proj;
+    int recon;
+};
+EnergyArgs energy_args(const float* I0, const float* I1, const float* u, const float* v,
+                       const float* X, const float* Y, const float* Z, float lambda,
+                       float alpha_proj, const double* R1, const double* t1, const double* K1,
+                       int recon);
+
+// One evaluation of a batched energy launch: its blocks are
+// [first_block, first_block + nblocks) of the launch.
+struct EnergyJob {
+    EnergyArgs a;
+    LevelDims d;
+    int nblocks, first_block;
+    double* partial;  // nblocks doubles
+    double* out;
+};
+
+constexpr int kEnergyMaxBlocks = 1024;
+// blocks of one evaluation of a level of these dimensions
+int energy_blocks(LevelDims d);
+// every job of the device array `jobs` (blocks in job order, total_blocks in
+// all): the same partials and sums as launch_energy of each job alone
+int launch_energy_jobs(const EnergyJob* jobs, int n, int total_blocks, cudaStream_t st);
+
 // Solution energy on one level (data + TV + reprojection) into *out (device
 // double); `partial` holds `nblocks` doubles.
 int launch_energy(const float* I0, const float* I1, const float* u, const float* v,

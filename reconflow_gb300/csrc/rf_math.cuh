@@ -379,21 +379,34 @@ __device__ __forceinline__ void sortnet25(float (&s)[25], std::integer_sequence<
     (cmp_exchange<sortnet25_count_or_pair(C, 0), sortnet25_count_or_pair(C, 1)>(s), ...);
 }
 
-// Median of 25 with the min/max network above.  For inputs without NaN its
-// value equals the exchange selection's except possibly the sign of a zero
-// result, so a NaN input or a zero result is recomputed with the reference's
-// exchange order (median25_exchange), and the result is bit-identical.
-__device__ __forceinline__ float median25(float (&m)[25]) {
+// Median of 25 with the min/max network above, sorting `s` in place.  For
+// inputs without NaN the network's key 12 is the value the exchange
+// selection (median25_exchange) returns, except possibly for the sign of a
+// zero; returns false when that answer is not certain (a NaN input or a zero
+// result), and the caller then takes the exchange path on the inputs.
+__device__ __forceinline__ bool median25_net(float (&s)[25], float& out) {
     bool nan_in = false;
 #pragma unroll
-    for (int k = 0; k < 25; k++) nan_in |= isnan(m[k]);
-    if (!nan_in) {
-        float s[25];
+    for (int k = 0; k < 25; k++) nan_in |= isnan(s[k]);
+    if (nan_in) return false;
+    sortnet25(s, std::make_integer_sequence<int, kSortNet25>{});
+    out = s[12];
+    return out != 0.0f;
+}
+
+// The exchange selection's answer when median25_net gave none: a zero result
+// whose inputs hold zeros of one sign only is that zero (the selection moves
+// values, it never makes one); otherwise the exchange order decides.
+__device__ __forceinline__ float median25_resolve(float (&m)[25]) {
+    bool nan_in = false, pos0 = false, neg0 = false;
 #pragma unroll
-        for (int k = 0; k < 25; k++) s[k] = m[k];
-        sortnet25(s, std::make_integer_sequence<int, kSortNet25>{});
-        if (s[12] != 0.0f) return s[12];
+    for (int k = 0; k < 25; k++) {
+        nan_in |= isnan(m[k]);
+        const unsigned b = __float_as_uint(m[k]);
+        pos0 |= b == 0u;
+        neg0 |= b == 0x80000000u;
     }
+    if (!nan_in && !(pos0 && neg0)) return neg0 ? -0.0f : 0.0f;
     return median25_exchange(m);
 }
 

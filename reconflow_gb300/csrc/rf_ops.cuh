@@ -263,25 +263,49 @@ __device__ __forceinline__ int median5_tap(int col, int row, int w, int h, int s
     return -1;
 }
 
-// `base` as recon_a_px
+// The 5x5 window of a field around (ix, iy) with the reference's border
+// rules (medianFilter.cu:26-53): taps off the image clamp to the nearest
+// row / column; off both, 0.  `base` as recon_a_px.
+__device__ __forceinline__ void load_window25(const float* __restrict__ a, int ix, int iy,
+                                              LevelDims d, int base, bool interior,
+                                              float (&m)[25]) {
+    if (interior) {
+        const float* p = a + base + ix + iy * d.s;
+#pragma unroll
+        for (int j = 0; j < 5; j++)
+#pragma unroll
+            for (int i = 0; i < 5; i++) m[j * 5 + i] = p[(i - 2) + (j - 2) * d.s];
+    } else {
+#pragma unroll
+        for (int j = 0; j < 5; j++)
+#pragma unroll
+            for (int i = 0; i < 5; i++) {
+                int at = median5_tap(ix + i - 2, iy + j - 2, d.w, d.h, d.s);
+                m[j * 5 + i] = at >= 0 ? a[base + at] : 0.0f;
+            }
+    }
+}
+
+// Exchange-path median of a window, re-read from memory (kept out of line:
+// it runs only for NaN inputs or a zero result).
+__device__ __noinline__ float median25_slow(const float* __restrict__ a, int ix, int iy,
+                                            LevelDims d, int base, bool interior) {
+    float m[25];
+    load_window25(a, ix, iy, d, base, interior, m);
+    return median25_resolve(m);
+}
+
+// MedianFilterKernel5 (medianFilter.cu:3-76) of two fields at one pixel.
 __device__ __forceinline__ void median5_pair(const float* __restrict__ a,
                                              const float* __restrict__ b, int ix, int iy,
                                              LevelDims d, float& ma, float& mb, int base = 0) {
+    const bool interior = ix >= 2 && iy >= 2 && ix + 2 < d.w && iy + 2 < d.h;
     float mu[25], mv[25];
-#pragma unroll
-    for (int j = 0; j < 5; j++) {
-#pragma unroll
-        for (int i = 0; i < 5; i++) {
-            int at = median5_tap(ix + i - 2, iy + j - 2, d.w, d.h, d.s);
-            mu[j * 5 + i] = at >= 0 ? a[base + at] : 0.0f;
-            mv[j * 5 + i] = at >= 0 ? b[base + at] : 0.0f;
-        }
-    }
-    ma = median25(mu);
-    mb = median25(mv);
+    load_window25(a, ix, iy, d, base, interior, mu);
+    load_window25(b, ix, iy, d, base, interior, mv);
+    if (!median25_net(mu, ma)) ma = median25_slow(a, ix, iy, d, base, interior);
+    if (!median25_net(mv, mb)) mb = median25_slow(b, ix, iy, d, base, interior);
 }
-
-
 
 // warpImage.cu:15-29
 __device__ __forceinline__ void warp_px(const float* __restrict__ I1, const float* __restrict__ u,

@@ -782,7 +782,7 @@ rf_status rf_energy(rf_handle* h, double* energy) {
     if (!h->solved) return fail(RF_ERR_STATE, "rf_energy: no solve has run");
     const bool recon = h->p.method != RF_METHOD_TVL1;
     LevelDims d{h->W[0], h->H[0], h->S[0]};
-    const int nb = std::min(1024, (d.w * d.h + 255) / 256);
+    const int nb = energy_blocks(d);
     if (launch_energy(h->I0[0], h->I1[0], h->res_u, h->res_v, recon ? h->X : nullptr,
                       recon ? h->Y : nullptr, recon ? h->Z : nullptr, d, h->p.lambda,
                       h->p.alpha_proj, recon ? h->last_R1 : nullptr, recon ? h->last_t1 : nullptr,

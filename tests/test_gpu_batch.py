@@ -56,6 +56,7 @@ def test_batch_recon_matches_single_pair(oracle, rf, fix):
         b.setCameraMatrices(i, K, K)
         b.copyImagesToDevice(i, pad_rows(I0, s), pad_rows(I1, s))
     b.solveR([d[5] for d in data], [d[6] for d in data])
+    E = b.energies()  # one batched evaluation of every pair
     for i, (w, h, I0, I1, K, R, t) in enumerate(data):
         s = align_up(w)
         got_u, got_v = b.copyOpticalFlowToHost(i)
@@ -70,6 +71,8 @@ def test_batch_recon_matches_single_pair(oracle, rf, fix):
         X1, Y1, Z1 = f.copy3dToHost()
         for a, c, nm in ((got_u, u1, "u"), (got_v, v1, "v"), (X, X1, "X"), (Y, Y1, "Y"), (Z, Z1, "Z")):
             assert_bitexact(a, c, f"pair {i} {nm}", region=(h, w))
+        e1 = f.energy()
+        assert np.float64(E[i]).tobytes() == np.float64(e1).tobytes(), (i, E[i], e1)
         if i == 2:
             p = oracle.make_params(w, h, L, lam=50.0, lambdaf=0.1, lambdams=100.0,
                                    alpha_tv=1 / 0.33, alpha_proj=60.0, tau=0.25,

@@ -59,6 +59,33 @@ def test_median5_bitexact(oracle, rf, torch_cuda, w, h, s):
         assert_bitexact(got.reshape(h + 1, s), want.reshape(h + 1, s), nm, region=(h, w))
 
 
+@pytest.mark.parametrize("case", ["pos_zero", "neg_zero", "mixed_zero", "nan"])
+def test_median5_zero_nan_bitexact(oracle, rf, torch_cuda, case):
+    """Windows whose median is a zero of one sign, of both signs, and windows
+    holding NaN (the exchange order decides those results), in the interior
+    and at the borders."""
+    w, h, s = 70, 45, 96
+    rng = np.random.default_rng(len(case))
+    n = (h + 1) * s
+    u = rng.integers(-2, 3, n).astype(np.float32)
+    v = rng.normal(size=n).astype(np.float32)
+    zero = u == 0
+    if case == "neg_zero":
+        u[zero] = -0.0
+    elif case == "mixed_zero":
+        u[zero & (rng.random(n) < 0.5)] = -0.0
+    elif case == "nan":
+        u[rng.random(n) < 0.04] = np.nan
+        v[rng.random(n) < 0.04] = np.nan
+    lib = rf.load()
+    du, dv = dev(torch_cuda, u), dev(torch_cuda, v)
+    ou, ov = torch_cuda.zeros_like(du), torch_cuda.zeros_like(dv)
+    ok(rf, lib.rfk_median5(P(du), P(dv), w, h, s, P(ou), P(ov), None))
+    wu, wv = oracle.median5(u, v, w, h, s)
+    for got, want, nm in ((host(ou), wu, "u"), (host(ov), wv, "v")):
+        assert_bitexact(got.reshape(h + 1, s), want.reshape(h + 1, s), nm, region=(h, w))
+
+
 @pytest.mark.parametrize("w,h,s", SIZES)
 def test_median3d_bitexact(oracle, rf, torch_cuda, w, h, s):
     rng = np.random.default_rng(w * 11 + h)
