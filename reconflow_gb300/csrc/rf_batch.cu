@@ -19,6 +19,7 @@
 // solved alone.
 #include <algorithm>
 #include <climits>
+#include <cstdlib>
 #include <cstring>
 #include <string>
 #include <vector>
@@ -74,6 +75,34 @@ __global__ void __launch_bounds__(kMaxTile) k_batch(BatchCtx ctx, int level, Op 
     const int ix = t.x0 + (int)threadIdx.x, iy = t.y0 + (int)threadIdx.y;
     if (ix >= d.w || iy >= d.h) return;
     op(ctx, t, level, d, ix, iy);
+}
+
+// Two operations in one launch on disjoint tile ranges of the level's table
+// (x: [x0, x0 + nx), y: [y0, y0 + ny)), their blocks interleaved (x, y, x,
+// y, ..., then the rest of the longer range) so that every SM holds blocks
+// of both: the instruction-bound data step of one pair group runs beside
+// the memory-bound dual step of the other.
+template <class OpX, class OpY>
+__global__ void __launch_bounds__(kMaxTile) k_batch_pair(BatchCtx ctx, int level, OpX opx, int x0,
+                                                         int nx, OpY opy, int y0, int ny) {
+    const int b = blockIdx.x, m = nx < ny ? nx : ny;
+    bool is_x;
+    int k;
+    if (b < 2 * m) {
+        is_x = (b & 1) == 0;
+        k = b >> 1;
+    } else {
+        is_x = nx > ny;
+        k = b - m;
+    }
+    const TileEntry t = ctx.tiles[is_x ? x0 + k : y0 + k];
+    const LevelDims d = ctx.pairs[t.pair].dims[level];
+    const int ix = t.x0 + (int)threadIdx.x, iy = t.y0 + (int)threadIdx.y;
+    if (ix >= d.w || iy >= d.h) return;
+    if (is_x)
+        opx(ctx, t, level, d, ix, iy);
+    else
+        opy(ctx, t, level, d, ix, iy);
 }
 
 // ---- per-step operations (plane indices resolved per pair) ----------------
@@ -298,6 +327,9 @@ struct rf_batch {
     EnergyJob* h_ejobs = nullptr;          // pinned staging of d_ejobs
     uint64_t launches = 0, graph_nodes = 0, enq = 0;
     int res_u = -1, res_v = -1;
+    // pipelined inner iterations (pairs [0, split) and [split, n) half an
+    // iteration apart); 0 = every inner half-iteration over all pairs at once
+    int split = 0;
     bool solved = false;
     int n_planes = 0;
     // plane indices
@@ -393,6 +425,43 @@ int launch_op(rf_batch* b, int level, const Op& op) {
     return cudaGetLastError() == cudaSuccess ? 0 : 1;
 }
 
+// Tile range of pair group g at `level`: group 0 = pairs [0, split), group
+// 1 = pairs [split, n).
+void group_tiles(const rf_batch* b, int level, int g, int& begin, int& count) {
+    const int* pre = &b->prefix[(size_t)level * (b->n + 1)];
+    const int lo = g == 0 ? 0 : b->split, hi = g == 0 ? b->split : b->n;
+    begin = pre[lo];
+    count = pre[hi] - pre[lo];
+}
+
+// `op` over the tiles of pair group g only
+template <class Op>
+int launch_group(rf_batch* b, int level, int g, const Op& op) {
+    int begin, count;
+    group_tiles(b, level, g, begin, count);
+    if (count <= 0) return 0;
+    BatchCtx c = ctx_of(b, level);
+    c.tiles += begin;
+    const dim3 block(b->tile_w[level], b->tile_h[level]);
+    k_batch<Op><<<count, block, 0, b->stream>>>(c, level, op);
+    b->enq++;
+    return cudaGetLastError() == cudaSuccess ? 0 : 1;
+}
+
+// `x` over pair group gx and `y` over the other group, in one launch
+template <class OpX, class OpY>
+int launch_pair(rf_batch* b, int level, int gx, const OpX& x, const OpY& y) {
+    int xb, nx, yb, ny;
+    group_tiles(b, level, gx, xb, nx);
+    group_tiles(b, level, 1 - gx, yb, ny);
+    if (nx + ny <= 0) return 0;
+    const dim3 block(b->tile_w[level], b->tile_h[level]);
+    k_batch_pair<OpX, OpY><<<nx + ny, block, 0, b->stream>>>(ctx_of(b, level), level, x, xb, nx,
+                                                             y, yb, ny);
+    b->enq++;
+    return cudaGetLastError() == cudaSuccess ? 0 : 1;
+}
+
 #define BL(expr)                                                                       \
     do {                                                                               \
         if ((expr) != 0)                                                               \
@@ -454,7 +523,24 @@ rf_status enqueue_batch(rf_batch* b, int kind) {
                 b, ReconIdx{u, v, P(P_DUHAT), P(P_DVHAT), P(P_PU1), P(P_PU2), P(P_PV1), P(P_PV2),
                             uproj, vproj, sku, skv, P(P_IX), P(P_IY), P(P_IZ), P(P_X), P(P_Y),
                             P(P_Z), P(P_X1), P(P_Y1), P(P_Z1), uc, vc});
-            for (int iter = 0; iter < n_iters; iter++) {
+            if (recon && b->split > 0 && n_iters > 0) {
+                // the two pair groups one half-iteration apart: each launch
+                // runs one group's data step (A) beside the other's dual step
+                // (B); every pair still sees A, B, A, B, ... in order
+                const int u0 = ucb ? 1 : 0;
+                BL(launch_group(b, level, 0, OpReconA{r, wt, 1, u0}));
+                for (int iter = 0; iter < n_iters; iter++) {
+                    const int first = iter == 0;
+                    BL(launch_pair(b, level, 0, OpReconB{r, wt, first},
+                                   OpReconA{r, wt, first, first ? u0 : 0}));
+                    if (iter + 1 < n_iters)
+                        BL(launch_pair(b, level, 0, OpReconA{r, wt, 0, 0}, OpReconB{r, wt, first}));
+                    else
+                        BL(launch_group(b, level, 1, OpReconB{r, wt, first}));
+                }
+                ucb = false;
+            }
+            for (int iter = 0; iter < n_iters && !(recon && b->split > 0); iter++) {
                 const int first = iter == 0;
                 if (recon) {
                     BL(launch_op(b, level, OpReconA{r, wt, first, ucb ? 1 : 0}));
@@ -618,6 +704,11 @@ rf_status rf_batch_create(const rf_params* p, int n_pairs, const int* widths, co
         for (int l = 0; l < b->L; l++) hp[i].dims[l] = b->dims[i][l];
     b->tile_w.assign(b->L, BX);
     b->tile_h.assign(b->L, BY);
+    {
+        const char* e = std::getenv("RF_BATCH_PIPELINE");
+        const bool on = !(e && e[0] == '0');
+        b->split = on && n_pairs >= 2 ? n_pairs / 2 : 0;
+    }
     if (e == cudaSuccess) e = fill_tiles(b);
     if (e == cudaSuccess) e = cudaMalloc(&b->d_pairs, sizeof(BatchPair) * n_pairs);
     if (e == cudaSuccess)
