@@ -83,6 +83,12 @@ WORKLOADS = {
     # 3.7 M pixels per launch, above the L2 size)
     "720p-x4-l0": dict(pairs=4, sizes=[(1280, 720)], levels=1, warps=1, iters=4, seed=2000,
                        tiles="reconflow_gb300/tuning/gb300_720p_x64.json"),
+    # pose front end (CameraPose): 64 pairs of 1280x720, features, matching,
+    # LMedS and pose recovery per pair, 8 handles on 8 host threads / streams;
+    # Hessian threshold 20 for the generator's texture (the reference's 2000
+    # is for camera images)
+    "pose-720p": dict(width=1280, height=720, pairs=64, seed=2000, threads=8, threshold=20.0,
+                      pose=True),
 }
 SOLVER = dict(method=14, lam=50.0, theta=0.33, tau=0.25, alpha_proj=60.0, lambdaf=0.1,
               lambdams=100.0, fix_quirks=1)
@@ -691,6 +697,224 @@ def run_learned(args, wl, world, rank, local):
     net.close()
 
 
+POSE_METRIC = "720p pose estimates/s (CameraPose: features, matching, LMedS, pose recovery)"
+
+
+def run_pose(args, wl, world, rank, local):
+    """Pose front end: one step = the relative pose of every pair through the
+    C ABI (rf_pose_solve_f32), `threads` handles each on its own host thread
+    and CUDA stream (the API is synchronous per handle).  `value`: frames
+    resident in HBM; `e2e`: frames in pinned host memory, copied by the call."""
+    import threading
+
+    import torch
+
+    import reconflow_gb300 as R
+    from reconflow_gb300 import _native as N
+    from reconflow_gb300.scene import make_scene
+
+    torch.cuda.set_device(local)
+    lib = R.load()
+    W, H, n = wl["width"], wl["height"], args.pairs or wl["pairs"]
+    T = min(wl["threads"], n)
+    t0 = time.perf_counter()
+    scenes = [make_scene(W, H, seed=wl["seed"] + 1000 * rank + i, device="cuda") for i in range(n)]
+    gen_s = time.perf_counter() - t0
+    dev = [tuple(torch.as_tensor(np.ascontiguousarray(sc[k], np.float32), device="cuda")
+                 for k in ("I0", "I1")) for sc in scenes]
+    Ks = [np.ascontiguousarray(sc["K"], np.float64) for sc in scenes]
+    streams = [torch.cuda.Stream() for _ in range(T)]
+    poses = []
+    for k in range(T):
+        cp = R.CameraPose()
+        cp.initialize(Ks[0], wl["threshold"])
+        cp.set_stream(streams[k].cuda_stream)
+        cp._handle(W, H)
+        poses.append(cp)
+    out_R = np.zeros((n, 9))
+    out_t = np.zeros((n, 3))
+    fails = []
+
+    def worker(k, frames):
+        h = poses[k]._h
+        for i in range(k, n, T):
+            a, b = frames[i]
+            st = lib.rf_pose_solve_f32(h, ctypes.c_void_p(a), ctypes.c_void_p(b), W,
+                                       Ks[i].ctypes.data_as(ctypes.c_void_p),
+                                       out_R[i].ctypes.data_as(ctypes.c_void_p),
+                                       out_t[i].ctypes.data_as(ctypes.c_void_p))
+            if st != 0:
+                fails.append(i)
+
+    def step(frames):
+        ths = [threading.Thread(target=worker, args=(k, frames)) for k in range(T)]
+        for th in ths:
+            th.start()
+        for th in ths:
+            th.join()
+
+    dptr = [(a.data_ptr(), b.data_ptr()) for a, b in dev]
+    torch.cuda.synchronize()
+    for _ in range(args.warmup):
+        step(dptr)
+    torch.cuda.synchronize()
+    barrier(world)
+    fails.clear()
+    times = []
+    with ClockSampler(local) as clk:
+        for _ in range(args.steps):
+            torch.cuda.synchronize()
+            t1 = time.perf_counter()
+            step(dptr)
+            torch.cuda.synchronize()
+            times.append(time.perf_counter() - t1)
+    total_s = max_over_ranks(sum(times), world)
+    value = world * n * args.steps / total_s
+    if args.solve_only:
+        if rank == 0:
+            print(json.dumps({"metric": POSE_METRIC, "value": value, "unit": "pairs/s",
+                              "note": "solve-only run"}), flush=True)
+        return
+    timed_fails = len(fails)
+
+    def errors():
+        rot, tra = [], []
+        for i, sc in enumerate(scenes):
+            if i in fails:
+                continue
+            Rm = out_R[i].reshape(3, 3)
+            rot.append(np.degrees(np.arccos(np.clip((np.trace(Rm.T @ sc["R"]) - 1) / 2, -1, 1))))
+            tg = sc["t"] / np.linalg.norm(sc["t"])
+            tra.append(np.degrees(np.arccos(np.clip(out_t[i] @ tg, -1, 1))))
+        return {"rot_err_deg_median": float(np.median(rot)), "rot_err_deg_max": float(np.max(rot)),
+                "t_dir_err_deg_median": float(np.median(tra)), "t_dir_err_deg_max": float(np.max(tra))}
+
+    acc = errors()
+    counts = [poses[0].counts()]
+    # refined poses (rf_pose_params.refine = 1) on the same frames, untimed
+    for cp in poses:
+        cp.params.refine = 1
+        cp._release()
+        cp._handle(W, H)
+        cp.set_stream(None)
+    fails.clear()
+    step(dptr)
+    torch.cuda.synchronize()
+    acc_refined = errors()
+    for cp in poses:
+        cp.params.refine = 0
+        cp._release()
+        cp._handle(W, H)
+
+    # end to end: frames in pinned host memory
+    e2e = None
+    if not args.no_e2e:
+        hosts = []
+        for i in range(n):
+            pr = []
+            for k in ("I0", "I1"):
+                p_ = ctypes.c_void_p()
+                R._native.check(lib.rf_host_alloc(W * H * 4, ctypes.byref(p_)))
+                arr = np.ctypeslib.as_array(ctypes.cast(p_, ctypes.POINTER(ctypes.c_float)),
+                                            shape=(H, W))
+                arr[:] = scenes[i][k]
+                pr.append(p_)
+            hosts.append(pr)
+        hptr = [(a.value, b.value) for a, b in hosts]
+        step(hptr)
+        et = []
+        for _ in range(args.steps):
+            t1 = time.perf_counter()
+            step(hptr)
+            et.append(time.perf_counter() - t1)
+        e2e = {"value": world * n * args.steps / max_over_ranks(sum(et), world), "unit": "pairs/s",
+               "h2d_bytes_per_step": 2 * n * W * H * 4, "d2h_bytes_per_step": n * 12 * 8}
+        for pr in hosts:
+            for p_ in pr:
+                lib.rf_host_free(p_)
+
+    # roofline: the dominant GPU stage of one solve, kernels timed with CUDA
+    # events on the handle's stream (rf_pose_profile)
+    ms = (ctypes.c_float * 8)()
+    a, b = dptr[0]
+    R._native.check(lib.rf_pose_profile(poses[0]._h, ctypes.c_void_p(a), ctypes.c_void_p(b), W,
+                                        Ks[0].ctypes.data_as(ctypes.c_void_p), 20, ms))
+    roofline = pose_roofline(list(ms), W, H, poses[0])
+    cpu = None
+    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+        cpu = pose_cpu_sample(scenes[:2], wl["threshold"])
+    if rank == 0:
+        line = {
+            "metric": POSE_METRIC, "value": value, "unit": "pairs/s", "n_gpus": world,
+            "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": 1000.0 * total_s / args.steps, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32 (features), f64 (geometry)",
+            "data": "synthetic (seeded scene generator)",
+            "config": {"workload": args.workload, "width": W, "height": H, "pairs_per_step": n,
+                       "handles_threads_streams": T, "hessian_threshold": wl["threshold"],
+                       "n_octaves": 4, "n_octave_layers": 2, "ratio": 0.6,
+                       "lmeds_confidence": 0.999, "scene_seeds": [wl["seed"], wl["seed"] + n - 1],
+                       "timing": "host clock around each step, device synchronized on both "
+                                 "sides (the call returns the pose)",
+                       "parallelism": "replicas"},
+            "accuracy": acc, "accuracy_refined": acc_refined, "failures": timed_fails,
+            "counts_first_handle": counts[0],
+            "e2e": e2e, "roofline": roofline, "cpu_baseline": cpu,
+            "clocks": clk.summary(), "gpu_launches": int(sum(cp.kernel_launches() for cp in poses)),
+            "scene_gen_s": gen_s,
+        }
+        print(json.dumps(line), flush=True)
+    for cp in poses:
+        cp.close()
+
+
+def pose_roofline(ms, W, H, cp):
+    """Roofline entry of the feature detector's Hessian-response kernel (every
+    octave of one frame) and the per-launch times of every GPU stage: ms =
+    [integral image, Hessian responses, keypoint selection, orientation,
+    descriptors, matching, LMedS scoring] of frame 0 / the pair, then the
+    keypoint count."""
+    names = ["integral", "hessian", "extrema", "orientation", "descriptor", "match", "lmeds"]
+    dom = max(range(len(names)), key=lambda k: ms[k])
+    peak, peak_kind = load_peaks()
+    layers = 4
+    # algorithmic bytes of the response kernels: the integral image read once
+    # per octave, every response written
+    cells = sum((W >> o) * (H >> o) for o in range(4))
+    a_bytes = 4 * (W + 1) * (H + 1) * 4 + layers * cells * 4
+    achieved = a_bytes / (ms[1] * 1e-3) / 1e9
+    return {"bound": "hbm", "kernel": "k_hessian (4 octaves)", "achieved": achieved, "peak": peak,
+            "peak_kind": peak_kind, "unit": "GB/s", "frac": achieved / peak, "traffic": None,
+            "alg_bytes_per_launch": a_bytes, "dominant_stage": names[dom],
+            "launch_ms": dict(zip(names, ms[:len(names)])), "keypoints": int(ms[7]),
+            "timing": "each stage's launches back to back, CUDA events on the handle's stream"}
+
+
+def pose_cpu_sample(scenes, threshold):
+    """The oracle's feature stages (one core) and the library's host LMedS on
+    a bounded sample of the workload's pairs."""
+    from oracle import oracle as O
+    from reconflow_gb300 import pose as P
+
+    O.build()
+    to8 = lambda a: np.clip(np.floor(a * 255 + 0.5), 0, 255).astype(np.uint8)  # noqa: E731
+    t0 = time.perf_counter()
+    for sc in scenes:
+        k0, d0 = O.surf_detect(to8(sc["I0"]), threshold=threshold)
+        k1, d1 = O.surf_detect(to8(sc["I1"]), threshold=threshold)
+        best, a, b = O.surf_match(d0, d1)
+        q = np.nonzero(np.sqrt(a).astype(np.float64) < 0.6 * np.sqrt(b).astype(np.float64))[0]
+        Ki = np.linalg.inv(sc["K"])
+        nrm = lambda p: (np.c_[p, np.ones(len(p))] @ Ki.T)[:, :2]  # noqa: E731
+        x0, x1 = nrm(k0[q, :2].astype(np.float64)), nrm(k1[best[q], :2].astype(np.float64))
+        E, m = P.essential_lmeds(x0, x1)
+        P.recover_pose(E, x0, x1, m)
+    dt = time.perf_counter() - t0
+    return {"value": len(scenes) / dt, "unit": "pairs/s", "cores": 1, "kind": "port",
+            "sample": f"{len(scenes)} pairs of the workload: oracle features and matching (one "
+                      f"core), the library's host LMedS and pose recovery; {dt:.1f} s"}
+
+
 def run_learned_mixed(args, wl, world, rank, local):
     """Batched + learned warm start on a mix of frame sizes (one batch, one
     network pass and one refinement per size group; BASELINE config 5 at a
@@ -950,8 +1174,8 @@ def main():
     ap.add_argument("--solve-only", action="store_true",
                     help="only warm-up + timed solves (for profiler launch lists)")
     ap.add_argument("--pairs", type=int, default=0,
-                    help="pairs per step of the 720p learned workload (profiling; default: the "
-                         "workload's)")
+                    help="pairs per step of the 720p learned or pose workload (profiling; "
+                         "default: the workload's)")
     args = ap.parse_args()
     wl = WORKLOADS[args.workload]
     world, rank, local = dist_setup(args)
@@ -966,6 +1190,9 @@ def main():
         elif "pairs" in wl:
             raise SystemExit("bench.py: the reference arm runs single-pair workloads")
         run_reference(args, wl, world, rank)
+        return
+    if "pose" in wl:
+        run_pose(args, wl, world, rank, local)
         return
     if "groups" in wl:
         run_learned_mixed(args, wl, world, rank, local)

@@ -432,6 +432,108 @@ RF_API rf_status rfk_remove_edge_artifacts(const float* X, const float* Y, const
 RF_API rf_status rfk_flow_to_color(const float* u, const float* v, int w, int h, int s,
                                    float flow_scale, float* rgb, void* stream);
 
+/* ---------------------------------------------------------------------------
+ * Pose front end: CameraPose (reconflow/CameraPose.h:11-64,
+ * CameraPose.cpp:11-128).  The reference detects SURF keypoints on the GPU
+ * (OpenCV's closed SURF_CUDA), matches them by brute force (k = 2, ratio
+ * 0.6), and estimates E by LMedS and the pose by recoverPose.  Here: SURF as
+ * published (H. Bay et al., CVIU 110(3), 2008) restated as CUDA kernels
+ * (integral image, box-filter Hessian responses over octaves, 3x3x3 maxima
+ * with quadratic refinement, dominant orientation, 64-value descriptor), a
+ * brute-force matcher kernel, and the five-point LMedS and pose recovery on
+ * the host.  Every GPU stage is exact FP32 and equals the CPU oracle bit
+ * for bit.
+ * ------------------------------------------------------------------------ */
+typedef struct rf_pose rf_pose;
+
+typedef struct rf_pose_params {
+    double hessian_threshold;  /* minHessian (CameraPose.cpp:21-24: 2000) */
+    int n_octaves;             /* 4 */
+    int n_octave_layers;       /* 2 (4 response layers per octave) */
+    int max_keypoints;         /* per frame, strongest kept; 0 = 1% of the pixels */
+    double ratio;              /* match ratio test (CameraPose.cpp:71: 0.6) */
+    double confidence;         /* LMedS confidence (CameraPose.cpp:80: 0.999) */
+    unsigned long long seed;   /* LMedS sampling */
+    int refine;                /* 1: refine (R, t) on the inliers by Levenberg-Marquardt
+                                  on their Sampson distances; 0 (default) = the
+                                  reference, which stops at the LMedS model */
+} rf_pose_params;
+
+/* One detected keypoint (the fields of cv::KeyPoint the path uses). */
+typedef struct rf_keypoint {
+    float x, y;      /* position in pixels */
+    float scale;     /* s = 1.2 L / 9 for the (interpolated) filter size L */
+    float angle;     /* dominant orientation, radians in [0, 2 pi) */
+    float response;  /* determinant-of-Hessian response */
+    int octave;
+} rf_keypoint;
+
+RF_API rf_status rf_pose_params_default(rf_pose_params* p);
+/* CameraPose::initialize: buffers for frames of width x height. */
+RF_API rf_status rf_pose_create(const rf_pose_params* p, int width, int height, rf_pose** out);
+RF_API rf_status rf_pose_destroy(rf_pose* h);
+RF_API rf_status rf_pose_set_stream(rf_pose* h, void* stream);
+/* CameraPose::solvePose_8uc1 (CameraPose.cpp:47-118): 8-bit gray frames
+ * (pitch in bytes; host or device memory), intrinsics K (row-major 3x3,
+ * both frames).
+ * Writes R (row-major) and unit t with x1 = R x0 + t.  RF_ERR_STATE when
+ * a frame has no keypoints, fewer than 5 matches survive, or no model is
+ * found (the reference's "return 1" cases). */
+RF_API rf_status rf_pose_solve_u8(rf_pose* h, const uint8_t* im0, const uint8_t* im1, int pitch,
+                                  const double K[9], double R[9], double t[3]);
+/* The same for float gray frames in [0, 1] (pitch in floats; host or device memory),
+ * converted to 8 bits on the GPU as round(255 v) clamped to [0, 255]. */
+RF_API rf_status rf_pose_solve_f32(rf_pose* h, const float* im0, const float* im1, int pitch,
+                                   const double K[9], double R[9], double t[3]);
+/* Keypoints, matches and inliers of the last solve. */
+RF_API rf_status rf_pose_counts(const rf_pose* h, int* n_kp0, int* n_kp1, int* n_matches,
+                                int* n_inliers);
+/* Keypoints (strongest first) and their 64-value descriptors of frame 0 or 1;
+ * at most `cap` of each. */
+RF_API rf_status rf_pose_keypoints(const rf_pose* h, int frame, rf_keypoint* kp, float* desc,
+                                   int cap);
+/* Matches that passed the ratio test: keypoint indices in frame 0 and 1,
+ * Euclidean descriptor distance, and the LMedS inlier flag. */
+RF_API rf_status rf_pose_matches(const rf_pose* h, int* idx0, int* idx1, float* dist,
+                                 uint8_t* inlier, int cap);
+/* Determinant-of-Hessian responses of one octave of frame 0 or 1 from the
+ * last solve: layers x (height >> octave) x (width >> octave) floats. */
+RF_API rf_status rf_pose_responses(const rf_pose* h, int frame, int octave, float* out,
+                                   size_t cap);
+
+/* Kernels this handle has launched. */
+RF_API uint64_t rf_pose_kernel_launches(const rf_pose* h);
+/* Solve once (as rf_pose_solve_f32), then time each GPU stage of frame 0,
+ * its launches repeated n_iters times back to back on the handle's stream
+ * (CUDA events): ms[0] integral image, [1] Hessian responses of every
+ * octave, [2] keypoint selection, [3] orientation, [4] descriptors, [5]
+ * matching, [6] LMedS scoring; ms[7] = keypoints of frame 0. */
+RF_API rf_status rf_pose_profile(rf_pose* h, const float* im0, const float* im1, int pitch,
+                                 const double K[9], int n_iters, float* ms);
+
+/* Host-side relative pose, also usable alone.  Normalized image points
+ * (K^-1 applied), [n][2] doubles.
+ * rf_essential_5pt: the five-point solver (D. Nister, IEEE PAMI 26(6), 2004)
+ *   on five matches; writes up to 10 essential matrices (row-major, unit
+ *   Frobenius norm) with x1^T E x0 = 0 and returns their number.
+ * rf_essential_lmeds: least median of squared Sampson distances over random
+ *   five-point samples (findEssentialMat with LMEDS, CameraPose.cpp:80);
+ *   writes E and the inlier mask (n bytes).
+ * rf_recover_pose: the (R, t) of E with the most triangulated inliers in
+ *   front of both cameras (recoverPose, CameraPose.cpp:100).
+ * Both samples and medians are deterministic for a seed. */
+RF_API int rf_essential_5pt(const double* x0, const double* x1, double* E);
+RF_API rf_status rf_essential_lmeds(const double* x0, const double* x1, int n, double confidence,
+                                    unsigned long long seed, double E[9], unsigned char* mask);
+RF_API rf_status rf_recover_pose(const double E[9], const double* x0, const double* x1, int n,
+                                 const unsigned char* mask, double R[9], double t[3],
+                                 int* n_good);
+/* No reference counterpart: Levenberg-Marquardt on the inliers' summed
+ * squared Sampson distances over the five degrees of freedom of (R, t);
+ * R, t are the start and the result. */
+RF_API rf_status rf_refine_pose(const double* x0, const double* x1, int n,
+                                const unsigned char* mask, double R[9], double t[3]);
+
 #ifdef __cplusplus
 }
 #endif

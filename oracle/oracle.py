@@ -40,8 +40,9 @@ class RfoParams(ctypes.Structure):
 
 def build(force: bool = False) -> str:
     """Compile the oracle library with its Makefile (g++, OpenMP)."""
+    srcs = [os.path.join(_HERE, f) for f in ("rf_oracle.cpp", "pose_oracle.cpp", "Makefile")]
     if force or not os.path.exists(_LIB_PATH) or (
-        os.path.getmtime(_LIB_PATH) < os.path.getmtime(os.path.join(_HERE, "rf_oracle.cpp"))
+        os.path.getmtime(_LIB_PATH) < max(os.path.getmtime(f) for f in srcs)
     ):
         subprocess.run(["make", "-s", "-C", _HERE], check=True)
     return _LIB_PATH
@@ -311,3 +312,62 @@ def energy(I0, I1, u, v, X, Y, Z, w, h, s, lam, alpha_proj, R1, t1, K1, recon=Tr
     K1 = np.ascontiguousarray(K1, np.float64)
     return float(fn(*[_ptr(a) for a in arrs], int(w), int(h), int(s), ctypes.c_float(lam),
                     ctypes.c_float(alpha_proj), _ptr(R1), _ptr(t1), _ptr(K1), int(recon)))
+
+
+# ---------------------------------------------------------------------------
+# Pose front end (pose_oracle.cpp): the feature stages the GPU runs
+# ---------------------------------------------------------------------------
+
+def surf_integral(img):
+    """Integral image of an 8-bit frame, (h + 1) x (w + 1) uint32."""
+    img = np.ascontiguousarray(img, np.uint8)
+    h, w = img.shape
+    out = np.zeros((h + 1, w + 1), np.uint32)
+    lib().rfo_surf_integral(img.ctypes.data_as(ctypes.c_void_p), w, h,
+                            out.ctypes.data_as(ctypes.c_void_p))
+    return out
+
+
+def surf_responses(img, octave, layers):
+    """Determinant-of-Hessian responses of one octave: layers x (h >> o) x (w >> o)."""
+    img = np.ascontiguousarray(img, np.uint8)
+    h, w = img.shape
+    out = np.zeros((layers, h >> octave, w >> octave), np.float32)
+    lib().rfo_surf_responses(img.ctypes.data_as(ctypes.c_void_p), w, h, octave, layers,
+                             out.ctypes.data_as(ctypes.c_void_p))
+    return out
+
+
+def surf_detect(img, threshold=2000.0, n_octaves=4, n_layers=2, max_kp=None, cand_cap=None):
+    """Keypoints [n][6] (x, y, scale, angle, response, octave) strongest first,
+    and descriptors [n][64]; None when the candidates exceed cand_cap."""
+    img = np.ascontiguousarray(img, np.uint8)
+    h, w = img.shape
+    max_kp = max_kp or max(16, w * h // 100)
+    cand_cap = cand_cap or max(4 * max_kp, 65536)
+    kp = np.zeros((max_kp, 6), np.float32)
+    desc = np.zeros((max_kp, 64), np.float32)
+    f = lib().rfo_surf_detect
+    f.restype = ctypes.c_int
+    n = f(img.ctypes.data_as(ctypes.c_void_p), w, h, ctypes.c_double(threshold), n_octaves,
+          n_layers, max_kp, cand_cap, kp.ctypes.data_as(ctypes.c_void_p),
+          desc.ctypes.data_as(ctypes.c_void_p))
+    if n < 0:
+        return None
+    return kp[:n].copy(), desc[:n].copy()
+
+
+def surf_match(d0, d1):
+    """Nearest and second-nearest descriptor of frame 1 for each of frame 0:
+    (index, squared distance 1, squared distance 2)."""
+    d0 = np.ascontiguousarray(d0, np.float32)
+    d1 = np.ascontiguousarray(d1, np.float32)
+    n0, n1 = len(d0), len(d1)
+    best = np.zeros(n0, np.int32)
+    b1 = np.zeros(n0, np.float32)
+    b2 = np.zeros(n0, np.float32)
+    lib().rfo_surf_match(d0.ctypes.data_as(ctypes.c_void_p), n0,
+                         d1.ctypes.data_as(ctypes.c_void_p), n1,
+                         best.ctypes.data_as(ctypes.c_void_p), b1.ctypes.data_as(ctypes.c_void_p),
+                         b2.ctypes.data_as(ctypes.c_void_p))
+    return best, b1, b2

@@ -44,6 +44,20 @@ class RfParams(ctypes.Structure):
     ]
 
 
+class RfPoseParams(ctypes.Structure):
+    _fields_ = [
+        ("hessian_threshold", ctypes.c_double), ("n_octaves", ctypes.c_int),
+        ("n_octave_layers", ctypes.c_int), ("max_keypoints", ctypes.c_int),
+        ("ratio", ctypes.c_double), ("confidence", ctypes.c_double), ("seed", ctypes.c_ulonglong),
+        ("refine", ctypes.c_int),
+    ]
+
+
+class RfKeypoint(ctypes.Structure):
+    _fields_ = [("x", ctypes.c_float), ("y", ctypes.c_float), ("scale", ctypes.c_float),
+                ("angle", ctypes.c_float), ("response", ctypes.c_float), ("octave", ctypes.c_int)]
+
+
 # (name, restype, argtypes) of every exported entry point
 _VP, _I, _F, _D = ctypes.c_void_p, ctypes.c_int, ctypes.c_float, ctypes.c_void_p
 _SIGS = [
@@ -126,6 +140,23 @@ _SIGS = [
     ("rfk_rgb_to_gray", _I, [_VP, _I, _I, _I, _VP, _VP]),
     ("rfk_remove_edge_artifacts", _I, [_VP, _VP, _VP, _I, _F, _I, _I, _I, _VP, _VP, _VP, _VP]),
     ("rfk_flow_to_color", _I, [_VP, _VP, _I, _I, _I, _F, _VP, _VP]),
+    # pose front end
+    ("rf_pose_params_default", _I, [ctypes.POINTER(RfPoseParams)]),
+    ("rf_pose_create", _I, [ctypes.POINTER(RfPoseParams), _I, _I, ctypes.POINTER(_VP)]),
+    ("rf_pose_destroy", _I, [_VP]),
+    ("rf_pose_set_stream", _I, [_VP, _VP]),
+    ("rf_pose_solve_u8", _I, [_VP, _VP, _VP, _I, _VP, _VP, _VP]),
+    ("rf_pose_solve_f32", _I, [_VP, _VP, _VP, _I, _VP, _VP, _VP]),
+    ("rf_pose_counts", _I, [_VP, _VP, _VP, _VP, _VP]),
+    ("rf_pose_keypoints", _I, [_VP, _I, _VP, _VP, _I]),
+    ("rf_pose_matches", _I, [_VP, _VP, _VP, _VP, _VP, _I]),
+    ("rf_pose_responses", _I, [_VP, _I, _I, _VP, ctypes.c_size_t]),
+    ("rf_pose_kernel_launches", ctypes.c_uint64, [_VP]),
+    ("rf_pose_profile", _I, [_VP, _VP, _VP, _I, _VP, _I, _VP]),
+    ("rf_essential_5pt", _I, [_VP, _VP, _VP]),
+    ("rf_essential_lmeds", _I, [_VP, _VP, _I, ctypes.c_double, ctypes.c_ulonglong, _VP, _VP]),
+    ("rf_recover_pose", _I, [_VP, _VP, _VP, _I, _VP, _VP, _VP, _VP]),
+    ("rf_refine_pose", _I, [_VP, _VP, _I, _VP, _VP, _VP]),
 ]
 
 EXPORTED = [s[0] for s in _SIGS]

@@ -32,6 +32,10 @@ SOURCES = {
     "rf_warm.cu": [],
     # the learned warm start: BF16 tensor-core convolutions, FP32 accumulation
     "rf_cnn.cu": [],
+    # pose front end: feature detection, description and matching (exact FP32,
+    # compared bit for bit with the oracle) and the host-side relative pose
+    "rf_pose.cu": ["-fmad=false"],
+    "rf_epipolar.cpp": [],
 }
 COMMON = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC,-ffp-contract=off,-fvisibility=hidden",
           "--expt-relaxed-constexpr", "-I" + os.path.join(ROOT, "include"), "-I" + CSRC]
@@ -66,7 +70,7 @@ def build(force: bool = False, verbose: bool = False) -> str:
     objs = []
     for src, flags in SOURCES.items():
         s = os.path.join(CSRC, src)
-        o = os.path.join(OBJ_DIR, src.replace(".cu", ".o"))
+        o = os.path.join(OBJ_DIR, os.path.splitext(src)[0] + ".o")
         objs.append(o)
         if force or _stale(o, [s] + hdrs):
             jobs.append([nv, "-c", s, "-o", o] + ARCH + COMMON + flags)
@@ -84,8 +88,9 @@ def build(force: bool = False, verbose: bool = False) -> str:
             if verbose and log.strip():
                 print(log)
     if force or jobs or _stale(LIB_PATH, objs):
-        run([nv, "-shared", "-o", LIB_PATH] + objs + ARCH + ["-Xcompiler", "-fPIC", "-lcudart_static",
-                                                              "-ldl", "-lrt", "-lpthread"])
+        run([nv, "-shared", "-o", LIB_PATH] + objs + ARCH + ["-Xcompiler", "-fPIC,-pthread",
+                                                              "-lcudart_static", "-ldl", "-lrt",
+                                                              "-lpthread"])
     return LIB_PATH
 
 

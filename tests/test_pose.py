@@ -1,0 +1,167 @@
+"""Pose front end on the CPU: the host-side relative pose of the C ABI
+(five-point solver, LMedS, pose recovery; CameraPose.cpp:79-104) on exact and
+noisy synthetic matches, and the feature oracle's properties (integral image,
+responses of a blob, rotation behaviour, the oracle's own pose on a rendered
+scene).  No GPU: the library's host functions run without a device."""
+import numpy as np
+import pytest
+
+from reconflow_gb300 import pose as P
+
+
+def _rot(rng, deg):
+    a = rng.normal(size=3)
+    a /= np.linalg.norm(a)
+    ang = np.radians(deg)
+    K = np.array([[0, -a[2], a[1]], [a[2], 0, -a[0]], [-a[1], a[0], 0]])
+    return np.eye(3) + np.sin(ang) * K + (1 - np.cos(ang)) * K @ K
+
+
+def _skew(t):
+    return np.array([[0, -t[2], t[1]], [t[2], 0, -t[0]], [-t[1], t[0], 0]])
+
+
+def _project(X, R, t):
+    X1 = X @ R.T + t
+    return X[:, :2] / X[:, 2:], X1[:, :2] / X1[:, 2:]
+
+
+def _angle(Ra, Rb):
+    return np.degrees(np.arccos(np.clip((np.trace(Ra.T @ Rb) - 1) / 2, -1, 1)))
+
+
+@pytest.mark.parametrize("seed", range(40))
+def test_five_point_recovers_E(seed):
+    """One of the (up to 10) solutions through five exact matches is
+    [t]x R up to sign."""
+    rng = np.random.default_rng(seed)
+    R = _rot(rng, rng.uniform(0.5, 25))
+    t = rng.normal(size=3)
+    t /= np.linalg.norm(t)
+    X = np.c_[rng.uniform(-2, 2, (5, 2)), rng.uniform(2, 12, 5)]
+    x0, x1 = _project(X, R, t)
+    Es = P.essential_5pt(x0, x1)
+    assert 1 <= len(Es) <= 10
+    E = _skew(t) @ R
+    E /= np.linalg.norm(E)
+    err = min(min(np.linalg.norm(e - E), np.linalg.norm(e + E)) for e in Es)
+    assert err < 1e-5, err
+    for e in Es:  # every solution satisfies the five epipolar constraints and det = 0
+        r = [np.r_[b, 1] @ e @ np.r_[a, 1] for a, b in zip(x0, x1)]
+        assert np.max(np.abs(r)) < 1e-8
+        assert abs(np.linalg.det(e)) < 1e-8
+
+
+@pytest.mark.parametrize("seed", range(6))
+def test_lmeds_and_recover_pose_with_outliers(seed):
+    rng = np.random.default_rng(100 + seed)
+    R = _rot(rng, rng.uniform(1, 5))
+    t = rng.normal(size=3)
+    t /= np.linalg.norm(t)
+    n = 400
+    X = np.c_[rng.uniform(-3, 3, (n, 2)), rng.uniform(3, 10, n)]
+    x0, x1 = _project(X, R, t)
+    out = rng.random(n) < 0.3
+    x1[out] = rng.uniform(-0.6, 0.6, (out.sum(), 2))
+    E, mask = P.essential_lmeds(x0, x1, seed=seed)
+    assert (mask == ~out).mean() > 0.98
+    Rg, tg, good = P.recover_pose(E, x0, x1, mask)
+    assert _angle(Rg, R) < 1e-4
+    # least squares over the mask (which admits the few outliers that lie on
+    # their epipolar lines) stays within a hundredth of a degree
+    Rr, tr = P.refine_pose(Rg, tg, x0, x1, mask)
+    assert _angle(Rr, R) < 0.01 and np.degrees(np.arccos(np.clip(tr @ t, -1, 1))) < 0.05
+    assert np.degrees(np.arccos(np.clip(tg @ t, -1, 1))) < 1e-3
+    assert good >= 0.95 * (~out).sum()
+    # deterministic for a seed
+    E2, mask2 = P.essential_lmeds(x0, x1, seed=seed)
+    assert np.array_equal(E, E2) and np.array_equal(mask, mask2)
+
+
+def test_lmeds_rejects_too_few_matches():
+    from reconflow_gb300._native import RfError
+
+    with pytest.raises(RfError):
+        P.essential_lmeds(np.zeros((4, 2)), np.zeros((4, 2)))
+
+
+def test_bgr_to_gray_fixed_point():
+    rng = np.random.default_rng(0)
+    img = rng.integers(0, 256, (7, 9, 3)).astype(np.uint8)
+    g = P.bgr_to_gray(img)
+    want = np.floor(0.299 * img[..., 2] + 0.587 * img[..., 1] + 0.114 * img[..., 0] + 0.5)
+    assert np.max(np.abs(g.astype(float) - want)) <= 1
+
+
+# ---- the feature oracle ----------------------------------------------------
+
+def _to8(a):
+    return np.clip(np.floor(a * 255 + 0.5), 0, 255).astype(np.uint8)
+
+
+def test_oracle_integral_image(oracle):
+    rng = np.random.default_rng(1)
+    img = rng.integers(0, 256, (37, 53)).astype(np.uint8)
+    S = oracle.surf_integral(img)
+    want = np.zeros((38, 54), np.uint64)
+    want[1:, 1:] = img.astype(np.uint64).cumsum(0).cumsum(1)
+    assert np.array_equal(S.astype(np.uint64), want)
+
+
+@pytest.mark.parametrize("sigma,layer", [(3.0, 1), (4.0, 2), (5.0, 3)])
+def test_oracle_blob_response_peaks_at_its_centre(oracle, sigma, layer):
+    """A dark Gaussian blob on a flat background: the strongest response of
+    octave 0 is at the blob centre, in a layer that grows with the blob
+    (filter sizes 15, 21, 27 for sigma 3, 4, 5), and it is a keypoint."""
+    h, w = 128, 160
+    y, x = np.mgrid[0:h, 0:w]
+    img = _to8(0.8 - 0.6 * np.exp(-((x - 80) ** 2 + (y - 64) ** 2) / (2 * sigma ** 2)))
+    R = oracle.surf_responses(img, 0, 4)
+    k, j, i = np.unravel_index(np.argmax(R), R.shape)
+    assert (i, j, k) == (80, 64, layer)
+    kp, _ = oracle.surf_detect(img, threshold=5.0)
+    assert len(kp) >= 1
+    assert abs(kp[0, 0] - 80) < 0.5 and abs(kp[0, 1] - 64) < 0.5
+
+
+def test_oracle_features_follow_a_rotation(oracle):
+    """Keypoints of a frame rotated by 90 degrees are the rotated keypoints,
+    and the descriptors match across the rotation."""
+    from reconflow_gb300.scene import make_scene
+
+    sc = make_scene(320, 240, seed=3)
+    a = _to8(sc["I0"])
+    b = np.ascontiguousarray(np.rot90(a))  # (x, y) -> (y, w - 1 - x)
+    ka, da = oracle.surf_detect(a, threshold=10.0)
+    kb, db = oracle.surf_detect(b, threshold=10.0)
+    assert len(ka) > 50 and abs(len(ka) - len(kb)) < 0.25 * len(ka)
+    best, d1, d2 = oracle.surf_match(da, db)
+    ok = np.sqrt(d1) < 0.6 * np.sqrt(d2)
+    assert ok.mean() > 0.3
+    pa = ka[ok, :2]
+    pb = kb[best[ok], :2]
+    want = np.c_[pa[:, 1], 320 - 1 - pa[:, 0]]
+    assert np.median(np.linalg.norm(pb - want, axis=1)) < 1.0
+
+
+def test_oracle_pose_on_a_rendered_scene(oracle):
+    """Oracle features + the library's host pose recover the generator's pose."""
+    from reconflow_gb300.scene import make_scene
+
+    sc = make_scene(640, 480, seed=0)
+    k0, d0 = oracle.surf_detect(_to8(sc["I0"]), threshold=20.0)
+    k1, d1_ = oracle.surf_detect(_to8(sc["I1"]), threshold=20.0)
+    best, a, b = oracle.surf_match(d0, d1_)
+    q = np.nonzero(np.sqrt(a).astype(np.float64) < 0.6 * np.sqrt(b).astype(np.float64))[0]
+    Ki = np.linalg.inv(sc["K"])
+    norm = lambda p: (np.c_[p, np.ones(len(p))] @ Ki.T)[:, :2]  # noqa: E731
+    x0, x1 = norm(k0[q, :2].astype(np.float64)), norm(k1[best[q], :2].astype(np.float64))
+    E, mask = P.essential_lmeds(x0, x1)
+    R, t, _ = P.recover_pose(E, x0, x1, mask)
+    tg = sc["t"] / np.linalg.norm(sc["t"])
+    assert _angle(R, sc["R"]) < 0.3
+    assert np.degrees(np.arccos(np.clip(t @ tg, -1, 1))) < 5.0
+    # refinement on the inliers brings both within a tenth of that
+    R2, t2 = P.refine_pose(R, t, x0, x1, mask)
+    assert _angle(R2, sc["R"]) < 0.05
+    assert np.degrees(np.arccos(np.clip(t2 @ tg, -1, 1))) < 0.5
