@@ -59,6 +59,7 @@ struct BatchCtx {
     size_t total;               // floats per plane
     int n;
     int L;
+    int prefetch;               // L2 prefetch distance in blocks (0 = none)
 };
 
 // plane k of the tile's pair
@@ -66,10 +67,41 @@ __device__ __forceinline__ float* plane_ptr(const BatchCtx& c, const TileEntry& 
     return c.pool + (size_t)k * c.total + t.off;
 }
 
+__device__ __forceinline__ void prefetch_l2(const void* p) {
+    asm volatile("prefetch.global.L2 [%0];" ::"l"(p));
+}
+
+// Operations with a `prefetch` member (the inner-iteration steps) first ask
+// L2 for their fields at the same pixel of the tile `ctx.prefetch` blocks
+// ahead -- the tile the next wave of blocks will run -- so its DRAM reads
+// overlap this wave's work.
+template <class Op, class = void>
+struct HasPrefetch {
+    static constexpr bool value = false;
+};
+template <class Op>
+struct HasPrefetch<Op, decltype(void(&Op::prefetch))> {
+    static constexpr bool value = true;
+};
+
+template <class Op>
+__device__ __forceinline__ void prefetch_ahead(const BatchCtx& ctx, const TileEntry* tiles,
+                                               int next, int count, int level, const Op& op) {
+    if constexpr (HasPrefetch<Op>::value) {
+        if (ctx.prefetch > 0 && next < count) {
+            const TileEntry tn = tiles[next];
+            const LevelDims dn = ctx.pairs[tn.pair].dims[level];
+            const int ix = tn.x0 + (int)threadIdx.x, iy = tn.y0 + (int)threadIdx.y;
+            if (ix < dn.w && iy < dn.h) op.prefetch(tn.off + ix + iy * dn.s);
+        }
+    }
+}
+
 // One block = one tile of one pair at `level` (the level's tile shape is
 // the block shape; the tile table gives the pair and the tile's origin).
 template <class Op>
 __global__ void __launch_bounds__(kMaxTile) k_batch(BatchCtx ctx, int level, Op op) {
+    prefetch_ahead(ctx, ctx.tiles, (int)blockIdx.x + ctx.prefetch, (int)gridDim.x, level, op);
     const TileEntry t = ctx.tiles[blockIdx.x];
     const LevelDims d = ctx.pairs[t.pair].dims[level];
     const int ix = t.x0 + (int)threadIdx.x, iy = t.y0 + (int)threadIdx.y;
@@ -95,6 +127,10 @@ __global__ void __launch_bounds__(kMaxTile) k_batch_pair(BatchCtx ctx, int level
         is_x = nx > ny;
         k = b - m;
     }
+    if (is_x)
+        prefetch_ahead(ctx, ctx.tiles + x0, k + ctx.prefetch / 2, nx, level, opx);
+    else
+        prefetch_ahead(ctx, ctx.tiles + y0, k + ctx.prefetch / 2, ny, level, opy);
     const TileEntry t = ctx.tiles[is_x ? x0 + k : y0 + k];
     const LevelDims d = ctx.pairs[t.pair].dims[level];
     const int ix = t.x0 + (int)threadIdx.x, iy = t.y0 + (int)threadIdx.y;
@@ -149,6 +185,8 @@ struct OpReconA {
                                int ix, int iy) const {
         recon_a_px<0>(f, ctx.consts[t.pair * ctx.L + level], wt, d, ix, iy, first, ucb, t.off);
     }
+    // (no prefetch: the data step is bound by instruction issue, and 18 more
+    // instructions per pixel cost more than the earlier reads save)
 };
 
 struct OpReconB {
@@ -158,6 +196,15 @@ struct OpReconB {
     __device__ void operator()(const BatchCtx&, const TileEntry& t, int, LevelDims d, int ix,
                                int iy) const {
         recon_b_px(f, wt, d, ix, iy, first, t.off);
+    }
+    // the fields recon_b_px reads at a pixel (element e of every plane); the
+    // dual / median step waits on memory, so reading the next wave's pixels
+    // into L2 early pays
+    __device__ void prefetch(int e) const {
+        const float* p[] = {f.duhat, f.dvhat, f.pu1, f.pu2, f.pv1, f.pv2, f.X1, f.Y1, f.Z1,
+                            f.sku, f.skv, f.u, f.v, f.uproj, f.vproj};
+#pragma unroll
+        for (const float* q : p) prefetch_l2(q + e);
     }
 };
 
@@ -330,6 +377,7 @@ struct rf_batch {
     // pipelined inner iterations (pairs [0, split) and [split, n) half an
     // iteration apart); 0 = every inner half-iteration over all pairs at once
     int split = 0;
+    int prefetch = 0;  // L2 prefetch distance of the inner-iteration launches, in blocks
     bool solved = false;
     int n_planes = 0;
     // plane indices
@@ -394,6 +442,7 @@ BatchCtx ctx_of(rf_batch* b, int level) {
     c.total = b->total;
     c.n = b->n;
     c.L = b->L;
+    c.prefetch = b->prefetch;
     return c;
 }
 
@@ -705,9 +754,19 @@ rf_status rf_batch_create(const rf_params* p, int n_pairs, const int* widths, co
     b->tile_w.assign(b->L, BX);
     b->tile_h.assign(b->L, BY);
     {
+        // pipelined pair groups: opt-in (RF_BATCH_PIPELINE=1); with the L2
+        // prefetch below the plain order measured as fast
         const char* e = std::getenv("RF_BATCH_PIPELINE");
-        const bool on = !(e && e[0] == '0');
+        const bool on = e && e[0] == '1';
         b->split = on && n_pairs >= 2 ? n_pairs / 2 : 0;
+        // distance = the blocks resident at once (one wave of 16 blocks per
+        // SM), RF_BATCH_PREFETCH times (default 1; 0 = off)
+        const char* pf = std::getenv("RF_BATCH_PREFETCH");
+        const double waves = pf ? std::atof(pf) : 1.0;
+        int dev = 0, sms = 0;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+        b->prefetch = waves > 0.0 ? (int)(waves * sms * 16) : 0;
     }
     if (e == cudaSuccess) e = fill_tiles(b);
     if (e == cudaSuccess) e = cudaMalloc(&b->d_pairs, sizeof(BatchPair) * n_pairs);

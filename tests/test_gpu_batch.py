@@ -44,8 +44,11 @@ def _inputs():
     return out
 
 
-@pytest.mark.parametrize("fix", [0, 1])
-def test_batch_recon_matches_single_pair(oracle, rf, fix):
+@pytest.mark.parametrize("fix,pipeline", [(0, "0"), (1, "0"), (1, "1")])
+def test_batch_recon_matches_single_pair(oracle, rf, fix, pipeline, monkeypatch):
+    """pipeline "1": the two pair groups half an inner iteration apart
+    (RF_BATCH_PIPELINE, read when the batch is created)."""
+    monkeypatch.setenv("RF_BATCH_PIPELINE", pipeline)
     L, warps, iters = 2, 2, 4
     data = _inputs()
     kw = dict(lambda_=50.0, lambdaf=0.1, lambdams=100.0, alphaTv=1 / 0.33, alphaProj=60.0,
