@@ -286,6 +286,36 @@ def run_reference(args, wl, world, rank):
     print(json.dumps(line), flush=True)
 
 
+def run_reference_pose(args, wl, world, rank):
+    """Reference arm of the pose workload: the oracle's feature stages and
+    the host LMedS / pose recovery (the reference's own CameraPose needs
+    OpenCV with CUDA), one pair per step, on the workload's pairs."""
+    if rank != 0:
+        return
+    from reconflow_gb300.scene import make_scene
+
+    n = max(1, args.steps)
+    scenes = [make_scene(wl["width"], wl["height"], seed=wl["seed"] + i) for i in range(n)]
+    pose_cpu_sample(scenes[:1], wl["threshold"])  # warm-up (builds the oracle)
+    t0 = time.perf_counter()
+    cpu = pose_cpu_sample(scenes, wl["threshold"])
+    total = time.perf_counter() - t0
+    value = n / total
+    cpu["value"] = value
+    line = {
+        "impl": "reference", "metric": POSE_METRIC, "value": value, "unit": "pairs/s",
+        "n_gpus": args.gpus, "steps": n, "warmup": args.warmup, "ms_per_step": 1000.0 * total / n,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "f32 (features), f64 (geometry)", "data": "synthetic (seeded scene generator)",
+        "config": {"workload": args.workload, "width": wl["width"], "height": wl["height"],
+                   "pairs_per_step": 1, "hessian_threshold": wl["threshold"],
+                   "parallelism": "replicas"},
+        "cpu_baseline": cpu,
+        "e2e": {"value": value, "unit": "pairs/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+
+
 def batch_sizes(wl):
     rng = np.random.default_rng(wl["seed"])
     idx = rng.integers(0, len(wl["sizes"]), wl["pairs"])
@@ -1182,6 +1212,9 @@ def main():
     wl = WORKLOADS[args.workload]
     world, rank, local = dist_setup(args)
     if args.impl == "reference":
+        if "pose" in wl:
+            run_reference_pose(args, wl, world, rank)
+            return
         if "groups" in wl:
             raise SystemExit("bench.py: the reference arm runs single-size workloads")
         if "checkpoint" in wl:

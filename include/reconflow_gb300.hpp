@@ -1,7 +1,8 @@
 // C++ class surface over the C ABI: drop-in replacements for the reference's
-// CudaFlow (reconflow/Cudaflow.h:17-362) and ReconFlow
-// (reconflow/Reconflow.h:9-160) with the same method names, argument meaning
-// and call order (test_reconflow/main.cpp:24-106).
+// CudaFlow (reconflow/Cudaflow.h:17-362), ReconFlow
+// (reconflow/Reconflow.h:9-160) and CameraPose (reconflow/CameraPose.h:11-64)
+// with the same method names, argument meaning and call order
+// (test_reconflow/main.cpp:24-106).
 //
 // Images and results are raw host pointers with a row pitch in elements
 // instead of cv::Mat (define RECONFLOW_GB300_WITH_OPENCV before including
@@ -11,6 +12,7 @@
 // checkCudaErrors).
 #pragma once
 
+#include <cstdint>
 #include <stdexcept>
 #include <string>
 
@@ -266,6 +268,59 @@ public:
 
 private:
     rf_batch* b_ = nullptr;
+};
+
+// CameraPose (reconflow/CameraPose.h:11-64): relative pose of two 8-bit gray
+// frames.  solvePose_8uc1 returns 0 and fills R (row-major 3x3) and t (unit,
+// x1 = R x0 + t) like the reference, or 1 when no keypoints / too few
+// matches / no model (the reference's "return 1" cases).
+class CameraPose {
+public:
+    CameraPose() { check(rf_pose_params_default(&p_)); }
+    ~CameraPose() { rf_pose_destroy(h_); }
+    CameraPose(const CameraPose&) = delete;
+    CameraPose& operator=(const CameraPose&) = delete;
+
+    int initialize(const double* intrinsic, int minHessian = 2000) {
+        for (int i = 0; i < 9; i++) K_[i] = intrinsic[i];
+        p_.hessian_threshold = minHessian;
+        release();
+        return 0;
+    }
+    int initialize(double focal, double ppx, double ppy, int minHessian = 2000) {
+        const double K[9] = {focal, 0.0, ppx, 0.0, focal, ppy, 0.0, 0.0, 1.0};
+        return initialize(K, minHessian);
+    }
+    int initialize(double focalx, double focaly, double ppx, double ppy, int minHessian) {
+        const double K[9] = {focalx, 0.0, ppx, 0.0, focaly, ppy, 0.0, 0.0, 1.0};
+        return initialize(K, minHessian);
+    }
+    // frames of width x height, `pitch` bytes per row
+    int solvePose_8uc1(const uint8_t* im1, const uint8_t* im2, int width, int height, int pitch,
+                       double* R, double* t) {
+        if (!h_ || width != w_ || height != hgt_) {
+            release();
+            check(rf_pose_create(&p_, width, height, &h_));
+            w_ = width;
+            hgt_ = height;
+        }
+        const rf_status s = rf_pose_solve_u8(h_, im1, im2, pitch, K_, R, t);
+        if (s == RF_ERR_STATE) return 1;
+        check(s);
+        return 0;
+    }
+    rf_pose_params& params() { return p_; }
+    rf_pose* handle() { return h_; }
+
+private:
+    void release() {
+        if (h_) rf_pose_destroy(h_);
+        h_ = nullptr;
+    }
+    rf_pose_params p_{};
+    rf_pose* h_ = nullptr;
+    double K_[9] = {1, 0, 0, 0, 1, 0, 0, 0, 1};
+    int w_ = 0, hgt_ = 0;
 };
 
 }  // namespace reconflow_gb300

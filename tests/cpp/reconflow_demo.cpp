@@ -1,6 +1,7 @@
 // Drives the C++ class surface in the call order of the reference demo
 // (test_reconflow/main.cpp:24-106): construct, initializeR, setCameraMatrices,
-// copyImagesToDevice, solveR, copyOpticalFlowToHost, copy3dToHost.  The input
+// copyImagesToDevice, solveR, copyOpticalFlowToHost, copy3dToHost; then the
+// batch class on the same pair and CameraPose on flat frames.  The input
 // is a synthetic textured pair shifted by one pixel.  Prints one line:
 // "ok <median u> <median Z>" or "error <status> <message>".
 #include <algorithm>
@@ -86,6 +87,15 @@ int main() {
         }
         if (!same) {
             std::printf("error 0 batch differs from the single-pair solve\n");
+            return 1;
+        }
+        // CameraPose: a flat frame pair has no keypoints -> 1, as the reference
+        reconflow_gb300::CameraPose pose;
+        pose.initialize(K, 2000);
+        std::vector<uint8_t> flat(width * height, 128);
+        double Rp[9], tp[3];
+        if (pose.solvePose_8uc1(flat.data(), flat.data(), width, height, width, Rp, tp) != 1) {
+            std::printf("error 0 CameraPose found a pose in flat frames\n");
             return 1;
         }
         std::printf("ok %.4f %.4f\n", uu[uu.size() / 2], zz[zz.size() / 2]);
