@@ -59,11 +59,11 @@ WORKLOADS = {
                     levels=6, warps=5, iters=100, seed=0),
     # batched + learned warm start: 64 pairs of 1280x720; the network predicts
     # inverse depth at 1/8, the solve refines from pyramid level 2 with the
-    # per-level schedule below (index = level, 0 = finest: 1 x 15, 1 x 30,
+    # per-level schedule below (index = level, 0 = finest: 1 x 4, 1 x 40,
     # 1 x 50); plain 5 x 100
     "720p-learned": dict(width=1280, height=720, pairs=64, levels=6, seed=2000, plain_warps=5,
                          plain_iters=100, warm_level=2, warm_warps=[1, 1, 1],
-                         warm_iters=[15, 30, 50], fallback_margin=0.02,
+                         warm_iters=[4, 40, 50], fallback_margin=0.02,
                          checkpoint="reconflow_gb300/weights/warmstart_f125.bin",
                          tiles="reconflow_gb300/tuning/gb300_720p_x64.json"),
     # batched + learned on mixed sizes (config 5 at a reduced count: 16 pairs
@@ -73,9 +73,9 @@ WORKLOADS = {
         levels=6, plain_warps=5, plain_iters=100, fallback_margin=0.02,
         checkpoint="reconflow_gb300/weights/warmstart_f125.bin",
         groups=[dict(width=3840, height=2160, pairs=16, seed=6000, warm_level=3,
-                     warm_warps=[1, 1, 1, 1], warm_iters=[15, 30, 50, 50]),
+                     warm_warps=[1, 1, 1, 1], warm_iters=[4, 30, 60, 80]),
                 dict(width=1920, height=1080, pairs=16, seed=6500, warm_level=2,
-                     warm_warps=[1, 1, 2], warm_iters=[20, 40, 60])]),
+                     warm_warps=[1, 1, 1], warm_iters=[4, 60, 80])]),
     # batched: 64 pairs of 1280x720 (per-pair throughput of the batched path)
     "batch64-720p": dict(pairs=64, sizes=[(1280, 720)], levels=6, warps=5, iters=100, seed=0),
     # profiling case of the batched kernels: 4 pairs of 1280x720 at their finest
