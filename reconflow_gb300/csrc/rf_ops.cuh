@@ -158,6 +158,56 @@ __device__ __forceinline__ int median3_tap(int col, int row, int w, int h, int s
 // ---------------------------------------------------------------------------
 // ReconFlow inner iteration, part B: dual step, 3D median, clean-up, sk
 // ---------------------------------------------------------------------------
+// Part B's arithmetic and stores at element `pos` from its loaded inputs.
+// xin / yin: the right / lower neighbour is inside the level.
+__device__ __forceinline__ void recon_b_finish(const ReconFields& f, const Weights& wt, int pos,
+                                               bool xin, bool yin, float duhat, float dvhat,
+                                               float duhr, float dvhr, float duhd, float dvhd,
+                                               float pu1, float pu2, float pv1, float pv2,
+                                               float (&mX)[9], float (&mY)[9], float (&mZ)[9],
+                                               float sku, float skv, float u, float v,
+                                               float uproj, float vproj) {
+    // --- dual TV step (solveSmoothDualTVGlobal.cu:26-64) ---
+    float dux, duy, dvx, dvy;
+    if (!xin) {
+        dux = 0.0f;
+        dvx = 0.0f;
+    } else {
+        dux = duhr - duhat;
+        dvx = dvhr - dvhat;
+    }
+    if (!yin) {
+        duy = 0.0f;
+        dvy = 0.0f;
+    } else {
+        duy = duhd - duhat;
+        dvy = dvhd - dvhat;
+    }
+    dual_step(dux, duy, wt.fac, pu1, pu2);
+    dual_step(dvx, dvy, wt.fac, pv1, pv2);
+
+    // --- 3x3 median of the triangulated points, then clean-up ---
+    // (Solve3d outputs are finite: non-finite results fall back to the
+    // previous, finite, state; so the min/max median network applies.)
+    float X1 = mX[4], Y1 = mY[4], Z1 = mZ[4];
+    float Xm = median9_finite(mX);
+    float Ym = median9_finite(mY);
+    float Zm = median9_finite(mZ);
+    float Xo, Yo, Zo;
+    cleanup_pixel(X1, Y1, Z1, Xm, Ym, Zm, Xo, Yo, Zo);
+
+    f.pu1[pos] = pu1;
+    f.pu2[pos] = pu2;
+    f.pv1[pos] = pv1;
+    f.pv2[pos] = pv2;
+    f.X[pos] = Xo;
+    f.Y[pos] = Yo;
+    f.Z[pos] = Zo;
+    // --- multiplier update (solveUcSk.cu:94-95) ---
+    f.sku[pos] = sku + u + duhat - uproj;
+    f.skv[pos] = skv + v + dvhat - vproj;
+}
+
 __device__ __forceinline__ void recon_b_px(const ReconFields& f, const Weights& wt, LevelDims d,
                                            int ix, int iy, int first, int base = 0) {
     const int s = d.s, w = d.w, h = d.h;
@@ -211,46 +261,8 @@ __device__ __forceinline__ void recon_b_px(const ReconFields& f, const Weights& 
     const float sku = f.sku[pos], skv = f.skv[pos];
     const float u = f.u[pos], v = f.v[pos];
     const float uproj = f.uproj[pos], vproj = f.vproj[pos];
-
-    // --- dual TV step (solveSmoothDualTVGlobal.cu:26-64) ---
-    float dux, duy, dvx, dvy;
-    if ((ix + 1) >= w) {
-        dux = 0.0f;
-        dvx = 0.0f;
-    } else {
-        dux = duhr - duhat;
-        dvx = dvhr - dvhat;
-    }
-    if ((iy + 1) >= h) {
-        duy = 0.0f;
-        dvy = 0.0f;
-    } else {
-        duy = duhd - duhat;
-        dvy = dvhd - dvhat;
-    }
-    dual_step(dux, duy, wt.fac, pu1, pu2);
-    dual_step(dvx, dvy, wt.fac, pv1, pv2);
-
-    // --- 3x3 median of the triangulated points, then clean-up ---
-    // (Solve3d outputs are finite: non-finite results fall back to the
-    // previous, finite, state; so the min/max median network applies.)
-    float X1 = mX[4], Y1 = mY[4], Z1 = mZ[4];
-    float Xm = median9_finite(mX);
-    float Ym = median9_finite(mY);
-    float Zm = median9_finite(mZ);
-    float Xo, Yo, Zo;
-    cleanup_pixel(X1, Y1, Z1, Xm, Ym, Zm, Xo, Yo, Zo);
-
-    f.pu1[pos] = pu1;
-    f.pu2[pos] = pu2;
-    f.pv1[pos] = pv1;
-    f.pv2[pos] = pv2;
-    f.X[pos] = Xo;
-    f.Y[pos] = Yo;
-    f.Z[pos] = Zo;
-    // --- multiplier update (solveUcSk.cu:94-95) ---
-    f.sku[pos] = sku + u + duhat - uproj;
-    f.skv[pos] = skv + v + dvhat - vproj;
+    recon_b_finish(f, wt, pos, (ix + 1) < w, (iy + 1) < h, duhat, dvhat, duhr, dvhr, duhd, dvhd,
+                   pu1, pu2, pv1, pv2, mX, mY, mZ, sku, skv, u, v, uproj, vproj);
 }
 
 __device__ __forceinline__ int median5_tap(int col, int row, int w, int h, int s) {

@@ -138,3 +138,36 @@ def test_bgr_frames(rf):
     r_gray = cp.solvePose_8uc1(g0, g1)
     r_bgr = cp.solvePose_8uc3(bgr0, bgr1)
     assert np.array_equal(r_gray[1], r_bgr[1]) and np.array_equal(r_gray[2], r_bgr[2])
+
+
+def test_keypoint_cap_keeps_the_strongest(oracle, rf):
+    """max_keypoints keeps the strongest keypoints (ties by octave, layer,
+    cell), exactly as the oracle's list cut at the same length."""
+    sc = _scene(640, 480, 11)
+    a, b = _to8(sc["I0"]), _to8(sc["I1"])
+    cp = _pose(rf, sc["K"])
+    cp.params.max_keypoints = 300
+    cp.solvePose_8uc1(a, b)
+    kp, desc = cp.keypoints(0)
+    kp_ref, desc_ref = oracle.surf_detect(a, threshold=THRESHOLD, max_kp=300)
+    assert len(kp) == 300
+    assert np.array_equal(_bits(kp), _bits(kp_ref))
+    assert np.array_equal(_bits(desc), _bits(desc_ref))
+    assert np.all(np.diff(kp[:, 4]) <= 0)  # strongest first
+
+
+def test_small_and_degenerate_frames(rf):
+    """Frames too small for the coarser octaves, and noise at threshold 0
+    (tens of thousands of candidates, possibly more than their buffer holds),
+    end in a pose or in 1 (no pose), never in an error."""
+    K = np.array([[100.0, 0, 24], [0, 100.0, 20], [0, 0, 1]])
+    rng = np.random.default_rng(0)
+    tiny = rng.integers(0, 256, (40, 48)).astype(np.uint8)
+    cp = _pose(rf, K)
+    ret, R, t = cp.solvePose_8uc1(tiny, tiny)
+    assert ret in (0, 1)
+    n0 = rng.integers(0, 256, (720, 1280)).astype(np.uint8)
+    n1 = rng.integers(0, 256, (720, 1280)).astype(np.uint8)
+    cp2 = _pose(rf, K, thr=0.0)
+    cp2.params.max_keypoints = 64
+    assert cp2.solvePose_8uc1(n0, n1)[0] in (0, 1)
