@@ -165,3 +165,29 @@ def test_oracle_pose_on_a_rendered_scene(oracle):
     R2, t2 = P.refine_pose(R, t, x0, x1, mask)
     assert _angle(R2, sc["R"]) < 0.05
     assert np.degrees(np.arccos(np.clip(t2 @ tg, -1, 1))) < 0.5
+
+
+def test_oracle_matches_committed_fixtures(oracle):
+    """The pose oracle's feature stages on the committed frames equal the
+    committed fixtures bit for bit (tests/golden/make_pose_golden.py)."""
+    import os
+
+    path = os.path.join(os.path.dirname(__file__), "golden", "pose_cases.npz")
+    g = np.load(path)
+    k0, d0 = oracle.surf_detect(g["frame0"], threshold=10.0)
+    k1, d1 = oracle.surf_detect(g["frame1"], threshold=10.0)
+    best, e1, e2 = oracle.surf_match(d0, d1)
+    for got, key in ((k0, "kp0"), (d0, "desc0"), (k1, "kp1"), (d1, "desc1"), (e1, "d1"),
+                     (e2, "d2")):
+        assert np.array_equal(got.view(np.uint32), g[key].view(np.uint32)), key
+    assert np.array_equal(best, g["best"])
+    # the frames differ by a 2.3 / -1.7 px shift and a 0.05 rad rotation about
+    # the centre: every ratio-tested match follows that motion
+    ok = np.sqrt(e1) < 0.6 * np.sqrt(e2)
+    assert ok.sum() >= 10
+    c, s = np.cos(0.05), np.sin(0.05)
+    R = np.array([[c, s], [-s, c]])
+    ctr = np.array([80.0, 60.0])
+    want = (k0[ok, :2].astype(np.float64) + np.array([2.3, -1.7]) - ctr) @ R + ctr
+    err = np.linalg.norm(k1[best[ok], :2] - want, axis=1)
+    assert np.max(err) < 0.5 and np.median(err) < 0.1, err
