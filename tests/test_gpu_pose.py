@@ -171,3 +171,20 @@ def test_small_and_degenerate_frames(rf):
     cp2 = _pose(rf, K, thr=0.0)
     cp2.params.max_keypoints = 64
     assert cp2.solvePose_8uc1(n0, n1)[0] in (0, 1)
+
+
+def test_gpu_matches_committed_fixtures(rf):
+    """The GPU's keypoints, descriptors and matches on the committed frames
+    equal the committed oracle fixtures bit for bit."""
+    import os
+
+    g = np.load(os.path.join(os.path.dirname(__file__), "golden", "pose_cases.npz"))
+    cp = _pose(rf, np.array([[150.0, 0, 80], [0, 150.0, 60], [0, 0, 1]]), thr=10.0)
+    cp.solvePose_8uc1(g["frame0"], g["frame1"])
+    for f in (0, 1):
+        kp, desc = cp.keypoints(f)
+        assert np.array_equal(_bits(kp), _bits(g[f"kp{f}"])), f
+        assert np.array_equal(_bits(desc), _bits(g[f"desc{f}"])), f
+    q = np.nonzero(np.sqrt(g["d1"]).astype(np.float64) < 0.6 * np.sqrt(g["d2"]).astype(np.float64))[0]
+    i0, i1, dist, _ = cp.matches()
+    assert np.array_equal(i0, q) and np.array_equal(i1, g["best"][q])
