@@ -89,6 +89,10 @@ WORKLOADS = {
     # is for camera images)
     "pose-720p": dict(width=1280, height=720, pairs=64, seed=2000, threads=8, threshold=20.0,
                       pose=True),
+    # the warm-start network alone: one forward pass over the 1/8-grid inputs
+    # of 64 720p pairs (64 x 90 x 160 x 16), the committed checkpoint
+    "warmstart-net-720p": dict(pairs=64, height=90, width=160,
+                               checkpoint="reconflow_gb300/weights/warmstart_f125.bin", net=True),
 }
 SOLVER = dict(method=14, lam=50.0, theta=0.33, tau=0.25, alpha_proj=60.0, lambdaf=0.1,
               lambdams=100.0, fix_quirks=1)
@@ -730,6 +734,93 @@ def run_learned(args, wl, world, rank, local):
 
 
 POSE_METRIC = "720p pose estimates/s (CameraPose: features, matching, LMedS, pose recovery)"
+NET_METRIC = "720p pairs/s through the warm-start network's forward pass (64 per pass)"
+
+# (cin, cout, stride) of the network's six convolutions; 3 and 4 run at half
+# resolution, 5 takes the upsampled 96 channels concatenated with layer 1's 32
+NET_LAYERS = [(16, 32, 1, 1), (32, 96, 2, 2), (96, 96, 1, 2), (96, 8, 1, 2), (128, 64, 1, 1),
+              (64, 8, 1, 1)]
+
+
+def run_net(args, wl, world, rank, local):
+    """The warm-start network's forward pass (six tcgen05 implicit-GEMM
+    convolutions, BF16 operands, FP32 accumulation) on seeded inputs of the
+    learned workload's shape; roofline against the measured BF16 GEMM peak."""
+    import torch
+
+    from reconflow_gb300.warmstart import WarmStartNet
+
+    torch.cuda.set_device(local)
+    B, H, W = wl["pairs"], wl["height"], wl["width"]
+    net = WarmStartNet(B, H + 1, W + 1, seed=0)
+    net.load(os.path.join(ROOT, wl["checkpoint"]))
+    stream = torch.cuda.Stream()
+    net.set_stream(stream.cuda_stream)
+    g = torch.Generator(device="cuda").manual_seed(1000 + rank)
+    x = (torch.randn(B, H, W, 16, device="cuda", generator=g) * 0.3).contiguous()
+    o16 = torch.empty(B, (H + 1) // 2, (W + 1) // 2, 8, device="cuda")
+    o8 = torch.empty(B, H, W, 8, device="cuda")
+    flops = 0
+    for cin, cout, stride, res in NET_LAYERS:
+        m = B * H * W if res == 1 else B * ((H + 1) // 2) * ((W + 1) // 2)
+        flops += 2 * m * cout * 9 * cin
+    with torch.cuda.stream(stream):
+        for _ in range(args.warmup):
+            net.forward(x, o16, o8)
+        torch.cuda.synchronize()
+        barrier(world)
+        l0 = net.kernel_launches()
+        evs = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
+               for _ in range(args.steps)]
+        with ClockSampler(local) as clk:
+            for a, e in evs:
+                a.record(stream)
+                net.forward(x, o16, o8)
+                e.record(stream)
+            torch.cuda.synchronize()
+        launches = net.kernel_launches() - l0
+        ms = [a.elapsed_time(e) for a, e in evs]
+        # end to end: inputs from pinned host memory in, both outputs back
+        xh = x.cpu().pin_memory()
+        h16 = torch.empty(o16.shape, pin_memory=True)
+        h8 = torch.empty(o8.shape, pin_memory=True)
+        et = []
+        for _ in range(args.steps):
+            torch.cuda.synchronize()
+            t1 = time.perf_counter()
+            x.copy_(xh, non_blocking=True)
+            net.forward(x, o16, o8)
+            h16.copy_(o16, non_blocking=True)
+            h8.copy_(o8, non_blocking=True)
+            torch.cuda.synchronize()
+            et.append(time.perf_counter() - t1)
+    total_s = max_over_ranks(sum(ms) / 1000.0, world)
+    per_pass = total_s / args.steps
+    peaks_path = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    peak, kind = 1900.0, "fallback"
+    if os.path.exists(peaks_path):
+        with open(peaks_path) as fh:
+            peak, kind = float(json.load(fh)["bf16_tflops"]), "measured"
+    achieved = flops / per_pass / 1e12
+    if rank == 0:
+        print(json.dumps({
+            "metric": NET_METRIC, "value": world * B / per_pass, "unit": "pairs/s",
+            "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": 1000.0 * per_pass, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "bf16 (FP32 accumulate)", "data": "synthetic (seeded)",
+            "config": {"workload": args.workload, "batch": B, "grid": [H, W], "channels_in": 16,
+                       "layers": NET_LAYERS, "checkpoint": wl["checkpoint"],
+                       "parallelism": "replicas"},
+            "e2e": {"value": world * B * len(et) / max_over_ranks(sum(et), world),
+                    "unit": "pairs/s", "h2d_bytes_per_step": x.numel() * 4,
+                    "d2h_bytes_per_step": (o16.numel() + o8.numel()) * 4},
+            "roofline": {"bound": "tensor", "kernel": "k_tc_gemm (six convolutions)",
+                         "achieved": achieved, "peak": peak, "peak_kind": kind,
+                         "unit": "TFLOP/s", "frac": achieved / peak, "traffic": None,
+                         "flops_per_pass": flops},
+            "clocks": clk.summary(), "gpu_launches": int(launches),
+        }), flush=True)
+    net.close()
 
 
 def run_pose(args, wl, world, rank, local):
@@ -1212,6 +1303,11 @@ def main():
     wl = WORKLOADS[args.workload]
     world, rank, local = dist_setup(args)
     if args.impl == "reference":
+        if "net" in wl:
+            if rank == 0:
+                print(json.dumps({"impl": "reference", "unavailable": "the reference has no "
+                                  "learned warm start (no network to time)"}), flush=True)
+            return
         if "pose" in wl:
             run_reference_pose(args, wl, world, rank)
             return
@@ -1228,6 +1324,9 @@ def main():
         return
     if "pose" in wl:
         run_pose(args, wl, world, rank, local)
+        return
+    if "net" in wl:
+        run_net(args, wl, world, rank, local)
         return
     if "groups" in wl:
         run_learned_mixed(args, wl, world, rank, local)
