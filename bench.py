@@ -66,9 +66,9 @@ WORKLOADS = {
                          warm_iters=[4, 40, 50], fallback_margin=0.02,
                          checkpoint="reconflow_gb300/weights/warmstart_f125.bin",
                          tiles="reconflow_gb300/tuning/gb300_720p_x64.json"),
-    # batched + learned on mixed sizes (config 5 at a reduced count: 16 pairs
-    # of 3840x2160 and 16 of 1920x1080, independent scenes); 4K starts the
-    # refinement at pyramid level 3 (its network grid is 1/32)
+    # batched + learned on mixed sizes (the 4K / 1080p stream at a reduced
+    # count: 16 pairs of 3840x2160 and 16 of 1920x1080, independent scenes);
+    # 4K starts the refinement at pyramid level 3 (its network grid is 1/32)
     "mixed-4k-1080p-learned": dict(
         levels=6, plain_warps=5, plain_iters=100, fallback_margin=0.02,
         checkpoint="reconflow_gb300/weights/warmstart_f125.bin",
@@ -1040,8 +1040,8 @@ def pose_cpu_sample(scenes, threshold):
 
 def run_learned_mixed(args, wl, world, rank, local):
     """Batched + learned warm start on a mix of frame sizes (one batch, one
-    network pass and one refinement per size group; BASELINE config 5 at a
-    reduced count, with independent seeded scenes instead of sequences).
+    network pass and one refinement per size group; the 4K / 1080p stream at
+    a reduced count, with independent seeded scenes instead of sequences).
     One step = every group through the learned path with its fallback; the
     plain solver's batched and single-pair times are measured per group."""
     import torch

@@ -1,7 +1,7 @@
 // Relative pose from point matches, host side of the pose front end
 // (CameraPose::solvePose_8uc1, reconflow/CameraPose.cpp:79-104, which calls
 // OpenCV's findEssentialMat(..., LMEDS, 0.999) and recoverPose).  OpenCV is
-// not part of this build; its published methods are restated here:
+// not used here; the published methods are restated:
 //
 // * five-point solver: D. Nister, "An efficient solution to the five-point
 //   relative pose problem", IEEE PAMI 26(6), 2004 -- null space of the 5x9
