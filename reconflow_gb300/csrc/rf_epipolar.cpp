@@ -3,12 +3,7 @@
 // OpenCV's findEssentialMat(..., LMEDS, 0.999) and recoverPose).  OpenCV is
 // not used here; the published methods are restated:
 //
-// * five-point solver: D. Nister, "An efficient solution to the five-point
-//   relative pose problem", IEEE PAMI 26(6), 2004 -- null space of the 5x9
-//   epipolar system, the ten cubic constraints det(E) = 0 and
-//   2 E E^T E - tr(E E^T) E = 0, Gauss-Jordan elimination in Nister's
-//   monomial order, the 3x3 polynomial matrix in z and its degree-10
-//   determinant, real roots, back-substitution;
+// * the five-point solver (rf_fivept.cuh, shared with the GPU);
 // * least median of squares (P. J. Rousseeuw, "Least median of squares
 //   regression", JASA 79, 1984) over random five-point samples with the
 //   squared Sampson distance, the sample count for confidence `conf` at an
@@ -21,17 +16,16 @@
 //
 // Everything is double precision and deterministic (seeded sampling).
 #include <algorithm>
-#include <array>
 #include <cmath>
 #include <cstdint>
 #include <cstring>
-#include <initializer_list>
 #include <atomic>
 #include <thread>
 #include <vector>
 
 #include "../../include/reconflow_gb300.h"
 #include "rf_epipolar.h"
+#include "rf_fivept.cuh"
 
 namespace rf_epi {
 
@@ -150,337 +144,7 @@ void svd3(const double* A, double* U, double* s, double* V) {
         for (int k = 0; k < 3; k++) U[i * 3 + k] = u[k][i];
 }
 
-// ---------------------------------------------------------------------------
-// Polynomials in (x, y, z) of degree <= 3 and in one variable
-// ---------------------------------------------------------------------------
-
-// Polynomials in (x, y, z): linear ones as [x, y, z, 1], quadratic ones over
-// the ten monomials of degree <= 2, cubic ones over the twenty monomials of
-// degree <= 3 in Nister's order (kMono below).  Products go through tables of
-// monomial indices built once from the exponents.
-using Lin = std::array<double, 4>;
-using Quad = std::array<double, 10>;
-using Cub = std::array<double, 20>;
-
-constexpr int kLinExp[4][3] = {{1, 0, 0}, {0, 1, 0}, {0, 0, 1}, {0, 0, 0}};
-constexpr int kQuadExp[10][3] = {{2, 0, 0}, {0, 2, 0}, {0, 0, 2}, {1, 1, 0}, {1, 0, 1},
-                                 {0, 1, 1}, {1, 0, 0}, {0, 1, 0}, {0, 0, 1}, {0, 0, 0}};
-// Nister's monomial order: x^3 y^3 x^2y xy^2 x^2z x^2 y^2z y^2 xyz xy | xz^2
-// xz x yz^2 yz y z^3 z^2 z 1
-constexpr int kMono[20][3] = {{3, 0, 0}, {0, 3, 0}, {2, 1, 0}, {1, 2, 0}, {2, 0, 1},
-                              {2, 0, 0}, {0, 2, 1}, {0, 2, 0}, {1, 1, 1}, {1, 1, 0},
-                              {1, 0, 2}, {1, 0, 1}, {1, 0, 0}, {0, 1, 2}, {0, 1, 1},
-                              {0, 1, 0}, {0, 0, 3}, {0, 0, 2}, {0, 0, 1}, {0, 0, 0}};
-
-struct MonoTables {
-    int ll[4][4];   // Lin x Lin -> Quad index
-    int ql[10][4];  // Quad x Lin -> Cub index
-    MonoTables() {
-        auto find = [](const int (*tab)[3], int n, int a, int b, int c) {
-            for (int i = 0; i < n; i++)
-                if (tab[i][0] == a && tab[i][1] == b && tab[i][2] == c) return i;
-            return -1;
-        };
-        for (int i = 0; i < 4; i++)
-            for (int j = 0; j < 4; j++)
-                ll[i][j] = find(kQuadExp, 10, kLinExp[i][0] + kLinExp[j][0],
-                                kLinExp[i][1] + kLinExp[j][1], kLinExp[i][2] + kLinExp[j][2]);
-        for (int i = 0; i < 10; i++)
-            for (int j = 0; j < 4; j++)
-                ql[i][j] = find(kMono, 20, kQuadExp[i][0] + kLinExp[j][0],
-                                kQuadExp[i][1] + kLinExp[j][1], kQuadExp[i][2] + kLinExp[j][2]);
-    }
-};
-const MonoTables& mono_tables() {
-    static const MonoTables t;
-    return t;
-}
-
-Quad mul(const Lin& a, const Lin& b) {
-    const MonoTables& T = mono_tables();
-    Quad r{};
-    for (int i = 0; i < 4; i++)
-        for (int j = 0; j < 4; j++) r[T.ll[i][j]] += a[i] * b[j];
-    return r;
-}
-
-Cub mul(const Quad& a, const Lin& b) {
-    const MonoTables& T = mono_tables();
-    Cub r{};
-    for (int i = 0; i < 10; i++)
-        for (int j = 0; j < 4; j++) r[T.ql[i][j]] += a[i] * b[j];
-    return r;
-}
-
-template <size_t N>
-std::array<double, N> lin_comb(const std::array<double, N>& a, double ka,
-                               const std::array<double, N>& b, double kb) {
-    std::array<double, N> r;
-    for (size_t i = 0; i < N; i++) r[i] = ka * a[i] + kb * b[i];
-    return r;
-}
-
-// one-variable polynomials of degree <= 10, coefficient k of z^k
-struct Poly1 {
-    double c[11] = {};
-    int n = 0;  // number of coefficients
-};
-
-Poly1 poly(std::initializer_list<double> v) {
-    Poly1 r;
-    for (double x : v) r.c[r.n++] = x;
-    return r;
-}
-
-Poly1 pmul(const Poly1& a, const Poly1& b) {
-    Poly1 r;
-    r.n = a.n + b.n - 1;
-    for (int i = 0; i < a.n; i++)
-        for (int j = 0; j < b.n; j++) r.c[i + j] += a.c[i] * b.c[j];
-    return r;
-}
-
-Poly1 padd(const Poly1& a, const Poly1& b, double kb) {
-    Poly1 r;
-    r.n = std::max(a.n, b.n);
-    for (int i = 0; i < a.n; i++) r.c[i] += a.c[i];
-    for (int i = 0; i < b.n; i++) r.c[i] += kb * b.c[i];
-    return r;
-}
-
-double peval(const Poly1& p, double z) {
-    double r = 0.0;
-    for (int i = p.n; i-- > 0;) r = r * z + p.c[i];
-    return r;
-}
-
-void ptrim(Poly1& p) {
-    double mx = 0.0;
-    for (int i = 0; i < p.n; i++) mx = std::max(mx, std::fabs(p.c[i]));
-    while (p.n > 1 && std::fabs(p.c[p.n - 1]) <= 1e-14 * mx) p.n--;
-}
-
-// Root of p in [lo, hi] where p changes sign: the Illinois variant of
-// regula falsi (M. Dowell, P. Jarratt, BIT 11, 1971), with a bisection step
-// whenever the secant point leaves the middle 98% of the bracket, until the
-// iterate moves by less than `rel` of its magnitude.
-double bracket_root(const Poly1& p, double lo, double hi, double rel) {
-    double flo = peval(p, lo), fhi = peval(p, hi);
-    double prev = lo;
-    int side = 0;
-    for (int it = 0; it < 100; it++) {
-        const double width = hi - lo;
-        double x = (lo * fhi - hi * flo) / (fhi - flo);
-        if (!(x > lo + 0.01 * width && x < hi - 0.01 * width)) x = 0.5 * (lo + hi);
-        const double fx = peval(p, x);
-        if (fx == 0.0 || std::fabs(x - prev) <= rel * std::max(1.0, std::fabs(x))) return x;
-        prev = x;
-        if ((fx < 0) == (flo < 0)) {
-            lo = x;
-            flo = fx;
-            if (side == -1) fhi *= 0.5;
-            side = -1;
-        } else {
-            hi = x;
-            fhi = fx;
-            if (side == 1) flo *= 0.5;
-            side = 1;
-        }
-    }
-    return 0.5 * (lo + hi);
-}
-
-// Real roots of p (ascending) into out, returns their number: p is monotonic
-// between consecutive real roots of p', which are found the same way (to a
-// looser tolerance: they only bracket), down to degree 1.
-int real_roots(Poly1 p, double rel, double* out) {
-    ptrim(p);
-    const int deg = p.n - 1;
-    if (deg < 1) return 0;
-    if (deg == 1) {
-        out[0] = -p.c[0] / p.c[1];
-        return 1;
-    }
-    // Fujiwara's bound on the magnitude of every root:
-    // 2 max_k |a_(n-k) / a_n|^(1/k), the k = n term halved first
-    double bound = 0.0;
-    for (int k = 1; k <= deg; k++) {
-        double r = std::fabs(p.c[deg - k] / p.c[deg]);
-        if (k == deg) r *= 0.5;
-        bound = std::max(bound, std::pow(r, 1.0 / k));
-    }
-    bound = 2.0 * bound * (1.0 + 1e-12) + 1e-300;
-    Poly1 d;
-    d.n = deg;
-    for (int i = 1; i <= deg; i++) d.c[i - 1] = i * p.c[i];
-    double crit[10];
-    const int nc = real_roots(d, 1e-9, crit);
-    double pts[12];
-    int np = 0;
-    pts[np++] = -bound;
-    for (int k = 0; k < nc; k++)
-        if (crit[k] > -bound && crit[k] < bound && crit[k] > pts[np - 1]) pts[np++] = crit[k];
-    pts[np++] = bound;
-    int n = 0;
-    for (int k = 0; k + 1 < np; k++) {
-        const double a = pts[k], b = pts[k + 1];
-        const double fa = peval(p, a), fb = peval(p, b);
-        if (fa == 0.0) {
-            if (n == 0 || out[n - 1] != a) out[n++] = a;
-            continue;
-        }
-        if ((fa < 0) != (fb < 0)) out[n++] = bracket_root(p, a, b, rel);
-    }
-    if (peval(p, pts[np - 1]) == 0.0 && (n == 0 || out[n - 1] != pts[np - 1])) out[n++] = pts[np - 1];
-    return n;
-}
-
-// ---------------------------------------------------------------------------
-// Five-point solver
-// ---------------------------------------------------------------------------
-
-// x0, x1: five normalized image points each ([5][2]); writes up to 10
-// essential matrices (row-major, unit Frobenius norm) with x1^T E x0 = 0.
-int five_point(const double* x0, const double* x1, double* Es) {
-    // epipolar rows: x1^T E x0 = sum_ij E_ij x1_i x0_j
-    double Q[5][9];
-    for (int k = 0; k < 5; k++) {
-        const double a[3] = {x0[2 * k], x0[2 * k + 1], 1.0};
-        const double b[3] = {x1[2 * k], x1[2 * k + 1], 1.0};
-        for (int i = 0; i < 3; i++)
-            for (int j = 0; j < 3; j++) Q[k][i * 3 + j] = b[i] * a[j];
-    }
-    // null space: Householder QR of Q^T (9 x 5), Q^T = H1 ... H5 [R; 0]; the
-    // last four columns of H1 ... H5 are orthogonal to every row of Q
-    double A[9][5], hv[5][9];
-    for (int i = 0; i < 9; i++)
-        for (int k = 0; k < 5; k++) A[i][k] = Q[k][i];
-    for (int k = 0; k < 5; k++) {
-        double nrm = 0.0;
-        for (int i = k; i < 9; i++) nrm += A[i][k] * A[i][k];
-        nrm = std::sqrt(nrm);
-        const double alpha = A[k][k] > 0 ? -nrm : nrm;
-        for (int i = 0; i < 9; i++) hv[k][i] = i < k ? 0.0 : A[i][k];
-        hv[k][k] -= alpha;
-        double vn = 0.0;
-        for (int i = k; i < 9; i++) vn += hv[k][i] * hv[k][i];
-        if (vn > 0.0)
-            for (int j = k; j < 5; j++) {
-                double d = 0.0;
-                for (int i = k; i < 9; i++) d += hv[k][i] * A[i][j];
-                const double f = 2.0 * d / vn;
-                for (int i = k; i < 9; i++) A[i][j] -= f * hv[k][i];
-            }
-        for (int i = k; i < 9; i++) hv[k][i] = vn > 0.0 ? hv[k][i] / std::sqrt(vn) : 0.0;
-    }
-    double basis[4][9];  // X, Y, Z, W = H1 ... H5 e_(6..9)
-    for (int b = 0; b < 4; b++) {
-        double v[9] = {};
-        v[5 + b] = 1.0;
-        for (int k = 4; k >= 0; k--) {
-            double d = 0.0;
-            for (int i = k; i < 9; i++) d += hv[k][i] * v[i];
-            for (int i = k; i < 9; i++) v[i] -= 2.0 * d * hv[k][i];
-        }
-        for (int i = 0; i < 9; i++) basis[b][i] = v[i];
-    }
-    // E_ij = x X_ij + y Y_ij + z Z_ij + W_ij as linear polynomials
-    Lin E[9];
-    for (int i = 0; i < 9; i++) E[i] = Lin{basis[0][i], basis[1][i], basis[2][i], basis[3][i]};
-    // ten cubic constraints: det(E) and 2 E E^T E - tr(E E^T) E
-    Cub cons[10];
-    {
-        const Quad m0 = lin_comb(mul(E[4], E[8]), 1.0, mul(E[5], E[7]), -1.0);
-        const Quad m1 = lin_comb(mul(E[3], E[8]), 1.0, mul(E[5], E[6]), -1.0);
-        const Quad m2 = lin_comb(mul(E[3], E[7]), 1.0, mul(E[4], E[6]), -1.0);
-        cons[0] = lin_comb(lin_comb(mul(m0, E[0]), 1.0, mul(m1, E[1]), -1.0), 1.0, mul(m2, E[2]),
-                           1.0);
-    }
-    Quad EEt[9];
-    for (int i = 0; i < 3; i++)
-        for (int j = 0; j < 3; j++) {
-            Quad q{};
-            for (int k = 0; k < 3; k++) q = lin_comb(q, 1.0, mul(E[i * 3 + k], E[j * 3 + k]), 1.0);
-            EEt[i * 3 + j] = q;
-        }
-    const Quad tr = lin_comb(lin_comb(EEt[0], 1.0, EEt[4], 1.0), 1.0, EEt[8], 1.0);
-    for (int i = 0; i < 3; i++)
-        for (int j = 0; j < 3; j++) {
-            Cub c{};
-            for (int k = 0; k < 3; k++) c = lin_comb(c, 1.0, mul(EEt[i * 3 + k], E[k * 3 + j]), 1.0);
-            cons[1 + i * 3 + j] = lin_comb(c, 2.0, mul(tr, E[i * 3 + j]), -1.0);
-        }
-    double M[10][20];
-    for (int r = 0; r < 10; r++)
-        for (int m = 0; m < 20; m++) M[r][m] = cons[r][m];
-    // Gauss-Jordan on the first ten columns (partial pivoting)
-    for (int c = 0; c < 10; c++) {
-        int piv = c;
-        for (int r = c + 1; r < 10; r++)
-            if (std::fabs(M[r][c]) > std::fabs(M[piv][c])) piv = r;
-        if (!(std::fabs(M[piv][c]) > 1e-300)) return 0;
-        if (piv != c)
-            for (int m = 0; m < 20; m++) std::swap(M[piv][m], M[c][m]);
-        const double inv = 1.0 / M[c][c];
-        for (int m = 0; m < 20; m++) M[c][m] *= inv;
-        for (int r = 0; r < 10; r++) {
-            if (r == c || M[r][c] == 0.0) continue;
-            const double f = M[r][c];
-            for (int m = 0; m < 20; m++) M[r][m] -= f * M[c][m];
-        }
-    }
-    // rows e..j (4..9) lead with x^2z, x^2, y^2z, y^2, xyz, xy; each remainder is
-    // x (B10 z^2 + B11 z + B12) + y (B13 z^2 + B14 z + B15) + B16 z^3 + B17 z^2 + B18 z + B19
-    auto xpart = [&](int r) { return poly({M[r][12], M[r][11], M[r][10]}); };
-    auto ypart = [&](int r) { return poly({M[r][15], M[r][14], M[r][13]}); };
-    auto cpart = [&](int r) { return poly({M[r][19], M[r][18], M[r][17], M[r][16]}); };
-    const Poly1 zpoly = poly({0.0, 1.0});
-    Poly1 B[3][3];
-    const int pairs[3][2] = {{4, 5}, {6, 7}, {8, 9}};  // <k> = <e> - z<f>, <l> = <g> - z<h>, <m> = <i> - z<j>
-    for (int q = 0; q < 3; q++) {
-        const int a = pairs[q][0], b = pairs[q][1];
-        B[q][0] = padd(xpart(a), pmul(zpoly, xpart(b)), -1.0);
-        B[q][1] = padd(ypart(a), pmul(zpoly, ypart(b)), -1.0);
-        B[q][2] = padd(cpart(a), pmul(zpoly, cpart(b)), -1.0);
-    }
-    const Poly1 c0 = padd(pmul(B[1][1], B[2][2]), pmul(B[1][2], B[2][1]), -1.0);
-    const Poly1 c1 = padd(pmul(B[1][0], B[2][2]), pmul(B[1][2], B[2][0]), -1.0);
-    const Poly1 c2 = padd(pmul(B[1][0], B[2][1]), pmul(B[1][1], B[2][0]), -1.0);
-    const Poly1 det = padd(padd(pmul(B[0][0], c0), pmul(B[0][1], c1), -1.0), pmul(B[0][2], c2), 1.0);
-    double zs[10];
-    const int nz = real_roots(det, 1e-15, zs);
-    int count = 0;
-    for (int zi = 0; zi < nz; zi++) {
-        const double z = zs[zi];
-        double Bz[3][3];
-        for (int q = 0; q < 3; q++)
-            for (int c = 0; c < 3; c++) Bz[q][c] = peval(B[q][c], z);
-        // null vector of B(z): the largest cross product of two of its rows
-        double best[3] = {0, 0, 0}, bn = -1.0;
-        const int rp[3][2] = {{0, 1}, {0, 2}, {1, 2}};
-        for (auto& pr : rp) {
-            double c[3];
-            cross3(Bz[pr[0]], Bz[pr[1]], c);
-            const double nn = c[0] * c[0] + c[1] * c[1] + c[2] * c[2];
-            if (nn > bn) {
-                bn = nn;
-                std::memcpy(best, c, sizeof(c));
-            }
-        }
-        if (!(std::fabs(best[2]) > 1e-300)) continue;
-        const double x = best[0] / best[2], y = best[1] / best[2];
-        double Em[9], nrm = 0.0;
-        for (int i = 0; i < 9; i++) {
-            Em[i] = x * basis[0][i] + y * basis[1][i] + z * basis[2][i] + basis[3][i];
-            nrm += Em[i] * Em[i];
-        }
-        nrm = std::sqrt(nrm);
-        if (!(nrm > 0.0) || !std::isfinite(nrm)) continue;
-        for (int i = 0; i < 9; i++) Es[count * 9 + i] = Em[i] / nrm;
-        if (++count == 10) break;
-    }
-    return count;
-}
+using rf_fivept::five_point;
 
 uint64_t splitmix64(uint64_t& s) {
     uint64_t z = (s += 0x9e3779b97f4a7c15ULL);
@@ -535,9 +199,9 @@ int lmeds_iterations(double conf) {
     return std::max(1, std::min(iters, 1000));
 }
 
-// Every five-point hypothesis of the seeded samples, in sample order.
-std::vector<double> lmeds_hypotheses(const double* x0, const double* x1, int n, double conf,
-                                     uint64_t seed) {
+// The seeded LMedS samples: lmeds_iterations(conf) sets of five distinct
+// match indices, [sample][5].
+std::vector<int> lmeds_samples(int n, double conf, uint64_t seed) {
     const int iters = lmeds_iterations(conf);
     std::vector<int> samples((size_t)iters * 5);
     uint64_t st = seed;
@@ -552,6 +216,14 @@ std::vector<double> lmeds_hypotheses(const double* x0, const double* x1, int n, 
             }
         }
     }
+    return samples;
+}
+
+// Every five-point hypothesis of the seeded samples, in sample order.
+std::vector<double> lmeds_hypotheses(const double* x0, const double* x1, int n, double conf,
+                                     uint64_t seed) {
+    const std::vector<int> samples = lmeds_samples(n, conf, seed);
+    const int iters = (int)(samples.size() / 5);
     std::vector<double> sols((size_t)iters * 90);
     std::vector<int> counts(iters);
     parallel_for(iters, [&](int it) {
@@ -565,10 +237,14 @@ std::vector<double> lmeds_hypotheses(const double* x0, const double* x1, int n, 
         }
         counts[it] = five_point(a, b, &sols[(size_t)it * 90]);
     });
+    return lmeds_collect(sols, counts);
+}
+
+// Hypotheses in sample order from per-sample slots of 10 (counts[s] used).
+std::vector<double> lmeds_collect(const std::vector<double>& sols, const std::vector<int>& counts) {
     std::vector<double> hyp;
-    for (int it = 0; it < iters; it++)
-        hyp.insert(hyp.end(), sols.begin() + (size_t)it * 90,
-                   sols.begin() + (size_t)it * 90 + 9 * counts[it]);
+    for (size_t it = 0; it < counts.size(); it++)
+        hyp.insert(hyp.end(), sols.begin() + it * 90, sols.begin() + it * 90 + 9 * counts[it]);
     return hyp;
 }
 

@@ -188,3 +188,30 @@ def test_gpu_matches_committed_fixtures(rf):
     q = np.nonzero(np.sqrt(g["d1"]).astype(np.float64) < 0.6 * np.sqrt(g["d2"]).astype(np.float64))[0]
     i0, i1, dist, _ = cp.matches()
     assert np.array_equal(i0, q) and np.array_equal(i1, g["best"][q])
+
+
+def test_gpu_lmeds_equals_host_lmeds(rf):
+    """The GPU's five-point solutions and medians pick the same model as the
+    host API on the same matches and seed: R and t bit for bit."""
+    from reconflow_gb300 import pose as P
+
+    sc = _scene(640, 480, 12)
+    cp = _pose(rf, sc["K"])
+    ret, R, t = cp.solvePose_8uc1(_to8(sc["I0"]), _to8(sc["I1"]))
+    assert ret == 0
+    k0, _ = cp.keypoints(0)
+    k1, _ = cp.keypoints(1)
+    i0, i1, _, inl = cp.matches()
+    K = sc["K"]
+    fx, sk, cx, fy, cy = K[0, 0], K[0, 1], K[0, 2], K[1, 1], K[1, 2]
+
+    def norm(k):
+        y = (k[:, 1].astype(np.float64) - cy) / fy
+        x = ((k[:, 0].astype(np.float64) - cx) - sk * y) / fx
+        return np.ascontiguousarray(np.stack([x, y], 1))
+
+    x0, x1 = norm(k0[i0]), norm(k1[i1])
+    E, mask = P.essential_lmeds(x0, x1, confidence=cp.params.confidence, seed=cp.params.seed)
+    assert np.array_equal(mask, inl)
+    Rh, th, _ = P.recover_pose(E, x0, x1, mask)
+    assert np.array_equal(Rh, R) and np.array_equal(th, t)
