@@ -307,6 +307,32 @@ RF_API rf_status rf_batch_upload_all(rf_batch* b, const float* const* i0, const 
 RF_API rf_status rf_batch_download_all(rf_batch* b, float* const* u, float* const* v,
                                        float* const* inv_depth, float* const* X,
                                        float* const* Y, float* const* Z, int pitch);
+/* Pipelined transfers for a serving loop: the frames of the next solve go
+ * up, and the results of the last solve come down, while a solve runs.
+ * Each direction has its own copy stream and a device staging area laid
+ * out like the batch's planes (made on first use).
+ *
+ * rf_batch_stage_upload queues every pair's frames (host arrays as for
+ * rf_batch_upload_all) into the staging area and returns at once; the host
+ * frames must stay unchanged until the solve that uses them has finished.
+ * rf_batch_take_upload makes the batch's stream wait for them and copies
+ * them into the pairs' frame planes (device to device), after which the
+ * next rf_batch_stage_upload may start.  RF_ERR_STATE if frames are staged
+ * twice without a take, or taken without being staged.
+ *
+ * rf_batch_stage_download copies the last solve's results (arguments as
+ * for rf_batch_download_all) into the staging area on the batch's stream,
+ * then to the host arrays on the copy stream, and returns at once: the next
+ * solve may be queued immediately.  rf_batch_wait_download blocks until
+ * the last staged download has reached the host.  The results are the same
+ * bytes rf_batch_download_all writes. */
+RF_API rf_status rf_batch_stage_upload(rf_batch* b, const float* const* i0,
+                                       const float* const* i1, int pitch);
+RF_API rf_status rf_batch_take_upload(rf_batch* b);
+RF_API rf_status rf_batch_stage_download(rf_batch* b, float* const* u, float* const* v,
+                                         float* const* inv_depth, float* const* X,
+                                         float* const* Y, float* const* Z, int pitch);
+RF_API rf_status rf_batch_wait_download(rf_batch* b);
 RF_API rf_status rf_batch_device_results(rf_batch* b, int pair, const float** u, const float** v,
                                          const float** X, const float** Y, const float** Z);
 RF_API rf_status rf_batch_set_stream(rf_batch* b, void* stream);

@@ -264,6 +264,25 @@ public:
         check(rf_batch_energies(b_, out));
         return 0;
     }
+    // pipelined transfers (rf_batch_stage_upload and its companions): i0 /
+    // i1 / outputs are arrays of n_pairs host pointers, one pitch
+    int stageUpload(const float* const* i0, const float* const* i1, int pitch) {
+        check(rf_batch_stage_upload(b_, i0, i1, pitch));
+        return 0;
+    }
+    int takeUpload() {
+        check(rf_batch_take_upload(b_));
+        return 0;
+    }
+    int stageDownload(float* const* u, float* const* v, float* const* inv_depth,
+                      float* const* X, float* const* Y, float* const* Z, int pitch) {
+        check(rf_batch_stage_download(b_, u, v, inv_depth, X, Y, Z, pitch));
+        return 0;
+    }
+    int waitDownload() {
+        check(rf_batch_wait_download(b_));
+        return 0;
+    }
     rf_batch* handle() { return b_; }
 
 private:

@@ -110,6 +110,10 @@ _SIGS = [
     ("rf_batch_download_inv_depth", _I, [_VP, _I, _VP, _I]),
     ("rf_batch_upload_all", _I, [_VP, _VP, _VP, _I]),
     ("rf_batch_download_all", _I, [_VP, _VP, _VP, _VP, _VP, _VP, _VP, _I]),
+    ("rf_batch_stage_upload", _I, [_VP, _VP, _VP, _I]),
+    ("rf_batch_take_upload", _I, [_VP]),
+    ("rf_batch_stage_download", _I, [_VP, _VP, _VP, _VP, _VP, _VP, _VP, _I]),
+    ("rf_batch_wait_download", _I, [_VP]),
     ("rf_batch_device_results", _I, [_VP, _I, _VP, _VP, _VP, _VP, _VP]),
     ("rf_batch_set_stream", _I, [_VP, _VP]),
     ("rf_batch_synchronize", _I, [_VP]),

@@ -381,6 +381,15 @@ struct rf_batch {
     int prefetch = 0;  // L2 prefetch distance of the inner-iteration launches, in blocks
     bool solved = false;
     int n_planes = 0;
+    // pipelined transfers (rf_batch_stage_upload / rf_batch_stage_download):
+    // device staging planes laid out like the pool's, one copy stream per
+    // direction and the events that order them against the solve stream,
+    // made on first use
+    float* stage_in = nullptr;   // 2 planes: frame 0, frame 1
+    float* stage_out = nullptr;  // 6 planes: u, v, inverse depth, X, Y, Z
+    cudaStream_t copy_in = nullptr, copy_out = nullptr;
+    cudaEvent_t in_staged = nullptr, in_free = nullptr, out_ready = nullptr, out_done = nullptr;
+    bool up_staged = false;
     // plane indices
     int pI0(int l) const { return l; }
     int pI1(int l) const { return L + l; }
@@ -792,6 +801,15 @@ rf_status rf_batch_create(const rf_params* p, int n_pairs, const int* widths, co
 rf_status rf_batch_destroy(rf_batch* b) {
     if (!b) return RF_OK;
     if (b->stream) cudaStreamSynchronize(b->stream);
+    for (cudaStream_t st : {b->copy_in, b->copy_out})
+        if (st) {
+            cudaStreamSynchronize(st);
+            cudaStreamDestroy(st);
+        }
+    for (cudaEvent_t ev : {b->in_staged, b->in_free, b->out_ready, b->out_done})
+        if (ev) cudaEventDestroy(ev);
+    if (b->stage_in) cudaFree(b->stage_in);
+    if (b->stage_out) cudaFree(b->stage_out);
     if (b->graph) cudaGraphExecDestroy(b->graph);
     if (b->pool) cudaFree(b->pool);
     if (b->d_pairs) cudaFree(b->d_pairs);
@@ -1133,6 +1151,111 @@ rf_status rf_batch_download_all(rf_batch* b, float* const* u, float* const* v,
     return RF_OK;
 }
 
+// Copy streams, events and the staging planes of one direction, made on
+// first use (a batch that never pipelines its transfers holds none of them).
+static rf_status ensure_staging(rf_batch* b, bool out) {
+    for (cudaStream_t* st : {&b->copy_in, &b->copy_out})
+        if (!*st) BC(cudaStreamCreateWithFlags(st, cudaStreamNonBlocking));
+    for (cudaEvent_t* ev : {&b->in_staged, &b->in_free, &b->out_ready, &b->out_done})
+        if (!*ev) BC(cudaEventCreateWithFlags(ev, cudaEventDisableTiming));
+    float** buf = out ? &b->stage_out : &b->stage_in;
+    if (!*buf) BC(cudaMalloc(buf, b->total * (out ? 6 : 2) * sizeof(float)));
+    return RF_OK;
+}
+
+rf_status rf_batch_stage_upload(rf_batch* b, const float* const* i0, const float* const* i1,
+                                int pitch) {
+    if (!b || !i0 || !i1) return bfail(RF_ERR_INVALID_ARG, "rf_batch_stage_upload: null argument");
+    if (b->up_staged)
+        return bfail(RF_ERR_STATE, "rf_batch_stage_upload: the staged frames were not taken yet");
+    for (int i = 0; i < b->n; i++) {
+        if (!i0[i] || !i1[i]) return bfail(RF_ERR_INVALID_ARG, "rf_batch_stage_upload: null image");
+        if (pitch < b->dims[i][0].w)
+            return bfail(RF_ERR_INVALID_ARG, "rf_batch_stage_upload: pitch < width");
+    }
+    rf_status rs = ensure_staging(b, false);
+    if (rs != RF_OK) return rs;
+    // the staging planes are free once the last rf_batch_take_upload's
+    // copies out of them have run on the solve stream
+    BC(cudaStreamWaitEvent(b->copy_in, b->in_free, 0));
+    for (int i = 0; i < b->n; i++) {
+        const LevelDims& d = b->dims[i][0];
+        for (int k = 0; k < 2; k++)
+            BC(cudaMemcpy2DAsync(b->stage_in + k * b->total + b->base_off[i], d.s * sizeof(float),
+                                 k ? i1[i] : i0[i], (size_t)pitch * sizeof(float),
+                                 d.w * sizeof(float), d.h, cudaMemcpyHostToDevice, b->copy_in));
+    }
+    BC(cudaEventRecord(b->in_staged, b->copy_in));
+    b->up_staged = true;
+    return RF_OK;
+}
+
+rf_status rf_batch_take_upload(rf_batch* b) {
+    if (!b) return bfail(RF_ERR_INVALID_ARG, "rf_batch_take_upload: null batch");
+    if (!b->up_staged) return bfail(RF_ERR_STATE, "rf_batch_take_upload: no frames staged");
+    BC(cudaStreamWaitEvent(b->stream, b->in_staged, 0));
+    // the same rows and columns as rf_batch_upload_images writes
+    for (int i = 0; i < b->n; i++) {
+        const LevelDims& d = b->dims[i][0];
+        for (int k = 0; k < 2; k++)
+            BC(cudaMemcpy2DAsync(pair_plane(b, i, k ? b->pI1(0) : b->pI0(0)), d.s * sizeof(float),
+                                 b->stage_in + k * b->total + b->base_off[i], d.s * sizeof(float),
+                                 d.w * sizeof(float), d.h, cudaMemcpyDeviceToDevice, b->stream));
+        b->imgs[i] = 1;
+    }
+    BC(cudaEventRecord(b->in_free, b->stream));
+    b->up_staged = false;
+    return RF_OK;
+}
+
+rf_status rf_batch_stage_download(rf_batch* b, float* const* u, float* const* v,
+                                  float* const* inv_depth, float* const* X, float* const* Y,
+                                  float* const* Z, int pitch) {
+    if (!b) return bfail(RF_ERR_INVALID_ARG, "rf_batch_stage_download: null batch");
+    if (!b->solved) return bfail(RF_ERR_STATE, "rf_batch_stage_download: no solve has run");
+    const bool recon = b->p.method != RF_METHOD_TVL1;
+    if (!recon && (inv_depth || X || Y || Z))
+        return bfail(RF_ERR_STATE, "rf_batch_stage_download: plain TV-L1 has no 3D output");
+    for (int i = 0; i < b->n; i++)
+        if (pitch < b->dims[i][0].w)
+            return bfail(RF_ERR_INVALID_ARG, "rf_batch_stage_download: pitch < width");
+    rf_status rs = ensure_staging(b, true);
+    if (rs != RF_OK) return rs;
+    const int B0 = b->base_idx();
+    // the staging planes are free once the last download out of them has run
+    BC(cudaStreamWaitEvent(b->stream, b->out_done, 0));
+    if (inv_depth) {
+        BL(launch_op(b, 0, OpInvDepth{B0 + P_Z, B0 + P_SCRATCH}));
+        b->launches++;
+    }
+    const int planes[6] = {b->res_u, b->res_v, B0 + P_SCRATCH, B0 + P_X, B0 + P_Y, B0 + P_Z};
+    float* const* dst[6] = {u, v, inv_depth, X, Y, Z};
+    for (int k = 0; k < 6; k++)
+        if (dst[k])
+            BC(cudaMemcpyAsync(b->stage_out + k * b->total, plane_base(b, planes[k]),
+                               b->total * sizeof(float), cudaMemcpyDeviceToDevice, b->stream));
+    BC(cudaEventRecord(b->out_ready, b->stream));
+    BC(cudaStreamWaitEvent(b->copy_out, b->out_ready, 0));
+    for (int k = 0; k < 6; k++) {
+        if (!dst[k]) continue;
+        for (int i = 0; i < b->n; i++) {
+            if (!dst[k][i]) continue;
+            const LevelDims& d = b->dims[i][0];
+            BC(cudaMemcpy2DAsync(dst[k][i], (size_t)pitch * sizeof(float),
+                                 b->stage_out + k * b->total + b->base_off[i], d.s * sizeof(float),
+                                 d.w * sizeof(float), d.h, cudaMemcpyDeviceToHost, b->copy_out));
+        }
+    }
+    BC(cudaEventRecord(b->out_done, b->copy_out));
+    return RF_OK;
+}
+
+rf_status rf_batch_wait_download(rf_batch* b) {
+    if (!b) return bfail(RF_ERR_INVALID_ARG, "rf_batch_wait_download: null batch");
+    if (b->out_done) BC(cudaEventSynchronize(b->out_done));
+    return RF_OK;
+}
+
 rf_status rf_batch_device_results(rf_batch* b, int pair, const float** u, const float** v,
                                   const float** X, const float** Y, const float** Z) {
     if (!b || pair < 0 || pair >= b->n)
@@ -1157,6 +1280,8 @@ rf_status rf_batch_set_stream(rf_batch* b, void* stream) {
 rf_status rf_batch_synchronize(rf_batch* b) {
     if (!b) return bfail(RF_ERR_INVALID_ARG, "rf_batch_synchronize: null batch");
     BC(cudaStreamSynchronize(b->stream));
+    for (cudaStream_t st : {b->copy_in, b->copy_out})
+        if (st) BC(cudaStreamSynchronize(st));
     return RF_OK;
 }
 

@@ -423,6 +423,34 @@ class ReconFlowBatch:
         N.check(self._lib.rf_batch_download_all(self._h, arr(u), arr(v), arr(inv_depth), arr(X),
                                                 arr(Y), arr(Z), int(pitch)))
 
+    def stageUpload(self, ptrs0, ptrs1, pitch):
+        """rf_batch_stage_upload: queue every pair's frames (host pointers,
+        unchanged until the solve that uses them has finished) on the upload
+        copy stream; returns at once."""
+        a = (ctypes.c_void_p * self.n)(*[ctypes.c_void_p(int(p)) for p in ptrs0])
+        b = (ctypes.c_void_p * self.n)(*[ctypes.c_void_p(int(p)) for p in ptrs1])
+        N.check(self._lib.rf_batch_stage_upload(self._h, a, b, int(pitch)))
+
+    def takeUpload(self):
+        """rf_batch_take_upload: the staged frames become the pairs' frames
+        for the next solve (ordered on the batch's stream)."""
+        N.check(self._lib.rf_batch_take_upload(self._h))
+
+    def stageDownload(self, pitch, u=None, v=None, inv_depth=None, X=None, Y=None, Z=None):
+        """rf_batch_stage_download: like downloadAll, but returns at once;
+        the host arrays are complete after waitDownload()."""
+        def arr(lst):
+            if lst is None:
+                return None
+            return (ctypes.c_void_p * self.n)(*[ctypes.c_void_p(int(p)) for p in lst])
+        N.check(self._lib.rf_batch_stage_download(self._h, arr(u), arr(v), arr(inv_depth),
+                                                  arr(X), arr(Y), arr(Z), int(pitch)))
+
+    def waitDownload(self):
+        """rf_batch_wait_download: block until the last staged download
+        has reached the host."""
+        N.check(self._lib.rf_batch_wait_download(self._h))
+
     def energies(self):
         """Energy of every pair's last solution (rf_batch_energies)."""
         out = np.zeros(self.n, np.float64)

@@ -196,3 +196,90 @@ def test_bulk_transfers_match_per_pair_calls(rf):
         assert_bitexact(b2.copyOpticalFlowToHost(i)[0][:, :w], outs[i][0][:, :w], f"pair {i}")
     b.close()
     b2.close()
+
+
+def test_pipelined_transfers_match_blocking_calls(rf):
+    """rf_batch_stage_upload / take_upload / stage_download / wait_download
+    in a serving loop (next frames up and last results down while a solve
+    runs, pinned host memory) give every step the bytes of a blocking
+    upload_all + solve + download_all of the same frames."""
+    import ctypes
+
+    from reconflow_gb300 import _native
+
+    lib = _native.load()
+    sizes = [(64, 48), (50, 40), (64, 30)]
+    pitch = 64
+    kw = dict(lambda_=50.0, lambdaf=0.1, lambdams=100.0, alphaTv=1 / 0.33, alphaProj=60.0,
+              tau=0.25, nWarpIters=1, nSolverIters=3, fix_quirks=1)
+    R_, t_ = zip(*[_pose(i) for i in range(len(sizes))])
+    held = []
+
+    def pinned(h):
+        p = ctypes.c_void_p()
+        _native.check(lib.rf_host_alloc(h * pitch * 4, ctypes.byref(p)))
+        held.append(p)
+        return np.ctypeslib.as_array(ctypes.cast(p, ctypes.POINTER(ctypes.c_float)),
+                                     shape=(h, pitch))
+
+    frames = []  # two frame sets, [set][pair] = (I0, I1) in pinned memory
+    for s in range(2):
+        fs = []
+        for i, (w, h) in enumerate(sizes):
+            I0, I1 = textured_pair(np.random.default_rng(70 + 10 * s + i), h, w)
+            a, c = pinned(h), pinned(h)
+            a[:] = pad_rows(I0, pitch)
+            c[:] = pad_rows(I1, pitch)
+            fs.append((a, c))
+        frames.append(fs)
+    try:
+        want = []
+        ref = rf.ReconFlowBatch(sizes, 2, method=14, **kw)
+        for i, (w, h) in enumerate(sizes):
+            ref.setCameraMatrices(i, _K(w, h), _K(w, h))
+        for fs in frames:
+            ref.uploadAll([a.ctypes.data for a, _ in fs], [c.ctypes.data for _, c in fs], pitch)
+            ref.solveR(list(R_), list(t_))
+            outs = [[np.full((h, pitch), 7.0, np.float32) for _ in range(6)] for (w, h) in sizes]
+            cols = [[outs[i][k].ctypes.data for i in range(len(sizes))] for k in range(6)]
+            ref.downloadAll(pitch, u=cols[0], v=cols[1], inv_depth=cols[2], X=cols[3],
+                            Y=cols[4], Z=cols[5])
+            want.append(outs)
+        ref.close()
+
+        b = rf.ReconFlowBatch(sizes, 2, method=14, **kw)
+        for i, (w, h) in enumerate(sizes):
+            b.setCameraMatrices(i, _K(w, h), _K(w, h))
+        with pytest.raises(Exception):
+            b.takeUpload()  # nothing staged
+        order = [0, 1, 0, 1]
+        got = []
+        b.stageUpload([a.ctypes.data for a, _ in frames[0]], [c.ctypes.data for _, c in frames[0]],
+                      pitch)
+        with pytest.raises(Exception):
+            b.stageUpload([a.ctypes.data for a, _ in frames[0]],
+                          [c.ctypes.data for _, c in frames[0]], pitch)  # staged twice
+        for k, s in enumerate(order):
+            b.takeUpload()
+            if k + 1 < len(order):
+                fs = frames[order[k + 1]]
+                b.stageUpload([a.ctypes.data for a, _ in fs], [c.ctypes.data for _, c in fs], pitch)
+            b.solveR(list(R_), list(t_))
+            outs = [[pinned(h) for _ in range(6)] for (w, h) in sizes]
+            for o in outs:
+                for x in o:
+                    x[:] = 7.0
+            cols = [[outs[i][q].ctypes.data for i in range(len(sizes))] for q in range(6)]
+            b.stageDownload(pitch, u=cols[0], v=cols[1], inv_depth=cols[2], X=cols[3], Y=cols[4],
+                            Z=cols[5])
+            got.append(outs)
+        b.waitDownload()
+        for k, s in enumerate(order):
+            for i, (w, h) in enumerate(sizes):
+                for q, nm in enumerate(("u", "v", "inv", "X", "Y", "Z")):
+                    assert_bitexact(got[k][i][q][:, :w], want[s][i][q][:, :w],
+                                    f"step {k} pair {i} {nm}")
+        b.close()
+    finally:
+        for p in held:
+            lib.rf_host_free(p)
