@@ -18,7 +18,7 @@ pairs.  Workload ``720p`` is the plain drop-in solve of one pair.
 ``value``: pairs/s with the frames already in HBM (CUDA events on the solve
 stream, L2 flushed between steps).  ``e2e``: the same through the C ABI with
 host buffers: pinned upload of both frames, solve, download of flow, inverse
-depth and 3D points, every step; for the batched workloads as a serving loop
+depth and 3D points, every step; for the learned workloads as a serving loop
 whose copies overlap the previous / next step's solve (pipelined transfers
 of the batch API), with the blocking per-step figure beside it
 (``serial_value``).  ``roofline``: the dominant kernel at level
