@@ -201,7 +201,7 @@ int lmeds_iterations(double conf) {
 
 // The seeded LMedS samples: lmeds_iterations(conf) sets of five distinct
 // match indices, [sample][5].
-std::vector<int> lmeds_samples(int n, double conf, uint64_t seed) {
+static std::vector<int> lmeds_samples(int n, double conf, uint64_t seed) {
     const int iters = lmeds_iterations(conf);
     std::vector<int> samples((size_t)iters * 5);
     uint64_t st = seed;
@@ -237,14 +237,11 @@ std::vector<double> lmeds_hypotheses(const double* x0, const double* x1, int n, 
         }
         counts[it] = five_point(a, b, &sols[(size_t)it * 90]);
     });
-    return lmeds_collect(sols, counts);
-}
-
-// Hypotheses in sample order from per-sample slots of 10 (counts[s] used).
-std::vector<double> lmeds_collect(const std::vector<double>& sols, const std::vector<int>& counts) {
+    // sample order: the first counts[s] matrices of each slot of 10
     std::vector<double> hyp;
-    for (size_t it = 0; it < counts.size(); it++)
-        hyp.insert(hyp.end(), sols.begin() + it * 90, sols.begin() + it * 90 + 9 * counts[it]);
+    for (int it = 0; it < iters; it++)
+        hyp.insert(hyp.end(), sols.begin() + (size_t)it * 90,
+                   sols.begin() + (size_t)it * 90 + 9 * counts[it]);
     return hyp;
 }
 

@@ -30,12 +30,6 @@ RF_HD inline double sampson2(const double* E, const double* a, const double* b) 
     return d > 0.0 ? r * r / d : (r == 0.0 ? 0.0 : INFINITY);
 }
 
-// Samples of the seeded LMedS: sets of five distinct match indices,
-// [sample][5], as many as the confidence needs at 45% outliers.
-std::vector<int> lmeds_samples(int n, double conf, uint64_t seed);
-// Hypotheses in sample order from per-sample slots of 10 essential matrices
-// (counts[s] of slot s used).
-std::vector<double> lmeds_collect(const std::vector<double>& sols, const std::vector<int>& counts);
 // Every five-point hypothesis (9 doubles each) of the seeded LMedS samples,
 // in sample order.
 std::vector<double> lmeds_hypotheses(const double* x0, const double* x1, int n, double conf,
