@@ -90,3 +90,23 @@ def test_null_handle_calls_fail_cleanly(rf):
     assert lib.rf_download_flow(None, None, None, 0) == 1
     assert lib.rf_destroy(None) == 0
     assert "null" in lib.rf_last_error_string().decode()
+
+
+def test_batch_null_handle_calls_fail_cleanly(rf):
+    """The batch entry points check their handle before any CUDA call, so
+    they fail with RF_ERR_INVALID_ARG (1) and a message on any host."""
+    lib = rf.load()
+    calls = [
+        ("rf_batch_upload_all", (None, None, None, 0)),
+        ("rf_batch_download_all", (None, None, None, None, None, None, None, 0)),
+        ("rf_batch_stage_upload", (None, None, None, 0)),
+        ("rf_batch_take_upload", (None,)),
+        ("rf_batch_stage_download", (None, None, None, None, None, None, None, 0)),
+        ("rf_batch_wait_download", (None,)),
+        ("rf_batch_synchronize", (None,)),
+        ("rf_batch_energies", (None, None)),
+    ]
+    for name, args in calls:
+        assert getattr(lib, name)(*args) == 1, name
+        assert "null" in lib.rf_last_error_string().decode(), name
+    assert lib.rf_batch_destroy(None) == 0
