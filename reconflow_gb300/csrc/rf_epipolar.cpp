@@ -3,7 +3,7 @@
 // OpenCV's findEssentialMat(..., LMEDS, 0.999) and recoverPose).  OpenCV is
 // not used here; the published methods are restated:
 //
-// * the five-point solver (rf_fivept.cuh, shared with the GPU);
+// * the five-point solver (rf_fivept.cuh);
 // * least median of squares (P. J. Rousseeuw, "Least median of squares
 //   regression", JASA 79, 1984) over random five-point samples with the
 //   squared Sampson distance, the sample count for confidence `conf` at an

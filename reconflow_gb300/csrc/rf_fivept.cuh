@@ -2,9 +2,10 @@
 // five-point relative pose problem", IEEE PAMI 26(6), 2004), written as host
 // and device code (no contraction on either side, correctly rounded
 // division and square root, exact frexp / ldexp, so both give the same
-// doubles).  The LMedS runs it on host threads: one GPU thread per sample
-// took 3.6 ms per pose against 0.3 ms on the host (a long chain of dependent
-// FP64 operations and ~6 KB of local arrays per thread).
+// doubles).  The LMedS runs it on host threads (~12 us a solve on one x86
+// core): one GPU thread per sample took 3.6 ms for a pose's 134 solves (a
+// long chain of dependent FP64 operations and ~6 KB of local arrays per
+// thread).
 //
 // Steps: null space of the 5 x 9 epipolar system by Householder QR, E = x X
 // + y Y + z Z + W; the ten cubic constraints det(E) = 0 and 2 E E^T E -
@@ -12,8 +13,8 @@
 // elimination of the first ten columns; the rows <k> = <e> - z<f>,
 // <l> = <g> - z<h>, <m> = <i> - z<j> as a 3 x 3 matrix of polynomials in z;
 // its degree-10 determinant; the real roots (bracketed between the real
-// roots of the derivatives, refined by the Illinois variant of regula falsi:
-// M. Dowell, P. Jarratt, BIT 11, 1971); x, y from the null vector of B(z).
+// roots of the derivatives, refined by Newton steps safeguarded by bisection
+// inside each bracket); x, y from the null vector of B(z).
 #pragma once
 
 #include <math.h>
@@ -117,34 +118,53 @@ RF_HD inline double peval(const Poly1& p, double z) {
     return r;
 }
 
-// Root of p in [lo, hi] where p changes sign: Illinois regula falsi, a
-// bisection step whenever the secant point leaves the middle 98% of the
-// bracket, until the iterate moves by less than `rel` of its magnitude.
-RF_HD inline double bracket_root(const Poly1& p, double lo, double hi, double rel) {
-    double flo = peval(p, lo), fhi = peval(p, hi);
-    double prev = lo;
-    int side = 0;
-    for (int it = 0; it < 100; it++) {
-        const double width = hi - lo;
-        double x = (lo * fhi - hi * flo) / (fhi - flo);
-        if (!(x > lo + 0.01 * width && x < hi - 0.01 * width)) x = 0.5 * (lo + hi);
-        const double fx = peval(p, x);
-        const double ax = fabs(x);
-        if (fx == 0.0 || fabs(x - prev) <= rel * (ax > 1.0 ? ax : 1.0)) return x;
-        prev = x;
-        if ((fx < 0) == (flo < 0)) {
-            lo = x;
-            flo = fx;
-            if (side == -1) fhi *= 0.5;
-            side = -1;
-        } else {
-            hi = x;
-            fhi = fx;
-            if (side == 1) flo *= 0.5;
-            side = 1;
-        }
+// p(z), p'(z) and sum |c_k| |z|^k (the scale of p's rounding error at z)
+// in one Horner pass.
+RF_HD inline void peval_d(const Poly1& p, double z, double& f, double& df, double& mag) {
+    const double az = fabs(z);
+    f = p.c[p.n - 1];
+    df = 0.0;
+    mag = fabs(f);
+    for (int i = p.n - 1; i-- > 0;) {
+        df = df * z + f;
+        f = f * z + p.c[i];
+        mag = mag * az + fabs(p.c[i]);
     }
-    return 0.5 * (lo + hi);
+}
+
+// Root of p in [lo, hi] where p changes sign (neg_lo: p(lo) < 0): Newton
+// steps safeguarded by the bracket (each evaluation shrinks it); a step
+// that would leave the bracket, or that is not at most half the previous
+// step, is replaced by a bisection.  Ends when p(x) is within about two
+// units in the last place of sum |c_k| |x|^k (the usual size of Horner's
+// rounding error), or when a Newton step or the bracket is below `rel` of
+// the root's magnitude (at least 1).
+RF_HD inline double bracket_root(const Poly1& p, double lo, double hi, bool neg_lo, double rel) {
+    double x = 0.5 * (lo + hi), last = hi - lo;
+    for (int it = 0; it < 200; it++) {
+        double f, df, mag;
+        peval_d(p, x, f, df, mag);
+        if (fabs(f) <= 2.5e-16 * mag) return x;
+        if ((f < 0.0) == neg_lo)
+            lo = x;
+        else
+            hi = x;
+        const double ax = fabs(x);
+        const double tol = rel * (ax > 1.0 ? ax : 1.0);
+        const double xn = x - f / df;  // inf / NaN when df = 0: fails the tests below
+        double step;
+        if (xn > lo && xn < hi && 2.0 * fabs(xn - x) <= last) {
+            step = fabs(xn - x);
+            x = xn;
+            if (step <= tol) return x;
+        } else {
+            x = 0.5 * (lo + hi);
+            step = 0.5 * (hi - lo);
+        }
+        if (hi - lo <= tol) return x;
+        last = step;
+    }
+    return x;
 }
 
 // A power of two above every root's magnitude (Fujiwara's bound
@@ -195,18 +215,20 @@ RF_HD inline int real_roots(Poly1 p, double* out) {
             if (roots[i] > -bound && roots[i] < bound && roots[i] > pts[np - 1]) pts[np++] = roots[i];
         pts[np++] = bound;
         const double rel = k == 0 ? 1e-15 : 1e-9;
+        // at most deg(q) <= 10 roots are kept, which bounds every array here
+        const int cap = q.n - 1;
         int n = 0;
         double found[10];
-        for (int i = 0; i + 1 < np; i++) {
+        for (int i = 0; i + 1 < np && n < cap; i++) {
             const double a = pts[i], b = pts[i + 1];
             const double fa = peval(q, a), fb = peval(q, b);
             if (fa == 0.0) {
                 if (n == 0 || found[n - 1] != a) found[n++] = a;
                 continue;
             }
-            if ((fa < 0) != (fb < 0)) found[n++] = bracket_root(q, a, b, rel);
+            if ((fa < 0) != (fb < 0)) found[n++] = bracket_root(q, a, b, fa < 0, rel);
         }
-        if (peval(q, pts[np - 1]) == 0.0 && (n == 0 || found[n - 1] != pts[np - 1]))
+        if (n < cap && peval(q, pts[np - 1]) == 0.0 && (n == 0 || found[n - 1] != pts[np - 1]))
             found[n++] = pts[np - 1];
         nr = n;
         for (int i = 0; i < n; i++) roots[i] = found[i];
