@@ -215,21 +215,27 @@ RF_HD inline int real_roots(Poly1 p, double* out) {
             if (roots[i] > -bound && roots[i] < bound && roots[i] > pts[np - 1]) pts[np++] = roots[i];
         pts[np++] = bound;
         const double rel = k == 0 ? 1e-15 : 1e-9;
+        // q at every bracket point; a point where q is within its rounding
+        // error (a root of even multiplicity sits at a root of q') is a root
+        double fv[12];
+        bool zero[12];
+        for (int i = 0; i < np; i++) {
+            double df, mag;
+            peval_d(q, pts[i], fv[i], df, mag);
+            zero[i] = fabs(fv[i]) <= 2.5e-16 * mag;
+        }
         // at most deg(q) <= 10 roots are kept, which bounds every array here
         const int cap = q.n - 1;
         int n = 0;
         double found[10];
-        for (int i = 0; i + 1 < np && n < cap; i++) {
-            const double a = pts[i], b = pts[i + 1];
-            const double fa = peval(q, a), fb = peval(q, b);
-            if (fa == 0.0) {
-                if (n == 0 || found[n - 1] != a) found[n++] = a;
+        for (int i = 0; i < np && n < cap; i++) {
+            if (zero[i]) {
+                found[n++] = pts[i];
                 continue;
             }
-            if ((fa < 0) != (fb < 0)) found[n++] = bracket_root(q, a, b, fa < 0, rel);
+            if (i + 1 < np && !zero[i + 1] && (fv[i] < 0) != (fv[i + 1] < 0))
+                found[n++] = bracket_root(q, pts[i], pts[i + 1], fv[i] < 0, rel);
         }
-        if (n < cap && peval(q, pts[np - 1]) == 0.0 && (n == 0 || found[n - 1] != pts[np - 1]))
-            found[n++] = pts[np - 1];
         nr = n;
         for (int i = 0; i < n; i++) roots[i] = found[i];
     }

@@ -191,3 +191,75 @@ def test_oracle_matches_committed_fixtures(oracle):
     want = (k0[ok, :2].astype(np.float64) + np.array([2.3, -1.7]) - ctr) @ R + ctr
     err = np.linalg.norm(k1[best[ok], :2] - want, axis=1)
     assert np.max(err) < 0.5 and np.median(err) < 0.1, err
+
+
+def _roots_tool(tmp_path):
+    import os
+    import subprocess
+
+    root = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+    exe = tmp_path / "fivept_roots"
+    subprocess.run(["g++", "-std=c++17", "-O2", "-ffp-contract=off", "-I",
+                    os.path.join(root, "reconflow_gb300", "csrc"),
+                    os.path.join(root, "tests", "cpp", "fivept_roots.cpp"), "-o", str(exe)],
+                   check=True, capture_output=True, text=True)
+
+    def run(polys):
+        txt = "".join(f"{len(c)} " + " ".join(repr(float(x)) for x in c) + "\n" for c in polys)
+        out = subprocess.run([str(exe)], input=txt, capture_output=True, text=True, check=True)
+        res = []
+        for line in out.stdout.splitlines():
+            v = line.split()
+            res.append(np.array([float(x) for x in v[1:1 + int(v[0])]]))
+        return res
+    return run
+
+
+def test_five_point_real_roots_against_numpy(tmp_path):
+    """The five-point solver's real-root finder (derivative bracketing,
+    safeguarded Newton) on polynomials of degree <= 10: Wilkinson-type
+    products, random real-rooted ones with clusters, random ones with
+    complex pairs, a double root and a vanishing leading coefficient."""
+    run = _roots_tool(tmp_path)
+    rng = np.random.default_rng(7)
+    cases, want = [], []
+
+    def from_roots(rs, scale=1.0, extra=()):
+        c = np.poly(list(rs) + list(extra))[::-1] * scale  # ascending
+        return c
+
+    cases.append(from_roots(range(1, 11)))  # (z-1)...(z-10)
+    want.append(np.arange(1.0, 11.0))
+    for _ in range(40):  # real-rooted, degree 3..10, some clustered pairs
+        d = int(rng.integers(3, 11))
+        rs = np.sort(rng.uniform(-5, 5, d))
+        if d > 3:
+            rs[1] = rs[0] + rng.uniform(1e-3, 1e-2)
+        rs = np.sort(rs)
+        cases.append(from_roots(rs, scale=rng.uniform(-100, 100)))
+        want.append(rs)
+    for _ in range(40):  # real roots plus complex pairs
+        nr = int(rng.integers(0, 7))
+        rs = np.sort(rng.uniform(-3, 3, nr))
+        quad = []
+        for _ in range((10 - nr) // 2):
+            a, b = rng.uniform(-3, 3), rng.uniform(0.3, 2)
+            quad += [a + 1j * b, a - 1j * b]
+        cases.append(np.real(from_roots(rs, extra=quad)))
+        want.append(rs)
+    got = run(cases)
+    for k, (g, w) in enumerate(zip(got, want)):
+        assert len(g) == len(w), (k, g, w)
+        assert np.all(np.diff(g) >= 0), k
+        assert np.allclose(g, w, rtol=1e-6, atol=1e-6), (k, g, w)
+
+    # a double root: found (once or twice) within the square root of the
+    # rounding error, the simple roots exactly
+    g = run([from_roots([-2.0, 1.0, 1.0, 3.0])])[0]
+    assert np.isclose(g[0], -2.0) and np.isclose(g[-1], 3.0)
+    assert np.all(np.abs(g[1:-1] - 1.0) < 1e-6) and 1 <= len(g) - 2 <= 2
+    # a leading coefficient at rounding level of the others: treated as
+    # degree 2
+    c = list(from_roots([0.5, 2.0])) + [1e-20]
+    g = run([c])[0]
+    assert np.allclose(g, [0.5, 2.0])
