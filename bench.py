@@ -1353,15 +1353,18 @@ def main():
         if "pose" in wl:
             run_reference_pose(args, wl, world, rank)
             return
-        if "groups" in wl:
-            raise SystemExit("bench.py: the reference arm runs single-size workloads")
+        if "groups" in wl or ("pairs" in wl and "checkpoint" not in wl):
+            if rank == 0:
+                print(json.dumps({"impl": "reference", "unavailable": "the reference solves "
+                                  "one pair at a time and has no batched path; its per-pair "
+                                  "rate is the reference arm of --workload 720p / 480p"}),
+                      flush=True)
+            return
         if "checkpoint" in wl:
             # the reference's counterpart of a learned batch: its plain solve, one pair
             wl = dict(width=wl["width"], height=wl["height"], levels=wl["levels"],
                       warps=wl["plain_warps"], iters=wl["plain_iters"], seed=wl["seed"],
                       metric=LEARNED_METRIC, workload=args.workload)
-        elif "pairs" in wl:
-            raise SystemExit("bench.py: the reference arm runs single-pair workloads")
         run_reference(args, wl, world, rank)
         return
     if "pose" in wl:
