@@ -238,7 +238,14 @@ RF_API const char* rf_version(void);
  * pose, share one parameter block (methods 0 and 14, float32 gray input) and
  * are solved together: every step of the schedule is one launch covering all
  * pairs, captured in one CUDA graph.  A pair's results are bit-identical to
- * solving it alone with rf_solve / rf_solve_flow.
+ * solving it alone with rf_solve / rf_solve_flow.  The per-pair calls take
+ * the single-pair entry points' arguments, and through them the reference's:
+ * rf_batch_set_cameras ~ setCameraMatrices (Reconflow.cu:78-116),
+ * rf_batch_upload_images ~ copyImagesToDevice (Cudaflow.cu:288-311),
+ * rf_batch_solve ~ solveR (Reconflow.cu:134-466), rf_batch_solve_flow ~
+ * solveOpticalFlow (Cudaflow.cu:394-621), rf_batch_download_flow ~
+ * copyOpticalFlowToHost (Cudaflow.cu:320-325), rf_batch_download_points ~
+ * copy3dToHost (Reconflow.cu:65-70).
  * ---------------------------------------------------------------------- */
 typedef struct rf_batch rf_batch;
 
