@@ -85,6 +85,17 @@ public:
         check(rf_download_flow_color(h_, flowScale_, uvrgb, pitch));
         return 0;
     }
+    // Cudaflow.h:47: the colour wheel is a constant table of the colour
+    // kernel here, so there is nothing to set up; kept for call sites
+    int initializeColorWheel() { return 0; }
+    // Cudaflow.h:52-53, the reference's older names of the image upload and
+    // the flow + colour download
+    int copyToDevice(const void* i0, const void* i1, int pitch) {
+        return copyImagesToDevice(i0, i1, pitch);
+    }
+    int copyToHost(float* u, float* v, float* uvrgb, int pitch) {
+        return copyOpticalFlowToHost(u, v, uvrgb, pitch);
+    }
     int close() {
         if (h_) rf_destroy(h_);
         h_ = nullptr;
@@ -169,6 +180,14 @@ public:
         check(rf_solve(h_, R0, t0, R1, t1));
         return 0;
     }
+    // Reconflow.h:76-77: the solve solveR forwards to
+    int solveReconFlow(const double* R1, const double* t1, float flowScale) {
+        return solveR(R1, t1, flowScale);
+    }
+    int solveReconFlow(const double* R0, const double* t0, const double* R1, const double* t1,
+                       float flowScale) {
+        return solveR(R0, t0, R1, t1, flowScale);
+    }
     // Reconflow.cu:65-70
     int copy3dToHost(float* X, float* Y, float* Z, int pitch) {
         check(rf_download_points(h_, X, Y, Z, pitch));
@@ -194,6 +213,12 @@ public:
     int solveR(cv::Mat R0, cv::Mat t0, cv::Mat R1, cv::Mat t1, float flowScale) {
         return solveR(R0.ptr<double>(), t0.ptr<double>(), R1.ptr<double>(), t1.ptr<double>(),
                       flowScale);
+    }
+    int solveReconFlow(cv::Mat R1, cv::Mat t1, float flowScale) {
+        return solveR(R1, t1, flowScale);
+    }
+    int solveReconFlow(cv::Mat R0, cv::Mat t0, cv::Mat R1, cv::Mat t1, float flowScale) {
+        return solveR(R0, t0, R1, t1, flowScale);
     }
     int copySparseOpticalFlowToDevice(cv::Mat u, cv::Mat v) {
         return copySparseOpticalFlowToDevice(u.ptr<float>(), v.ptr<float>(), nullptr,

@@ -151,6 +151,20 @@ class CudaFlow:
                                                  _ptr(uvrgb), uvrgb.shape[1]))
         return uvrgb
 
+    def initializeColorWheel(self) -> int:
+        """CudaFlow::initializeColorWheel (Cudaflow.h:47): the colour wheel
+        is a constant table of the colour kernel, nothing to set up."""
+        return 0
+
+    # the reference's older names (Cudaflow.h:52-53)
+    def copyToDevice(self, i0, i1) -> int:
+        return self.copyImagesToDevice(i0, i1)
+
+    def copyToHost(self, u=None, v=None, uvrgb=None):
+        if uvrgb is None:
+            uvrgb = self._out(None, 3)
+        return self.copyOpticalFlowToHost(u, v, uvrgb)
+
     # -- solve -------------------------------------------------------------
     def solveOpticalFlow(self, flowScale: float = 5.0) -> int:
         """CudaFlow::solveOpticalFlow (Cudaflow.cu:394-621)."""
