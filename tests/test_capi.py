@@ -110,3 +110,26 @@ def test_batch_null_handle_calls_fail_cleanly(rf):
         assert getattr(lib, name)(*args) == 1, name
         assert "null" in lib.rf_last_error_string().decode(), name
     assert lib.rf_batch_destroy(None) == 0
+
+
+def test_class_surface_keeps_reference_member_names():
+    """The Python classes carry the reference's public members on this path
+    (Reconflow.h:67-83, Cudaflow.h:36-63), aliases included; calls before
+    initialisation fail with the library's error, not an AttributeError."""
+    import numpy as np
+
+    import reconflow_gb300 as R
+    from reconflow_gb300._native import RfError
+
+    names = ["initialize", "copyImagesToDevice", "copyOpticalFlowToHost", "solveOpticalFlow",
+             "initializeColorWheel", "copyToDevice", "copyToHost", "close", "initializeR",
+             "setCameraMatrices", "copySparseOpticalFlowToDevice",
+             "copyInitialOpticalFlowToDevice", "solveR", "solveReconFlow", "copy3dToHost",
+             "removeEdgeArtifacts3D"]
+    f = R.ReconFlow()
+    for nm in names:
+        assert callable(getattr(f, nm, None)), nm
+    assert f.initializeColorWheel() == 0
+    with pytest.raises(RfError):
+        f.solveReconFlow(np.eye(3), np.zeros(3), 5.0)
+    assert f.close() == 0
