@@ -25,7 +25,8 @@ import math
 
 import numpy as np
 
-__all__ = ["make_scene", "intrinsics_for", "random_pose", "render_pair"]
+__all__ = ["make_scene", "make_sequence", "smooth_path", "intrinsics_for", "random_pose",
+           "render_pair"]
 
 
 def intrinsics_for(width: int, height: int) -> np.ndarray:
@@ -209,6 +210,95 @@ def make_scene(width: int, height: int, seed: int = 0, K=None, n_planes: int = 8
         out = _render_pair_torch(width, height, K, R, t, planes, tex, rng, noise, device)
     out.update({"K": K, "R": R, "t": t, "seed": seed})
     return out
+
+
+# ---------------------------------------------------------------------------
+# Sequences: one scene seen along a smooth camera path
+# ---------------------------------------------------------------------------
+
+def smooth_path(rng: np.random.Generator, n_frames: int, step: float = 0.05,
+                max_turn_deg: float = 0.3):
+    """Poses (R_k, t_k), X_k = R_k X + t_k, of a camera moving `step` metres
+    per frame from the origin: mostly forward (the heading starts within
+    ~17 degrees of the optical axis and drifts by a small random amount per
+    frame), the orientation turning by at most `max_turn_deg` per frame
+    about a slowly varying axis.  Frame 0 is the identity."""
+    heading = np.array([rng.uniform(-0.3, 0.3), rng.uniform(-0.3, 0.3), 1.0])
+    heading /= np.linalg.norm(heading)
+    axis = rng.normal(size=3)
+    C = np.zeros(3)
+    R = np.eye(3)
+    poses = [(R.copy(), np.zeros(3))]
+    for _ in range(1, n_frames):
+        heading = heading + rng.normal(0.0, 0.02, 3)
+        heading /= np.linalg.norm(heading)
+        C = C + step * heading
+        axis = axis + rng.normal(0.0, 0.2, 3)
+        R = _rodrigues(axis, math.radians(rng.uniform(0.0, max_turn_deg))) @ R
+        poses.append((R.copy(), -R @ C))
+    return poses
+
+
+def _render_view(width, height, K, R, t, planes, tex):
+    """Frame of the camera X' = R X + t (noise-free) and the scene point of
+    every pixel in camera-0 coordinates (3, N) with its found mask."""
+    Kinv = np.linalg.inv(K)
+    ys, xs = np.mgrid[0:height, 0:width].astype(np.float64)
+    X, found = _raycast(planes, K, Kinv, R, t, xs, ys)
+    with np.errstate(divide="ignore", invalid="ignore"):
+        px = K[0, 0] * X[0] / X[2] + K[0, 2]
+        py = K[1, 1] * X[1] / X[2] + K[1, 2]
+    px = np.where(found, px, xs.ravel())
+    py = np.where(found, py, ys.ravel())
+    return tex(px, py).reshape(height, width), X, found
+
+
+def make_sequence(width: int, height: int, n_frames: int = 32, seed: int = 0, K=None,
+                  n_planes: int = 8, n_blobs: int = 200, step: float = 0.05,
+                  max_turn_deg: float = 0.3, noise: float = 0.01) -> dict:
+    """One seeded scene (planes and texture as in make_scene) seen from
+    `n_frames` cameras along smooth_path, rendered with numpy.
+
+    Returns frames (float32, N(0, noise) added), poses [(R_k, t_k)] and, for
+    each consecutive pair (k, k + 1), the ground truth in frame k's pixels:
+    flow, inverse depth in camera k, a validity mask (the point is seen by
+    camera k + 1: inside its image and not occluded), and the relative pose
+    (R, t) mapping camera-k coordinates to camera k + 1's, which is what a
+    solve with camera k at the identity takes.
+    """
+    rng = np.random.default_rng(seed)
+    K = intrinsics_for(width, height) if K is None else np.asarray(K, np.float64)
+    Kinv = np.linalg.inv(K)
+    planes = _Planes(rng, width, height, K, n_planes)
+    tex = _Texture(rng, width, height, n_blobs)
+    gy, gx = np.mgrid[0:height:4, 0:width:4].astype(np.float64)
+    raw = tex.raw(gx, gy)
+    tex.lo, tex.hi = float(np.percentile(raw, 0.5)), float(np.percentile(raw, 99.5))
+    poses = smooth_path(rng, n_frames, step, max_turn_deg)
+    views = [_render_view(width, height, K, R, t, planes, tex) for R, t in poses]
+    frames = [(I + rng.normal(0.0, noise, I.shape)).astype(np.float32) for I, _, _ in views]
+    ys, xs = np.mgrid[0:height, 0:width].astype(np.float64)
+    pairs = []
+    for k in range(n_frames - 1):
+        (Ra, ta), (Rb, tb) = poses[k], poses[k + 1]
+        _, X, found = views[k]
+        Xa = Ra @ X + ta[:, None]
+        Xb = Rb @ X + tb[:, None]
+        with np.errstate(divide="ignore", invalid="ignore"):
+            u1 = K[0, 0] * Xb[0] / Xb[2] + K[0, 2]
+            v1 = K[1, 1] * Xb[1] / Xb[2] + K[1, 2]
+            inv = np.where(found, 1.0 / Xa[2], 0.0)
+        inb = found & (Xb[2] > 1e-6) & (u1 >= 0) & (u1 <= width - 1) & (v1 >= 0) & (v1 <= height - 1)
+        Xv, fv = _raycast(planes, K, Kinv, Rb, tb, np.where(inb, u1, 0.0), np.where(inb, v1, 0.0))
+        same = fv & (np.linalg.norm(Xv - X, axis=0) < 1e-3 * np.maximum(np.abs(Xa[2]), 1.0))
+        flow = np.stack([np.where(found, u1 - xs.ravel(), 0.0).reshape(height, width),
+                         np.where(found, v1 - ys.ravel(), 0.0).reshape(height, width)], -1)
+        Rr = Rb @ Ra.T
+        pairs.append({"flow": flow.astype(np.float32),
+                      "inv_depth": inv.reshape(height, width).astype(np.float32),
+                      "valid": (inb & same).reshape(height, width),
+                      "R": Rr, "t": tb - Rr @ ta})
+    return {"frames": frames, "poses": poses, "pairs": pairs, "K": K, "seed": seed}
 
 
 # ---------------------------------------------------------------------------
