@@ -255,9 +255,10 @@ def _render_view(width, height, K, R, t, planes, tex):
 
 def make_sequence(width: int, height: int, n_frames: int = 32, seed: int = 0, K=None,
                   n_planes: int = 8, n_blobs: int = 200, step: float = 0.05,
-                  max_turn_deg: float = 0.3, noise: float = 0.01) -> dict:
+                  max_turn_deg: float = 0.3, noise: float = 0.01, device=None) -> dict:
     """One seeded scene (planes and texture as in make_scene) seen from
-    `n_frames` cameras along smooth_path, rendered with numpy.
+    `n_frames` cameras along smooth_path, rendered with numpy, or with torch
+    (float64) on `device` (the same seeded parameters and formulas).
 
     Returns frames (float32, N(0, noise) added), poses [(R_k, t_k)] and, for
     each consecutive pair (k, k + 1), the ground truth in frame k's pixels:
@@ -275,6 +276,10 @@ def make_sequence(width: int, height: int, n_frames: int = 32, seed: int = 0, K=
     raw = tex.raw(gx, gy)
     tex.lo, tex.hi = float(np.percentile(raw, 0.5)), float(np.percentile(raw, 99.5))
     poses = smooth_path(rng, n_frames, step, max_turn_deg)
+    if device is not None:
+        images, pairs = _sequence_torch(width, height, K, poses, planes, tex, device)
+        frames = [(I + rng.normal(0.0, noise, I.shape)).astype(np.float32) for I in images]
+        return {"frames": frames, "poses": poses, "pairs": pairs, "K": K, "seed": seed}
     views = [_render_view(width, height, K, R, t, planes, tex) for R, t in poses]
     frames = [(I + rng.normal(0.0, noise, I.shape)).astype(np.float32) for I, _, _ in views]
     ys, xs = np.mgrid[0:height, 0:width].astype(np.float64)
@@ -402,3 +407,81 @@ def _render_pair_torch(width, height, K, R, t, planes, tex, rng, noise, device):
         "inv_depth": inv_depth.reshape(sh).cpu().numpy().astype(np.float32),
         "depth": Z.reshape(sh).cpu().numpy().astype(np.float32), "valid": valid.cpu().numpy(),
     }
+
+
+def _sequence_torch(width, height, K, poses, planes, tex, device):
+    """The views and per-pair ground truth of make_sequence with torch
+    (float64) on `device`: the same ray casts and projections as the numpy
+    path, frame after frame."""
+    import torch
+
+    dev = torch.device(device)
+    T = lambda a: torch.as_tensor(np.asarray(a, np.float64), device=dev)  # noqa: E731
+    Kt = T(K)
+    Kinv = T(np.linalg.inv(np.asarray(K, np.float64)))
+    fx, fy, cx, cy = float(K[0, 0]), float(K[1, 1]), float(K[0, 2]), float(K[1, 2])
+    ys, xs = torch.meshgrid(torch.arange(height, device=dev, dtype=torch.float64),
+                            torch.arange(width, device=dev, dtype=torch.float64), indexing="ij")
+    xs, ys = xs.reshape(-1), ys.reshape(-1)
+    seeds = T(planes.seeds)
+    nrm = T(planes.n)
+
+    def label(x, y):
+        d = (x[:, None] - seeds[None, :, 0]) ** 2 + (y[:, None] - seeds[None, :, 1]) ** 2
+        return torch.argmin(d, dim=1)
+
+    def texture(x, y):
+        v = (torch.as_tensor(_raw_torch(tex, x.cpu().numpy(), y.cpu().numpy(), dev), device=dev)
+             - tex.lo) / (tex.hi - tex.lo)
+        return v.clamp(0.0, 1.0)
+
+    def raycast(Rt, tt, px, py):
+        C = -Rt.T @ tt
+        d = Rt.T @ (Kinv @ torch.stack([px, py, torch.ones_like(px)], 0))
+        best = torch.full_like(px, float("inf"))
+        hit = torch.zeros((3, px.numel()), dtype=torch.float64, device=dev)
+        nC = nrm @ C
+        nd = nrm @ d
+        for k in range(nrm.shape[0]):
+            lam = (1.0 - nC[k]) / nd[k]
+            X = C[:, None] + lam[None, :] * d
+            z = X[2]
+            ok = (lam > 0) & (z > 1e-6) & torch.isfinite(lam)
+            qx = torch.where(ok, fx * X[0] / z + cx, torch.zeros_like(z))
+            qy = torch.where(ok, fy * X[1] / z + cy, torch.zeros_like(z))
+            ok &= label(qx, qy) == k
+            better = ok & (lam < best)
+            best = torch.where(better, lam, best)
+            hit[:, better] = X[:, better]
+        return hit, torch.isfinite(best)
+
+    sh = (height, width)
+    views = []
+    for R, t in poses:
+        X, found = raycast(T(R), T(t), xs, ys)
+        px = torch.where(found, fx * X[0] / X[2] + cx, xs)
+        py = torch.where(found, fy * X[1] / X[2] + cy, ys)
+        views.append((texture(px, py).reshape(sh).cpu().numpy(), X, found))
+    pairs = []
+    for k in range(len(poses) - 1):
+        (Ra, ta), (Rb, tb) = poses[k], poses[k + 1]
+        _, X, found = views[k]
+        Xa = T(Ra) @ X + T(ta)[:, None]
+        Xb = T(Rb) @ X + T(tb)[:, None]
+        u1 = fx * Xb[0] / Xb[2] + cx
+        v1 = fy * Xb[1] / Xb[2] + cy
+        inv = torch.where(found, 1.0 / Xa[2], torch.zeros_like(Xa[2]))
+        inb = (found & (Xb[2] > 1e-6) & (u1 >= 0) & (u1 <= width - 1) & (v1 >= 0)
+               & (v1 <= height - 1))
+        zero = torch.zeros_like(u1)
+        Xv, fv = raycast(T(Rb), T(tb), torch.where(inb, u1, zero), torch.where(inb, v1, zero))
+        same = fv & (torch.sqrt(((Xv - X) ** 2).sum(0))
+                     < 1e-3 * torch.clamp(Xa[2].abs(), min=1.0))
+        flow = torch.stack([torch.where(found, u1 - xs, zero).reshape(sh),
+                            torch.where(found, v1 - ys, zero).reshape(sh)], -1)
+        Rr = Rb @ Ra.T
+        pairs.append({"flow": flow.cpu().numpy().astype(np.float32),
+                      "inv_depth": inv.reshape(sh).cpu().numpy().astype(np.float32),
+                      "valid": (inb & same).reshape(sh).cpu().numpy(),
+                      "R": Rr, "t": tb - Rr @ ta})
+    return [v[0] for v in views], pairs

@@ -74,3 +74,21 @@ def test_sequence_is_seeded():
     c = S.make_sequence(64, 48, 3, seed=10)
     assert all(np.array_equal(x, y) for x, y in zip(a["frames"], b["frames"]))
     assert not np.array_equal(a["frames"][1], c["frames"][1])
+
+
+def test_sequence_torch_renderer_matches_numpy():
+    """The torch renderer (run here on the CPU; on a GPU it renders the
+    full-size streams) gives the numpy path's frames and ground truth."""
+    import pytest
+
+    pytest.importorskip("torch")
+    a = S.make_sequence(80, 60, 3, seed=5)
+    b = S.make_sequence(80, 60, 3, seed=5, device="cpu")
+    for x, y in zip(a["frames"], b["frames"]):
+        assert np.allclose(x, y, atol=1e-6)
+    for p, q in zip(a["pairs"], b["pairs"]):
+        assert (p["valid"] == q["valid"]).mean() > 0.999
+        both = p["valid"] & q["valid"]
+        assert np.allclose(p["flow"][both], q["flow"][both], atol=1e-5)
+        assert np.allclose(p["inv_depth"], q["inv_depth"], atol=1e-6)
+        assert np.array_equal(p["R"], q["R"]) and np.array_equal(p["t"], q["t"])
