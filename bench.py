@@ -646,6 +646,13 @@ def run_learned(args, wl, world, rank, local):
             torch.cuda.synchronize()
             step_ms = timed(step, args.steps)
         launches = b.kernelLaunches() + net.kernel_launches() + f.kernelLaunches() - l0
+    # the network's tensor-core launches flag a bounded wait that gave up
+    try:
+        tc_gave_up = net.wait_gave_up()
+    except Exception as exc:  # report a failed read instead of hiding it
+        tc_gave_up = f"status read failed: {exc}"
+    if tc_gave_up is not False:
+        print(f"bench.py: tensor-core wait status: {tc_gave_up}", file=sys.stderr)
     timed_fallbacks = list(fallbacks)
     total_s = max_over_ranks(sum(step_ms) / 1000.0, world)
     value = world * n * args.steps / total_s
@@ -757,6 +764,7 @@ def run_learned(args, wl, world, rank, local):
                       "batched_pairs_per_s": 1000.0 * n / statistics.median(plain_batch_ms),
                       "accuracy": plain_acc},
             "learned": {"accuracy": learned_acc, "fallbacks_per_step": timed_fallbacks,
+                        "tc_wait_gave_up": tc_gave_up,
                         "energy_ratio_median": float(np.median(e_learned / e_plain))},
             "speedup_vs_plain_single_pair": value / single_pps,
             "equal_epe": {"mean": learned_acc["epe_mean_px"] <= plain_acc["epe_mean_px"] + tol,

@@ -378,6 +378,11 @@ RF_API rf_status rf_cnn_backward(rf_cnn* c, const float* input, const float* tgt
                                  int batch, int height, int width, const float* w, double* loss);
 RF_API rf_status rf_cnn_adam_step(rf_cnn* c, float lr, float beta1, float beta2, float eps);
 RF_API uint64_t rf_cnn_kernel_launches(const rf_cnn* c);
+/* Whether a tensor-core launch of this network gave up on a bounded
+ * mbarrier wait since the last call (its outputs are then undefined): sets
+ * *gave_up to 1 or 0 and clears the flag.  Synchronizes the network's
+ * stream. */
+RF_API rf_status rf_cnn_status(rf_cnn* c, int* gave_up);
 
 /* Warm-start network input (no reference counterpart): for n frame pairs
  * (device planes of w0 x h0 float32 pixels, s0 floats per row; host arrays

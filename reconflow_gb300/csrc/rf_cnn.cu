@@ -701,4 +701,14 @@ rf_status rf_cnn_adam_step(rf_cnn* c, float lr, float beta1, float beta2, float 
 
 uint64_t rf_cnn_kernel_launches(const rf_cnn* c) { return c ? c->launches : 0; }
 
+rf_status rf_cnn_status(rf_cnn* c, int* gave_up) {
+    if (!c || !gave_up) return cfail(RF_ERR_INVALID_ARG, "rf_cnn_status: null");
+    int v = 0;
+    CN(cudaMemcpyAsync(&v, c->d_status, sizeof(int), cudaMemcpyDeviceToHost, c->stream));
+    CN(cudaStreamSynchronize(c->stream));
+    if (v) CN(cudaMemsetAsync(c->d_status, 0, sizeof(int), c->stream));
+    *gave_up = v;
+    return RF_OK;
+}
+
 }  // extern "C"

@@ -126,6 +126,13 @@ class WarmStartNet:
     def kernel_launches(self) -> int:
         return int(self._lib.rf_cnn_kernel_launches(self._h))
 
+    def wait_gave_up(self) -> bool:
+        """rf_cnn_status: whether a tensor-core launch gave up on a bounded
+        wait since the last call (clears the flag; synchronizes)."""
+        v = ctypes.c_int(0)
+        N.check(self._lib.rf_cnn_status(self._h, ctypes.byref(v)))
+        return bool(v.value)
+
     def params(self) -> np.ndarray:
         out = np.zeros(self.n_params, np.float32)
         N.check(self._lib.rf_cnn_get_params(self._h, out.ctypes.data_as(ctypes.c_void_p)))

@@ -93,8 +93,9 @@ def test_null_handle_calls_fail_cleanly(rf):
 
 
 def test_batch_null_handle_calls_fail_cleanly(rf):
-    """The batch entry points check their handle before any CUDA call, so
-    they fail with RF_ERR_INVALID_ARG (1) and a message on any host."""
+    """The batch entry points (and the network's status read) check their
+    handle before any CUDA call, so they fail with RF_ERR_INVALID_ARG (1)
+    and a message on any host."""
     lib = rf.load()
     calls = [
         ("rf_batch_upload_all", (None, None, None, 0)),
@@ -106,6 +107,7 @@ def test_batch_null_handle_calls_fail_cleanly(rf):
         ("rf_batch_synchronize", (None,)),
         ("rf_batch_energies", (None, None)),
     ]
+    calls.append(("rf_cnn_status", (None, None)))
     for name, args in calls:
         assert getattr(lib, name)(*args) == 1, name
         assert "null" in lib.rf_last_error_string().decode(), name

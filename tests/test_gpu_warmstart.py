@@ -56,6 +56,8 @@ def test_gradients_match_fp64_oracle(torch_cuda):
             assert rel < 3e-2, (cin, cout, n, rel)
             off += n
     assert off == net.n_params
+    # no tensor-core launch gave up on its bounded mbarrier waits
+    assert net.wait_gave_up() is False
 
 
 def test_training_reduces_loss_and_is_deterministic(torch_cuda):
