@@ -104,6 +104,8 @@ SOLVER = dict(method=14, lam=50.0, theta=0.33, tau=0.25, alpha_proj=60.0, lambda
 # duhat(2),uproj(2),X1,Y1,Z1 = 7; B reads duhat(2),p(4),X1(3),sk(2),u,v,uproj(2)
 # = 15, writes p(4),X,Y,Z,sk(2) = 9.
 ALG_BYTES = {"recon_a": 25 * 4, "recon_b": 24 * 4}
+# compulsory bytes of one inner iteration per pixel (both kernels together)
+ITER_BYTES = 31 * 4
 L2_FLUSH_BYTES = 512 << 20
 E2E_MODE = ("pipelined: the frames of step k+1 go up and the results of step k come down on "
             "copy streams while step k solves (rf_batch_stage_upload / "
@@ -269,8 +271,9 @@ def make_inputs(wl):
 
 
 def cpu_sample(wl, sc, I0, I1, threads=None):
-    """FP32 reference-semantics oracle on this host: the full schedule at 1
-    and 5 inner iterations, extrapolated linearly to the workload's count."""
+    """FP32 reference-semantics oracle on this host: ``run(iters)`` times one
+    plain solve of the pair with the workload's levels and warps and `iters`
+    inner iterations."""
     from oracle import oracle as O
 
     O.build()
@@ -291,27 +294,31 @@ def cpu_sample(wl, sc, I0, I1, threads=None):
     return run, O.num_threads()
 
 
-def extrapolate(t1, t5, iters):
-    per_iter = max(t5 - t1, 1e-9) / 4.0
-    return t1 + per_iter * (iters - 1)
-
-
 def run_reference(args, wl, world, rank):
+    """The reference semantics on the host CPU: every timed step is one full
+    plain solve of one pair of the workload's size (all levels, warps and
+    inner iterations), timed on its own; the warm-up steps are the same
+    solve at one inner iteration (they only page the buffers in and start
+    the thread pool)."""
     if rank != 0:
         return
     sc, I0, I1, s = make_inputs(wl)
     run, cores = cpu_sample(wl, sc, I0, I1)
-    t1 = min(run(1) for _ in range(max(1, args.warmup)))
-    per_pair = []
-    for _ in range(args.steps):
-        per_pair.append(extrapolate(t1, run(5), wl["iters"]))
+    for _ in range(args.warmup):
+        run(1)
+    per_pair = [run(wl["iters"]) for _ in range(args.steps)]
     total = sum(per_pair)
     value = args.steps / total
-    sample = (f"{wl['width']}x{wl['height']} pair, full {wl['levels']}-level x {wl['warps']}-warp "
-              f"schedule at 1 and 5 inner iterations, extrapolated linearly to {wl['iters']}")
+    sample = (f"one {wl['width']}x{wl['height']} pair per step, the full {wl['levels']}-level x "
+              f"{wl['warps']}-warp x {wl['iters']}-iteration plain schedule, measured "
+              f"(median {statistics.median(per_pair):.2f} s per pair on {cores} threads); "
+              f"warm-up steps at 1 inner iteration")
     cfg = config_of(wl)
+    cfg["l2"] = "not applicable (host CPU)"
     if "workload" in wl:
         cfg["workload"] = wl["workload"]
+        cfg["reference_path"] = ("the plain solve of one pair: the reference has no batched "
+                                 "or learned path, so this arm times its counterpart")
     line = {
         "impl": "reference", "metric": wl.get("metric", PLAIN_METRIC),
         "value": value, "unit": "pairs/s", "n_gpus": args.gpus, "steps": args.steps,
@@ -729,12 +736,12 @@ def run_learned(args, wl, world, rank, local):
         s_ = (W + 31) // 32 * 32
         pad = lambda a: np.pad(a, ((0, 0), (0, s_ - W))).astype(np.float32)  # noqa: E731
         run, cores = cpu_sample(wl1, sc0, pad(sc0["I0"]), pad(sc0["I1"]))
-        t1, t5 = run(1), run(5)
-        per_pair = extrapolate(t1, t5, wl["plain_iters"])
+        run(1)
+        per_pair = run(wl["plain_iters"])
         cpu = {"value": 1.0 / per_pair, "unit": "pairs/s", "cores": cores, "kind": "port",
-               "sample": f"plain solve of one {W}x{H} pair, full schedule at 1 and 5 inner "
-                         f"iterations ({t1:.2f} s, {t5:.2f} s), extrapolated linearly to "
-                         f"{wl['plain_iters']}"}
+               "sample": f"one plain solve of one {W}x{H} pair, the full {wl['levels']}-level x "
+                         f"{wl['plain_warps']}-warp x {wl['plain_iters']}-iteration schedule, "
+                         f"measured ({per_pair:.2f} s)"}
     if rank == 0:
         single_pps = 1000.0 / statistics.median(single_ms)
         tol = 0.05
@@ -1320,7 +1327,18 @@ def roofline_of(ms, px, batched=False):
             "launch_ms": {names[0]: ms[0], names[1]: ms[1]},
             "frac_each": {names[k]: ALG_BYTES[names[k]] * px / (ms[k] * 1e-3) / 1e9 / peak
                           for k in range(2)},
+            "iteration": iteration_roofline(ms, px, peak),
             "timing": "launches of one kernel back to back in a CUDA graph, CUDA events"}
+
+
+def iteration_roofline(ms, px, peak):
+    """The whole inner iteration against its compulsory traffic: 13 state
+    floats read and written plus 5 per-warp constants read = 124 B per
+    pixel-iteration, over the time of both inner-iteration kernels."""
+    t = (ms[0] + ms[1]) * 1e-3
+    achieved = ITER_BYTES * px / t / 1e9
+    return {"alg_bytes_per_pixel": ITER_BYTES, "ms": ms[0] + ms[1], "achieved": achieved,
+            "frac": achieved / peak}
 
 
 def config_of(wl):
@@ -1507,12 +1525,12 @@ def main():
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         run, cores = cpu_sample(wl, sc, I0, I1)
-        t1 = run(1)
-        t5 = run(5)
-        per_pair = extrapolate(t1, t5, wl["iters"])
+        run(1)
+        per_pair = run(wl["iters"])
         cpu = {"value": 1.0 / per_pair, "unit": "pairs/s", "cores": cores, "kind": "port",
-               "sample": f"{w}x{h} pair, full schedule at 1 and 5 inner iterations "
-                         f"({t1:.2f} s, {t5:.2f} s), extrapolated linearly to {wl['iters']}"}
+               "sample": f"one plain solve of one {w}x{h} pair, the full {wl['levels']}-level x "
+                         f"{wl['warps']}-warp x {wl['iters']}-iteration schedule, measured "
+                         f"({per_pair:.2f} s)"}
 
     if rank == 0:
         line = {

@@ -332,7 +332,13 @@ RF_API rf_status rf_batch_download_all(rf_batch* b, float* const* u, float* cons
  * then to the host arrays on the copy stream, and returns at once: the next
  * solve may be queued immediately.  rf_batch_wait_download blocks until
  * the last staged download has reached the host.  The results are the same
- * bytes rf_batch_download_all writes. */
+ * bytes rf_batch_download_all writes.
+ *
+ * The calls return at once only when the host arrays are pinned
+ * (rf_host_alloc, or cudaHostRegister on the caller's memory): with pageable
+ * arrays the CUDA runtime stages the copies through its own buffers, so the
+ * upload blocks while it copies and the download blocks until the solve it
+ * follows has finished, and nothing overlaps. */
 RF_API rf_status rf_batch_stage_upload(rf_batch* b, const float* const* i0,
                                        const float* const* i1, int pitch);
 RF_API rf_status rf_batch_take_upload(rf_batch* b);
@@ -383,6 +389,13 @@ RF_API uint64_t rf_cnn_kernel_launches(const rf_cnn* c);
  * *gave_up to 1 or 0 and clears the flag.  Synchronizes the network's
  * stream. */
 RF_API rf_status rf_cnn_status(rf_cnn* c, int* gave_up);
+/* Test hook for the bounded waits (no reference counterpart): polls >= 0
+ * caps the first ring-slot wait of every tensor-core CTA at that many polls
+ * (0: it gives up at once, while the MMAs it waited for still complete), so
+ * a test can drive the give-up path without a wait that never ends; the
+ * launches then report through rf_cnn_status and write no outputs.  polls < 0
+ * restores the normal limit. */
+RF_API rf_status rf_cnn_set_test_wait_limit(rf_cnn* c, int polls);
 
 /* Warm-start network input (no reference counterpart): for n frame pairs
  * (device planes of w0 x h0 float32 pixels, s0 floats per row; host arrays
@@ -455,7 +468,9 @@ RF_API rf_status rfk_warp_update(const float* duhat, const float* dvhat, const f
  * order them on one stream.  height * stride above RF_NOALLOC_MAX_PLANE is
  * rejected with RF_ERR_INVALID_ARG.  The first call on each device looks up
  * the array's device address with that device current; make it before any
- * stream capture on that device. */
+ * stream capture on that device.  The address is kept for the life of the
+ * process: do not call it again on a device after cudaDeviceReset (the reset
+ * drops the module that held the array, and the kept address goes stale). */
 RF_API rf_status rfk_warp_update_noalloc(const float* duhat, const float* dvhat, const float* u,
                                          const float* v, int w, int h, int s, float* out_u,
                                          float* out_v, void* stream);

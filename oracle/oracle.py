@@ -276,9 +276,10 @@ def solve(params: RfoParams, I0, I1, K0=None, K1=None, R0=None, t0=None, R1=None
 
 
 def solve_warm(params: RfoParams, I0, I1, level, u0, v0, X0, Y0, Z0, warps, iters, K0=None,
-               K1=None, R0=None, t0=None, R1=None, t1=None):
-    """FP32 schedule started at pyramid `level` from the given flow and points
-    (planes with that level's stride).  Returns dict of (height, stride) arrays."""
+               K1=None, R0=None, t0=None, R1=None, t1=None, dtype=np.float32):
+    """Schedule started at pyramid `level` from the given flow and points
+    (float planes with that level's stride), in FP32 or FP64.  Returns dict of
+    (height, stride) arrays."""
     W, H, S = pyramid_dims(params.width, params.height, params.n_levels, params.scale,
                            params.stride_alignment)
     s, h = S[0], H[0]
@@ -290,13 +291,13 @@ def solve_warm(params: RfoParams, I0, I1, level, u0, v0, X0, Y0, Z0, warps, iter
     R1 = np.ascontiguousarray(eye if R1 is None else R1, np.float64)
     t1 = np.ascontiguousarray(z3 if t1 is None else t1, np.float64)
     ws = [np.ascontiguousarray(a, np.float32) for a in (u0, v0, X0, Y0, Z0)]
-    out = {k: np.zeros((h, s), np.float32) for k in ("u", "v", "X", "Y", "Z")}
+    out = {k: np.zeros((h, s), dtype) for k in ("u", "v", "X", "Y", "Z")}
     I0 = np.ascontiguousarray(I0, np.float32)
     I1 = np.ascontiguousarray(I1, np.float32)
-    rc = lib().rfo_solve_warm_f32(ctypes.byref(params), _ptr(I0), _ptr(I1), int(s), _ptr(K0),
-                                  _ptr(K1), _ptr(R0), _ptr(t0), _ptr(R1), _ptr(t1), int(level),
-                                  *[_ptr(a) for a in ws], int(warps), int(iters),
-                                  *[_ptr(out[k]) for k in ("u", "v", "X", "Y", "Z")])
+    fn = getattr(lib(), f"rfo_solve_warm_{_sfx(dtype)}")
+    rc = fn(ctypes.byref(params), _ptr(I0), _ptr(I1), int(s), _ptr(K0), _ptr(K1), _ptr(R0),
+            _ptr(t0), _ptr(R1), _ptr(t1), int(level), *[_ptr(a) for a in ws], int(warps),
+            int(iters), *[_ptr(out[k]) for k in ("u", "v", "X", "Y", "Z")])
     if rc != 0:
         raise RuntimeError(f"oracle warm solve failed: {rc}")
     return out

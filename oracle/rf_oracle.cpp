@@ -1149,6 +1149,21 @@ int rfo_solve_warm_f32(const rfo_params* p, const float* i0, const float* i1, in
                         u, v, X, Y, Z, &ws);
 }
 
+// The same warm-started schedule in FP64 (the warm state is given in float,
+// as the FP32 path receives it).
+int rfo_solve_warm_f64(const rfo_params* p, const float* i0, const float* i1, int in_stride,
+                       const double* K0, const double* K1, const double* R0, const double* t0,
+                       const double* R1, const double* t1, int level, const float* wu,
+                       const float* wv, const float* wX, const float* wY, const float* wZ,
+                       int warps, int iters, double* u, double* v, double* X, double* Y,
+                       double* Z) {
+    WarmStart ws;
+    ws.level = level; ws.u = wu; ws.v = wv; ws.X = wX; ws.Y = wY; ws.Z = wZ;
+    ws.warps = warps; ws.iters = iters;
+    return solve<double>(*p, i0, i1, in_stride, K0, K1, R0, t0, R1, t1, nullptr, nullptr,
+                         nullptr, u, v, X, Y, Z, &ws);
+}
+
 double rfo_energy(const float* I0, const float* I1, const float* u, const float* v,
                   const float* X, const float* Y, const float* Z, int w, int h, int s,
                   float lambda, float alpha_proj, const double* R1, const double* t1,

@@ -131,6 +131,7 @@ _SIGS = [
     ("rf_cnn_adam_step", _I, [_VP, _F, _F, _F, _F]),
     ("rf_cnn_kernel_launches", ctypes.c_uint64, [_VP]),
     ("rf_cnn_status", _I, [_VP, ctypes.POINTER(ctypes.c_int)]),
+    ("rf_cnn_set_test_wait_limit", _I, [_VP, ctypes.c_int]),
     ("rf_ws_features", _I, [_I, _VP, _VP, _I, _I, _I, _I, _D, _D, _D, _VP, _VP]),
     ("rf_ws_state", _I, [_I, _VP, _I, _I, _I, _I, _I, _I, _F, _D, _D, _D, _VP, _VP, _VP, _VP,
                          _VP, _VP]),

@@ -481,7 +481,7 @@ int launch_op(rf_batch* b, int level, const Op& op) {
     const dim3 block(b->tile_w[level], b->tile_h[level]);
     k_batch<Op><<<tiles, block, 0, b->stream>>>(ctx_of(b, level), level, op);
     b->enq++;
-    return cudaGetLastError() == cudaSuccess ? 0 : 1;
+    return rf::launch_status();
 }
 
 // Tile range of pair group g at `level`: group 0 = pairs [0, split), group
@@ -504,7 +504,7 @@ int launch_group(rf_batch* b, int level, int g, const Op& op) {
     const dim3 block(b->tile_w[level], b->tile_h[level]);
     k_batch<Op><<<count, block, 0, b->stream>>>(c, level, op);
     b->enq++;
-    return cudaGetLastError() == cudaSuccess ? 0 : 1;
+    return rf::launch_status();
 }
 
 // `x` over pair group gx and `y` over the other group, in one launch
@@ -518,14 +518,14 @@ int launch_pair(rf_batch* b, int level, int gx, const OpX& x, const OpY& y) {
     k_batch_pair<OpX, OpY><<<nx + ny, block, 0, b->stream>>>(ctx_of(b, level), level, x, xb, nx,
                                                              y, yb, ny);
     b->enq++;
-    return cudaGetLastError() == cudaSuccess ? 0 : 1;
+    return rf::launch_status();
 }
 
 #define BL(expr)                                                                       \
     do {                                                                               \
         if ((expr) != 0)                                                               \
             return bfail(RF_ERR_CUDA, std::string("batch launch: ") +                 \
-                                          cudaGetErrorString(cudaGetLastError()));     \
+                                          cudaGetErrorString(rf::last_launch_error())); \
     } while (0)
 #define BC(call)                                                                       \
     do {                                                                               \

@@ -326,6 +326,7 @@ struct rf_cnn {
     bf16* wb = nullptr;               // BF16 copy used by the kernels
     bf16* wt = nullptr;               // BF16 weights per layer as [ci][tap][co]
     int* d_status = nullptr;          // set by a tensor-core launch whose wait gave up
+    int test_first_wait_polls = -1;   // rf_cnn_set_test_wait_limit (-1: the normal limit)
     int step = 0;
     // activations (BF16) and gradients (FP32 / BF16)
     bf16 *x = nullptr, *a1 = nullptr, *a2 = nullptr, *a3 = nullptr, *cat = nullptr, *a4 = nullptr;
@@ -368,7 +369,7 @@ rf_status tc_launch(rf_cnn* c, int M, int N, int K, int splits, LA la, LB lb, EP
     splits = (K + kspan - 1) / kspan;
     dim3 grid((M + rf_tc::kTM - 1) / rf_tc::kTM, (N + NT - 1) / NT, splits);
     rf_tc::k_tc_gemm<NT, LA, LB, EP><<<grid, rf_tc::kThreads, S::kBytes, c->stream>>>(
-        M, N, K, kspan, la, lb, ep, c->d_status);
+        M, N, K, kspan, la, lb, ep, c->d_status, c->test_first_wait_polls);
     c->launches++;
     CN(cudaGetLastError());
     return RF_OK;
@@ -708,6 +709,12 @@ rf_status rf_cnn_status(rf_cnn* c, int* gave_up) {
     CN(cudaStreamSynchronize(c->stream));
     if (v) CN(cudaMemsetAsync(c->d_status, 0, sizeof(int), c->stream));
     *gave_up = v;
+    return RF_OK;
+}
+
+rf_status rf_cnn_set_test_wait_limit(rf_cnn* c, int polls) {
+    if (!c) return cfail(RF_ERR_INVALID_ARG, "rf_cnn_set_test_wait_limit: null");
+    c->test_first_wait_polls = polls < 0 ? -1 : polls;
     return RF_OK;
 }
 

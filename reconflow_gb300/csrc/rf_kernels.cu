@@ -31,7 +31,15 @@ constexpr int BY = 8;
 
 inline dim3 grid_for(int w, int h) { return dim3((w + BX - 1) / BX, (h + BY - 1) / BY); }
 
-inline int check_launch() { return cudaGetLastError() == cudaSuccess ? 0 : 1; }
+// the error the last failed launch helper consumed (cudaGetLastError clears
+// it), for the caller's message
+thread_local cudaError_t t_launch_error = cudaSuccess;
+
+inline int check_launch() {
+    const cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) t_launch_error = e;
+    return e == cudaSuccess ? 0 : 1;
+}
 
 // ---------------------------------------------------------------------------
 // Input conversion (rgbToGray.cu:3-77)
@@ -309,25 +317,29 @@ __global__ void k_flow_color(const float* __restrict__ u, const float* __restric
     int r = blockIdx.y * blockDim.y + threadIdx.y;
     if (c >= d.w || r >= d.h) return;
     int pos = c + d.s * r;
-    float du = u[pos] / flow_scale;
-    float dv = v[pos] / flow_scale;
-    const int ncols = 55;
-    float rad = sqrtf(du * du + dv * dv);
-    float a = atan2f(-dv, -du) / 3.14159f;
-    float fk = (a + 1) / 2 * ((float)ncols - 1) + 1;
-    int k0 = (int)floorf(fk);
-    int k1 = k0 + 1;
-    if (k1 == ncols + 1) k1 = 1;
-    float fr = fk - (float)k0;
-    k0 %= ncols;
-    k1 %= ncols;
+    // the flow vector in units of flow_scale, its length and its angle
+    // mapped onto the wheel's 55 hues (the hue position wraps from the last
+    // entry back to the first)
+    float fx = u[pos] / flow_scale;
+    float fy = v[pos] / flow_scale;
+    const int n_hues = 55;
+    float len = sqrtf(fx * fx + fy * fy);
+    float ang = atan2f(-fy, -fx) / 3.14159f;
+    float hue = (ang + 1) / 2 * ((float)n_hues - 1) + 1;
+    int lo = (int)floorf(hue);
+    int hi = lo + 1;
+    if (hi == n_hues + 1) hi = 1;
+    float t = hue - (float)lo;
+    lo %= n_hues;
+    hi %= n_hues;
     float col[3];
 #pragma unroll
     for (int ch = 0; ch < 3; ch++) {
-        float cv = (1 - fr) * (c_wheel[ch][k0] / 255.0f) + fr * (c_wheel[ch][k1] / 255.0f);
-        if (rad <= 1) cv = 1 - rad * (1 - cv);
-        else cv = cv * 0.75f;
-        col[ch] = cv;
+        float mix = (1 - t) * (c_wheel[ch][lo] / 255.0f) + t * (c_wheel[ch][hi] / 255.0f);
+        // inside the unit circle, desaturate towards white; outside, darken
+        if (len <= 1) mix = 1 - len * (1 - mix);
+        else mix = mix * 0.75f;
+        col[ch] = mix;
     }
     // float3 (x, y, z) = (B, G, R) as the reference stores it
     rgb[3 * pos + 0] = col[2];
@@ -433,6 +445,14 @@ __global__ void k_energy_final_jobs(const EnergyJob* jobs) {
 // ---------------------------------------------------------------------------
 // Launchers
 // ---------------------------------------------------------------------------
+int launch_status() { return check_launch(); }
+
+cudaError_t last_launch_error() {
+    const cudaError_t e = t_launch_error;
+    t_launch_error = cudaSuccess;
+    return e;
+}
+
 int launch_convert(const void* in, int type, int w, int h, int in_pitch, float* out, int s,
                    cudaStream_t st) {
     k_convert<<<grid_for(w, h), dim3(BX, BY), 0, st>>>(in, type, w, h, in_pitch, out, s);
@@ -487,7 +507,9 @@ int launch_pdl(void (*kern)(KArgs...), dim3 g, dim3 b, cudaStream_t st, Args... 
     attr[0].val.programmaticStreamSerializationAllowed = use_pdl() ? 1 : 0;
     cfg.attrs = attr;
     cfg.numAttrs = 1;
-    return cudaLaunchKernelEx(&cfg, kern, args...) == cudaSuccess ? 0 : 1;
+    const cudaError_t e = cudaLaunchKernelEx(&cfg, kern, args...);
+    if (e != cudaSuccess) t_launch_error = e;
+    return e == cudaSuccess ? 0 : 1;
 }
 
 int launch_recon_a(const ReconFields& f, const LevelConsts* lc, const Weights& wt, LevelDims d,
@@ -498,10 +520,6 @@ int launch_recon_a(const ReconFields& f, const LevelConsts* lc, const Weights& w
     if (prior == 2) return launch_pdl(k_recon_a<2>, g, b, st, f, lc, wt, d, fi, ub);
     return launch_pdl(k_recon_a<0>, g, b, st, f, lc, wt, d, fi, ub);
 }
-
-
-
-
 
 int launch_recon_b(const ReconFields& f, const Weights& wt, LevelDims d, bool first,
                    cudaStream_t st, dim3 b) {

@@ -94,6 +94,13 @@ int launch_plain_tv(const float* duhat, const float* dvhat, float* pu1, float* p
 // out = u + median5(duhat) (out may alias u)
 int launch_median_add(const float* duhat, const float* dvhat, const float* u, const float* v,
                       float* ou, float* ov, LevelDims d, cudaStream_t st);
+// 0 if the last kernel launch on this thread succeeded, else 1; a failure's
+// error is kept for last_launch_error (cudaGetLastError clears it).
+int launch_status();
+// The CUDA error of the last launch helper on this thread that returned
+// nonzero (cudaSuccess if none since the previous call); reading it clears it.
+cudaError_t last_launch_error();
+
 int launch_median5(const float* u, const float* v, float* ou, float* ov, LevelDims d,
                    cudaStream_t st);
 int launch_median3d(const float* X, const float* Y, const float* Z, float* X1, float* Y1,

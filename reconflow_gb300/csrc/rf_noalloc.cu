@@ -21,7 +21,9 @@
 //  * host code cannot use the array's name as a device address, so the first
 //    call on each device looks the address up (cudaGetSymbolAddress) with that
 //    device current and caches it; make that first call before any stream
-//    capture on the device.
+//    capture on the device.  The cached address lives as long as the
+//    process's context on that device: after cudaDeviceReset it is stale,
+//    so the entry point must not be used on that device again.
 #include <mutex>
 #include <string>
 
@@ -85,6 +87,6 @@ extern "C" rf_status rfk_warp_update_noalloc(const float* duhat, const float* dv
     if (rf::launch_median_add(duhat, dvhat, u, v, base, base + kMaxPlane, d, st) != 0 ||
         rf::launch_median5(base, base + kMaxPlane, out_u, out_v, d, st) != 0)
         return noalloc_fail(RF_ERR_CUDA, std::string("rfk_warp_update_noalloc: launch: ") +
-                                             cudaGetErrorString(cudaGetLastError()));
+                                             cudaGetErrorString(rf::last_launch_error()));
     return RF_OK;
 }

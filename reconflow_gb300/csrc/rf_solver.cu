@@ -227,7 +227,8 @@ namespace {
 
 #define RF_LAUNCH(expr)                                                               \
     do {                                                                              \
-        if ((expr) != 0) return cuda_fail(cudaGetLastError(), "kernel launch " #expr); \
+        if ((expr) != 0)                                                              \
+            return cuda_fail(rf::last_launch_error(), "kernel launch " #expr);        \
         h->enqueue_launches++;                                                        \
     } while (0)
 
@@ -788,7 +789,7 @@ rf_status rf_energy(rf_handle* h, double* energy) {
                       h->p.alpha_proj, recon ? h->last_R1 : nullptr, recon ? h->last_t1 : nullptr,
                       recon ? h->K1 : nullptr, recon ? 1 : 0, h->d_energy + 1, nb, h->d_energy,
                       h->stream) != 0)
-        return cuda_fail(cudaGetLastError(), "rf_energy: launch");
+        return cuda_fail(rf::last_launch_error(), "rf_energy: launch");
     h->launches += 2;
     RF_CUDA(cudaMemcpyAsync(energy, h->d_energy, sizeof(double), cudaMemcpyDeviceToHost,
                             h->stream));
@@ -845,7 +846,7 @@ rf_status rf_download_inv_depth(rf_handle* h, float* inv, int pitch) {
     if (pitch < h->p.width) return fail(RF_ERR_INVALID_ARG, "rf_download_inv_depth: pitch < width");
     LevelDims d{h->W[0], h->H[0], h->S[0]};
     if (launch_inv_depth(h->Z, d, h->scratch, h->stream) != 0)
-        return cuda_fail(cudaGetLastError(), "rf_download_inv_depth: launch");
+        return cuda_fail(rf::last_launch_error(), "rf_download_inv_depth: launch");
     h->launches++;
     rf_status rs = download(h, h->scratch, inv, pitch);
     if (rs == RF_OK) RF_CUDA(cudaStreamSynchronize(h->stream));
@@ -859,7 +860,7 @@ rf_status rf_download_flow_color(rf_handle* h, float flow_scale, float* rgb, int
     float* out = h->pool + (h->pool_floats - ((h->plane + 63) / 64 * 64) * 3);
     LevelDims d{h->W[0], h->H[0], h->S[0]};
     if (launch_flow_color(h->res_u, h->res_v, d, flow_scale, out, h->stream) != 0)
-        return cuda_fail(cudaGetLastError(), "rf_download_flow_color: launch");
+        return cuda_fail(rf::last_launch_error(), "rf_download_flow_color: launch");
     h->launches++;
     RF_CUDA(cudaMemcpy2DAsync(rgb, (size_t)pitch * 3 * sizeof(float), out,
                               (size_t)h->stride * 3 * sizeof(float), h->p.width * 3 * sizeof(float),
@@ -878,7 +879,7 @@ rf_status rf_remove_edge_artifacts(rf_handle* h, int surface_width, float max_ar
     LevelDims d{h->W[0], h->H[0], h->S[0]};
     if (launch_remove_edge(h->X, h->Y, h->Z, surface_width, max_area, d, h->X1, h->Y1, h->Z1,
                            h->stream) != 0)
-        return cuda_fail(cudaGetLastError(), "rf_remove_edge_artifacts: launch");
+        return cuda_fail(rf::last_launch_error(), "rf_remove_edge_artifacts: launch");
     h->launches++;
     // the reference swaps X <-> Xs; copy back so X keeps its buffer
     const size_t bytes = (size_t)h->stride * h->height * sizeof(float);
@@ -987,7 +988,8 @@ rf_status rf_profile_iterations(rf_handle* h, int level, int n_iters, float* ms)
         cudaError_t ce = cudaStreamEndCapture(st, &g);
         if (bad || ce != cudaSuccess) {
             if (g) cudaGraphDestroy(g);
-            return cuda_fail(bad ? cudaGetLastError() : ce, "rf_profile_iterations: capture");
+            return cuda_fail(bad ? rf::last_launch_error() : ce,
+                             "rf_profile_iterations: capture");
         }
         ce = cudaGraphInstantiate(&ge, g, 0);
         cudaGraphDestroy(g);
@@ -1024,7 +1026,7 @@ const char* rf_version(void) { return "reconflow_gb300 0.1 (sm_103a)"; }
 #define RFK_CHECK(cond, name) \
     if (!(cond)) return fail(RF_ERR_INVALID_ARG, name ": bad argument")
 #define RFK_RET(expr, name) \
-    return (expr) == 0 ? RF_OK : cuda_fail(cudaGetLastError(), name)
+    return (expr) == 0 ? RF_OK : cuda_fail(rf::last_launch_error(), name)
 
 rf_status rfk_downscale(const float* src, int w, int h, int s, int nw, int nh, int ns, float scale,
                         int scaled, float* out, void* stream) {
@@ -1076,7 +1078,7 @@ rf_status rfk_warp_update(const float* duhat, const float* dvhat, const float* u
               "rfk_warp_update");
     LevelDims d{w, h, s};
     if (launch_median_add(duhat, dvhat, u, v, tmp_u, tmp_v, d, (cudaStream_t)stream) != 0)
-        return cuda_fail(cudaGetLastError(), "rfk_warp_update");
+        return cuda_fail(rf::last_launch_error(), "rfk_warp_update");
     RFK_RET(launch_median5(tmp_u, tmp_v, out_u, out_v, d, (cudaStream_t)stream), "rfk_warp_update");
 }
 

@@ -68,10 +68,12 @@ __device__ __forceinline__ void mbar_init(uint64_t* bar, unsigned count) {
                  : "memory");
 }
 
-// bounded wait on an mbarrier phase; false if it did not complete
-__device__ __forceinline__ bool mbar_wait(uint64_t* bar, unsigned parity) {
+// bounded wait on an mbarrier phase (at most `limit` polls); false if it did
+// not complete
+__device__ __forceinline__ bool mbar_wait(uint64_t* bar, unsigned parity,
+                                          unsigned limit = kSpinLimit) {
     const uint32_t a = smem_u32(bar);
-    for (unsigned i = 0; i < kSpinLimit; i++) {
+    for (unsigned i = 0; i < limit; i++) {
         uint32_t done;
         asm volatile(
             "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n"
@@ -175,10 +177,19 @@ struct TcSmem {
 };
 
 // grid: x = M tiles, y = N tiles, z = K splits (each `kspan` long, a multiple
-// of kTK).  `status` (device int) is set to 1 if a wait gave up.
+// of kTK).  `status` (device int) is set to 1 if a wait gave up; the launch's
+// outputs are then not written.  A thread whose wait for a ring slot gives up
+// writes no further chunks (an MMA may still be reading that slot); the MMA
+// thread keeps issuing and committing, and every thread drains the last
+// commit with the full limit before TMEM is released, so TMEM is freed under
+// MMAs in flight only if that second wait runs out too.  `first_wait_polls`
+// >= 0 caps the first slot wait of each CTA at that many polls (a test hook:
+// 0 makes it give up at once while the MMAs still complete); -1 = the
+// normal limit.
 template <int NT, class LA, class LB, class EP>
 __global__ void __launch_bounds__(kThreads) k_tc_gemm(int M, int N, int K, int kspan, LA la,
-                                                     LB lb, EP ep, int* status) {
+                                                     LB lb, EP ep, int* status,
+                                                     int first_wait_polls) {
     extern __shared__ __align__(1024) unsigned char smem_raw[];
     constexpr int kStages = stages_for<LA, LB>();
     using S = TcSmem<NT, kStages>;
@@ -265,6 +276,7 @@ __global__ void __launch_bounds__(kThreads) k_tc_gemm(int M, int N, int K, int k
         if (c < nchunks) issue(c);
         cp_async_commit();
     }
+    bool gave_up = false;  // this thread's slot wait ran out: it writes no more chunks
     for (int c = 0; c < nchunks; c++) {
         const int q = c % kStages;
         cp_async_wait<kStages - 2>();  // chunk c has landed
@@ -284,12 +296,17 @@ __global__ void __launch_bounds__(kThreads) k_tc_gemm(int M, int N, int K, int k
         }
         // refill the slot chunk c - 1 used once its MMAs are done
         const int nc = c + kStages - 1;
-        if (nc < nchunks) {
+        if (nc < nchunks && !gave_up) {
             if (c >= 1) {
                 const int pc = c - 1;
-                if (!mbar_wait(&bars[pc % kStages], (unsigned)(pc / kStages) & 1u)) *fail = 1;
+                const unsigned lim = (c == 1 && first_wait_polls >= 0) ? (unsigned)first_wait_polls
+                                                                       : kSpinLimit;
+                if (!mbar_wait(&bars[pc % kStages], (unsigned)(pc / kStages) & 1u, lim)) {
+                    gave_up = true;
+                    *fail = 1;
+                }
             }
-            issue(nc);
+            if (!gave_up) issue(nc);
         }
         cp_async_commit();
     }

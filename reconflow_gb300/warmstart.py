@@ -133,6 +133,12 @@ class WarmStartNet:
         N.check(self._lib.rf_cnn_status(self._h, ctypes.byref(v)))
         return bool(v.value)
 
+    def set_test_wait_limit(self, polls: int):
+        """rf_cnn_set_test_wait_limit: cap the first ring-slot wait of every
+        tensor-core CTA at `polls` polls (0: give up at once); -1 restores
+        the normal limit.  For tests of the give-up path."""
+        N.check(self._lib.rf_cnn_set_test_wait_limit(self._h, int(polls)))
+
     def params(self) -> np.ndarray:
         out = np.zeros(self.n_params, np.float32)
         N.check(self._lib.rf_cnn_get_params(self._h, out.ctypes.data_as(ctypes.c_void_p)))

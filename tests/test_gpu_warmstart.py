@@ -60,6 +60,30 @@ def test_gradients_match_fp64_oracle(torch_cuda):
     assert net.wait_gave_up() is False
 
 
+def test_wait_give_up_is_reported_and_recovers(torch_cuda):
+    """The bounded ring-slot wait of the tensor-core GEMM: with the test hook
+    its first wait gives up at once (the MMAs it waited for still complete,
+    so nothing hangs); the launch reports it through rf_cnn_status, and a
+    normal forward pass afterwards is bit-identical to one before."""
+    from reconflow_gb300.warmstart import WarmStartNet
+
+    rng = np.random.default_rng(5)
+    B, H, W = 2, 40, 48
+    net = WarmStartNet(B, H, W, seed=7)
+    x = torch_cuda.as_tensor(rng.normal(0, 0.5, (B, H, W, 16)).astype(np.float32),
+                             device="cuda")
+    ref16, ref8 = (t.clone() for t in net.forward(x))
+    assert net.wait_gave_up() is False
+    net.set_test_wait_limit(0)
+    net.forward(x)
+    assert net.wait_gave_up() is True
+    net.set_test_wait_limit(-1)
+    o16, o8 = net.forward(x)
+    assert net.wait_gave_up() is False
+    assert torch_cuda.equal(o16, ref16) and torch_cuda.equal(o8, ref8)
+    net.close()
+
+
 def test_training_reduces_loss_and_is_deterministic(torch_cuda):
     from reconflow_gb300.warmstart import WarmStartNet, train
 

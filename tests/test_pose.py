@@ -263,3 +263,26 @@ def test_five_point_real_roots_against_numpy(tmp_path):
     c = list(from_roots([0.5, 2.0])) + [1e-20]
     g = run([c])[0]
     assert np.allclose(g, [0.5, 2.0])
+
+
+def test_five_point_near_tangent_complex_pair(tmp_path):
+    """A complex pair close to the real axis.  At 1e-4 from it the
+    polynomial's minimum between the pair (1e-8 relative) is far above the
+    rounding level, and no real root comes back there.  At 1e-9 the minimum
+    (1e-18) is below the rounding error of evaluating the polynomial in
+    double precision, so it cannot be told from a real double root: the
+    finder reports one or two roots there, and the essential-matrix LMedS
+    scores that extra candidate like any other (it is kept only if its
+    median residual wins)."""
+    run = _roots_tool(tmp_path)
+    real = [-2.5, -1.0, 1.5, 3.0]
+    for dist, expect_root in ((1e-4, False), (1e-9, True)):
+        c = np.real(np.poly(real + [0.7 + 1j * dist, 0.7 - 1j * dist]))[::-1]
+        g = run([c])[0]
+        near = np.abs(g - 0.7) < 1e-3
+        others = g[~near]
+        assert np.allclose(others, real, atol=1e-9), (dist, g)
+        if expect_root:
+            assert 1 <= near.sum() <= 2 and np.all(np.abs(g[near] - 0.7) < 1e-6), (dist, g)
+        else:
+            assert near.sum() == 0, (dist, g)
