@@ -92,6 +92,21 @@ WORKLOADS = {
     # is for camera images)
     "pose-720p": dict(width=1280, height=720, pairs=64, seed=2000, threads=8, threshold=20.0,
                       pose=True),
+    # the C5 stream: 8 seeded moving-camera sequences of 33 frames (0.05 m per
+    # frame), 4 at 3840x2160 and 4 at 1920x1080: 256 consecutive pairs, solved
+    # in 32 waves of one pair per sequence.  Wave 0 starts from the network;
+    # every later wave starts from the previous wave's solved depth carried
+    # into the new frame (rf_ws_propagate); a pair whose energy fails the
+    # fallback test is solved again with the full plain schedule.
+    "c5-stream": dict(
+        levels=6, plain_warps=5, plain_iters=100, frames=33, fallback_margin=0.02,
+        checkpoint="reconflow_gb300/weights/warmstart_f125.bin",
+        groups=[dict(width=3840, height=2160, sequences=4, seed=7000, warm_level=3,
+                     warm_warps=[1, 1, 1, 1], warm_iters=[4, 30, 60, 80],
+                     temporal_warps=[1, 1, 1, 1], temporal_iters=[4, 30, 60, 80]),
+                dict(width=1920, height=1080, sequences=4, seed=7500, warm_level=2,
+                     warm_warps=[1, 1, 1], warm_iters=[4, 60, 80],
+                     temporal_warps=[1, 1, 1], temporal_iters=[4, 60, 80])]),
     # the warm-start network alone: one forward pass over the 1/8-grid inputs
     # of 64 720p pairs (64 x 90 x 160 x 16), the committed checkpoint
     "warmstart-net-720p": dict(pairs=64, height=90, width=160,
@@ -632,11 +647,12 @@ def run_learned(args, wl, world, rank, local):
     def step():
         ls.solve(Ks, Rs, ts)
         e = b.energies()
-        bad = [i for i in range(n) if not (e[i] <= (1.0 + margin) * e_plain[i])]
+        bad = [i for i in range(n) if over_margin(e[i], e_plain[i], margin)]
         for i in bad:  # fall back to the plain solve, one pair at a time
             f.setCameraMatrices(Ks[i], Ks[i])
             f.copyImagesToDeviceFromDevice(*b.imagePlanes(i, 0), b.strides[i])
             f.solveR(Rs[i], ts[i], 5.0)
+            b.importResults(i, f.deviceResults(), f.stride)  # the accepted solution
         fallbacks.append(len(bad))
 
     with torch.cuda.stream(stream):
@@ -1190,12 +1206,13 @@ def run_learned_mixed(args, wl, world, rank, local):
         for G in groups:
             G["ls"].solve(G["Ks"], G["Rs"], G["ts"])
             e = G["b"].energies()
-            bad = [i for i in range(G["n"]) if not (e[i] <= (1.0 + margin) * G["e_plain"][i])]
+            bad = [i for i in range(G["n"]) if over_margin(e[i], G["e_plain"][i], margin)]
             for i in bad:
                 f = G["f"]
                 f.setCameraMatrices(G["Ks"][i], G["Ks"][i])
                 f.copyImagesToDeviceFromDevice(*G["b"].imagePlanes(i, 0), G["b"].strides[i])
                 f.solveR(G["Rs"][i], G["ts"][i], 5.0)
+                G["b"].importResults(i, f.deviceResults(), f.stride)
             nbad += len(bad)
         fallbacks.append(nbad)
 
@@ -1302,6 +1319,332 @@ def run_learned_mixed(args, wl, world, rank, local):
         G["f"].close()
 
 
+def over_margin(e, ref, margin):
+    """The fallback test: a solution whose energy is not finite always falls
+    back; one whose reference energy is not finite never has to."""
+    if not np.isfinite(e):
+        return True
+    return bool(np.isfinite(ref) and e > (1.0 + margin) * ref)
+
+
+C5_METRIC = ("frame pairs/s, C5 stream: 256 pairs of 3840x2160 / 1920x1080 from 32-frame "
+             "sequences, batched + learned / temporal warm start")
+
+
+def run_c5_stream(args, wl, world, rank, local):
+    """The C5 stream.  One step = the whole stream: 32 waves; in each wave
+    every sequence's next pair is solved, the pairs of a size together in
+    one batch.  Wave 0 warm-starts from the network; wave k > 0 from wave
+    k-1's solved depth of the same sequence carried into frame k
+    (rf_ws_propagate -> rf_ws_state), refined from the same pyramid level.
+    After each wave the pairs' energies are compared with the fallback
+    reference; a pair over the margin is solved again with the full plain
+    schedule (single-pair drop-in solver, from the batch's frames).  The
+    accuracy pass (untimed) also solves every pair with the plain batched
+    solver for its energy and endpoint error."""
+    import torch
+
+    import reconflow_gb300 as R
+    from reconflow_gb300.scene import make_sequence
+    from reconflow_gb300.warmstart import (LearnedBatchSolver, WarmStartNet, level_intrinsics,
+                                           net_factor, propagate, state)
+
+    torch.cuda.set_device(local)
+    lib = R.load()
+    stream = torch.cuda.Stream()
+    flush = torch.empty(L2_FLUSH_BYTES // 4, dtype=torch.float32, device="cuda")
+    nf = wl["frames"]
+    nw = nf - 1  # waves (pairs per sequence)
+    mode = args.fallback or "plain"
+    warm_mode = args.warm or "temporal"
+    groups = []
+    t0 = time.perf_counter()
+    for g in wl["groups"]:
+        W, H, n = g["width"], g["height"], g["sequences"]
+        s = (W + 31) // 32 * 32
+        seqs = [make_sequence(W, H, nf, seed=g["seed"] + 1000 * rank + j, device="cuda")
+                for j in range(n)]
+        frames = [[torch.nn.functional.pad(torch.as_tensor(f_, device="cuda"), (0, s - W))
+                   .contiguous() for f_ in q["frames"]] for q in seqs]
+        groups.append(dict(g=g, W=W, H=H, n=n, s=s, seqs=seqs, frames=frames,
+                           Ks=[q["K"] for q in seqs]))
+    gen_s = time.perf_counter() - t0
+
+    def new_batch(G, warps, iters):
+        b = R.ReconFlowBatch([(G["W"], G["H"])] * G["n"], wl["levels"], method=SOLVER["method"],
+                             lambda_=SOLVER["lam"], lambdaf=SOLVER["lambdaf"],
+                             lambdams=SOLVER["lambdams"], alphaTv=1.0 / SOLVER["theta"],
+                             alphaProj=SOLVER["alpha_proj"], tau=SOLVER["tau"],
+                             nWarpIters=warps, nSolverIters=iters,
+                             fix_quirks=SOLVER["fix_quirks"])
+        b.setStream(stream.cuda_stream)
+        for i, K in enumerate(G["Ks"]):
+            b.setCameraMatrices(i, K, K)
+        return b
+
+    def load_wave(G, b, k):
+        for i in range(G["n"]):
+            b.copyImagesToDeviceFromDevice(i, G["frames"][i][k].data_ptr(),
+                                           G["frames"][i][k + 1].data_ptr(), G["s"])
+
+    def pose(G, k):
+        return ([q["pairs"][k]["R"] for q in G["seqs"]], [q["pairs"][k]["t"] for q in G["seqs"]])
+
+    def epe(G, b, i, k):
+        u, v = b.copyOpticalFlowToHost(i)
+        pr = G["seqs"][i]["pairs"][k]
+        W = G["W"]
+        e = np.sqrt((u[:, :W] - pr["flow"][..., 0]) ** 2 + (v[:, :W] - pr["flow"][..., 1]) ** 2)
+        e = e[pr["valid"]]
+        e = np.where(np.isfinite(e), e, np.float32(1e4))
+        return float(e.mean()), float(np.median(e))
+
+    with torch.cuda.stream(stream):
+        for G in groups:
+            g = G["g"]
+            fct = net_factor(G["Ks"][0])
+            G["factor"] = fct
+            G["hn"], G["wn"] = G["H"] // fct, G["W"] // fct
+            net = WarmStartNet(G["n"], G["hn"] + 1, G["wn"] + 1, seed=0)
+            net.load(os.path.join(ROOT, wl["checkpoint"]))
+            b = new_batch(G, wl["plain_warps"], wl["plain_iters"])
+            ls = LearnedBatchSolver(net, b, (G["W"], G["H"]), G["Ks"][0],
+                                    warm_level=g["warm_level"], warps=g["warm_warps"],
+                                    iters=g["warm_iters"])
+            ls.set_stream(stream.cuda_stream)
+            G.update(net=net, b=b, ls=ls, grid=torch.zeros((G["n"], G["hn"], G["wn"], 3),
+                                                           device="cuda"),
+                     scratch=torch.zeros(2 * G["n"] * G["hn"] * G["wn"], dtype=torch.int32,
+                                         device="cuda"))
+            lw, lh, lsd = b.levelDims(0, g["warm_level"])
+            G["level_dims"] = (lw, lh, lsd)
+            G["Kl"] = [level_intrinsics(K, g["warm_level"]) for K in G["Ks"]]
+            G["up"] = float(fct) / float(2 ** g["warm_level"])
+            G["planes"] = [b.warmPlanes(i) for i in range(G["n"])]
+            f = R.ReconFlow()
+            f.initializeR(G["W"], G["H"], 1, wl["levels"], 2.0, SOLVER["method"], SOLVER["lam"],
+                          0.0, SOLVER["lambdaf"], SOLVER["lambdams"], 1.0 / SOLVER["theta"],
+                          SOLVER["alpha_proj"], 0.5, SOLVER["tau"], wl["plain_warps"],
+                          wl["plain_iters"], cvType=5, fix_quirks=SOLVER["fix_quirks"])
+            f.setStream(stream.cuda_stream)
+            G["f"] = f
+
+    def solve_wave(G, k):
+        """Warm-started solve of wave k for group G (no fallback)."""
+        b, g = G["b"], G["g"]
+        Rs, ts = pose(G, k)
+        if k == 0 or warm_mode == "network":
+            load_wave(G, b, k)
+            G["ls"].solve(G["Ks"], Rs, ts)
+            return
+        Rp, tp = pose(G, k - 1)
+        zs = [b.deviceResults(i)[4] for i in range(G["n"])]
+        propagate(zs, G["W"], G["H"], G["s"], G["Ks"], Rp, tp, G["factor"], G["grid"],
+                  stream=stream.cuda_stream, scratch=G["scratch"])
+        load_wave(G, b, k)
+        lw, lh, lsd = G["level_dims"]
+        state(G["grid"], lw, lh, lsd, G["up"], G["Kl"], Rs, ts, G["planes"], stream.cuda_stream)
+        b.solveWarm(g["warm_level"], Rs, ts, g["temporal_warps"], g["temporal_iters"])
+
+    margin = wl["fallback_margin"]
+    refs = {}  # (group, pair, wave) -> reference energy for the fallback test
+    fallbacks = []
+    record = []
+
+    def stream_once(collect=False):
+        nbad = 0
+        for k in range(nw):
+            for G in groups:
+                solve_wave(G, k)
+            for gi, G in enumerate(groups):
+                e = G["b"].energies()
+                bad = [i for i in range(G["n"])
+                       if mode != "none" and over_margin(e[i], refs[(gi, i, k)], margin)]
+                if collect:
+                    for i in range(G["n"]):
+                        record.append(dict(group=gi, seq=i, wave=k, e_learned=float(e[i]),
+                                           epe_learned=epe(G, G["b"], i, k)))
+                for i in bad:
+                    # the full plain solve of the pair, in place of the learned result
+                    f = G["f"]
+                    Rs, ts = pose(G, k)
+                    f.setCameraMatrices(G["Ks"][i], G["Ks"][i])
+                    f.copyImagesToDeviceFromDevice(G["frames"][i][k].data_ptr(),
+                                                   G["frames"][i][k + 1].data_ptr(), G["s"])
+                    f.solveR(Rs[i], ts[i], 5.0)
+                    G["b"].importResults(i, f.deviceResults(), f.stride)
+                nbad += len(bad)
+        fallbacks.append(nbad)
+
+    # the plain solve of every pair (untimed): its energy is the fallback
+    # reference ("plain") and its endpoint error the accuracy reference
+    plain_rec = {}
+    with torch.cuda.stream(stream):
+        for gi, G in enumerate(groups):
+            pb = new_batch(G, wl["plain_warps"], wl["plain_iters"])
+            for k in range(nw):
+                load_wave(G, pb, k)
+                Rs, ts = pose(G, k)
+                pb.solveR(Rs, ts)
+                e = pb.energies()
+                for i in range(G["n"]):
+                    refs[(gi, i, k)] = float(e[i])
+                    plain_rec[(gi, i, k)] = (float(e[i]), epe(G, pb, i, k))
+            pb.close()
+        torch.cuda.synchronize()
+        plain_gen_s = time.perf_counter() - t0 - gen_s
+        stream_once(collect=True)
+        for _ in range(max(0, args.warmup - 1)):
+            stream_once()
+        torch.cuda.synchronize()
+        barrier(world)
+        fallbacks.clear()
+        evs = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
+               for _ in range(args.steps)]
+        with ClockSampler(local) as clk:
+            torch.cuda.synchronize()
+            for a, e_ in evs:
+                flush.zero_()
+                a.record(stream)
+                stream_once()
+                e_.record(stream)
+            torch.cuda.synchronize()
+        step_ms = [a.elapsed_time(e_) for a, e_ in evs]
+    timed_fallbacks = list(fallbacks)
+    npairs = nw * sum(G["n"] for G in groups)
+    total_s = max_over_ranks(sum(step_ms) / 1000.0, world)
+    value = world * npairs * args.steps / total_s
+
+    e2e = None
+    if not args.no_e2e:
+        # every wave's frames from pinned host memory and every pair's
+        # results back to it, inside the timed wall time
+        host_frames = {}
+        outs = {}
+        for gi, G in enumerate(groups):
+            nb = G["H"] * G["s"] * 4
+            for i in range(G["n"]):
+                for k in range(nf):
+                    p_ = ctypes.c_void_p()
+                    R._native.check(lib.rf_host_alloc(nb, ctypes.byref(p_)))
+                    a_ = np.ctypeslib.as_array(ctypes.cast(p_, ctypes.POINTER(ctypes.c_float)),
+                                               shape=(G["H"], G["s"]))
+                    a_[:] = 0.0
+                    a_[:, :G["W"]] = G["seqs"][i]["frames"][k]
+                    host_frames[(gi, i, k)] = p_
+                ptrs = []
+                for _ in range(6):
+                    p_ = ctypes.c_void_p()
+                    R._native.check(lib.rf_host_alloc(nb, ctypes.byref(p_)))
+                    ptrs.append(p_)
+                outs[(gi, i)] = ptrs
+
+        def e2e_stream():
+            for k in range(nw):
+                for gi, G in enumerate(groups):
+                    n = G["n"]
+                    G["b"].uploadAll([host_frames[(gi, i, k)].value for i in range(n)],
+                                     [host_frames[(gi, i, k + 1)].value for i in range(n)],
+                                     G["s"])
+                    b, g = G["b"], G["g"]
+                    Rs, ts = pose(G, k)
+                    if k == 0 or warm_mode == "network":
+                        G["ls"].solve(G["Ks"], Rs, ts)
+                    else:
+                        lw, lh, lsd = G["level_dims"]
+                        state(G["grid"], lw, lh, lsd, G["up"], G["Kl"], Rs, ts, G["planes"],
+                              stream.cuda_stream)
+                        b.solveWarm(g["warm_level"], Rs, ts, g["temporal_warps"],
+                                    g["temporal_iters"])
+                    e = b.energies()
+                    for i in range(n):
+                        if mode != "none" and over_margin(e[i], refs[(gi, i, k)], margin):
+                            f = G["f"]
+                            f.setCameraMatrices(G["Ks"][i], G["Ks"][i])
+                            f.copyImagesToDeviceFromDevice(*b.imagePlanes(i, 0), G["s"])
+                            f.solveR(Rs[i], ts[i], 5.0)
+                            b.importResults(i, f.deviceResults(), f.stride)
+                    if k + 1 < nw and warm_mode == "temporal":
+                        Rp, tp = Rs, ts
+                        zs = [b.deviceResults(i)[4] for i in range(n)]
+                        propagate(zs, G["W"], G["H"], G["s"], G["Ks"], Rp, tp, G["factor"],
+                                  G["grid"], stream=stream.cuda_stream, scratch=G["scratch"])
+                    o = [outs[(gi, i)] for i in range(n)]
+                    b.downloadAll(G["s"], *[[o[i][c].value for i in range(n)] for c in range(6)])
+
+        with torch.cuda.stream(stream):
+            e2e_stream()
+            torch.cuda.synchronize()
+            times = []
+            for _ in range(args.steps):
+                flush.zero_()
+                torch.cuda.synchronize()
+                t1 = time.perf_counter()
+                e2e_stream()
+                torch.cuda.synchronize()
+                times.append(time.perf_counter() - t1)
+        px = nw * sum(G["n"] * G["W"] * G["H"] for G in groups)
+        e2e = {"value": world * npairs * args.steps / max_over_ranks(sum(times), world),
+               "unit": "pairs/s", "h2d_bytes_per_step": 2 * px * 4,
+               "d2h_bytes_per_step": 6 * px * 4,
+               "mode": "blocking: each wave's frames uploaded from pinned host memory and its "
+                       "results (flow, inverse depth, points) downloaded to it, every wave"}
+        for p_ in list(host_frames.values()) + [q for v in outs.values() for q in v]:
+            lib.rf_host_free(p_)
+
+    if rank == 0:
+        per = {}
+        for gi, G in enumerate(groups):
+            rec = [r for r in record if r["group"] == gi]
+            plain = [plain_rec[(gi, r["seq"], r["wave"])] for r in rec]
+            lm = [r["epe_learned"][0] for r in rec]
+            lmed = [r["epe_learned"][1] for r in rec]
+            pm = [p_[1][0] for p_ in plain]
+            pmed = [p_[1][1] for p_ in plain]
+            ratio = [r["e_learned"] / p_[0] for r, p_ in zip(rec, plain)]
+            per[f"{G['W']}x{G['H']}"] = {
+                "sequences": G["n"], "pairs": G["n"] * nw, "warm_level": G["g"]["warm_level"],
+                "network_iters_per_level": G["g"]["warm_iters"],
+                "temporal_iters_per_level": G["g"]["temporal_iters"],
+                "learned_epe_mean_px": float(np.mean(lm)),
+                "learned_epe_median_px": float(np.mean(lmed)),
+                "plain_epe_mean_px": float(np.mean(pm)),
+                "plain_epe_median_px": float(np.mean(pmed)),
+                "energy_ratio_median": float(np.median(ratio)),
+                "energy_ratio_max": float(np.max(ratio)),
+                "over_margin": int(sum(x > 1.0 + margin for x in ratio))}
+        if args.dump:
+            np.savez(args.dump, group=[r["group"] for r in record],
+                     seq=[r["seq"] for r in record], wave=[r["wave"] for r in record],
+                     e_learned=[r["e_learned"] for r in record],
+                     epe_learned=[r["epe_learned"] for r in record],
+                     e_plain=[plain_rec[(r["group"], r["seq"], r["wave"])][0] for r in record],
+                     epe_plain=[plain_rec[(r["group"], r["seq"], r["wave"])][1] for r in record])
+        print(json.dumps({
+            "metric": C5_METRIC, "value": value, "unit": "pairs/s", "n_gpus": world,
+            "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": 1000.0 * total_s / args.steps, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+            "data": "synthetic (seeded moving-camera sequences of the scene generator)",
+            "config": {"workload": args.workload, "frames_per_sequence": nf,
+                       "pairs_per_step": npairs, "groups": per, "pyramid_levels": wl["levels"],
+                       "plain_schedule": [wl["plain_warps"], wl["plain_iters"]],
+                       "warm_start": "network at wave 0, then the previous wave's depth "
+                                     "carried into the new frame (rf_ws_propagate)"
+                                     if warm_mode == "temporal" else "network for every pair",
+                       "fallback": f"{mode}: plain re-solve when energy > (1 + {margin}) x "
+                                   f"reference energy",
+                       "checkpoint": wl["checkpoint"], "l2": "flushed between steps",
+                       "parallelism": "replicas"},
+            "fallbacks_per_step": timed_fallbacks, "e2e": e2e, "clocks": clk.summary(),
+            "scene_gen_s": gen_s, "plain_reference_s": plain_gen_s,
+        }), flush=True)
+    for G in groups:
+        G["b"].close()
+        G["net"].close()
+        G["f"].close()
+
+
 def roofline_of(ms, px, batched=False):
     """Roofline entry of the dominant level-0 kernel from per-launch times
     (`px` pixels per launch; `batched`: the batched solver's kernels)."""
@@ -1328,7 +1671,34 @@ def roofline_of(ms, px, batched=False):
             "frac_each": {names[k]: ALG_BYTES[names[k]] * px / (ms[k] * 1e-3) / 1e9 / peak
                           for k in range(2)},
             "iteration": iteration_roofline(ms, px, peak),
+            "issue": issue_roofline(ms, px, tr.get("warp_instructions_per_32px")
+                                    if os.path.exists(tpath) else None),
             "timing": "launches of one kernel back to back in a CUDA graph, CUDA events"}
+
+
+def issue_roofline(ms, px, inst):
+    """The data step against the SMs' instruction-issue rate (it is bound by
+    issue, not by DRAM): warp instructions per 32 pixels from the committed
+    ncu capture x pixels / launch time, against 152 SMs x 4 schedulers x
+    one warp instruction per cycle at the maximum SM clock."""
+    if not inst:
+        return None
+    peak = 152 * 4 * measured_sm_mhz() * 1e6
+    out = {}
+    for k, name in enumerate(("recon_a", "recon_b")):
+        if name in inst:
+            rate = inst[name] * px / 32.0 / (ms[k] * 1e-3)
+            out[name] = {"warp_inst_per_32px": inst[name], "achieved_ginst_s": rate / 1e9,
+                         "peak_ginst_s": peak / 1e9, "frac": rate / peak}
+    return out
+
+
+def measured_sm_mhz():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as fh:
+            return float(json.load(fh).get("sm_max_mhz", 2070.0))
+    except (OSError, ValueError):
+        return 2070.0
 
 
 def iteration_roofline(ms, px, peak):
@@ -1364,6 +1734,12 @@ def main():
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--solve-only", action="store_true",
                     help="only warm-up + timed solves (for profiler launch lists)")
+    ap.add_argument("--fallback", default=None, choices=["plain", "none"],
+                    help="c5-stream: the fallback test's reference energy (default plain)")
+    ap.add_argument("--warm", default=None, choices=["temporal", "network"],
+                    help="c5-stream: warm start of waves after the first (default temporal)")
+    ap.add_argument("--dump", default=None,
+                    help="c5-stream: write per-pair energies and endpoint errors to this .npz")
     ap.add_argument("--pairs", type=int, default=0,
                     help="pairs per step of the 720p learned or pose workload (profiling; "
                          "default: the workload's)")
@@ -1379,7 +1755,7 @@ def main():
         if "pose" in wl:
             run_reference_pose(args, wl, world, rank)
             return
-        if "groups" in wl or ("pairs" in wl and "checkpoint" not in wl):
+        if "groups" in wl or "frames" in wl or ("pairs" in wl and "checkpoint" not in wl):
             if rank == 0:
                 print(json.dumps({"impl": "reference", "unavailable": "the reference solves "
                                   "one pair at a time and has no batched path; its per-pair "
@@ -1398,6 +1774,9 @@ def main():
         return
     if "net" in wl:
         run_net(args, wl, world, rank, local)
+        return
+    if "frames" in wl:
+        run_c5_stream(args, wl, world, rank, local)
         return
     if "groups" in wl:
         run_learned_mixed(args, wl, world, rank, local)

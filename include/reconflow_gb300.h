@@ -348,6 +348,14 @@ RF_API rf_status rf_batch_stage_download(rf_batch* b, float* const* u, float* co
 RF_API rf_status rf_batch_wait_download(rf_batch* b);
 RF_API rf_status rf_batch_device_results(rf_batch* b, int pair, const float** u, const float** v,
                                          const float** X, const float** Y, const float** Z);
+/* Replace one pair's solution (u, v and, for ReconFlow methods, X, Y, Z)
+ * with device planes of `pitch` floats per row, on the batch's stream: a
+ * pair solved again outside the batch (the learned path's plain fallback)
+ * then is what downloads, energies and later warm starts read.  No
+ * reference counterpart. */
+RF_API rf_status rf_batch_import_results(rf_batch* b, int pair, const float* u, const float* v,
+                                         const float* X, const float* Y, const float* Z,
+                                         int pitch);
 RF_API rf_status rf_batch_set_stream(rf_batch* b, void* stream);
 RF_API rf_status rf_batch_synchronize(rf_batch* b);
 RF_API uint64_t rf_batch_kernel_launches(const rf_batch* b);
@@ -410,6 +418,23 @@ RF_API rf_status rf_cnn_set_test_wait_limit(rf_cnn* c, int polls);
 RF_API rf_status rf_ws_features(int n, const float* const* I0, const float* const* I1, int w0,
                                 int h0, int s0, int factor, const double* K, const double* R,
                                 const double* t, float* out, void* stream);
+/* Temporal warm start for frame sequences (no reference counterpart): for n
+ * pairs, frame k's inverse depth on the wn x hn grid of `factor` x `factor`
+ * level-0 cells (factor 1 .. 32) from frame k-1's solved depth Z (host array
+ * of n device planes, w x h pixels, s floats per row; non-finite or <= 0 =
+ * unknown): each pixel lifted to 3D with K (n x 9 host doubles, level 0),
+ * moved by R, t (n x 9, n x 3: camera k-1 -> camera k, the previous pair's
+ * pose) and projected; the points landing at 0.5 .. 50 m give each cell the
+ * mean of their inverse depths (fixed-point sums: reproducible bit for bit),
+ * cells nothing reaches take the median of the filled cells (0 if none).
+ * Written to channel `channel` of the pair-major NHWC map `grid` (device,
+ * n x hn x wn x channels floats), which rf_ws_state reads as it reads the
+ * network's output (channel 2).  `scratch`: device, 2 x n x wn x hn unsigned
+ * ints (cleared here). */
+RF_API rf_status rf_ws_propagate(int n, const float* const* Z, int w, int h, int s,
+                                 const double* K, const double* R, const double* t, int factor,
+                                 int wn, int hn, int channels, int channel, float* grid,
+                                 unsigned int* scratch, void* stream);
 /* Warm-start state from the network's inverse depth (channel 2 of an NHWC
  * map of `channels` channels on a wn x hn grid per pair, device): for each
  * pixel of a w x h pyramid level (s floats per row) the inverse depth
@@ -442,6 +467,14 @@ RF_API rf_status rfk_warp(const float* src, int w, int h, int s, const float* u,
 /* ComputeDerivativesKernel (computeDerivatives.cu:8-57). */
 RF_API rf_status rfk_derivatives(const float* I0, const float* I1w, int w, int h, int s,
                                  float* Ix, float* Iy, float* Iz, void* stream);
+/* WarpingKernel then ComputeDerivativesKernel (warpImage.cu:15-29,
+ * computeDerivatives.cu:8-57) in one launch, as the solver runs them: the
+ * warped I1 is formed in shared memory with a 2-pixel halo and never
+ * written; Ix, Iy, Iz equal rfk_warp followed by rfk_derivatives bit for
+ * bit. */
+RF_API rf_status rfk_warp_derivatives(const float* I0, const float* I1, const float* u,
+                                      const float* v, int w, int h, int s, float* Ix, float* Iy,
+                                      float* Iz, void* stream);
 /* MedianFilterKernel5 (medianFilter.cu:3-75). */
 RF_API rf_status rfk_median5(const float* u, const float* v, int w, int h, int s, float* ou,
                              float* ov, void* stream);
@@ -474,6 +507,12 @@ RF_API rf_status rfk_warp_update(const float* duhat, const float* dvhat, const f
 RF_API rf_status rfk_warp_update_noalloc(const float* duhat, const float* dvhat, const float* u,
                                          const float* v, int w, int h, int s, float* out_u,
                                          float* out_v, void* stream);
+/* Fault injection for tests (no reference counterpart): from this call on,
+ * the k-th device or pinned-host allocation the library makes fails as if
+ * the device were out of memory (k = 0: none).  RF_FAIL_ALLOC=k in the
+ * environment sets the same before the first allocation.  Every create
+ * call then returns RF_ERR_OOM and releases what it had allocated. */
+RF_API void rf_test_fail_alloc(long long k);
 /* rgbaToGrayKernel (rgbToGray.cu:3-19). */
 RF_API rf_status rfk_rgb_to_gray(const uint8_t* rgb, int w, int h, int s, float* out,
                                  void* stream);

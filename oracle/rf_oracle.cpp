@@ -979,6 +979,8 @@ int solve(const rfo_params& p, const void* i0, const void* i1, int in_stride,
 // + alpha_proj / 2 * min(|(u, v) - uc(X)|^2, 1)       (reprojection of the
 //                                                      solved 3D point, truncated
 //                                                      at 1 px^2; recon only)
+// A pixel whose sum is not finite (non-finite flow) counts every term at its
+// cap: lambda + 2 + alpha_proj / 2.
 double energy(const float* I0, const float* I1, const float* u, const float* v, const float* X,
               const float* Y, const float* Z, int w, int h, int s, float lambda,
               float alpha_proj, const double* R1, const double* t1, const double* K1,
@@ -1009,7 +1011,11 @@ double energy(const float* I0, const float* I1, const float* u, const float* v, 
                 if (!(r2 < 1.0)) r2 = 1.0;  // truncated at 1 px^2 (NaN included)
                 proj = 0.5 * (double)alpha_proj * r2;
             }
-            e += data + tv + proj;
+            double px_e = data + tv + proj;
+            // a non-finite pixel term counts each term at its cap
+            if (!std::isfinite(px_e))
+                px_e = (double)lambda + 2.0 + (recon ? 0.5 * (double)alpha_proj : 0.0);
+            e += px_e;
         }
     return e;
 }

@@ -115,6 +115,7 @@ _SIGS = [
     ("rf_batch_stage_download", _I, [_VP, _VP, _VP, _VP, _VP, _VP, _VP, _I]),
     ("rf_batch_wait_download", _I, [_VP]),
     ("rf_batch_device_results", _I, [_VP, _I, _VP, _VP, _VP, _VP, _VP]),
+    ("rf_batch_import_results", _I, [_VP, _I, _VP, _VP, _VP, _VP, _VP, _I]),
     ("rf_batch_set_stream", _I, [_VP, _VP]),
     ("rf_batch_synchronize", _I, [_VP]),
     ("rf_batch_kernel_launches", ctypes.c_uint64, [_VP]),
@@ -135,10 +136,14 @@ _SIGS = [
     ("rf_ws_features", _I, [_I, _VP, _VP, _I, _I, _I, _I, _D, _D, _D, _VP, _VP]),
     ("rf_ws_state", _I, [_I, _VP, _I, _I, _I, _I, _I, _I, _F, _D, _D, _D, _VP, _VP, _VP, _VP,
                          _VP, _VP]),
+    ("rf_test_fail_alloc", None, [ctypes.c_longlong]),
+    ("rf_ws_propagate", _I, [_I, _VP, _I, _I, _I, _D, _D, _D, _I, _I, _I, _I, _I, _VP, _VP,
+                             _VP]),
     ("rfk_downscale", _I, [_VP, _I, _I, _I, _I, _I, _I, _F, _I, _VP, _VP]),
     ("rfk_upscale", _I, [_VP, _I, _I, _I, _I, _I, _I, _F, _VP, _VP]),
     ("rfk_warp", _I, [_VP, _I, _I, _I, _VP, _VP, _VP, _VP]),
     ("rfk_derivatives", _I, [_VP, _VP, _I, _I, _I, _VP, _VP, _VP, _VP]),
+    ("rfk_warp_derivatives", _I, [_VP, _VP, _VP, _VP, _I, _I, _I, _VP, _VP, _VP, _VP]),
     ("rfk_median5", _I, [_VP, _VP, _I, _I, _I, _VP, _VP, _VP]),
     ("rfk_median3d", _I, [_VP, _VP, _VP, _I, _I, _I, _VP, _VP, _VP, _VP]),
     ("rfk_warp_update", _I, [_VP, _VP, _VP, _VP, _I, _I, _I, _VP, _VP, _VP, _VP, _VP]),

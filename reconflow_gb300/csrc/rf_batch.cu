@@ -27,6 +27,8 @@
 #include <cuda_runtime.h>
 
 #include "../../include/reconflow_gb300.h"
+#include "rf_alloc.h"
+#include "rf_nvtx.h"
 #include "rf_kernels.cuh"
 #include "rf_ops.cuh"
 
@@ -107,6 +109,20 @@ __global__ void __launch_bounds__(kMaxTile) k_batch(BatchCtx ctx, int level, Op 
     const int ix = t.x0 + (int)threadIdx.x, iy = t.y0 + (int)threadIdx.y;
     if (ix >= d.w || iy >= d.h) return;
     op(ctx, t, level, d, ix, iy);
+}
+
+// WarpImage + ComputeDerivatives fused (warp_deriv_tile): one block = one
+// tile of one pair; the warped image stays in shared memory (dynamic,
+// 2 (tile_w + 4)(tile_h + 4) floats)
+__global__ void __launch_bounds__(kMaxTile) k_batch_warp_deriv(BatchCtx ctx, int level, int I0,
+                                                               int I1, int u, int v, int Ix,
+                                                               int Iy, int Iz) {
+    extern __shared__ float sm[];
+    const TileEntry t = ctx.tiles[blockIdx.x];
+    const LevelDims d = ctx.pairs[t.pair].dims[level];
+    warp_deriv_tile(plane_ptr(ctx, t, I0), plane_ptr(ctx, t, I1), plane_ptr(ctx, t, u),
+                    plane_ptr(ctx, t, v), d, t.x0, t.y0, (int)blockDim.x, (int)blockDim.y, sm,
+                    plane_ptr(ctx, t, Ix), plane_ptr(ctx, t, Iy), plane_ptr(ctx, t, Iz));
 }
 
 // Two operations in one launch on disjoint tile ranges of the level's table
@@ -435,7 +451,7 @@ cudaError_t fill_tiles(rf_batch* b) {
         if (b->d_tiles) cudaFree(b->d_tiles);
         b->d_tiles = nullptr;
         b->tiles_cap = 0;
-        cudaError_t e = cudaMalloc(&b->d_tiles, sizeof(TileEntry) * tab.size());
+        cudaError_t e = rf::dev_malloc((void**)&b->d_tiles, sizeof(TileEntry) * tab.size());
         if (e != cudaSuccess) return e;
         b->tiles_cap = tab.size();
     }
@@ -480,6 +496,18 @@ int launch_op(rf_batch* b, int level, const Op& op) {
     if (tiles <= 0) return 0;
     const dim3 block(b->tile_w[level], b->tile_h[level]);
     k_batch<Op><<<tiles, block, 0, b->stream>>>(ctx_of(b, level), level, op);
+    b->enq++;
+    return rf::launch_status();
+}
+
+int launch_warp_deriv(rf_batch* b, int level, int I0, int I1, int u, int v, int Ix, int Iy,
+                      int Iz) {
+    int tiles = b->prefix[level * (b->n + 1) + b->n];
+    if (tiles <= 0) return 0;
+    const int tw = b->tile_w[level], th = b->tile_h[level];
+    const size_t smem = sizeof(float) * 2 * (size_t)(tw + 4) * (th + 4);
+    k_batch_warp_deriv<<<tiles, dim3(tw, th), smem, b->stream>>>(ctx_of(b, level), level, I0, I1,
+                                                                 u, v, Ix, Iy, Iz);
     b->enq++;
     return rf::launch_status();
 }
@@ -573,11 +601,13 @@ rf_status enqueue_batch(rf_batch* b, int kind) {
         ucb = false;  // uc from the warm 3D state in the first iteration
     }
     for (int level = top; level >= 0; level--) {
+        NvtxRange level_range("batch level %d", level);
         const int n_warps = warm ? b->warm_warps[level] : p.n_warp_iters;
         const int n_iters = warm ? b->warm_iters[level] : p.n_solver_iters;
         for (int warp = 0; warp < n_warps; warp++) {
-            BL(launch_op(b, level, OpWarp{b->pI1(level), u, v, P(P_I1W)}));
-            BL(launch_op(b, level, OpDeriv{b->pI0(level), P(P_I1W), P(P_IX), P(P_IY), P(P_IZ)}));
+            NvtxRange warp_range("batch level %d warp %d", level, warp);
+            BL(launch_warp_deriv(b, level, b->pI0(level), b->pI1(level), u, v, P(P_IX),
+                                 P(P_IY), P(P_IZ)));
             const ReconFields r = fields_of(
                 b, ReconIdx{u, v, P(P_DUHAT), P(P_DVHAT), P(P_PU1), P(P_PU2), P(P_PV1), P(P_PV2),
                             uproj, vproj, sku, skv, P(P_IX), P(P_IY), P(P_IZ), P(P_X), P(P_Y),
@@ -659,6 +689,7 @@ rf_status enqueue_batch(rf_batch* b, int kind) {
 }
 
 rf_status run_batch(rf_batch* b, int kind) {
+    NvtxRange range(kind == 2 ? "rf_batch_solve_warm" : "rf_batch_solve");
     std::vector<int> sched;
     if (kind == 2) {
         sched.push_back(b->warm_level);
@@ -756,7 +787,7 @@ rf_status rf_batch_create(const rf_params* p, int n_pairs, const int* widths, co
         return bfail(RF_ERR_NO_DEVICE, "rf_batch_create: no CUDA device");
     }
     const size_t pool_floats = total * (size_t)b->n_planes;
-    cudaError_t e = cudaMalloc(&b->pool, pool_floats * sizeof(float));
+    cudaError_t e = rf::dev_malloc((void**)&b->pool, pool_floats * sizeof(float));
     if (e == cudaSuccess) e = cudaMemset(b->pool, 0, pool_floats * sizeof(float));
     std::vector<BatchPair> hp(n_pairs);
     for (int i = 0; i < n_pairs; i++)
@@ -779,11 +810,11 @@ rf_status rf_batch_create(const rf_params* p, int n_pairs, const int* widths, co
         b->prefetch = waves > 0.0 ? (int)(waves * sms * 16) : 0;
     }
     if (e == cudaSuccess) e = fill_tiles(b);
-    if (e == cudaSuccess) e = cudaMalloc(&b->d_pairs, sizeof(BatchPair) * n_pairs);
+    if (e == cudaSuccess) e = rf::dev_malloc((void**)&b->d_pairs, sizeof(BatchPair) * n_pairs);
     if (e == cudaSuccess)
         e = cudaMemcpy(b->d_pairs, hp.data(), sizeof(BatchPair) * n_pairs, cudaMemcpyHostToDevice);
-    if (e == cudaSuccess) e = cudaMalloc(&b->d_consts, sizeof(LevelConsts) * n_pairs * b->L);
-    if (e == cudaSuccess) e = cudaMallocHost(&b->h_consts, sizeof(LevelConsts) * n_pairs * b->L);
+    if (e == cudaSuccess) e = rf::dev_malloc((void**)&b->d_consts, sizeof(LevelConsts) * n_pairs * b->L);
+    if (e == cudaSuccess) e = rf::host_malloc((void**)&b->h_consts, sizeof(LevelConsts) * n_pairs * b->L);
     if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&b->own, cudaStreamNonBlocking);
     if (e != cudaSuccess) {
         rf_batch_destroy(b);
@@ -907,9 +938,9 @@ rf_status rf_batch_energies(rf_batch* b, double* out) {
     if (!b || !out) return bfail(RF_ERR_INVALID_ARG, "rf_batch_energies: null argument");
     if (!b->solved || b->p.method == RF_METHOD_TVL1 || b->last_R1.size() != (size_t)9 * b->n)
         return bfail(RF_ERR_STATE, "rf_batch_energies: needs a ReconFlow solve");
-    if (!b->d_energy) BC(cudaMalloc(&b->d_energy, sizeof(double) * b->n * (kEnergyMaxBlocks + 1)));
-    if (!b->d_ejobs) BC(cudaMalloc(&b->d_ejobs, sizeof(EnergyJob) * b->n));
-    if (!b->h_ejobs) BC(cudaMallocHost(&b->h_ejobs, sizeof(EnergyJob) * b->n));
+    if (!b->d_energy) BC(rf::dev_malloc((void**)&b->d_energy, sizeof(double) * b->n * (kEnergyMaxBlocks + 1)));
+    if (!b->d_ejobs) BC(rf::dev_malloc((void**)&b->d_ejobs, sizeof(EnergyJob) * b->n));
+    if (!b->h_ejobs) BC(rf::host_malloc((void**)&b->h_ejobs, sizeof(EnergyJob) * b->n));
     BC(cudaStreamSynchronize(b->stream));  // the staging buffer is free to refill
     const int B0 = b->base_idx();
     double* sums = b->d_energy + (size_t)b->n * kEnergyMaxBlocks;
@@ -1159,7 +1190,7 @@ static rf_status ensure_staging(rf_batch* b, bool out) {
     for (cudaEvent_t* ev : {&b->in_staged, &b->in_free, &b->out_ready, &b->out_done})
         if (!*ev) BC(cudaEventCreateWithFlags(ev, cudaEventDisableTiming));
     float** buf = out ? &b->stage_out : &b->stage_in;
-    if (!*buf) BC(cudaMalloc(buf, b->total * (out ? 6 : 2) * sizeof(float)));
+    if (!*buf) BC(rf::dev_malloc((void**)buf, b->total * (out ? 6 : 2) * sizeof(float)));
     return RF_OK;
 }
 
@@ -1267,6 +1298,28 @@ rf_status rf_batch_device_results(rf_batch* b, int pair, const float** u, const 
     if (X) *X = pair_plane(b, pair, B0 + P_X);
     if (Y) *Y = pair_plane(b, pair, B0 + P_Y);
     if (Z) *Z = pair_plane(b, pair, B0 + P_Z);
+    return RF_OK;
+}
+
+rf_status rf_batch_import_results(rf_batch* b, int pair, const float* u, const float* v,
+                                  const float* X, const float* Y, const float* Z, int pitch) {
+    if (!b || pair < 0 || pair >= b->n || !u || !v)
+        return bfail(RF_ERR_INVALID_ARG, "rf_batch_import_results: bad argument");
+    if (!b->solved) return bfail(RF_ERR_STATE, "rf_batch_import_results: no solve has run");
+    const LevelDims d = b->dims[pair][0];
+    if (pitch < d.w) return bfail(RF_ERR_INVALID_ARG, "rf_batch_import_results: pitch < width");
+    const bool recon = b->p.method != RF_METHOD_TVL1;
+    if (recon && (!X || !Y || !Z))
+        return bfail(RF_ERR_INVALID_ARG, "rf_batch_import_results: 3D planes missing");
+    const int B0 = b->base_idx();
+    const struct {
+        const float* src;
+        int plane;
+    } in[5] = {{u, b->res_u}, {v, b->res_v}, {X, B0 + P_X}, {Y, B0 + P_Y}, {Z, B0 + P_Z}};
+    for (int k = 0; k < (recon ? 5 : 2); k++)
+        BC(cudaMemcpy2DAsync(pair_plane(b, pair, in[k].plane), d.s * sizeof(float), in[k].src,
+                             (size_t)pitch * sizeof(float), d.w * sizeof(float), d.h,
+                             cudaMemcpyDeviceToDevice, b->stream));
     return RF_OK;
 }
 

@@ -34,6 +34,8 @@
 #include <cuda_runtime.h>
 
 #include "../../include/reconflow_gb300.h"
+#include "rf_alloc.h"
+#include "rf_nvtx.h"
 #include "rf_kernels.cuh"
 #include "rf_tc.cuh"
 
@@ -559,7 +561,7 @@ rf_status rf_cnn_create(int max_batch, int height, int width, unsigned long long
     const size_t P2 = (size_t)((height + 1) / 2) * ((width + 1) / 2);
     cudaError_t e = cudaSuccess;
     auto alloc = [&](auto** p, size_t bytes) {
-        if (e == cudaSuccess) e = cudaMalloc((void**)p, bytes);
+        if (e == cudaSuccess) e = rf::dev_malloc((void**)p, bytes);
     };
     alloc(&c->w, off * 4); alloc(&c->g, off * 4); alloc(&c->m, off * 4); alloc(&c->v, off * 4);
     alloc(&c->wb, off * 2);
@@ -647,6 +649,7 @@ static rf_status check_batch(rf_cnn* c, int B, int H, int W) {
 
 rf_status rf_cnn_forward(rf_cnn* c, const float* input, int B, int H, int W, float* out16,
                          float* out8) {
+    rf::NvtxRange range("rf_cnn_forward");
     if (!c || !input) return cfail(RF_ERR_INVALID_ARG, "rf_cnn_forward: null");
     rf_status rs = check_batch(c, B, H, W);
     if (rs == RF_OK) rs = forward(c, input, B, H, W);
@@ -664,6 +667,7 @@ rf_status rf_cnn_forward(rf_cnn* c, const float* input, int B, int H, int W, flo
 rf_status rf_cnn_backward(rf_cnn* c, const float* input, const float* tgt16, const float* mask16,
                           const float* tgt8, const float* mask8, int B, int H, int W,
                           const float* weights, double* loss) {
+    rf::NvtxRange range("rf_cnn_backward");
     if (!c || !input || !tgt16 || !mask16 || !tgt8 || !mask8 || !weights)
         return cfail(RF_ERR_INVALID_ARG, "rf_cnn_backward: null");
     rf_status rs = check_batch(c, B, H, W);
@@ -689,6 +693,7 @@ rf_status rf_cnn_backward(rf_cnn* c, const float* input, const float* tgt16, con
 }
 
 rf_status rf_cnn_adam_step(rf_cnn* c, float lr, float beta1, float beta2, float eps) {
+    rf::NvtxRange range("rf_cnn_adam_step");
     if (!c) return cfail(RF_ERR_INVALID_ARG, "rf_cnn_adam_step: null");
     c->step++;
     float c1 = 1.0f - std::pow(beta1, (float)c->step);

@@ -16,13 +16,58 @@
 //            (solveUcSk.cu:80-97).
 // All pixel-local state (duhat, p, uproj, sk) is updated in place: each is
 // read at a neighbour only by the other kernel of the pair.
+#include <atomic>
 #include <cstdint>
 #include <cstdlib>
 
+#include "../../include/reconflow_gb300.h"
+#include "rf_alloc.h"
 #include "rf_kernels.cuh"
 #include "rf_ops.cuh"
 
+namespace {
+
+// allocation gate (rf_alloc.h): the allocation numbered g_fail_at since the
+// last rf_test_fail_alloc call fails; 0 = none
+std::atomic<long long> g_alloc_count{0};
+std::atomic<long long> g_fail_at{-1};
+
+long long fail_at() {
+    long long v = g_fail_at.load();
+    if (v < 0) {
+        const char* e = std::getenv("RF_FAIL_ALLOC");
+        long long k = e ? std::atoll(e) : 0;
+        long long expect = -1;
+        g_fail_at.compare_exchange_strong(expect, k < 0 ? 0 : k);
+        v = g_fail_at.load();
+    }
+    return v;
+}
+
+bool injected_failure() {
+    const long long k = fail_at();
+    return k > 0 && g_alloc_count.fetch_add(1) + 1 == k;
+}
+
+}  // namespace
+
 namespace rf {
+
+cudaError_t dev_malloc(void** p, size_t bytes) {
+    if (injected_failure()) {
+        *p = nullptr;
+        return cudaErrorMemoryAllocation;
+    }
+    return cudaMalloc(p, bytes);
+}
+
+cudaError_t host_malloc(void** p, size_t bytes) {
+    if (injected_failure()) {
+        *p = nullptr;
+        return cudaErrorMemoryAllocation;
+    }
+    return cudaMallocHost(p, bytes);
+}
 
 namespace {
 
@@ -124,6 +169,18 @@ __global__ void k_derivatives(const float* __restrict__ I0, const float* __restr
     int iy = blockIdx.y * blockDim.y + threadIdx.y;
     if (ix >= d.w || iy >= d.h) return;
     derivatives_px(I0, I1, d, Ix, Iy, Iz, ix, iy);
+}
+
+// the two fused (warp_deriv_tile): one BX x BY tile per block
+__global__ void __launch_bounds__(BX* BY) k_warp_deriv(const float* __restrict__ I0,
+                                                       const float* __restrict__ I1,
+                                                       const float* __restrict__ u,
+                                                       const float* __restrict__ v, LevelDims d,
+                                                       float* __restrict__ Ix,
+                                                       float* __restrict__ Iy,
+                                                       float* __restrict__ Iz) {
+    __shared__ float sm[2 * (BX + 4) * (BY + 4)];
+    warp_deriv_tile(I0, I1, u, v, d, blockIdx.x * BX, blockIdx.y * BY, BX, BY, sm, Ix, Iy, Iz);
 }
 
 // ---------------------------------------------------------------------------
@@ -388,7 +445,12 @@ __device__ __forceinline__ void energy_block(const EnergyArgs& a, LevelDims d, i
             if (!(r2 < 1.0f)) r2 = 1.0f;  // truncated at 1 px^2 (NaN included)
             proj = 0.5f * a.alpha_proj * r2;
         }
-        e += (double)data + (double)tv + (double)proj;
+        float px_e = data + tv + proj;
+        // a pixel whose flow is not finite (a NaN or infinite gradient)
+        // counts each term at its cap: a unit brightness residual, unit
+        // gradients of u and v, the truncated reprojection residual
+        if (!isfinite(px_e)) px_e = a.lambda + 2.0f + (a.recon ? 0.5f * a.alpha_proj : 0.0f);
+        e += (double)px_e;
     }
     for (int o = 16; o > 0; o >>= 1) e += __shfl_down_sync(0xffffffffu, e, o);
     if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = e;
@@ -475,6 +537,12 @@ int launch_downscale(const float* src, LevelDims fine, LevelDims coarse, float s
 int launch_warp(const float* I1, const float* u, const float* v, LevelDims d, float* out,
                 cudaStream_t st) {
     k_warp<<<grid_for(d.w, d.h), dim3(BX, BY), 0, st>>>(I1, u, v, d, out);
+    return check_launch();
+}
+
+int launch_warp_deriv(const float* I0, const float* I1, const float* u, const float* v,
+                      LevelDims d, float* Ix, float* Iy, float* Iz, cudaStream_t st) {
+    k_warp_deriv<<<grid_for(d.w, d.h), dim3(BX, BY), 0, st>>>(I0, I1, u, v, d, Ix, Iy, Iz);
     return check_launch();
 }
 
@@ -648,3 +716,8 @@ int launch_energy_jobs(const EnergyJob* jobs, int n, int total_blocks, cudaStrea
     return check_launch();
 }
 }  // namespace rf
+
+extern "C" void rf_test_fail_alloc(long long k) {
+    g_fail_at.store(k < 0 ? 0 : k);
+    g_alloc_count.store(0);
+}

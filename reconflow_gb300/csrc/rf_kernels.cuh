@@ -77,6 +77,9 @@ int launch_downscale(const float* src, LevelDims fine, LevelDims coarse, float s
                      float* out, cudaStream_t st);
 int launch_warp(const float* I1, const float* u, const float* v, LevelDims d, float* out,
                 cudaStream_t st);
+// WarpImage + ComputeDerivatives in one launch; the warped image stays on chip
+int launch_warp_deriv(const float* I0, const float* I1, const float* u, const float* v,
+                      LevelDims d, float* Ix, float* Iy, float* Iz, cudaStream_t st);
 int launch_derivatives(const float* I0, const float* I1w, LevelDims d, float* Ix, float* Iy,
                        float* Iz, cudaStream_t st);
 // `block` = the level's tile (default 32 x 8; at most 256 threads)

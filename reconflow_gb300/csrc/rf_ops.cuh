@@ -329,6 +329,50 @@ __device__ __forceinline__ void warp_px(const float* __restrict__ I1, const floa
     out[pos] = tex2d(I1, d.w, d.h, d.s, x, y);
 }
 
+// WarpImage and ComputeDerivatives fused through shared memory, for one
+// block-shaped tile (tw x th pixels at x0, y0; the block's threads).  The
+// tile plus a 2-pixel halo of I0 and of the warped I1 are staged in `sm`
+// ((tw + 4) x (th + 4) floats each); a halo cell outside the level holds the
+// value at its mirrored pixel, which is what the derivative taps read
+// (computeDerivatives.cu:26-56), and the warped value of every cell is
+// warp_px's arithmetic at that pixel, so Ix, Iy, Iz are bit-identical to
+// the two-kernel path while the warped image never leaves the chip.  Every
+// thread of the block must call it (it synchronises the block).
+__device__ __forceinline__ void warp_deriv_tile(const float* __restrict__ I0,
+                                                const float* __restrict__ I1,
+                                                const float* __restrict__ u,
+                                                const float* __restrict__ v, LevelDims d, int x0,
+                                                int y0, int tw, int th, float* sm,
+                                                float* __restrict__ Ix, float* __restrict__ Iy,
+                                                float* __restrict__ Iz) {
+    const int sw = tw + 4, cells = sw * (th + 4);
+    float* sI0 = sm;
+    float* sW = sm + cells;
+    const int tid = threadIdx.x + threadIdx.y * blockDim.x;
+    const int nthr = blockDim.x * blockDim.y;
+    for (int c = tid; c < cells; c += nthr) {
+        const int mx = mirror_index(x0 + c % sw - 2, d.w);
+        const int my = mirror_index(y0 + c / sw - 2, d.h);
+        const int p = mx + my * d.s;
+        const float x = ((float)mx + u[p] + 0.5f) / (float)d.w;
+        const float y = ((float)my + v[p] + 0.5f) / (float)d.h;
+        sI0[c] = I0[p];
+        sW[c] = tex2d(I1, d.w, d.h, d.s, x, y);
+    }
+    __syncthreads();
+    const int ix = x0 + (int)threadIdx.x, iy = y0 + (int)threadIdx.y;
+    if (ix >= d.w || iy >= d.h) return;
+    const int c = (threadIdx.x + 2) + (threadIdx.y + 2) * sw;
+    const int pos = ix + iy * d.s;
+    float t0 = deriv5(sI0[c - 2], sI0[c - 1], sI0[c + 1], sI0[c + 2]);
+    float t1 = deriv5(sW[c - 2], sW[c - 1], sW[c + 1], sW[c + 2]);
+    Ix[pos] = (t0 + t1) * 0.5f;
+    Iz[pos] = sW[c] - sI0[c];
+    t0 = deriv5(sI0[c - 2 * sw], sI0[c - sw], sI0[c + sw], sI0[c + 2 * sw]);
+    t1 = deriv5(sW[c - 2 * sw], sW[c - sw], sW[c + sw], sW[c + 2 * sw]);
+    Iy[pos] = (t0 + t1) * 0.5f;
+}
+
 // computeDerivatives.cu:8-57 (taps on texel centres: mirrored gathers)
 __device__ __forceinline__ void derivatives_px(const float* __restrict__ I0,
                                                const float* __restrict__ I1, LevelDims d,

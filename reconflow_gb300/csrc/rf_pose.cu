@@ -44,6 +44,8 @@
 #include <cuda_runtime.h>
 
 #include "../../include/reconflow_gb300.h"
+#include "rf_alloc.h"
+#include "rf_nvtx.h"
 #include "rf_epipolar.h"
 #include "rf_kernels.cuh"
 
@@ -744,7 +746,7 @@ rf_status solve(rf_pose* h, const double* K, double* R, double* t) {
             cudaFree(h->d_x);
             h->d_x = nullptr;
             h->x_cap = 0;
-            PC(cudaMalloc(&h->d_x, sizeof(double) * 4 * nm));
+            PC(rf::dev_malloc((void**)&h->d_x, sizeof(double) * 4 * nm));
             h->x_cap = nm;
         }
         if ((size_t)H > h->hyp_cap) {
@@ -753,8 +755,8 @@ rf_status solve(rf_pose* h, const double* K, double* R, double* t) {
             h->d_hyp = nullptr;
             h->d_med = nullptr;
             h->hyp_cap = 0;
-            PC(cudaMalloc(&h->d_hyp, sizeof(double) * 9 * H));
-            PC(cudaMalloc(&h->d_med, sizeof(double) * H));
+            PC(rf::dev_malloc((void**)&h->d_hyp, sizeof(double) * 9 * H));
+            PC(rf::dev_malloc((void**)&h->d_med, sizeof(double) * H));
             h->hyp_cap = H;
         }
         PC(cudaMemcpyAsync(h->d_x, x0.data(), sizeof(double) * 2 * nm, cudaMemcpyHostToDevice,
@@ -825,26 +827,26 @@ rf_status rf_pose_create(const rf_pose_params* p, int width, int height, rf_pose
     const size_t npx = (size_t)width * height, nint = (size_t)(width + 1) * (height + 1);
     cudaError_t e = cudaStreamCreateWithFlags(&h->own, cudaStreamNonBlocking);
     for (int f = 0; f < 2 && e == cudaSuccess; f++) {
-        e = cudaMalloc(&h->d_img[f], npx);
-        if (e == cudaSuccess) e = cudaMalloc(&h->d_int[f], nint * sizeof(uint32_t));
+        e = rf::dev_malloc((void**)&h->d_img[f], npx);
+        if (e == cudaSuccess) e = rf::dev_malloc((void**)&h->d_int[f], nint * sizeof(uint32_t));
         for (int o = 0; o < p->n_octaves && e == cudaSuccess; o++) {
             const size_t cells = (size_t)(width >> o) * (height >> o);
             if (cells == 0) break;
-            e = cudaMalloc(&h->d_resp[f][o], cells * (p->n_octave_layers + 2) * sizeof(float));
+            e = rf::dev_malloc((void**)&h->d_resp[f][o], cells * (p->n_octave_layers + 2) * sizeof(float));
         }
-        if (e == cudaSuccess) e = cudaMalloc(&h->d_cand[f], sizeof(DevKp) * h->cand_cap);
-        if (e == cudaSuccess) e = cudaMalloc(&h->d_kp[f], sizeof(DevKp) * h->max_kp);
-        if (e == cudaSuccess) e = cudaMalloc(&h->d_desc[f], sizeof(float) * kDesc * h->max_kp);
+        if (e == cudaSuccess) e = rf::dev_malloc((void**)&h->d_cand[f], sizeof(DevKp) * h->cand_cap);
+        if (e == cudaSuccess) e = rf::dev_malloc((void**)&h->d_kp[f], sizeof(DevKp) * h->max_kp);
+        if (e == cudaSuccess) e = rf::dev_malloc((void**)&h->d_desc[f], sizeof(float) * kDesc * h->max_kp);
     }
-    if (e == cudaSuccess) e = cudaMalloc(&h->d_f32, npx * sizeof(float));
-    if (e == cudaSuccess) e = cudaMalloc(&h->d_count, 2 * sizeof(int));
-    if (e == cudaSuccess) e = cudaMalloc(&h->d_descT, sizeof(float) * kDesc * h->max_kp);
-    if (e == cudaSuccess) e = cudaMalloc(&h->d_best, sizeof(int) * h->max_kp);
-    if (e == cudaSuccess) e = cudaMalloc(&h->d_d1, sizeof(float) * h->max_kp);
-    if (e == cudaSuccess) e = cudaMalloc(&h->d_d2, sizeof(float) * h->max_kp);
-    if (e == cudaSuccess) e = cudaMalloc(&h->d_tab, sizeof(Tables));
+    if (e == cudaSuccess) e = rf::dev_malloc((void**)&h->d_f32, npx * sizeof(float));
+    if (e == cudaSuccess) e = rf::dev_malloc((void**)&h->d_count, 2 * sizeof(int));
+    if (e == cudaSuccess) e = rf::dev_malloc((void**)&h->d_descT, sizeof(float) * kDesc * h->max_kp);
+    if (e == cudaSuccess) e = rf::dev_malloc((void**)&h->d_best, sizeof(int) * h->max_kp);
+    if (e == cudaSuccess) e = rf::dev_malloc((void**)&h->d_d1, sizeof(float) * h->max_kp);
+    if (e == cudaSuccess) e = rf::dev_malloc((void**)&h->d_d2, sizeof(float) * h->max_kp);
+    if (e == cudaSuccess) e = rf::dev_malloc((void**)&h->d_tab, sizeof(Tables));
     if (e == cudaSuccess)
-        e = cudaMalloc(&h->d_seg, sizeof(uint32_t) * (width + 1) * ((height + kSeg - 1) / kSeg));
+        e = rf::dev_malloc((void**)&h->d_seg, sizeof(uint32_t) * (width + 1) * ((height + kSeg - 1) / kSeg));
     // the scoring kernel's largest shared-memory need, set once (the same
     // value from every handle)
     if (e == cudaSuccess)
@@ -899,6 +901,7 @@ rf_status rf_pose_set_stream(rf_pose* h, void* stream) {
 
 rf_status rf_pose_solve_u8(rf_pose* h, const uint8_t* im0, const uint8_t* im1, int pitch,
                            const double K[9], double R[9], double t[3]) {
+    rf::NvtxRange range("rf_pose_solve");
     if (!h || !im0 || !im1 || !K || !R || !t || pitch < h->w)
         return pfail(RF_ERR_INVALID_ARG, "rf_pose_solve_u8: bad argument");
     const uint8_t* src[2] = {im0, im1};
@@ -910,6 +913,7 @@ rf_status rf_pose_solve_u8(rf_pose* h, const uint8_t* im0, const uint8_t* im1, i
 
 rf_status rf_pose_solve_f32(rf_pose* h, const float* im0, const float* im1, int pitch,
                             const double K[9], double R[9], double t[3]) {
+    rf::NvtxRange range("rf_pose_solve");
     if (!h || !im0 || !im1 || !K || !R || !t || pitch < h->w)
         return pfail(RF_ERR_INVALID_ARG, "rf_pose_solve_f32: bad argument");
     const float* src[2] = {im0, im1};

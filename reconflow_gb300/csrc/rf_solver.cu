@@ -17,6 +17,8 @@
 #include <cuda_runtime.h>
 
 #include "../../include/reconflow_gb300.h"
+#include "rf_alloc.h"
+#include "rf_nvtx.h"
 #include "rf_kernels.cuh"
 
 using namespace rf;
@@ -295,6 +297,7 @@ rf_status enqueue_recon(rf_handle* h, float** res_u, float** res_v, bool warm = 
     }
 
     for (int level = top; level >= 0; level--) {
+        NvtxRange level_range("level %d", level);
         LevelDims d{h->W[level], h->H[level], h->S[level]};
         const LevelConsts* lc = h->d_consts + level;
         ReconFields f{};
@@ -307,8 +310,9 @@ rf_status enqueue_recon(rf_handle* h, float** res_u, float** res_v, bool warm = 
             RF_LAUNCH(launch_downscale(h->mask, d0, d, 1.0f, false, h->mask_l, st));
         }
         for (int warp = 0; warp < n_warps; warp++) {
-            RF_LAUNCH(launch_warp(h->I1[level], u, v, d, h->i1w, st));
-            RF_LAUNCH(launch_derivatives(h->I0[level], h->i1w, d, h->Ix, h->Iy, h->Iz, st));
+            NvtxRange warp_range("level %d warp %d", level, warp);
+            RF_LAUNCH(launch_warp_deriv(h->I0[level], h->I1[level], u, v, d, h->Ix, h->Iy,
+                                        h->Iz, st));
             f.u = u; f.v = v;
             f.duhat = h->duhat; f.dvhat = h->dvhat;
             f.pu1 = h->pu1; f.pu2 = h->pu2; f.pv1 = h->pv1; f.pv2 = h->pv2;
@@ -390,10 +394,12 @@ rf_status enqueue_plain(rf_handle* h, float** res_u, float** res_v, bool warm = 
         if (ws != RF_OK) return ws;
     }
     for (int level = top; level >= 0; level--) {
+        NvtxRange level_range("level %d", level);
         LevelDims d{h->W[level], h->H[level], h->S[level]};
         for (int warp = 0; warp < n_warps; warp++) {
-            RF_LAUNCH(launch_warp(h->I1[level], u, v, d, h->i1w, st));
-            RF_LAUNCH(launch_derivatives(h->I0[level], h->i1w, d, h->Ix, h->Iy, h->Iz, st));
+            NvtxRange warp_range("level %d warp %d", level, warp);
+            RF_LAUNCH(launch_warp_deriv(h->I0[level], h->I1[level], u, v, d, h->Ix, h->Iy,
+                                        h->Iz, st));
             for (int iter = 0; iter < n_iters; iter++) {
                 RF_LAUNCH(launch_plain_data(h->duhat, h->dvhat, h->pu1, h->pu2, h->pv1, h->pv2,
                                             h->Ix, h->Iy, h->Iz, wt, d, iter == 0, st));
@@ -429,6 +435,7 @@ bool use_graphs() {
 
 // Record the schedule into a graph on first use, then replay it.
 rf_status run_schedule(rf_handle* h, int kind) {
+    NvtxRange range(kind == 1 || kind == 3 ? "rf_solve_flow" : "rf_solve");
     auto enqueue = [&](float** ru, float** rv) {
         if (kind == 1) return enqueue_plain(h, ru, rv);
         if (kind == 2) return enqueue_recon(h, ru, rv, true);
@@ -560,7 +567,7 @@ rf_status rf_create(const rf_params* p, rf_handle** out) {
     n_planes += n_spare;
     const size_t plane_alloc = (h->plane + 63) / 64 * 64;
     h->pool_floats = plane_alloc * (size_t)n_planes + plane_alloc * 3 /* colour output */;
-    cudaError_t e = cudaMalloc(&h->pool, h->pool_floats * sizeof(float));
+    cudaError_t e = rf::dev_malloc((void**)&h->pool, h->pool_floats * sizeof(float));
     if (e != cudaSuccess) {
         delete h;
         return fail(RF_ERR_OOM, std::string("rf_create: device allocation: ") + cudaGetErrorString(e));
@@ -586,13 +593,13 @@ rf_status rf_create(const rf_params* p, rf_handle** out) {
     // zero everything once: guard rows and never-written padding read as 0
     e = cudaMemset(h->pool, 0, h->pool_floats * sizeof(float));
     if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&h->own_stream, cudaStreamNonBlocking);
-    if (e == cudaSuccess) e = cudaMalloc(&h->d_consts, sizeof(LevelConsts) * h->L);
-    if (e == cudaSuccess) e = cudaMalloc(&h->d_energy, 1025 * sizeof(double));
-    if (e == cudaSuccess) e = cudaMallocHost(&h->h_consts, sizeof(LevelConsts) * h->L);
+    if (e == cudaSuccess) e = rf::dev_malloc((void**)&h->d_consts, sizeof(LevelConsts) * h->L);
+    if (e == cudaSuccess) e = rf::dev_malloc((void**)&h->d_energy, 1025 * sizeof(double));
+    if (e == cudaSuccess) e = rf::host_malloc((void**)&h->h_consts, sizeof(LevelConsts) * h->L);
     if (e == cudaSuccess && p->input_type != RF_INPUT_F32) {
         h->staging_bytes = (size_t)h->stride * h->height * input_elem_bytes(p->input_type);
-        e = cudaMalloc(&h->staging[0], h->staging_bytes);
-        if (e == cudaSuccess) e = cudaMalloc(&h->staging[1], h->staging_bytes);
+        e = rf::dev_malloc((void**)&h->staging[0], h->staging_bytes);
+        if (e == cudaSuccess) e = rf::dev_malloc((void**)&h->staging[1], h->staging_bytes);
     }
     if (e != cudaSuccess) {
         rf_destroy(h);
@@ -935,7 +942,7 @@ rf_status rf_synchronize(rf_handle* h) {
 
 rf_status rf_host_alloc(size_t bytes, void** ptr) {
     if (!ptr) return fail(RF_ERR_INVALID_ARG, "rf_host_alloc: null argument");
-    cudaError_t e = cudaMallocHost(ptr, bytes);
+    cudaError_t e = rf::host_malloc(ptr, bytes);
     if (e != cudaSuccess) return fail(RF_ERR_OOM, std::string("rf_host_alloc: ") + cudaGetErrorString(e));
     return RF_OK;
 }
@@ -1048,6 +1055,16 @@ rf_status rfk_warp(const float* src, int w, int h, int s, const float* u, const 
                    float* out, void* stream) {
     RFK_CHECK(src && u && v && out && w > 0 && h > 0 && s >= w, "rfk_warp");
     RFK_RET(launch_warp(src, u, v, LevelDims{w, h, s}, out, (cudaStream_t)stream), "rfk_warp");
+}
+
+rf_status rfk_warp_derivatives(const float* I0, const float* I1, const float* u, const float* v,
+                               int w, int h, int s, float* Ix, float* Iy, float* Iz,
+                               void* stream) {
+    RFK_CHECK(I0 && I1 && u && v && Ix && Iy && Iz && w > 0 && h > 0 && s >= w,
+              "rfk_warp_derivatives");
+    RFK_RET(launch_warp_deriv(I0, I1, u, v, LevelDims{w, h, s}, Ix, Iy, Iz,
+                              (cudaStream_t)stream),
+            "rfk_warp_derivatives");
 }
 
 rf_status rfk_derivatives(const float* I0, const float* I1w, int w, int h, int s, float* Ix,

@@ -28,6 +28,7 @@
 
 #include "../../include/reconflow_gb300.h"
 #include "rf_kernels.cuh"
+#include "rf_nvtx.h"
 
 namespace rf_warm_impl {
 
@@ -167,6 +168,131 @@ __global__ void k_ws_state(StateArgs a, const float* __restrict__ net, int C, in
     a.Z[p][pos] = Z;
 }
 
+// Temporal warm start for frame sequences: frame k's coarse inverse-depth
+// grid from frame k-1's solved depth.  Every pixel of frame k-1 with a finite
+// positive depth is lifted to 3D in camera k-1 (X = z K^-1 x~), moved by the
+// relative pose (camera k-1 -> camera k, the previous pair's R, t) and
+// projected into frame k; a point that lands at a depth of 0.5 .. 50 m adds
+// its inverse depth to the cell of the factor-times-coarser grid it lands
+// in, and a cell takes the mean of its points (the box mean the network's
+// training targets use; a nearest-point z-buffer would let the few badly
+// conditioned depths of a solve win whole cells).  The sums are fixed point
+// (2^-16 1/m; a cell holds up to 2^15 points) in unsigned integers, so they
+// do not depend on the order of
+// the atomic adds and the grid is reproducible bit for bit.  Cells no point
+// reaches take the median of the filled cells.  Every floating-point
+// operation is an explicitly rounded intrinsic in a fixed order;
+// oracle/temporal_oracle.py's float32 restatement gives the same bits.
+constexpr float kPropScale = 65536.0f;  // 2^16 per 1/m
+
+struct PropArgs {
+    const float* Z[kWsChunk];
+    WsCam cam[kWsChunk];  // level-0 intrinsics, relative pose
+};
+
+__global__ void k_ws_prop_clear(unsigned* __restrict__ acc, int n) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) acc[i] = 0u;
+}
+
+// acc: per pair, `cells` sums then `cells` counts
+__global__ void k_ws_prop_scatter(PropArgs a, int w, int h, int s, int factor, int wn, int hn,
+                                  int first_pair, unsigned* __restrict__ acc) {
+    const int x = blockIdx.x * blockDim.x + threadIdx.x;
+    const int y = blockIdx.y * blockDim.y + threadIdx.y;
+    const int p = blockIdx.z;
+    if (x >= w || y >= h) return;
+    const float z = a.Z[p][x + y * s];
+    if (!(isfinite(z) && z > 0.0f)) return;
+    const WsCam& c = a.cam[p];
+    const float X = __fdiv_rn(__fmul_rn(__fsub_rn((float)x, c.cx), z), c.fx);
+    const float Y = __fdiv_rn(__fmul_rn(__fsub_rn((float)y, c.cy), z), c.fy);
+    const float Q0 = __fadd_rn(__fadd_rn(__fadd_rn(__fmul_rn(c.R[0], X), __fmul_rn(c.R[1], Y)),
+                                         __fmul_rn(c.R[2], z)), c.t[0]);
+    const float Q1 = __fadd_rn(__fadd_rn(__fadd_rn(__fmul_rn(c.R[3], X), __fmul_rn(c.R[4], Y)),
+                                         __fmul_rn(c.R[5], z)), c.t[1]);
+    const float Q2 = __fadd_rn(__fadd_rn(__fadd_rn(__fmul_rn(c.R[6], X), __fmul_rn(c.R[7], Y)),
+                                         __fmul_rn(c.R[8], z)), c.t[2]);
+    if (!(Q2 >= 0.5f && Q2 <= 50.0f)) return;
+    const float u = __fadd_rn(__fdiv_rn(__fmul_rn(c.fx, Q0), Q2), c.cx);
+    const float v = __fadd_rn(__fdiv_rn(__fmul_rn(c.fy, Q1), Q2), c.cy);
+    const float fu = floorf(__fdiv_rn(u, (float)factor));
+    const float fv = floorf(__fdiv_rn(v, (float)factor));
+    if (!(fu >= 0.0f && fu < (float)wn && fv >= 0.0f && fv < (float)hn)) return;
+    const unsigned q = __float2uint_rn(__fmul_rn(__fdiv_rn(1.0f, Q2), kPropScale));
+    const size_t cells = (size_t)wn * hn;
+    const size_t cell = (size_t)fv * wn + (size_t)fu;
+    unsigned* pa = acc + (size_t)(first_pair + p) * 2 * cells;
+    atomicAdd(pa + cell, q);
+    atomicAdd(pa + cells + cell, 1u);
+}
+
+// one block per pair: every filled cell's mean into channel `ch` of the
+// grid; the median of those means (the mean of the two middle ones for an
+// even count), found by a radix select on their bit patterns, into every
+// empty cell; no filled cell: every cell 0
+__global__ void __launch_bounds__(1024) k_ws_prop_fill(int cells, int C, int ch,
+                                                       const unsigned* __restrict__ acc,
+                                                       float* __restrict__ grid) {
+    const unsigned* sum = acc + (size_t)blockIdx.x * 2 * cells;
+    const unsigned* cnt = sum + cells;
+    float* g = grid + (size_t)blockIdx.x * cells * C + ch;
+    unsigned* gb = reinterpret_cast<unsigned*>(g);
+    __shared__ unsigned hist[256];
+    __shared__ unsigned s_prefix, s_rank, s_n;
+    __shared__ float s_med[2];
+    if (threadIdx.x == 0) s_n = 0u;
+    __syncthreads();
+    unsigned nf = 0;
+    for (int i = threadIdx.x; i < cells; i += blockDim.x) {
+        float m = 0.0f;
+        if (cnt[i] != 0u) {
+            m = (float)((double)sum[i] / (double)cnt[i] / (double)kPropScale);
+            nf++;
+        }
+        g[(size_t)i * C] = m;
+    }
+    atomicAdd(&s_n, nf);
+    __syncthreads();
+    const unsigned n = s_n;
+    if (n == 0u) return;
+    for (int r = 0; r < 2; r++) {
+        const unsigned want = r == 0 ? (n - 1u) / 2u : n / 2u;
+        if (threadIdx.x == 0) {
+            s_prefix = 0u;
+            s_rank = want;
+        }
+        __syncthreads();
+        for (int shift = 24; shift >= 0; shift -= 8) {
+            for (int b = threadIdx.x; b < 256; b += blockDim.x) hist[b] = 0u;
+            __syncthreads();
+            const unsigned prefix = s_prefix;
+            const unsigned hi_mask = shift == 24 ? 0u : (0xFFFFFFFFu << (shift + 8));
+            for (int i = threadIdx.x; i < cells; i += blockDim.x) {
+                const unsigned b = gb[(size_t)i * C];
+                if (cnt[i] != 0u && (b & hi_mask) == prefix)
+                    atomicAdd(&hist[(b >> shift) & 255u], 1u);
+            }
+            __syncthreads();
+            if (threadIdx.x == 0) {
+                unsigned rank = s_rank, k = 0;
+                while (hist[k] <= rank) {
+                    rank -= hist[k];
+                    k++;
+                }
+                s_rank = rank;
+                s_prefix = prefix | (k << shift);
+            }
+            __syncthreads();
+        }
+        if (threadIdx.x == 0) s_med[r] = __uint_as_float(s_prefix);
+        __syncthreads();
+    }
+    const float med = (n & 1u) ? s_med[0] : __fmul_rn(__fadd_rn(s_med[0], s_med[1]), 0.5f);
+    for (int i = threadIdx.x; i < cells; i += blockDim.x)
+        if (cnt[i] == 0u) g[(size_t)i * C] = med;
+}
+
 WsCam make_cam(const double* K, const double* R, const double* t, double kscale) {
     WsCam c;
     c.fx = (float)(K[0] * kscale);
@@ -191,6 +317,7 @@ extern "C" {
 rf_status rf_ws_features(int n, const float* const* I0, const float* const* I1, int w0, int h0,
                          int s0, int factor, const double* K, const double* R, const double* t,
                          float* out, void* stream) {
+    rf::NvtxRange range("rf_ws_features");
     if (n < 1 || !I0 || !I1 || !K || !R || !t || !out)
         return wfail(RF_ERR_INVALID_ARG, "rf_ws_features: null argument");
     if (factor < 1 || w0 < factor || h0 < factor || s0 < w0)
@@ -218,10 +345,44 @@ rf_status rf_ws_features(int n, const float* const* I0, const float* const* I1, 
     return RF_OK;
 }
 
+rf_status rf_ws_propagate(int n, const float* const* Z, int w, int h, int s, const double* K,
+                          const double* R, const double* t, int factor, int wn, int hn,
+                          int channels, int channel, float* grid, unsigned int* scratch,
+                          void* stream) {
+    rf::NvtxRange range("rf_ws_propagate");
+    if (n < 1 || !Z || !K || !R || !t || !grid || !scratch)
+        return wfail(RF_ERR_INVALID_ARG, "rf_ws_propagate: null argument");
+    if (w < 1 || h < 1 || s < w || factor < 1 || factor > 32 || wn < 1 || hn < 1 ||
+        channels < 1 || channel < 0 || channel >= channels)
+        return wfail(RF_ERR_INVALID_ARG, "rf_ws_propagate: bad size or factor (1 .. 32)");
+    cudaStream_t st = static_cast<cudaStream_t>(stream);
+    const int cells = wn * hn;
+    const int total = 2 * cells * n;
+    k_ws_prop_clear<<<(total + 255) / 256, 256, 0, st>>>(scratch, total);
+    for (int p0 = 0; p0 < n; p0 += kWsChunk) {
+        const int m = n - p0 < kWsChunk ? n - p0 : kWsChunk;
+        PropArgs a;
+        std::memset(&a, 0, sizeof a);
+        for (int i = 0; i < m; i++) {
+            if (!Z[p0 + i]) return wfail(RF_ERR_INVALID_ARG, "rf_ws_propagate: null depth plane");
+            a.Z[i] = Z[p0 + i];
+            a.cam[i] = make_cam(K + 9 * (p0 + i), R + 9 * (p0 + i), t + 3 * (p0 + i), 1.0);
+        }
+        dim3 blk(32, 8), grd((w + 31) / 32, (h + 7) / 8, m);
+        k_ws_prop_scatter<<<grd, blk, 0, st>>>(a, w, h, s, factor, wn, hn, p0, scratch);
+    }
+    k_ws_prop_fill<<<n, 1024, 0, st>>>(cells, channels, channel, scratch, grid);
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess)
+        return wfail(RF_ERR_CUDA, std::string("rf_ws_propagate: ") + cudaGetErrorString(e));
+    return RF_OK;
+}
+
 rf_status rf_ws_state(int n, const float* net, int channels, int wn, int hn, int w, int h, int s,
                       float up, const double* K_level, const double* R, const double* t,
                       float* const* u, float* const* v, float* const* X, float* const* Y,
                       float* const* Z, void* stream) {
+    rf::NvtxRange range("rf_ws_state");
     if (n < 1 || !net || !K_level || !R || !t || !u || !v || !X || !Y || !Z)
         return wfail(RF_ERR_INVALID_ARG, "rf_ws_state: null argument");
     if (channels < 3 || wn < 1 || hn < 1 || w < 1 || h < 1 || s < w || !(up > 0.0f))

@@ -539,6 +539,13 @@ class ReconFlowBatch:
         N.check(self._lib.rf_batch_download_inv_depth(self._h, int(pair), _ptr(o), o.shape[1]))
         return o
 
+    def importResults(self, pair, ptrs, pitch):
+        """rf_batch_import_results: pair's solution replaced by device planes
+        (u, v, X, Y, Z pointers, e.g. another solver's deviceResults())."""
+        N.check(self._lib.rf_batch_import_results(self._h, int(pair),
+                                                  *[ctypes.c_void_p(p or 0) for p in ptrs],
+                                                  int(pitch)))
+
     def setStream(self, stream_ptr):
         N.check(self._lib.rf_batch_set_stream(self._h, ctypes.c_void_p(stream_ptr or 0)))
 

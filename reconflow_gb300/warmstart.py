@@ -85,6 +85,29 @@ def state(net_out, w, h, s, up, K_level, Rs, ts, planes, stream=0):
                             *[_dptr_array(c) for c in cols], ctypes.c_void_p(stream or 0)))
 
 
+def propagate(Z_ptrs, w, h, s, Ks, Rs, ts, factor, out, channel=2, stream=0, scratch=None):
+    """rf_ws_propagate: frame k's inverse-depth grid from frame k-1's solved
+    depth planes (device pointers, one per pair) into channel `channel` of
+    the (n, hn, wn, C) float32 CUDA tensor `out` (R, t: camera k-1 -> k);
+    `scratch`: an int32 CUDA tensor of 2 n hn wn elements (made if None)."""
+    import torch
+
+    lib = N.load()
+    n, hn, wn, C = out.shape
+    assert len(Z_ptrs) == n and out.is_contiguous()
+    if scratch is None:
+        scratch = torch.empty(2 * n * hn * wn, dtype=torch.int32, device=out.device)
+    assert scratch.numel() >= 2 * n * hn * wn
+    K, pK = _dbl_rows(Ks, 9)
+    R, pR = _dbl_rows(Rs, 9)
+    t, pt = _dbl_rows(ts, 3)
+    N.check(lib.rf_ws_propagate(n, _dptr_array(Z_ptrs), int(w), int(h), int(s), pK, pR, pt,
+                                int(factor), int(wn), int(hn), int(C), int(channel),
+                                ctypes.c_void_p(out.data_ptr()),
+                                ctypes.c_void_p(scratch.data_ptr()), ctypes.c_void_p(stream or 0)))
+    return out
+
+
 def level_intrinsics(K, level, scale=2.0):
     """K at a pyramid level with K[2][2] = 1 (the K-pyramid fix)."""
     Kl = np.array(K, np.float64).copy()

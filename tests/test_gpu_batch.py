@@ -283,3 +283,36 @@ def test_pipelined_transfers_match_blocking_calls(rf):
     finally:
         for p in held:
             lib.rf_host_free(p)
+
+
+def test_imported_results_replace_a_pair(rf):
+    """rf_batch_import_results: a pair solved again by the single-pair solver
+    (the learned path's fallback) and imported into the batch is what the
+    batch downloads, bit for bit; the other pairs keep their own results."""
+    ins = _inputs()[:2]
+    kw = dict(method=14, lambda_=50.0, lambdaf=0.1, lambdams=100.0, alphaTv=1 / 0.33,
+              alphaProj=60.0, tau=0.25, nWarpIters=1, nSolverIters=6, fix_quirks=1)
+    b = rf.ReconFlowBatch([(w, h) for w, h, *_ in ins], 3, **kw)
+    for i, (w, h, I0, I1, K, R, t) in enumerate(ins):
+        b.setCameraMatrices(i, K, K)
+        b.copyImagesToDevice(i, pad_rows(I0, b.strides[i]), pad_rows(I1, b.strides[i]))
+    b.solveR([x[5] for x in ins], [x[6] for x in ins])
+    keep = [b.copyOpticalFlowToHost(0)[0].copy()]
+    # pair 1 solved alone with a longer schedule, then imported
+    w, h, I0, I1, K, R, t = ins[1]
+    f = rf.ReconFlow()
+    f.initializeR(w, h, 1, 3, 2.0, 14, 50.0, 0.0, 0.1, 100.0, 1 / 0.33, 60.0, 0.5, 0.25, 2, 20,
+                  cvType=5, fix_quirks=1)
+    f.setCameraMatrices(K, K)
+    f.copyImagesToDevice(pad_rows(I0, f.stride), pad_rows(I1, f.stride))
+    f.solveR(R, t, 5.0)
+    u1, v1 = f.copyOpticalFlowToHost()
+    X1, Y1, Z1 = f.copy3dToHost()
+    b.importResults(1, f.deviceResults(), f.stride)
+    u, v = b.copyOpticalFlowToHost(1)
+    X, Y, Z = b.copy3dToHost(1)
+    for got, want, nm in ((u, u1, "u"), (v, v1, "v"), (X, X1, "X"), (Y, Y1, "Y"), (Z, Z1, "Z")):
+        assert_bitexact(got[:, :w], want[:, :w], nm)
+    assert_bitexact(b.copyOpticalFlowToHost(0)[0], keep[0], "pair 0 untouched")
+    f.close()
+    b.close()

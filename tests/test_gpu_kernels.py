@@ -166,6 +166,29 @@ def test_derivatives_bitexact(oracle, rf, torch_cuda, w, h, s):
         assert_bitexact(host(got).reshape(h + 1, s), wt.reshape(h + 1, s), nm, region=(h, w))
 
 
+@pytest.mark.parametrize("w,h,s", SIZES + [(70, 45, 96), (2, 2, 32)])
+def test_fused_warp_derivatives_bitexact(oracle, rf, torch_cuda, w, h, s):
+    """The solver's fused warp + derivatives kernel (shared-memory tile with
+    a mirrored 2-pixel halo) against the oracle's warp followed by its
+    derivatives, including tiles whose halo wraps several times (w, h < 5)."""
+    rng = np.random.default_rng(w * 13 + h)
+    n = (h + 1) * s
+    I0 = rng.random(n).astype(np.float32)
+    I1 = rng.random(n).astype(np.float32)
+    u = (rng.normal(size=n) * 3).astype(np.float32)
+    v = (rng.normal(size=n) * 3).astype(np.float32)
+    u[::7] = 2.5 * w
+    v[::11] = -1.7 * h
+    lib = rf.load()
+    d = [dev(torch_cuda, a) for a in (I0, I1, u, v)]
+    o = [torch_cuda.zeros_like(d[0]) for _ in range(3)]
+    ok(rf, lib.rfk_warp_derivatives(*[P(t) for t in d], w, h, s, *[P(t) for t in o], None))
+    i1w = oracle.warp(I1, w, h, s, u, v)
+    want = oracle.derivatives(I0, i1w, w, h, s)
+    for got, wt, nm in zip(o, want, ("Ix", "Iy", "Iz")):
+        assert_bitexact(host(got).reshape(h + 1, s), wt.reshape(h + 1, s), nm, region=(h, w))
+
+
 def test_rgb_to_gray_bitexact(oracle, rf, torch_cuda):
     rng = np.random.default_rng(9)
     w, h, s = 37, 23, 64

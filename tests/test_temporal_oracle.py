@@ -46,3 +46,27 @@ def test_empty_and_behind_camera_inputs():
     # a pure translation along the axis scales the inverse depth exactly
     g, m = TO.propagate_inv_depth(np.full((48, 64), 0.25), K, np.eye(3), np.array([0, 0, -1.0]), 8)
     assert m.any() and np.allclose(g[m], 1.0 / 3.0)
+
+
+def test_float32_mean_carry_matches_the_next_frame():
+    """propagate_depth_f32 (the device kernel's restatement: the mean
+    inverse depth of the points landing in a cell) carries frame k-1's true
+    depth into frame k's true box-mean inverse depth."""
+    q = S.make_sequence(160, 120, 3, seed=9)
+    f = 8
+    prev, cur = q["pairs"][0], q["pairs"][1]
+    with np.errstate(divide="ignore"):
+        Z = np.where(prev["valid"], 1.0 / prev["inv_depth"], np.nan).astype(np.float32)
+    hc, wc = 120 // f, 160 // f
+    grid = TO.propagate_depth_f32(Z, q["K"], prev["R"], prev["t"], f, (hc, wc))
+    assert grid.dtype == np.float32 and grid.shape == (hc, wc)
+    inv = np.where(cur["valid"], cur["inv_depth"], np.nan)[:hc * f, :wc * f]
+    with np.errstate(invalid="ignore"):
+        truth = np.nanmean(inv.reshape(hc, f, wc, f), axis=(1, 3))
+    ok = np.isfinite(truth)
+    rel = np.abs(grid[ok] - truth[ok]) / truth[ok]
+    assert np.median(rel) < 0.01 and np.mean(rel < 0.05) > 0.9
+    # unknown depth everywhere: all zeros
+    empty = TO.propagate_depth_f32(np.full((120, 160), np.nan, np.float32), q["K"], prev["R"],
+                                   prev["t"], f, (hc, wc))
+    assert np.all(empty == 0.0)
