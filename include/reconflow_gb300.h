@@ -195,6 +195,14 @@ RF_API rf_status rf_remove_edge_artifacts(rf_handle* h, int surface_width, float
 RF_API rf_status rf_device_results(rf_handle* h, const float** u, const float** v,
                                    const float** X, const float** Y, const float** Z);
 
+/* Levels of at most max_px pixels run all inner iterations of a warp in
+ * one launch of a 16-CTA thread-block cluster with cluster barriers between
+ * the half-steps, instead of two launches per iteration (the same values:
+ * the per-pixel code is shared).  Applies to every single-pair handle of the
+ * process from its next solve; 0 = never; negative = the default (16384
+ * pixels, or RF_CLUSTER_PX from the environment).  No reference
+ * counterpart. */
+RF_API rf_status rf_set_cluster_pixels(long long max_px);
 /* Tile shape of the inner-iteration kernels at each pyramid level
  * (tile_w[l] x tile_h[l] pixels, one thread each; 32 .. 256 threads, a
  * multiple of 32; default 32 x 8), as reconflow_gb300/autotune.py picks

@@ -81,6 +81,7 @@ _SIGS = [
     ("rf_download_flow_color", _I, [_VP, _F, _VP, _I]),
     ("rf_remove_edge_artifacts", _I, [_VP, _I, _F]),
     ("rf_device_results", _I, [_VP, _VP, _VP, _VP, _VP, _VP]),
+    ("rf_set_cluster_pixels", _I, [ctypes.c_longlong]),
     ("rf_set_tiles", _I, [_VP, _VP, _VP]),
     ("rf_set_stream", _I, [_VP, _VP]),
     ("rf_synchronize", _I, [_VP]),

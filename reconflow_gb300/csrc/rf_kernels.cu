@@ -17,6 +17,7 @@
 // All pixel-local state (duhat, p, uproj, sk) is updated in place: each is
 // read at a neighbour only by the other kernel of the pair.
 #include <atomic>
+#include <cooperative_groups.h>
 #include <cstdint>
 #include <cstdlib>
 
@@ -222,6 +223,41 @@ __global__ void __launch_bounds__(BX* BY, RF_MINB_B) k_recon_b(ReconFields f, We
     int iy = blockIdx.y * blockDim.y + threadIdx.y;
     if (ix >= d.w || iy >= d.h) return;
     recon_b_px(f, wt, d, ix, iy, first);
+}
+
+// ---------------------------------------------------------------------------
+// Every inner iteration of one warp of a small level in one launch: a
+// thread-block cluster of kClusterCtas CTAs covers the level (grid-stride
+// over its pixels) and runs part A, a cluster barrier, part B, a cluster
+// barrier, n_iters times.  The barrier (barrier.cluster arrive.release /
+// wait.acquire) stands where the launch boundary was: part A reads p, X and
+// sk that part B wrote at other pixels, B reads duhat and X1 that A wrote,
+// and within a part no thread reads what another writes, so the per-pixel
+// code and every value are those of the two-launch loop.  The state stays
+// in global memory (a level this small lives in L2).  Every thread runs
+// every loop iteration and reaches every barrier (no early exit).
+// ---------------------------------------------------------------------------
+constexpr int kClusterCtas = 16;
+constexpr int kClusterThreads = 512;
+
+template <int PRIOR>
+__global__ void __launch_bounds__(kClusterThreads, 1)
+    k_recon_cluster(ReconFields f, const LevelConsts* __restrict__ lcp, Weights wt, LevelDims d,
+                    int n_iters, int uc_from_buffer) {
+    namespace cg = cooperative_groups;
+    cg::cluster_group cluster = cg::this_cluster();
+    const int nthr = gridDim.x * blockDim.x;
+    const int tid = blockIdx.x * blockDim.x + threadIdx.x;
+    const int npx = d.w * d.h;
+    for (int it = 0; it < n_iters; it++) {
+        const int first = it == 0 ? 1 : 0;
+        const int ucb = it == 0 ? uc_from_buffer : 0;
+        for (int i = tid; i < npx; i += nthr)
+            recon_a_px<PRIOR>(f, *lcp, wt, d, i % d.w, i / d.w, first, ucb);
+        cluster.sync();
+        for (int i = tid; i < npx; i += nthr) recon_b_px(f, wt, d, i % d.w, i / d.w, first);
+        cluster.sync();
+    }
 }
 
 // ---------------------------------------------------------------------------
@@ -593,6 +629,62 @@ int launch_recon_b(const ReconFields& f, const Weights& wt, LevelDims d, bool fi
                    cudaStream_t st, dim3 b) {
     dim3 g((d.w + b.x - 1) / b.x, (d.h + b.y - 1) / b.y);
     return launch_pdl(k_recon_b, g, b, st, f, wt, d, first ? 1 : 0);
+}
+
+int launch_recon_cluster(const ReconFields& f, const LevelConsts* lc, const Weights& wt,
+                         LevelDims d, int n_iters, bool uc_from_buffer, int prior,
+                         cudaStream_t st) {
+    void (*kern)(ReconFields, const LevelConsts*, Weights, LevelDims, int, int) =
+        prior == 1 ? k_recon_cluster<1> : (prior == 2 ? k_recon_cluster<2> : k_recon_cluster<0>);
+    static bool attr_set[3] = {false, false, false};
+    const int k = prior < 0 || prior > 2 ? 0 : prior;
+    if (!attr_set[k]) {
+        // 16 CTAs is above the portable cluster size of 8
+        cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeNonPortableClusterSizeAllowed, 1);
+        if (e != cudaSuccess) {
+            t_launch_error = e;
+            return 1;
+        }
+        attr_set[k] = true;
+    }
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3(kClusterCtas);
+    cfg.blockDim = dim3(kClusterThreads);
+    cfg.stream = st;
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeClusterDimension;
+    attr[0].val.clusterDim.x = kClusterCtas;
+    attr[0].val.clusterDim.y = 1;
+    attr[0].val.clusterDim.z = 1;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    const cudaError_t e =
+        cudaLaunchKernelEx(&cfg, kern, f, lc, wt, d, n_iters, uc_from_buffer ? 1 : 0);
+    if (e != cudaSuccess) t_launch_error = e;
+    return e == cudaSuccess ? 0 : 1;
+}
+
+bool cluster_supported() {
+    static int v = -1;
+    if (v < 0) {
+        // a 16-CTA cluster of the kernel must fit on the device
+        cudaFuncSetAttribute(k_recon_cluster<0>, cudaFuncAttributeNonPortableClusterSizeAllowed, 1);
+        cudaLaunchConfig_t cfg = {};
+        cfg.gridDim = dim3(kClusterCtas);
+        cfg.blockDim = dim3(kClusterThreads);
+        cudaLaunchAttribute attr[1];
+        attr[0].id = cudaLaunchAttributeClusterDimension;
+        attr[0].val.clusterDim.x = kClusterCtas;
+        attr[0].val.clusterDim.y = 1;
+        attr[0].val.clusterDim.z = 1;
+        cfg.attrs = attr;
+        cfg.numAttrs = 1;
+        int n = 0;
+        const cudaError_t e = cudaOccupancyMaxActiveClusters(&n, k_recon_cluster<0>, &cfg);
+        v = (e == cudaSuccess && n >= 1) ? 1 : 0;
+        cudaGetLastError();
+    }
+    return v == 1;
 }
 
 int launch_plain_data(float* duhat, float* dvhat, const float* pu1, const float* pu2,

@@ -77,6 +77,14 @@ int launch_downscale(const float* src, LevelDims fine, LevelDims coarse, float s
                      float* out, cudaStream_t st);
 int launch_warp(const float* I1, const float* u, const float* v, LevelDims d, float* out,
                 cudaStream_t st);
+// Every inner iteration of a warp of a small level in one launch of a
+// 16-CTA thread-block cluster (barriers between the half-steps); results
+// equal n_iters x (launch_recon_a, launch_recon_b).
+int launch_recon_cluster(const ReconFields& f, const LevelConsts* lc, const Weights& wt,
+                         LevelDims d, int n_iters, bool uc_from_buffer, int prior,
+                         cudaStream_t st);
+// whether a 16-CTA cluster of that kernel can run on the current device
+bool cluster_supported();
 // WarpImage + ComputeDerivatives in one launch; the warped image stays on chip
 int launch_warp_deriv(const float* I0, const float* I1, const float* u, const float* v,
                       LevelDims d, float* Ix, float* Iy, float* Iz, cudaStream_t st);

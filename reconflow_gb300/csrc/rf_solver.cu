@@ -7,6 +7,7 @@
 // every solve; the per-solve camera constants live in a small device block
 // that the kernels read, so one graph serves every pose.
 #include <algorithm>
+#include <atomic>
 #include <cmath>
 #include <cstdio>
 #include <cstdlib>
@@ -227,6 +228,29 @@ void rf::camera_level_consts(const double* K0in, const double* K1in, int L, floa
 
 namespace {
 
+// Levels of at most this many pixels run a warp's inner iterations as one
+// thread-block-cluster launch (launch_recon_cluster); RF_CLUSTER_PX
+// overrides the default (0 = never).  At 1280x720 that is levels 3-5.
+std::atomic<long long> g_cluster_px{-1};
+
+long long cluster_max_px() {
+    long long v = g_cluster_px.load();
+    if (v < 0) {
+        const char* e = std::getenv("RF_CLUSTER_PX");
+        v = e ? std::atoll(e) : 16384;
+        if (v < 0) v = 0;
+        long long expect = -1;
+        g_cluster_px.compare_exchange_strong(expect, v);
+        v = g_cluster_px.load();
+    }
+    return v;
+}
+
+bool use_cluster_at(const rf_handle*, LevelDims d) {
+    const long long m = cluster_max_px();
+    return m > 0 && (long long)d.w * d.h <= m && cluster_supported();
+}
+
 #define RF_LAUNCH(expr)                                                               \
     do {                                                                              \
         if ((expr) != 0)                                                              \
@@ -321,7 +345,12 @@ rf_status enqueue_recon(rf_handle* h, float** res_u, float** res_v, bool warm = 
             f.X = h->X; f.Y = h->Y; f.Z = h->Z; f.X1 = h->X1; f.Y1 = h->Y1; f.Z1 = h->Z1;
             f.uc = uc; f.vc = vc;
             f.ufn = h->ufn_l; f.vfn = h->vfn_l; f.mask = h->mask_l;
-            for (int iter = 0; iter < n_iters; iter++) {
+            if (n_iters > 0 && use_cluster_at(h, d)) {
+                // a small level: all of the warp's iterations in one cluster launch
+                RF_LAUNCH(launch_recon_cluster(f, lc, wt, d, n_iters, uc_in_buffer, prior, st));
+                uc_in_buffer = false;
+            }
+            for (int iter = 0; iter < n_iters && !use_cluster_at(h, d); iter++) {
                 const dim3 tile(h->tile_w[level], h->tile_h[level]);
                 RF_LAUNCH(launch_recon_a(f, lc, wt, d, iter == 0, uc_in_buffer, prior, st, tile));
                 RF_LAUNCH(launch_recon_b(f, wt, d, iter == 0, st, tile));
@@ -905,6 +934,11 @@ rf_status rf_device_results(rf_handle* h, const float** u, const float** v, cons
     if (X) *X = h->X;
     if (Y) *Y = h->Y;
     if (Z) *Z = h->Z;
+    return RF_OK;
+}
+
+rf_status rf_set_cluster_pixels(long long max_px) {
+    g_cluster_px.store(max_px < 0 ? 16384 : max_px);
     return RF_OK;
 }
 

@@ -89,9 +89,18 @@ def test_network_create_failures_leak_nothing(rf, torch_cuda):
 
 
 def test_pose_create_failures_leak_nothing(rf, torch_cuda):
+    # CameraPose creates its device handle for the frame size of its first
+    # solve (rf_pose_create)
+    frame = (np.arange(240 * 320, dtype=np.int64).reshape(240, 320) * 37 % 251).astype(np.uint8)
+
     def make():
         cp = rf.CameraPose()
         cp.initialize(np.array([[300.0, 0, 160], [0, 300.0, 120], [0, 0, 1]]), 20.0)
+        try:
+            cp.solvePose_8uc1(frame, frame)
+        except Exception:
+            cp.close()
+            raise
         return cp
 
     failed, leaked = _sweep(rf, torch_cuda, make, lambda cp: cp.close())

@@ -398,3 +398,52 @@ def test_tiles_do_not_change_single_pair_results(rf):
     with pytest.raises(RfError):
         f.setTiles([32, 32, 32], [8, 8, 9])
     f.close()
+
+
+@pytest.mark.parametrize("w,h,L,method", [(160, 90, 2, 14), (96, 72, 3, 17), (37, 23, 2, 14),
+                                          (330, 200, 3, 20)])
+def test_cluster_levels_equal_two_launch_loop(oracle, rf, w, h, L, method):
+    """A warp's inner iterations as one thread-block-cluster launch (cluster
+    barriers between the half-steps) give exactly the two-launches-per-
+    iteration loop's results, at every level (forced on) and never (off),
+    and the oracle's."""
+    lib = rf.load()
+    s = align_up(w)
+    rng = np.random.default_rng(w + h)
+    I0, I1 = textured_pair(rng, h, s, shift=(1.3, -0.6))
+    K = np.array([[0.8 * w, 0, w / 2], [0, 0.8 * w, h / 2], [0, 0, 1.0]])
+    c, sn = np.cos(0.01), np.sin(0.01)
+    R = np.array([[c, 0, sn], [0, 1, 0], [-sn, 0, c]])
+    t = np.array([-0.1, 0.01, 0.02])
+    ufn = (rng.normal(size=(h, s)) * 0.5 + 1.0).astype(np.float32)
+    vfn = (rng.normal(size=(h, s)) * 0.5).astype(np.float32)
+    mask = (rng.random((h, s)) < 0.3).astype(np.float32)
+    outs = []
+    try:
+        for px in (0, 1 << 40):
+            lib.rf_set_cluster_pixels(px)
+            f = rf.ReconFlow()
+            f.initializeR(w, h, 1, L, 2.0, method, 50.0, 0.0, 0.1, 100.0, 1 / 0.33, 60.0, 0.5,
+                          0.25, 2, 7, cvType=5, fix_quirks=1)
+            f.setCameraMatrices(K, K)
+            f.copyImagesToDevice(I0, I1)
+            if method in (17, 20):
+                f.copySparseOpticalFlowToDevice(ufn, vfn, mask if method == 20 else None)
+            f.solveR(R, t, 5.0)
+            u, v = f.copyOpticalFlowToHost()
+            X, Y, Z = f.copy3dToHost()
+            f.close()
+            outs.append((u, v, X, Y, Z))
+    finally:
+        lib.rf_set_cluster_pixels(-1)
+    for a, b, nm in zip(outs[0], outs[1], "uvXYZ"):
+        assert_bitexact(b, a, f"{nm}: cluster vs two-launch", region=(h, w))
+    p = oracle.make_params(w, h, L, method=method, lam=50.0, lambdaf=0.1, lambdams=100.0,
+                           alpha_tv=1 / 0.33, alpha_proj=60.0, tau=0.25, n_warp_iters=2,
+                           n_solver_iters=7, fix_quirks=1)
+    kw = {}
+    if method in (17, 20):
+        kw = dict(ufn=ufn, vfn=vfn, mask=mask if method == 20 else None)
+    want = oracle.solve(p, I0, I1, K0=K, K1=K, R1=R, t1=t, dtype=np.float32, **kw)
+    for k, got in zip("uvXYZ", outs[1]):
+        assert_bitexact(got, want[k], f"{k}: cluster vs oracle", region=(h, w))
