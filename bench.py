@@ -643,11 +643,12 @@ def run_learned(args, wl, world, rank, local):
     ls.set_stream(stream.cuda_stream)
     margin = wl["fallback_margin"]
     fallbacks = []
+    mode, ceil = fallback_setup(args, W, H, "network")
 
     def step():
         ls.solve(Ks, Rs, ts)
         e = b.energies()
-        bad = [i for i in range(n) if over_margin(e[i], e_plain[i], margin)]
+        bad = [i for i in range(n) if fallback_test(mode, e[i], e_plain[i], W * H, ceil, margin)]
         for i in bad:  # fall back to the plain solve, one pair at a time
             f.setCameraMatrices(Ks[i], Ks[i])
             f.copyImagesToDeviceFromDevice(*b.imagePlanes(i, 0), b.strides[i])
@@ -772,7 +773,7 @@ def run_learned(args, wl, world, rank, local):
                                                                           wl["plain_iters"]],
                        "warm_level": wl["warm_level"], "warm_warps_per_level": wl["warm_warps"],
                        "warm_iters_per_level": wl["warm_iters"],
-                       "fallback": f"plain re-solve when energy > (1 + {margin}) x plain energy",
+                       "fallback": fallback_desc(mode, ceil, margin),
                        "checkpoint": wl["checkpoint"],
                        "tiles": wl.get("tiles") if tiles is not None else "default 32x8",
                        "single_pair_tiles": SINGLE_TILES if single_tiles is not None
@@ -788,7 +789,10 @@ def run_learned(args, wl, world, rank, local):
                       "accuracy": plain_acc},
             "learned": {"accuracy": learned_acc, "fallbacks_per_step": timed_fallbacks,
                         "tc_wait_gave_up": tc_gave_up,
-                        "energy_ratio_median": float(np.median(e_learned / e_plain))},
+                        "energy_ratio_median": float(np.median(e_learned / e_plain)),
+                        "energy_per_px_max": float(np.max(e_learned) / (W * H)),
+                        "plain_energy_test_flags": int(sum(
+                            over_margin(a, c, margin) for a, c in zip(e_learned, e_plain)))},
             "speedup_vs_plain_single_pair": value / single_pps,
             "equal_epe": {"mean": learned_acc["epe_mean_px"] <= plain_acc["epe_mean_px"] + tol,
                           "median": learned_acc["epe_median_px"] <= plain_acc["epe_median_px"] + tol,
@@ -1200,13 +1204,17 @@ def run_learned_mixed(args, wl, world, rank, local):
             G["ls"].set_stream(stream.cuda_stream)
     margin = wl["fallback_margin"]
     fallbacks = []
+    for G in groups:
+        G["mode"], G["ceil"] = fallback_setup(args, G["W"], G["H"], "network")
 
     def step():
         nbad = 0
         for G in groups:
             G["ls"].solve(G["Ks"], G["Rs"], G["ts"])
             e = G["b"].energies()
-            bad = [i for i in range(G["n"]) if over_margin(e[i], G["e_plain"][i], margin)]
+            bad = [i for i in range(G["n"])
+                   if fallback_test(G["mode"], e[i], G["e_plain"][i], G["W"] * G["H"], G["ceil"],
+                                    margin)]
             for i in bad:
                 f = G["f"]
                 f.setCameraMatrices(G["Ks"][i], G["Ks"][i])
@@ -1306,7 +1314,9 @@ def run_learned_mixed(args, wl, world, rank, local):
             "data": "synthetic (seeded scene generator, independent scenes, not sequences)",
             "config": {"workload": args.workload, "groups": per, "pyramid_levels": wl["levels"],
                        "plain_schedule": [wl["plain_warps"], wl["plain_iters"]],
-                       "fallback": f"plain re-solve when energy > (1 + {margin}) x plain energy",
+                       "fallback": {f"{G['W']}x{G['H']}": fallback_desc(G["mode"], G["ceil"],
+                                                                         margin)
+                                    for G in groups},
                        "checkpoint": wl["checkpoint"], "l2": "flushed between steps",
                        "parallelism": "replicas"},
             "speedup_vs_plain_single_pair": single_step_ms / (1000.0 * total_s / args.steps),
@@ -1317,6 +1327,43 @@ def run_learned_mixed(args, wl, world, rank, local):
         G["b"].close()
         G["net"].close()
         G["f"].close()
+
+
+def fallback_setup(args, W, H, source):
+    """The fallback test of the learned workloads: "calibrated" (default,
+    deployable: the learned energy per pixel against the ceiling measured on
+    calibration scenes, reconflow_gb300/tuning/fallback_energy.json),
+    "plain" (the pair's own plain-solve energy, computed untimed beforehand)
+    or "none".  Returns (mode, ceiling)."""
+    from reconflow_gb300 import fallback as FB
+
+    mode = args.fallback or "calibrated"
+    ceil = None
+    if mode == "calibrated":
+        try:
+            ceil = FB.ceiling(FB.load(), W, H, source)
+        except OSError:
+            ceil = None
+    return mode, ceil
+
+
+def fallback_test(mode, e, e_plain, pixels, ceil, margin):
+    from reconflow_gb300 import fallback as FB
+
+    if mode == "none":
+        return False
+    if mode == "plain":
+        return over_margin(e, e_plain, margin)
+    return FB.over(e, pixels, ceil)
+
+
+def fallback_desc(mode, ceil, margin):
+    if mode == "calibrated":
+        return (f"calibrated: plain re-solve when the learned energy per pixel > {ceil} "
+                f"((1 + {margin}) x the calibration scenes' largest) or not finite")
+    if mode == "plain":
+        return f"plain re-solve when energy > (1 + {margin}) x the pair's plain-solve energy"
+    return "none"
 
 
 def over_margin(e, ref, margin):
@@ -1346,8 +1393,7 @@ def run_c5_stream(args, wl, world, rank, local):
 
     import reconflow_gb300 as R
     from reconflow_gb300.scene import make_sequence
-    from reconflow_gb300.warmstart import (LearnedBatchSolver, WarmStartNet, level_intrinsics,
-                                           net_factor, propagate, state)
+    from reconflow_gb300.warmstart import TemporalBatchSolver, WarmStartNet, net_factor
 
     torch.cuda.set_device(local)
     lib = R.load()
@@ -1355,7 +1401,6 @@ def run_c5_stream(args, wl, world, rank, local):
     flush = torch.empty(L2_FLUSH_BYTES // 4, dtype=torch.float32, device="cuda")
     nf = wl["frames"]
     nw = nf - 1  # waves (pairs per sequence)
-    mode = args.fallback or "plain"
     warm_mode = args.warm or "temporal"
     groups = []
     t0 = time.perf_counter()
@@ -1408,19 +1453,14 @@ def run_c5_stream(args, wl, world, rank, local):
             net = WarmStartNet(G["n"], G["hn"] + 1, G["wn"] + 1, seed=0)
             net.load(os.path.join(ROOT, wl["checkpoint"]))
             b = new_batch(G, wl["plain_warps"], wl["plain_iters"])
-            ls = LearnedBatchSolver(net, b, (G["W"], G["H"]), G["Ks"][0],
-                                    warm_level=g["warm_level"], warps=g["warm_warps"],
-                                    iters=g["warm_iters"])
-            ls.set_stream(stream.cuda_stream)
-            G.update(net=net, b=b, ls=ls, grid=torch.zeros((G["n"], G["hn"], G["wn"], 3),
-                                                           device="cuda"),
-                     scratch=torch.zeros(2 * G["n"] * G["hn"] * G["wn"], dtype=torch.int32,
-                                         device="cuda"))
-            lw, lh, lsd = b.levelDims(0, g["warm_level"])
-            G["level_dims"] = (lw, lh, lsd)
-            G["Kl"] = [level_intrinsics(K, g["warm_level"]) for K in G["Ks"]]
-            G["up"] = float(fct) / float(2 ** g["warm_level"])
-            G["planes"] = [b.warmPlanes(i) for i in range(G["n"])]
+            tsol = TemporalBatchSolver(net, b, (G["W"], G["H"]), G["Ks"][0],
+                                       warm_level=g["warm_level"], warps=g["warm_warps"],
+                                       iters=g["warm_iters"], temporal_warps=g["temporal_warps"],
+                                       temporal_iters=g["temporal_iters"])
+            tsol.set_stream(stream.cuda_stream)
+            G.update(net=net, b=b, tsol=tsol)
+            G["mode"], G["ceil_net"] = fallback_setup(args, G["W"], G["H"], "network")
+            G["ceil_tmp"] = fallback_setup(args, G["W"], G["H"], "temporal")[1]
             f = R.ReconFlow()
             f.initializeR(G["W"], G["H"], 1, wl["levels"], 2.0, SOLVER["method"], SOLVER["lam"],
                           0.0, SOLVER["lambdaf"], SOLVER["lambdams"], 1.0 / SOLVER["theta"],
@@ -1431,20 +1471,15 @@ def run_c5_stream(args, wl, world, rank, local):
 
     def solve_wave(G, k):
         """Warm-started solve of wave k for group G (no fallback)."""
-        b, g = G["b"], G["g"]
         Rs, ts = pose(G, k)
+        load_wave(G, G["b"], k)
         if k == 0 or warm_mode == "network":
-            load_wave(G, b, k)
-            G["ls"].solve(G["Ks"], Rs, ts)
-            return
-        Rp, tp = pose(G, k - 1)
-        zs = [b.deviceResults(i)[4] for i in range(G["n"])]
-        propagate(zs, G["W"], G["H"], G["s"], G["Ks"], Rp, tp, G["factor"], G["grid"],
-                  stream=stream.cuda_stream, scratch=G["scratch"])
-        load_wave(G, b, k)
-        lw, lh, lsd = G["level_dims"]
-        state(G["grid"], lw, lh, lsd, G["up"], G["Kl"], Rs, ts, G["planes"], stream.cuda_stream)
-        b.solveWarm(g["warm_level"], Rs, ts, g["temporal_warps"], g["temporal_iters"])
+            G["tsol"].first(G["Ks"], Rs, ts)
+        else:
+            G["tsol"].next(G["Ks"], *pose(G, k - 1), Rs, ts)
+
+    def ceil_at(G, k):
+        return G["ceil_net"] if k == 0 or warm_mode == "network" else G["ceil_tmp"]
 
     margin = wl["fallback_margin"]
     refs = {}  # (group, pair, wave) -> reference energy for the fallback test
@@ -1459,7 +1494,8 @@ def run_c5_stream(args, wl, world, rank, local):
             for gi, G in enumerate(groups):
                 e = G["b"].energies()
                 bad = [i for i in range(G["n"])
-                       if mode != "none" and over_margin(e[i], refs[(gi, i, k)], margin)]
+                       if fallback_test(G["mode"], e[i], refs[(gi, i, k)], G["W"] * G["H"],
+                                        ceil_at(G, k), margin)]
                 if collect:
                     for i in range(G["n"]):
                         record.append(dict(group=gi, seq=i, wave=k, e_learned=float(e[i]),
@@ -1546,29 +1582,21 @@ def run_c5_stream(args, wl, world, rank, local):
                     G["b"].uploadAll([host_frames[(gi, i, k)].value for i in range(n)],
                                      [host_frames[(gi, i, k + 1)].value for i in range(n)],
                                      G["s"])
-                    b, g = G["b"], G["g"]
+                    b = G["b"]
                     Rs, ts = pose(G, k)
                     if k == 0 or warm_mode == "network":
-                        G["ls"].solve(G["Ks"], Rs, ts)
+                        G["tsol"].first(G["Ks"], Rs, ts)
                     else:
-                        lw, lh, lsd = G["level_dims"]
-                        state(G["grid"], lw, lh, lsd, G["up"], G["Kl"], Rs, ts, G["planes"],
-                              stream.cuda_stream)
-                        b.solveWarm(g["warm_level"], Rs, ts, g["temporal_warps"],
-                                    g["temporal_iters"])
+                        G["tsol"].next(G["Ks"], *pose(G, k - 1), Rs, ts)
                     e = b.energies()
                     for i in range(n):
-                        if mode != "none" and over_margin(e[i], refs[(gi, i, k)], margin):
+                        if fallback_test(G["mode"], e[i], refs[(gi, i, k)], G["W"] * G["H"],
+                                         ceil_at(G, k), margin):
                             f = G["f"]
                             f.setCameraMatrices(G["Ks"][i], G["Ks"][i])
                             f.copyImagesToDeviceFromDevice(*b.imagePlanes(i, 0), G["s"])
                             f.solveR(Rs[i], ts[i], 5.0)
                             b.importResults(i, f.deviceResults(), f.stride)
-                    if k + 1 < nw and warm_mode == "temporal":
-                        Rp, tp = Rs, ts
-                        zs = [b.deviceResults(i)[4] for i in range(n)]
-                        propagate(zs, G["W"], G["H"], G["s"], G["Ks"], Rp, tp, G["factor"],
-                                  G["grid"], stream=stream.cuda_stream, scratch=G["scratch"])
                     o = [outs[(gi, i)] for i in range(n)]
                     b.downloadAll(G["s"], *[[o[i][c].value for i in range(n)] for c in range(6)])
 
@@ -1632,8 +1660,9 @@ def run_c5_stream(args, wl, world, rank, local):
                        "warm_start": "network at wave 0, then the previous wave's depth "
                                      "carried into the new frame (rf_ws_propagate)"
                                      if warm_mode == "temporal" else "network for every pair",
-                       "fallback": f"{mode}: plain re-solve when energy > (1 + {margin}) x "
-                                   f"reference energy",
+                       "fallback": {f"{G['W']}x{G['H']}": fallback_desc(G["mode"], G["ceil_tmp"],
+                                                                         margin)
+                                    for G in groups},
                        "checkpoint": wl["checkpoint"], "l2": "flushed between steps",
                        "parallelism": "replicas"},
             "fallbacks_per_step": timed_fallbacks, "e2e": e2e, "clocks": clk.summary(),

@@ -559,7 +559,8 @@ int launch_pair(rf_batch* b, int level, int gx, const OpX& x, const OpY& y) {
     do {                                                                               \
         cudaError_t e__ = (call);                                                      \
         if (e__ != cudaSuccess)                                                        \
-            return bfail(RF_ERR_CUDA, std::string(#call ": ") + cudaGetErrorString(e__)); \
+            return bfail(e__ == cudaErrorMemoryAllocation ? RF_ERR_OOM : RF_ERR_CUDA,         \
+                        std::string(#call ": ") + cudaGetErrorString(e__));            \
     } while (0)
 
 // zero `count` planes starting at index k for every pair

@@ -353,7 +353,8 @@ rf_status cfail(rf_status st, const std::string& msg) {
     do {                                                                              \
         cudaError_t e__ = (call);                                                     \
         if (e__ != cudaSuccess)                                                       \
-            return cfail(RF_ERR_CUDA, std::string(#call ": ") + cudaGetErrorString(e__)); \
+            return cfail(e__ == cudaErrorMemoryAllocation ? RF_ERR_OOM : RF_ERR_CUDA,         \
+                        std::string(#call ": ") + cudaGetErrorString(e__));            \
     } while (0)
 
 int Ho_of(int H, int s) { return s == 1 ? H : (H + 1) / 2; }

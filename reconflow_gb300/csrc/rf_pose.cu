@@ -562,7 +562,8 @@ rf_status pfail(rf_status st, const std::string& msg) {
     do {                                                                               \
         cudaError_t e__ = (call);                                                      \
         if (e__ != cudaSuccess)                                                        \
-            return pfail(RF_ERR_CUDA, std::string(#call ": ") + cudaGetErrorString(e__)); \
+            return pfail(e__ == cudaErrorMemoryAllocation ? RF_ERR_OOM : RF_ERR_CUDA,         \
+                        std::string(#call ": ") + cudaGetErrorString(e__));            \
     } while (0)
 #define PL()                                                                           \
     do {                                                                               \

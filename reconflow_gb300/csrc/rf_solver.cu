@@ -48,7 +48,7 @@ namespace {
 
 rf_status cuda_fail(cudaError_t e, const char* what) {
     g_err = std::string(what) + ": " + cudaGetErrorString(e);
-    return RF_ERR_CUDA;
+    return e == cudaErrorMemoryAllocation ? RF_ERR_OOM : RF_ERR_CUDA;
 }
 
 #define RF_CUDA(call)                                   \

@@ -38,6 +38,16 @@ OUT_CH = 8
 LOSS_WEIGHTS = (0.1, 0.1, 10.0)
 F_NET = 125.0  # focal length (pixels) of the network's input grid
 
+# Refinement schedules of the learned path by frame size (warps and
+# iterations per pyramid level, index 0 = finest), chosen on held-out
+# scenes: few level-0 iterations, more at the coarser levels.  The temporal
+# warm start of sequences refines with the same schedules.
+SCHEDULES = {
+    (1280, 720): dict(warm_level=2, warps=[1, 1, 1], iters=[4, 40, 50]),
+    (1920, 1080): dict(warm_level=2, warps=[1, 1, 1], iters=[4, 60, 80]),
+    (3840, 2160): dict(warm_level=3, warps=[1, 1, 1, 1], iters=[4, 30, 60, 80]),
+}
+
 
 def box_down(a: np.ndarray, f: int) -> np.ndarray:
     """Mean over f x f blocks (the solver's 2x downscale applied log2(f)
@@ -394,6 +404,55 @@ class LearnedBatchSolver:
         Kl = [level_intrinsics(K, self.warm_level) for K in Ks]
         state(self.o8, lw, lh, ls, self.up, Kl, Rs, ts, self.planes, self.stream)
         self.batch.solveWarm(self.warm_level, Rs, ts, self.warps, self.iters)
+
+
+class TemporalBatchSolver:
+    """Batched ReconFlow solve of frame sequences: slot i of the batch
+    follows sequence i, one pair (frame k, frame k + 1) per wave.  Wave 0
+    starts from the network (LearnedBatchSolver); every later wave starts
+    from the previous wave's solved depth carried into the new frame
+    (rf_ws_propagate, the previous pair's pose) and turned into the warm
+    planes (rf_ws_state), then refines from `warm_level` with the temporal
+    schedule.  The caller uploads each wave's frames into the batch before
+    calling first() / next()."""
+
+    def __init__(self, net: WarmStartNet, batch, size, K, warm_level=2, warps=1, iters=20,
+                 temporal_warps=None, temporal_iters=None):
+        import torch
+
+        self.learned = LearnedBatchSolver(net, batch, size, K, warm_level, warps, iters)
+        self.batch = batch
+        self.w, self.h = size
+        ls = self.learned
+        self.factor, self.hn, self.wn = ls.factor, ls.hn, ls.wn
+        n = batch.n
+        self.grid = torch.zeros((n, self.hn, self.wn, 3), device="cuda")
+        self.scratch = torch.zeros(2 * n * self.hn * self.wn, dtype=torch.int32, device="cuda")
+        self.warm_level = warm_level
+        self.t_warps = warps if temporal_warps is None else temporal_warps
+        self.t_iters = iters if temporal_iters is None else temporal_iters
+        self.stream = 0
+
+    def set_stream(self, stream_ptr):
+        self.stream = stream_ptr or 0
+        self.learned.set_stream(stream_ptr)
+
+    def first(self, Ks, Rs, ts):
+        """Wave 0: the network's warm start."""
+        self.learned.solve(Ks, Rs, ts)
+
+    def next(self, Ks, R_prev, t_prev, Rs, ts):
+        """Wave k > 0 from wave k - 1's solutions still in the batch (its
+        pairs' poses R_prev, t_prev carry them into the new frames)."""
+        b = self.batch
+        zs = [b.deviceResults(i)[4] for i in range(b.n)]
+        propagate(zs, self.w, self.h, b.strides[0], Ks, R_prev, t_prev, self.factor, self.grid,
+                  stream=self.stream, scratch=self.scratch)
+        lw, lh, lsd = self.learned.level_dims
+        Kl = [level_intrinsics(K, self.warm_level) for K in Ks]
+        state(self.grid, lw, lh, lsd, self.learned.up, Kl, Rs, ts, self.learned.planes,
+              self.stream)
+        b.solveWarm(self.warm_level, Rs, ts, self.t_warps, self.t_iters)
 
 
 # ---------------------------------------------------------------------------

@@ -61,3 +61,51 @@ def test_serving_loop_moves_every_step_once_in_order(monkeypatch):
     # each batch's own columns and pitch
     assert ("A", "up", ["c0"], ["c1"], 64) in log and ("B", "up", ["c0"], ["c1"], 32) in log
     assert ("A", "down", ["c2"], ["c3"], ["c4"], ["c5"], ["c6"], ["c7"], 64) in log
+
+
+def test_learned_schedules_match_the_package():
+    """The bench's learned workloads refine with the schedules the package
+    defines (reconflow_gb300.warmstart.SCHEDULES), which the fallback
+    calibration also uses."""
+    import bench
+    from reconflow_gb300.warmstart import SCHEDULES
+
+    wl = bench.WORKLOADS["720p-learned"]
+    assert SCHEDULES[(1280, 720)] == dict(warm_level=wl["warm_level"], warps=wl["warm_warps"],
+                                          iters=wl["warm_iters"])
+    for key in ("mixed-4k-1080p-learned", "c5-stream"):
+        for g in bench.WORKLOADS[key]["groups"]:
+            sch = SCHEDULES[(g["width"], g["height"])]
+            assert sch == dict(warm_level=g["warm_level"], warps=g["warm_warps"],
+                               iters=g["warm_iters"])
+            if "temporal_iters" in g:
+                assert g["temporal_iters"] == sch["iters"]
+                assert g["temporal_warps"] == sch["warps"]
+
+
+def test_fallback_ceiling_and_test(tmp_path):
+    """The deployable fallback test: non-finite energies always fall back,
+    finite ones above the table's per-pixel ceiling do; a size without an
+    entry has no ceiling."""
+    import json
+    import math
+
+    from reconflow_gb300 import fallback as FB
+
+    table = {"margin": 0.02, "entries": {"1280x720/network": {"ceiling": 3.0}}}
+    p = tmp_path / "t.json"
+    p.write_text(json.dumps(table))
+    t = FB.load(str(p))
+    c = FB.ceiling(t, 1280, 720, "network")
+    assert c == 3.0 and FB.ceiling(t, 640, 480, "network") is None
+    npx = 1280 * 720
+    assert not FB.over(2.9 * npx, npx, c)
+    assert FB.over(3.1 * npx, npx, c)
+    assert FB.over(math.nan, npx, c) and FB.over(math.inf, npx, None)
+    assert not FB.over(1e9, npx, None)
+    # the committed table covers the bench's sizes and sources
+    committed = FB.load()
+    for key in ("1280x720/network", "1920x1080/network", "3840x2160/network",
+                "1920x1080/temporal", "3840x2160/temporal"):
+        ent = committed["entries"][key]
+        assert ent["ceiling"] > ent["energy_per_px_max"] > 0
