@@ -203,6 +203,15 @@ RF_API rf_status rf_device_results(rf_handle* h, const float** u, const float** 
  * pixels, or RF_CLUSTER_PX from the environment).  No reference
  * counterpart. */
 RF_API rf_status rf_set_cluster_pixels(long long max_px);
+/* Debug builds compiled with RF_BOUNDS_CHECK (reconflow_gb300/build.py
+ * --bounds-check, a separate library): every field access of the inner
+ * iteration is checked against its plane; an index outside is counted and
+ * redirected to a sink cell instead of touching memory.  rf_debug_bounds
+ * returns (and clears) the count and the first offending index;
+ * rf_debug_bounds_selftest makes one such access on purpose.  Other builds:
+ * RF_ERR_UNSUPPORTED.  No reference counterpart. */
+RF_API rf_status rf_debug_bounds(unsigned long long* count, long long* first);
+RF_API rf_status rf_debug_bounds_selftest(void);
 /* Tile shape of the inner-iteration kernels at each pyramid level
  * (tile_w[l] x tile_h[l] pixels, one thread each; 32 .. 256 threads, a
  * multiple of 32; default 32 x 8), as reconflow_gb300/autotune.py picks

@@ -11,6 +11,8 @@ import os
 
 _HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(_HERE, "lib", "librfgb300.so")
+# RF_BOUNDS_CHECK=1 in the environment loads the bounds-checked debug build
+CHECK_LIB_PATH = os.path.join(_HERE, "lib", "librfgb300_check.so")
 
 RF_OK = 0
 STATUS_NAMES = {0: "RF_OK", 1: "RF_ERR_INVALID_ARG", 2: "RF_ERR_UNSUPPORTED", 3: "RF_ERR_CUDA",
@@ -81,6 +83,8 @@ _SIGS = [
     ("rf_download_flow_color", _I, [_VP, _F, _VP, _I]),
     ("rf_remove_edge_artifacts", _I, [_VP, _I, _F]),
     ("rf_device_results", _I, [_VP, _VP, _VP, _VP, _VP, _VP]),
+    ("rf_debug_bounds", _I, [ctypes.POINTER(ctypes.c_ulonglong), ctypes.POINTER(ctypes.c_longlong)]),
+    ("rf_debug_bounds_selftest", _I, []),
     ("rf_set_cluster_pixels", _I, [ctypes.c_longlong]),
     ("rf_set_tiles", _I, [_VP, _VP, _VP]),
     ("rf_set_stream", _I, [_VP, _VP]),
@@ -181,11 +185,12 @@ def load(path: str | None = None):
     global _lib
     if _lib is not None:
         return _lib
-    path = path or LIB_PATH
+    checked = path is None and os.environ.get("RF_BOUNDS_CHECK", "0") not in ("", "0")
+    path = path or (CHECK_LIB_PATH if checked else LIB_PATH)
     if not os.path.exists(path):
         from . import build as _build
 
-        _build.build()
+        _build.build(bounds_check=checked)
     lib = ctypes.CDLL(path)
     for name, res, args in _SIGS:
         fn = getattr(lib, name)

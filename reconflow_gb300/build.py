@@ -20,6 +20,10 @@ CSRC = os.path.join(HERE, "csrc")
 LIB_DIR = os.path.join(HERE, "lib")
 LIB_PATH = os.path.join(LIB_DIR, "librfgb300.so")
 OBJ_DIR = os.path.join(HERE, "_build")
+# debug variant: every field access of the inner iteration checked against its
+# plane (-DRF_BOUNDS_CHECK); out-of-range indices are counted, not followed
+CHECK_LIB_PATH = os.path.join(LIB_DIR, "librfgb300_check.so")
+CHECK_OBJ_DIR = os.path.join(HERE, "_build_check")
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 # per-file flags: the solver keeps exact IEEE arithmetic without contraction
@@ -61,19 +65,24 @@ def _headers():
     return out
 
 
-def build(force: bool = False, verbose: bool = False) -> str:
+def build(force: bool = False, verbose: bool = False, bounds_check: bool = False) -> str:
+    """Compile the library (only stale objects unless ``force``); with
+    ``bounds_check`` the debug variant ``lib/librfgb300_check.so`` instead."""
+    lib_path = CHECK_LIB_PATH if bounds_check else LIB_PATH
+    obj_dir = CHECK_OBJ_DIR if bounds_check else OBJ_DIR
+    extra = ["-DRF_BOUNDS_CHECK"] if bounds_check else []
     os.makedirs(LIB_DIR, exist_ok=True)
-    os.makedirs(OBJ_DIR, exist_ok=True)
+    os.makedirs(obj_dir, exist_ok=True)
     nv = nvcc()
     hdrs = _headers()
     jobs = []
     objs = []
     for src, flags in SOURCES.items():
         s = os.path.join(CSRC, src)
-        o = os.path.join(OBJ_DIR, os.path.splitext(src)[0] + ".o")
+        o = os.path.join(obj_dir, os.path.splitext(src)[0] + ".o")
         objs.append(o)
         if force or _stale(o, [s] + hdrs):
-            jobs.append([nv, "-c", s, "-o", o] + ARCH + COMMON + flags)
+            jobs.append([nv, "-c", s, "-o", o] + ARCH + COMMON + extra + flags)
 
     def run(cmd):
         if verbose:
@@ -87,12 +96,13 @@ def build(force: bool = False, verbose: bool = False) -> str:
         for log in ex.map(run, jobs):
             if verbose and log.strip():
                 print(log)
-    if force or jobs or _stale(LIB_PATH, objs):
-        run([nv, "-shared", "-o", LIB_PATH] + objs + ARCH + ["-Xcompiler", "-fPIC,-pthread",
+    if force or jobs or _stale(lib_path, objs):
+        run([nv, "-shared", "-o", lib_path] + objs + ARCH + ["-Xcompiler", "-fPIC,-pthread",
                                                               "-lcudart_static", "-ldl", "-lrt",
                                                               "-lpthread"])
-    return LIB_PATH
+    return lib_path
 
 
 if __name__ == "__main__":
-    print(build(force="--force" in sys.argv, verbose=True))
+    print(build(force="--force" in sys.argv, verbose=True,
+                bounds_check="--bounds-check" in sys.argv))

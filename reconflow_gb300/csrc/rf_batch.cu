@@ -477,6 +477,7 @@ float* plane_base(rf_batch* b, int k) { return b->pool + (size_t)k * b->total; }
 
 ReconFields fields_of(rf_batch* b, const ReconIdx& r) {
     ReconFields f{};
+    f.extent = (long long)b->total;
     f.u = plane_base(b, r.u); f.v = plane_base(b, r.v);
     f.duhat = plane_base(b, r.duhat); f.dvhat = plane_base(b, r.dvhat);
     f.pu1 = plane_base(b, r.pu1); f.pu2 = plane_base(b, r.pu2);
@@ -729,7 +730,19 @@ rf_status run_batch(rf_batch* b, int kind) {
 
 float* pair_plane(rf_batch* b, int i, int k) { return plane_base(b, k) + b->base_off[i]; }
 
+
 }  // namespace rf_batch_impl
+
+namespace rf {
+unsigned long long batch_oob_take(long long* first) {
+#ifdef RF_BOUNDS_CHECK
+    return rf_oob_take(first);
+#else
+    (void)first;
+    return 0;
+#endif
+}
+}  // namespace rf
 
 extern "C" {
 

@@ -631,6 +631,30 @@ int launch_recon_b(const ReconFields& f, const Weights& wt, LevelDims d, bool fi
     return launch_pdl(k_recon_b, g, b, st, f, wt, d, first ? 1 : 0);
 }
 
+#ifdef RF_BOUNDS_CHECK
+__global__ void k_oob_selftest(ReconFields f) { RF_AT(f, duhat, f.extent) += 0.0f; }
+#endif
+
+unsigned long long kernels_oob_take(long long* first) {
+#ifdef RF_BOUNDS_CHECK
+    return rf_oob_take(first);
+#else
+    (void)first;
+    return 0;
+#endif
+}
+
+int launch_oob_selftest() {
+#ifdef RF_BOUNDS_CHECK
+    ReconFields f{};
+    f.extent = 1;  // f.duhat is never dereferenced: index 1 is redirected to the sink
+    k_oob_selftest<<<1, 1>>>(f);
+    return check_launch();
+#else
+    return 1;
+#endif
+}
+
 int launch_recon_cluster(const ReconFields& f, const LevelConsts* lc, const Weights& wt,
                          LevelDims d, int n_iters, bool uc_from_buffer, int prior,
                          cudaStream_t st) {

@@ -55,7 +55,50 @@ struct ReconFields {
     const float* ufn; // prior flow at this level (methods 17 / 20)
     const float* vfn;
     const float* mask;
+    long long extent; // floats every field pointer may be indexed with: [0, extent)
 };
+
+// A field element of the inner iteration, f.name[i].  Built with
+// RF_BOUNDS_CHECK, every index is checked against [0, f.extent): an index
+// outside is counted (with the first offender kept) and the access goes to
+// a sink cell instead of memory, so a bad index is reported, never used.
+// Read the counts with rf_debug_bounds.
+#ifdef RF_BOUNDS_CHECK
+static __device__ unsigned long long g_oob_count;
+static __device__ long long g_oob_first;
+static __device__ float g_oob_sink;
+
+__device__ __forceinline__ float& rf_checked(float* p, long long i, long long n) {
+    if (i < 0 || i >= n) {
+        if (atomicAdd(&g_oob_count, 1ull) == 0ull) g_oob_first = i;
+        return g_oob_sink;
+    }
+    return p[i];
+}
+__device__ __forceinline__ const float& rf_checked(const float* p, long long i, long long n) {
+    if (i < 0 || i >= n) {
+        if (atomicAdd(&g_oob_count, 1ull) == 0ull) g_oob_first = i;
+        return g_oob_sink;
+    }
+    return p[i];
+}
+#define RF_AT(f, name, idx) rf_checked((f).name, (long long)(idx), (f).extent)
+
+// this translation unit's counts (and reset them)
+static inline unsigned long long rf_oob_take(long long* first) {
+    unsigned long long c = 0;
+    long long fi = -1;
+    cudaDeviceSynchronize();
+    cudaMemcpyFromSymbol(&c, g_oob_count, sizeof c);
+    cudaMemcpyFromSymbol(&fi, g_oob_first, sizeof fi);
+    const unsigned long long zero = 0;
+    cudaMemcpyToSymbol(g_oob_count, &zero, sizeof zero);
+    if (first && c) *first = fi;
+    return c;
+}
+#else
+#define RF_AT(f, name, idx) (f).name[idx]
+#endif
 
 // Per-level camera constants of one pair (K pyramid, P = K0 [R0|t0],
 // Q = K1 [R1|t1], float copies), fix_quirks as rf_params.
@@ -83,6 +126,13 @@ int launch_warp(const float* I1, const float* u, const float* v, LevelDims d, fl
 int launch_recon_cluster(const ReconFields& f, const LevelConsts* lc, const Weights& wt,
                          LevelDims d, int n_iters, bool uc_from_buffer, int prior,
                          cudaStream_t st);
+// RF_BOUNDS_CHECK builds: the out-of-range field accesses counted by this
+// file's kernels (and those of the batched kernels), cleared when read; 0 in
+// other builds.  launch_oob_selftest makes one checked access one past a
+// field's extent (redirected to the sink: nothing outside is touched).
+unsigned long long kernels_oob_take(long long* first);
+unsigned long long batch_oob_take(long long* first);
+int launch_oob_selftest();
 // whether a 16-CTA cluster of that kernel can run on the current device
 bool cluster_supported();
 // WarpImage + ComputeDerivatives in one launch; the warped image stays on chip

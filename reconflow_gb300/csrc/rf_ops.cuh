@@ -43,64 +43,64 @@ __device__ __forceinline__ void recon_a_px(const ReconFields& f, const LevelCons
     // thread waits for memory once.  The kernel writes only duhat, uproj and
     // X1 at its own pixel, and reads none of those at another pixel, so the
     // order of loads and stores does not change any value.
-    float u = f.u[pos], v = f.v[pos];
-    float dix = f.Ix[pos], diy = f.Iy[pos], dit = f.Iz[pos];
-    float uproj = f.uproj[pos], vproj = f.vproj[pos];
-    float sku = f.sku[pos], skv = f.skv[pos];
+    float u = RF_AT(f, u, pos), v = RF_AT(f, v, pos);
+    float dix = RF_AT(f, Ix, pos), diy = RF_AT(f, Iy, pos), dit = RF_AT(f, Iz, pos);
+    float uproj = RF_AT(f, uproj, pos), vproj = RF_AT(f, vproj, pos);
+    float sku = RF_AT(f, sku, pos), skv = RF_AT(f, skv, pos);
     float duhat = 0.0f, dvhat = 0.0f;
     float pu1 = 0.0f, pu2 = 0.0f, pv1 = 0.0f, pv2 = 0.0f;
     float pu1l = 0.0f, pv1l = 0.0f, pu2d = 0.0f, pv2d = 0.0f;
     if (!first) {
-        duhat = f.duhat[pos];
-        dvhat = f.dvhat[pos];
-        pu1 = f.pu1[pos];
-        pu2 = f.pu2[pos];
-        pv1 = f.pv1[pos];
-        pv2 = f.pv2[pos];
+        duhat = RF_AT(f, duhat, pos);
+        dvhat = RF_AT(f, dvhat, pos);
+        pu1 = RF_AT(f, pu1, pos);
+        pu2 = RF_AT(f, pu2, pos);
+        pv1 = RF_AT(f, pv1, pos);
+        pv2 = RF_AT(f, pv2, pos);
         if (ix > 0) {
-            pu1l = f.pu1[pos - 1];
-            pv1l = f.pv1[pos - 1];
+            pu1l = RF_AT(f, pu1, pos - 1);
+            pv1l = RF_AT(f, pv1, pos - 1);
         }
         if (iy > 0) {
-            pu2d = f.pu2[pos - s];
-            pv2d = f.pv2[pos - s];
+            pu2d = RF_AT(f, pu2, pos - s);
+            pv2d = RF_AT(f, pv2, pos - s);
         }
     }
     // X0, Y0, Z0 at: 0 = pos, 1 = x+1 (flat pos+1), 2 = y+1 (flat pos+s),
     // 3 = x-1, 4 = y-1.  x+1 / y+1 are read at flat pos+1 / pos+s even on the
     // last column / row (solve3dMinimalArea.cu:65,76).
     float Xn[5], Yn[5], Zn[5];
-    Xn[0] = f.X[pos];
-    Yn[0] = f.Y[pos];
-    Zn[0] = f.Z[pos];
-    Xn[1] = f.X[pos + 1];
-    Yn[1] = f.Y[pos + 1];
-    Zn[1] = f.Z[pos + 1];
-    Xn[2] = f.X[pos + s];
-    Yn[2] = f.Y[pos + s];
-    Zn[2] = f.Z[pos + s];
+    Xn[0] = RF_AT(f, X, pos);
+    Yn[0] = RF_AT(f, Y, pos);
+    Zn[0] = RF_AT(f, Z, pos);
+    Xn[1] = RF_AT(f, X, pos + 1);
+    Yn[1] = RF_AT(f, Y, pos + 1);
+    Zn[1] = RF_AT(f, Z, pos + 1);
+    Xn[2] = RF_AT(f, X, pos + s);
+    Yn[2] = RF_AT(f, Y, pos + s);
+    Zn[2] = RF_AT(f, Z, pos + s);
     Xn[3] = Yn[3] = Zn[3] = 0.0f;
     Xn[4] = Yn[4] = Zn[4] = 0.0f;
     if (ix > 0) {
-        Xn[3] = f.X[pos - 1];
-        Yn[3] = f.Y[pos - 1];
-        Zn[3] = f.Z[pos - 1];
+        Xn[3] = RF_AT(f, X, pos - 1);
+        Yn[3] = RF_AT(f, Y, pos - 1);
+        Zn[3] = RF_AT(f, Z, pos - 1);
     }
     if (iy > 0) {
-        Xn[4] = f.X[pos - s];
-        Yn[4] = f.Y[pos - s];
-        Zn[4] = f.Z[pos - s];
+        Xn[4] = RF_AT(f, X, pos - s);
+        Yn[4] = RF_AT(f, Y, pos - s);
+        Zn[4] = RF_AT(f, Z, pos - s);
     }
     float ucb = 0.0f, vcb = 0.0f;
     if (uc_from_buffer) {
-        ucb = f.uc[pos];
-        vcb = f.vc[pos];
+        ucb = RF_AT(f, uc, pos);
+        vcb = RF_AT(f, vc, pos);
     }
     float ufn = 0.0f, vfn = 0.0f, mk = 1.0f;
     if (PRIOR != 0) {
-        ufn = f.ufn[pos];
-        vfn = f.vfn[pos];
-        if (PRIOR == 2) mk = f.mask[pos];
+        ufn = RF_AT(f, ufn, pos);
+        vfn = RF_AT(f, vfn, pos);
+        if (PRIOR == 2) mk = RF_AT(f, mask, pos);
     }
 
     // --- data step (solveReconDataL1.cu:24-100) ---
@@ -137,13 +137,13 @@ __device__ __forceinline__ void recon_a_px(const ReconFields& f, const LevelCons
     float Xo, Yo, Zo;
     solve3d_pixel(c, uproj1, vproj1, ix, iy, Xn, Yn, Zn, wt.lambdaf, wt.lambdams, Xo, Yo, Zo);
 
-    f.duhat[pos] = duhat1;
-    f.dvhat[pos] = dvhat1;
-    f.uproj[pos] = uproj1;
-    f.vproj[pos] = vproj1;
-    f.X1[pos] = Xo;
-    f.Y1[pos] = Yo;
-    f.Z1[pos] = Zo;
+    RF_AT(f, duhat, pos) = duhat1;
+    RF_AT(f, dvhat, pos) = dvhat1;
+    RF_AT(f, uproj, pos) = uproj1;
+    RF_AT(f, vproj, pos) = vproj1;
+    RF_AT(f, X1, pos) = Xo;
+    RF_AT(f, Y1, pos) = Yo;
+    RF_AT(f, Z1, pos) = Zo;
 }
 
 // 3x3 tap of the reference's 3D median with its border rules
@@ -196,16 +196,16 @@ __device__ __forceinline__ void recon_b_finish(const ReconFields& f, const Weigh
     float Xo, Yo, Zo;
     cleanup_pixel(X1, Y1, Z1, Xm, Ym, Zm, Xo, Yo, Zo);
 
-    f.pu1[pos] = pu1;
-    f.pu2[pos] = pu2;
-    f.pv1[pos] = pv1;
-    f.pv2[pos] = pv2;
-    f.X[pos] = Xo;
-    f.Y[pos] = Yo;
-    f.Z[pos] = Zo;
+    RF_AT(f, pu1, pos) = pu1;
+    RF_AT(f, pu2, pos) = pu2;
+    RF_AT(f, pv1, pos) = pv1;
+    RF_AT(f, pv2, pos) = pv2;
+    RF_AT(f, X, pos) = Xo;
+    RF_AT(f, Y, pos) = Yo;
+    RF_AT(f, Z, pos) = Zo;
     // --- multiplier update (solveUcSk.cu:94-95) ---
-    f.sku[pos] = sku + u + duhat - uproj;
-    f.skv[pos] = skv + v + dvhat - vproj;
+    RF_AT(f, sku, pos) = sku + u + duhat - uproj;
+    RF_AT(f, skv, pos) = skv + v + dvhat - vproj;
 }
 
 __device__ __forceinline__ void recon_b_px(const ReconFields& f, const Weights& wt, LevelDims d,
@@ -215,22 +215,22 @@ __device__ __forceinline__ void recon_b_px(const ReconFields& f, const Weights& 
 
     // All loads first (see recon_a_px): the kernel writes p, X and sk only at
     // its own pixel and reads p and sk only there, and reads no X.
-    float duhat = f.duhat[pos], dvhat = f.dvhat[pos];
+    float duhat = RF_AT(f, duhat, pos), dvhat = RF_AT(f, dvhat, pos);
     float duhr = 0.0f, dvhr = 0.0f, duhd = 0.0f, dvhd = 0.0f;
     if ((ix + 1) < w) {
-        duhr = f.duhat[pos + 1];
-        dvhr = f.dvhat[pos + 1];
+        duhr = RF_AT(f, duhat, pos + 1);
+        dvhr = RF_AT(f, dvhat, pos + 1);
     }
     if ((iy + 1) < h) {
-        duhd = f.duhat[pos + s];
-        dvhd = f.dvhat[pos + s];
+        duhd = RF_AT(f, duhat, pos + s);
+        dvhd = RF_AT(f, dvhat, pos + s);
     }
     float pu1 = 0.0f, pu2 = 0.0f, pv1 = 0.0f, pv2 = 0.0f;
     if (!first) {
-        pu1 = f.pu1[pos];
-        pu2 = f.pu2[pos];
-        pv1 = f.pv1[pos];
-        pv2 = f.pv2[pos];
+        pu1 = RF_AT(f, pu1, pos);
+        pu2 = RF_AT(f, pu2, pos);
+        pv1 = RF_AT(f, pv1, pos);
+        pv2 = RF_AT(f, pv2, pos);
     }
     float mX[9], mY[9], mZ[9];
     if (ix > 0 && iy > 0 && ix + 1 < w && iy + 1 < h) {
@@ -239,9 +239,9 @@ __device__ __forceinline__ void recon_b_px(const ReconFields& f, const Weights& 
 #pragma unroll
             for (int i = 0; i < 3; i++) {
                 int at = pos + (j - 1) * s + (i - 1);
-                mX[j * 3 + i] = f.X1[at];
-                mY[j * 3 + i] = f.Y1[at];
-                mZ[j * 3 + i] = f.Z1[at];
+                mX[j * 3 + i] = RF_AT(f, X1, at);
+                mY[j * 3 + i] = RF_AT(f, Y1, at);
+                mZ[j * 3 + i] = RF_AT(f, Z1, at);
             }
         }
     } else {
@@ -252,15 +252,15 @@ __device__ __forceinline__ void recon_b_px(const ReconFields& f, const Weights& 
             for (int i = 0; i < 3; i++) {
                 int at = median3_tap(ix + i - 1, iy + j - 1, w, h, s);
                 int k = j * 3 + i;
-                mX[k] = at >= 0 ? f.X1[base + at] : 0.0f;
-                mY[k] = at >= 0 ? f.Y1[base + at] : 0.0f;
-                mZ[k] = at >= 0 ? f.Z1[base + at] : 0.0f;
+                mX[k] = at >= 0 ? RF_AT(f, X1, base + at) : 0.0f;
+                mY[k] = at >= 0 ? RF_AT(f, Y1, base + at) : 0.0f;
+                mZ[k] = at >= 0 ? RF_AT(f, Z1, base + at) : 0.0f;
             }
         }
     }
-    const float sku = f.sku[pos], skv = f.skv[pos];
-    const float u = f.u[pos], v = f.v[pos];
-    const float uproj = f.uproj[pos], vproj = f.vproj[pos];
+    const float sku = RF_AT(f, sku, pos), skv = RF_AT(f, skv, pos);
+    const float u = RF_AT(f, u, pos), v = RF_AT(f, v, pos);
+    const float uproj = RF_AT(f, uproj, pos), vproj = RF_AT(f, vproj, pos);
     recon_b_finish(f, wt, pos, (ix + 1) < w, (iy + 1) < h, duhat, dvhat, duhr, dvhr, duhd, dvhd,
                    pu1, pu2, pv1, pv2, mX, mY, mZ, sku, skv, u, v, uproj, vproj);
 }

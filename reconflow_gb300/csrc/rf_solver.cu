@@ -325,6 +325,7 @@ rf_status enqueue_recon(rf_handle* h, float** res_u, float** res_v, bool warm = 
         LevelDims d{h->W[level], h->H[level], h->S[level]};
         const LevelConsts* lc = h->d_consts + level;
         ReconFields f{};
+        f.extent = (long long)h->plane;
         if (prior) {
             // Reconflow.cu:232-241: prior resampled from level 0 at every level
             LevelDims d0{h->W[0], h->H[0], h->S[0]};
@@ -937,6 +938,28 @@ rf_status rf_device_results(rf_handle* h, const float** u, const float** v, cons
     return RF_OK;
 }
 
+rf_status rf_debug_bounds(unsigned long long* count, long long* first) {
+#ifdef RF_BOUNDS_CHECK
+    if (!count) return fail(RF_ERR_INVALID_ARG, "rf_debug_bounds: null count");
+    long long f1 = -1, f2 = -1;
+    const unsigned long long c1 = rf::kernels_oob_take(&f1);
+    const unsigned long long c2 = rf::batch_oob_take(&f2);
+    *count = c1 + c2;
+    if (first) *first = c1 ? f1 : (c2 ? f2 : -1);
+    return RF_OK;
+#else
+    (void)count;
+    (void)first;
+    return fail(RF_ERR_UNSUPPORTED, "rf_debug_bounds: library built without RF_BOUNDS_CHECK");
+#endif
+}
+
+rf_status rf_debug_bounds_selftest() {
+    if (rf::launch_oob_selftest() != 0)
+        return fail(RF_ERR_UNSUPPORTED, "rf_debug_bounds_selftest: needs an RF_BOUNDS_CHECK build");
+    return RF_OK;
+}
+
 rf_status rf_set_cluster_pixels(long long max_px) {
     g_cluster_px.store(max_px < 0 ? 16384 : max_px);
     return RF_OK;
@@ -995,6 +1018,7 @@ rf_status rf_profile_iterations(rf_handle* h, int level, int n_iters, float* ms)
     LevelDims d{h->W[level], h->H[level], h->S[level]};
     const bool recon = h->p.method != RF_METHOD_TVL1;
     ReconFields f{};
+    f.extent = (long long)h->plane;
     if (recon) {
         f.u = h->res_u; f.v = h->res_v;
         f.duhat = h->duhat; f.dvhat = h->dvhat;
