@@ -1374,6 +1374,17 @@ def over_margin(e, ref, margin):
     return bool(np.isfinite(ref) and e > (1.0 + margin) * ref)
 
 
+def c5_fallback_desc(G, warm_mode, margin):
+    from reconflow_gb300 import fallback as FB
+
+    if G["mode"] == "calibrated" and warm_mode == "temporal":
+        return (f"calibrated: wave 0 (network start) plain re-solve when the learned energy per "
+                f"pixel > {G['ceil_net']} ((1 + {margin}) x the calibration scenes' largest); "
+                f"later waves when it exceeds {FB.HISTORY_FACTOR} x the median of the "
+                f"sequence's last {FB.HISTORY} pairs; always when not finite")
+    return fallback_desc(G["mode"], G["ceil_net"], margin)
+
+
 C5_METRIC = ("frame pairs/s, C5 stream: 256 pairs of 3840x2160 / 1920x1080 from 32-frame "
              "sequences, batched + learned / temporal warm start")
 
@@ -1392,6 +1403,7 @@ def run_c5_stream(args, wl, world, rank, local):
     import torch
 
     import reconflow_gb300 as R
+    from reconflow_gb300 import fallback as FB
     from reconflow_gb300.scene import make_sequence
     from reconflow_gb300.warmstart import TemporalBatchSolver, WarmStartNet, net_factor
 
@@ -1460,7 +1472,7 @@ def run_c5_stream(args, wl, world, rank, local):
             tsol.set_stream(stream.cuda_stream)
             G.update(net=net, b=b, tsol=tsol)
             G["mode"], G["ceil_net"] = fallback_setup(args, G["W"], G["H"], "network")
-            G["ceil_tmp"] = fallback_setup(args, G["W"], G["H"], "temporal")[1]
+            G["guard"] = FB.SequenceGuard(G["n"])
             f = R.ReconFlow()
             f.initializeR(G["W"], G["H"], 1, wl["levels"], 2.0, SOLVER["method"], SOLVER["lam"],
                           0.0, SOLVER["lambdaf"], SOLVER["lambdams"], 1.0 / SOLVER["theta"],
@@ -1478,8 +1490,15 @@ def run_c5_stream(args, wl, world, rank, local):
         else:
             G["tsol"].next(G["Ks"], *pose(G, k - 1), Rs, ts)
 
-    def ceil_at(G, k):
-        return G["ceil_net"] if k == 0 or warm_mode == "network" else G["ceil_tmp"]
+    def must_fall_back(G, gi, i, k, e):
+        """The fallback test of pair i of wave k (call in wave order: the
+        calibrated temporal test keeps each sequence's energy history)."""
+        if G["mode"] == "calibrated" and warm_mode == "temporal":
+            if k == 0 and i == 0:
+                G["guard"].reset()
+            return G["guard"].over(i, e, G["W"] * G["H"], G["ceil_net"])
+        return fallback_test(G["mode"], e, refs[(gi, i, k)], G["W"] * G["H"], G["ceil_net"],
+                             margin)
 
     margin = wl["fallback_margin"]
     refs = {}  # (group, pair, wave) -> reference energy for the fallback test
@@ -1493,13 +1512,12 @@ def run_c5_stream(args, wl, world, rank, local):
                 solve_wave(G, k)
             for gi, G in enumerate(groups):
                 e = G["b"].energies()
-                bad = [i for i in range(G["n"])
-                       if fallback_test(G["mode"], e[i], refs[(gi, i, k)], G["W"] * G["H"],
-                                        ceil_at(G, k), margin)]
+                bad = [i for i in range(G["n"]) if must_fall_back(G, gi, i, k, e[i])]
                 if collect:
                     for i in range(G["n"]):
                         record.append(dict(group=gi, seq=i, wave=k, e_learned=float(e[i]),
-                                           epe_learned=epe(G, G["b"], i, k)))
+                                           epe_learned=epe(G, G["b"], i, k),
+                                           fell_back=i in bad))
                 for i in bad:
                     # the full plain solve of the pair, in place of the learned result
                     f = G["f"]
@@ -1590,8 +1608,7 @@ def run_c5_stream(args, wl, world, rank, local):
                         G["tsol"].next(G["Ks"], *pose(G, k - 1), Rs, ts)
                     e = b.energies()
                     for i in range(n):
-                        if fallback_test(G["mode"], e[i], refs[(gi, i, k)], G["W"] * G["H"],
-                                         ceil_at(G, k), margin):
+                        if must_fall_back(G, gi, i, k, e[i]):
                             f = G["f"]
                             f.setCameraMatrices(G["Ks"][i], G["Ks"][i])
                             f.copyImagesToDeviceFromDevice(*b.imagePlanes(i, 0), G["s"])
@@ -1640,12 +1657,16 @@ def run_c5_stream(args, wl, world, rank, local):
                 "plain_epe_median_px": float(np.mean(pmed)),
                 "energy_ratio_median": float(np.median(ratio)),
                 "energy_ratio_max": float(np.max(ratio)),
-                "over_margin": int(sum(x > 1.0 + margin for x in ratio))}
+                "over_margin": int(sum(x > 1.0 + margin for x in ratio)),
+                "fell_back": int(sum(r["fell_back"] for r in rec)),
+                "fell_back_and_over_margin": int(sum(r["fell_back"] and x > 1.0 + margin
+                                                     for r, x in zip(rec, ratio)))}
         if args.dump:
             np.savez(args.dump, group=[r["group"] for r in record],
                      seq=[r["seq"] for r in record], wave=[r["wave"] for r in record],
                      e_learned=[r["e_learned"] for r in record],
                      epe_learned=[r["epe_learned"] for r in record],
+                     fell_back=[r["fell_back"] for r in record],
                      e_plain=[plain_rec[(r["group"], r["seq"], r["wave"])][0] for r in record],
                      epe_plain=[plain_rec[(r["group"], r["seq"], r["wave"])][1] for r in record])
         print(json.dumps({
@@ -1660,8 +1681,7 @@ def run_c5_stream(args, wl, world, rank, local):
                        "warm_start": "network at wave 0, then the previous wave's depth "
                                      "carried into the new frame (rf_ws_propagate)"
                                      if warm_mode == "temporal" else "network for every pair",
-                       "fallback": {f"{G['W']}x{G['H']}": fallback_desc(G["mode"], G["ceil_tmp"],
-                                                                         margin)
+                       "fallback": {f"{G['W']}x{G['H']}": c5_fallback_desc(G, warm_mode, margin)
                                     for G in groups},
                        "checkpoint": wl["checkpoint"], "l2": "flushed between steps",
                        "parallelism": "replicas"},

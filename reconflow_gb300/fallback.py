@@ -16,6 +16,19 @@ the learned energy per pixel spans 1.0 .. 3.2 while the plain solve's spans
 solve diverged, not how good the learned solution is; the ceiling flags the
 learned solutions that are outliers among learned solutions.
 
+Along a sequence (the temporal warm start) the energy per pixel drifts with
+the scene: over 32 frames of a moving camera both the learned and the plain
+solutions' energies per pixel grow about threefold, so a fixed ceiling
+measured on short sequences flags correct solutions late in a stream.  There
+the reference is the sequence's own recent history: a pair falls back when
+its energy per pixel exceeds ``HISTORY_FACTOR`` times the median of the
+sequence's last ``HISTORY`` pairs (``SequenceGuard``); the first pair of a
+sequence, warm-started by the network, uses the network ceiling.  The
+history holds every pair's learned energy, accepted or not, so a lasting
+change of the scene is accepted after two pairs while a single outlier is
+not.  The calibration records the distribution of that ratio on its
+sequences.
+
 The table is ``tuning/fallback_energy.json``, written by
 ``python -m reconflow_gb300.fallback --calibrate``.
 """
@@ -30,6 +43,8 @@ import numpy as np
 HERE = os.path.dirname(os.path.abspath(__file__))
 TABLE = os.path.join(HERE, "tuning", "fallback_energy.json")
 MARGIN = 0.02
+HISTORY = 3
+HISTORY_FACTOR = 2.0
 
 # calibration sets: (width, height, source, count, first seed); sequences
 # give count - 1 pairs per sequence of `frames` frames
@@ -37,8 +52,8 @@ CALIBRATION = [
     (1280, 720, "network", 128, 8000, None),
     (1920, 1080, "network", 16, 8500, None),
     (3840, 2160, "network", 16, 8700, None),
-    (1920, 1080, "temporal", 2, 8800, 9),
-    (3840, 2160, "temporal", 2, 8900, 9),
+    (1920, 1080, "temporal", 2, 8800, 33),
+    (3840, 2160, "temporal", 2, 8900, 33),
 ]
 
 
@@ -51,11 +66,12 @@ def load(path: str = TABLE) -> dict:
         return json.load(fh)
 
 
-def ceiling(table: dict, width: int, height: int, source: str):
-    """Energy-per-pixel ceiling for this frame size and warm-start source
-    ("network" or "temporal"), or None when the table has no entry."""
+def ceiling(table: dict, width: int, height: int, source: str = "network"):
+    """Energy-per-pixel ceiling for this frame size and warm-start source,
+    or None when the table has no ceiling for it (temporal sources are
+    tested against their sequence's history instead)."""
     ent = table.get("entries", {}).get(key(width, height, source))
-    return None if ent is None else float(ent["ceiling"])
+    return None if ent is None or "ceiling" not in ent else float(ent["ceiling"])
 
 
 def over(energy: float, pixels: int, ceil) -> bool:
@@ -64,6 +80,39 @@ def over(energy: float, pixels: int, ceil) -> bool:
     if not np.isfinite(energy):
         return True
     return ceil is not None and energy / pixels > ceil
+
+
+class SequenceGuard:
+    """The fallback test along sequences: one history per sequence."""
+
+    def __init__(self, n: int, factor: float = HISTORY_FACTOR, length: int = HISTORY):
+        self.factor = factor
+        self.length = length
+        self.hist = [[] for _ in range(n)]
+
+    def reset(self) -> None:
+        for h in self.hist:
+            h.clear()
+
+    def ratio(self, i: int, energy_per_px: float):
+        """Energy per pixel over the median of sequence i's history (None
+        while the history is empty)."""
+        h = self.hist[i]
+        return None if not h else energy_per_px / float(np.median(h))
+
+    def over(self, i: int, energy: float, pixels: int, first_ceil) -> bool:
+        """True: fall back.  Non-finite energies always fall back (and are
+        kept out of the history); the first pair of a sequence is tested
+        against `first_ceil` (the network ceiling, None: no test), later
+        pairs against the factor x the history median."""
+        if not np.isfinite(energy):
+            return True
+        e = energy / pixels
+        q = self.ratio(i, e)
+        bad = (first_ceil is not None and e > first_ceil) if q is None else q > self.factor
+        self.hist[i].append(e)
+        del self.hist[i][:-self.length]
+        return bool(bad)
 
 
 def calibrate(out: str = TABLE, log=print) -> dict:
@@ -118,6 +167,8 @@ def calibrate(out: str = TABLE, log=print) -> dict:
             pad = lambda a: np.pad(a, ((0, 0), (0, s - W))).astype(np.float32)  # noqa: E731
             ts_ = TemporalBatchSolver(net, b, (W, H), Ks[0], sch["warm_level"], sch["warps"],
                                       sch["iters"])
+            guard = SequenceGuard(n)
+            ratios = []
             for k in range(frames - 1):
                 for i, q in enumerate(seqs):
                     b.copyImagesToDevice(i, pad(q["frames"][k]), pad(q["frames"][k + 1]))
@@ -128,7 +179,13 @@ def calibrate(out: str = TABLE, log=print) -> dict:
                 else:
                     ts_.next(Ks, [q["pairs"][k - 1]["R"] for q in seqs],
                              [q["pairs"][k - 1]["t"] for q in seqs], Rs, tt)
-                per_px += list(b.energies() / (W * H))
+                e_k = b.energies()
+                for i in range(n):
+                    q = guard.ratio(i, e_k[i] / (W * H))
+                    if q is not None and np.isfinite(q):
+                        ratios.append(q)
+                    guard.over(i, e_k[i], W * H, None)
+                per_px += list(e_k / (W * H))
             b.close()
             net.close()
             seeds = [seed0, seed0 + n - 1]
@@ -136,16 +193,31 @@ def calibrate(out: str = TABLE, log=print) -> dict:
         e = np.array(per_px)
         finite = e[np.isfinite(e)]
         top = float(finite.max()) if finite.size else float("nan")
-        entries[key(W, H, source)] = {
-            "pairs": int(e.size), "seeds": seeds, "frames": frames,
-            "energy_per_px_median": float(np.median(finite)) if finite.size else None,
-            "energy_per_px_max": top, "ceiling": top * (1.0 + MARGIN)}
+        ent = {"pairs": int(e.size), "seeds": seeds, "frames": frames,
+               "energy_per_px_median": float(np.median(finite)) if finite.size else None,
+               "energy_per_px_max": top}
+        if source == "network":
+            ent["ceiling"] = top * (1.0 + MARGIN)
+            tail = ""
+        else:
+            r = np.array(ratios)
+            ent.update(history=HISTORY, history_factor=HISTORY_FACTOR,
+                       history_ratio_median=float(np.median(r)),
+                       history_ratio_p99=float(np.percentile(r, 99)),
+                       history_ratio_max=float(r.max()),
+                       history_flags=int((r > HISTORY_FACTOR).sum()))
+            tail = (f"; history ratio median {ent['history_ratio_median']:.3f}, max "
+                    f"{ent['history_ratio_max']:.3f}, flags {ent['history_flags']}")
+        entries[key(W, H, source)] = ent
         log(f"{key(W, H, source)}: {e.size} pairs, energy per pixel median "
-            f"{entries[key(W, H, source)]['energy_per_px_median']:.3f}, max {top:.3f}")
+            f"{ent['energy_per_px_median']:.3f}, max {top:.3f}" + tail)
     table = {"margin": MARGIN, "entries": entries,
              "command": "python -m reconflow_gb300.fallback --calibrate",
-             "what": "ceiling = (1 + margin) x the largest learned-solution energy per pixel "
-                     "of the calibration set"}
+             "what": "network: ceiling = (1 + margin) x the largest learned-solution energy "
+                     "per pixel of the calibration set; temporal: a pair falls back when its "
+                     "energy per pixel exceeds history_factor x the median of its sequence's "
+                     "last `history` pairs (the ratio's distribution on the calibration "
+                     "sequences recorded)"}
     with open(out, "w") as fh:
         json.dump(table, fh, indent=1)
     return table

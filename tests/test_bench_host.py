@@ -105,7 +105,35 @@ def test_fallback_ceiling_and_test(tmp_path):
     assert not FB.over(1e9, npx, None)
     # the committed table covers the bench's sizes and sources
     committed = FB.load()
-    for key in ("1280x720/network", "1920x1080/network", "3840x2160/network",
-                "1920x1080/temporal", "3840x2160/temporal"):
+    for key in ("1280x720/network", "1920x1080/network", "3840x2160/network"):
         ent = committed["entries"][key]
         assert ent["ceiling"] > ent["energy_per_px_max"] > 0
+    for key in ("1920x1080/temporal", "3840x2160/temporal"):
+        ent = committed["entries"][key]
+        assert ent["history_factor"] == FB.HISTORY_FACTOR and ent["pairs"] >= 64
+        assert 0 < ent["history_ratio_median"] <= ent["history_ratio_max"]
+        assert FB.ceiling(committed, *map(int, key.split("/")[0].split("x")), "temporal") is None
+
+
+def test_sequence_guard():
+    """Along a sequence a pair falls back when its energy per pixel exceeds
+    twice the median of the sequence's last three; the first pair is held
+    to the network ceiling; a single outlier does not move the median, a
+    lasting change is accepted after two pairs; sequences are independent."""
+    import math
+
+    from reconflow_gb300 import fallback as FB
+
+    g = FB.SequenceGuard(2)
+    px = 100
+    assert g.over(0, 5.0 * px, px, 4.0)          # first pair over the network ceiling
+    g.reset()
+    assert not g.over(0, 2.0 * px, px, 4.0)
+    assert not g.over(1, 9.0 * px, px, None)     # no ceiling: the first pair passes
+    seq = [2.2, 2.4, 2.6, 7.0, 2.8, 3.0]         # one outlier (7.0 > 2 x 2.4)
+    flags = [g.over(0, e * px, px, 4.0) for e in seq]
+    assert flags == [False, False, False, True, False, False]
+    assert g.over(0, math.nan, px, 4.0) and len(g.hist[0]) == 3   # NaN kept out
+    flags = [g.over(0, e * px, px, 4.0) for e in (8.0, 8.5, 9.0)]  # a lasting jump
+    assert flags == [True, True, False]
+    assert g.hist[1] == [9.0]

@@ -108,16 +108,7 @@ def test_pose_create_failures_leak_nothing(rf, torch_cuda):
     assert abs(leaked) < (8 << 20), leaked
 
 
-def test_failed_create_then_normal_use(rf, torch_cuda):
-    """After an injected failure the library works normally: a solve on a
-    fresh handle succeeds and gives finite flow."""
-    from reconflow_gb300 import _native as N
-
-    lib = rf.load()
-    lib.rf_test_fail_alloc(1)
-    with pytest.raises(N.RfError):
-        rf.ReconFlowBatch([(64, 48)], 2, method=14, nWarpIters=1, nSolverIters=2)
-    lib.rf_test_fail_alloc(0)
+def _small_solve(rf):
     y, x = np.mgrid[0:48, 0:64].astype(np.float64)
     I0 = (0.5 + 0.2 * np.sin(0.3 * x + 0.2 * y)).astype(np.float32)
     I1 = np.roll(I0, 1, axis=1)
@@ -128,6 +119,24 @@ def test_failed_create_then_normal_use(rf, torch_cuda):
     f.setCameraMatrices(K, K)
     f.copyImagesToDevice(I0, I1)
     f.solveR(np.eye(3), np.array([0.1, 0.0, 0.0]), 5.0)
-    u, _ = f.copyOpticalFlowToHost()
+    u, v = f.copyOpticalFlowToHost()
     f.close()
-    assert np.isfinite(u[:, :64]).all()
+    return u, v
+
+
+def test_failed_create_then_normal_use(rf, torch_cuda):
+    """After an injected failure the library works normally: a solve on a
+    fresh handle gives bit for bit the results of the same solve before."""
+    from reconflow_gb300 import _native as N
+
+    lib = rf.load()
+    before = _small_solve(rf)
+    lib.rf_test_fail_alloc(1)
+    try:
+        with pytest.raises(N.RfError):
+            rf.ReconFlowBatch([(64, 48)], 2, method=14, nWarpIters=1, nSolverIters=2)
+    finally:
+        lib.rf_test_fail_alloc(0)
+    after = _small_solve(rf)
+    for a, b in zip(before, after):
+        assert a.tobytes() == b.tobytes()
