@@ -199,8 +199,8 @@ RF_API rf_status rf_device_results(rf_handle* h, const float** u, const float** 
  * one launch of a 16-CTA thread-block cluster with cluster barriers between
  * the half-steps, instead of two launches per iteration (the same values:
  * the per-pixel code is shared).  Applies to every single-pair handle of the
- * process from its next solve; 0 = never; negative = the default (16384
- * pixels, or RF_CLUSTER_PX from the environment).  No reference
+ * process from its next solve; 0 = never; negative = the default (0, or
+ * RF_CLUSTER_PX from the environment).  No reference
  * counterpart. */
 RF_API rf_status rf_set_cluster_pixels(long long max_px);
 /* Debug builds compiled with RF_BOUNDS_CHECK (reconflow_gb300/build.py

@@ -229,15 +229,18 @@ void rf::camera_level_consts(const double* K0in, const double* K1in, int L, floa
 namespace {
 
 // Levels of at most this many pixels run a warp's inner iterations as one
-// thread-block-cluster launch (launch_recon_cluster); RF_CLUSTER_PX
-// overrides the default (0 = never).  At 1280x720 that is levels 3-5.
+// thread-block-cluster launch (launch_recon_cluster); RF_CLUSTER_PX sets it.
+// Off by default: on GB300 the graph of two launches per iteration was
+// faster at every level size tried (the 16 SMs of one cluster issue too
+// slowly for a level of thousands of pixels, and a cluster barrier costs
+// more than a launch boundary inside a graph for the smallest levels).
 std::atomic<long long> g_cluster_px{-1};
 
 long long cluster_max_px() {
     long long v = g_cluster_px.load();
     if (v < 0) {
         const char* e = std::getenv("RF_CLUSTER_PX");
-        v = e ? std::atoll(e) : 16384;
+        v = e ? std::atoll(e) : 0;
         if (v < 0) v = 0;
         long long expect = -1;
         g_cluster_px.compare_exchange_strong(expect, v);

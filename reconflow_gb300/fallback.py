@@ -117,8 +117,14 @@ class SequenceGuard:
 
 def calibrate(out: str = TABLE, log=print) -> dict:
     """Solve the calibration sets with the learned path on the GPU and write
-    the ceilings.  Network: independent scenes (scene.make_scene); temporal:
-    sequences (scene.make_sequence) through TemporalBatchSolver."""
+    the table.  Network: independent scenes (scene.make_scene); temporal:
+    sequences (scene.make_sequence) through TemporalBatchSolver, with a
+    flagged pair re-solved by the plain single-pair solver and its result
+    imported before the next frame, as a deployment does.  For validation
+    every pair is also solved with the plain batched schedule (outside the
+    test itself): the table records how many pairs the test flags, how many
+    have an energy over (1 + margin) x their plain solve's, and how many
+    both."""
     import torch
 
     import reconflow_gb300 as R
@@ -129,29 +135,43 @@ def calibrate(out: str = TABLE, log=print) -> dict:
 
     R.load()
     ckpt = os.path.join(HERE, "weights", "warmstart_f125.bin")
+    levels, plain_warps, plain_iters = 6, 5, 100
     entries = {}
+    table0 = {}
     for W, H, source, count, seed0, frames in CALIBRATION:
         sch = SCHEDULES[(W, H)]
-        levels = 6
         n = count
-        per_px = []
+        npx = W * H
+
+        def batch(warps, iters):
+            return R.ReconFlowBatch([(W, H)] * n, levels, method=14, nWarpIters=warps,
+                                    nSolverIters=iters, **SOLVER_WEIGHTS)
+
+        per_px, flags, over_plain = [], [], []
+        ratios = []
         if source == "network":
             scenes = [make_scene(W, H, seed=seed0 + i, device="cuda") for i in range(n)]
             Ks = [sc["K"] for sc in scenes]
+            Rs, ts = [sc["R"] for sc in scenes], [sc["t"] for sc in scenes]
             fct = net_factor(Ks[0])
             net = WarmStartNet(n, H // fct + 1, W // fct + 1, seed=0)
             net.load(ckpt)
-            b = R.ReconFlowBatch([(W, H)] * n, levels, method=14, nWarpIters=5,
-                                 nSolverIters=100, **SOLVER_WEIGHTS)
+            b, pb = batch(plain_warps, plain_iters), batch(plain_warps, plain_iters)
             for i, sc in enumerate(scenes):
-                b.setCameraMatrices(i, sc["K"], sc["K"])
-                b.copyImagesToDevice(i, sc["I0"], sc["I1"])
+                for x in (b, pb):
+                    x.setCameraMatrices(i, sc["K"], sc["K"])
+                    x.copyImagesToDevice(i, sc["I0"], sc["I1"])
             ls = LearnedBatchSolver(net, b, (W, H), Ks[0], sch["warm_level"], sch["warps"],
                                     sch["iters"])
-            ls.solve(Ks, [sc["R"] for sc in scenes], [sc["t"] for sc in scenes])
-            per_px += list(b.energies() / (W * H))
-            b.close()
-            net.close()
+            ls.solve(Ks, Rs, ts)
+            e = b.energies()
+            pb.solveR(Rs, ts)
+            ep = pb.energies()
+            per_px += list(e / npx)
+            over_plain += [bool(np.isfinite(a) and (not np.isfinite(c) or a > (1 + MARGIN) * c))
+                           for a, c in zip(e, ep)]
+            for x in (b, pb, net):
+                x.close()
             seeds = [seed0, seed0 + n - 1]
         else:
             seqs = [make_sequence(W, H, frames, seed=seed0 + j, device="cuda") for j in range(n)]
@@ -159,19 +179,25 @@ def calibrate(out: str = TABLE, log=print) -> dict:
             fct = net_factor(Ks[0])
             net = WarmStartNet(n, H // fct + 1, W // fct + 1, seed=0)
             net.load(ckpt)
-            b = R.ReconFlowBatch([(W, H)] * n, levels, method=14, nWarpIters=5,
-                                 nSolverIters=100, **SOLVER_WEIGHTS)
+            b, pb = batch(plain_warps, plain_iters), batch(plain_warps, plain_iters)
             for i, K in enumerate(Ks):
                 b.setCameraMatrices(i, K, K)
+                pb.setCameraMatrices(i, K, K)
+            f = R.ReconFlow()
+            wt = SOLVER_WEIGHTS
+            f.initializeR(W, H, 1, levels, 2.0, 14, wt["lambda_"], 0.0, wt["lambdaf"],
+                          wt["lambdams"], wt["alphaTv"], wt["alphaProj"], 0.5, wt["tau"],
+                          plain_warps, plain_iters, cvType=5, fix_quirks=wt["fix_quirks"])
             s = b.strides[0]
             pad = lambda a: np.pad(a, ((0, 0), (0, s - W))).astype(np.float32)  # noqa: E731
             ts_ = TemporalBatchSolver(net, b, (W, H), Ks[0], sch["warm_level"], sch["warps"],
                                       sch["iters"])
             guard = SequenceGuard(n)
-            ratios = []
+            ceil_net = table0.get(key(W, H, "network"), {}).get("ceiling")
             for k in range(frames - 1):
                 for i, q in enumerate(seqs):
-                    b.copyImagesToDevice(i, pad(q["frames"][k]), pad(q["frames"][k + 1]))
+                    for x in (b, pb):
+                        x.copyImagesToDevice(i, pad(q["frames"][k]), pad(q["frames"][k + 1]))
                 Rs = [q["pairs"][k]["R"] for q in seqs]
                 tt = [q["pairs"][k]["t"] for q in seqs]
                 if k == 0:
@@ -179,15 +205,25 @@ def calibrate(out: str = TABLE, log=print) -> dict:
                 else:
                     ts_.next(Ks, [q["pairs"][k - 1]["R"] for q in seqs],
                              [q["pairs"][k - 1]["t"] for q in seqs], Rs, tt)
-                e_k = b.energies()
+                e = b.energies()
+                pb.solveR(Rs, tt)
+                ep = pb.energies()
                 for i in range(n):
-                    q = guard.ratio(i, e_k[i] / (W * H))
+                    q = guard.ratio(i, e[i] / npx)
                     if q is not None and np.isfinite(q):
                         ratios.append(q)
-                    guard.over(i, e_k[i], W * H, None)
-                per_px += list(e_k / (W * H))
-            b.close()
-            net.close()
+                    bad = guard.over(i, e[i], npx, ceil_net)
+                    flags.append(bad)
+                    over_plain.append(bool(np.isfinite(e[i]) and (
+                        not np.isfinite(ep[i]) or e[i] > (1 + MARGIN) * ep[i])))
+                    if bad:
+                        f.setCameraMatrices(Ks[i], Ks[i])
+                        f.copyImagesToDeviceFromDevice(*b.imagePlanes(i, 0), s)
+                        f.solveR(Rs[i], tt[i], 5.0)
+                        b.importResults(i, f.deviceResults(), f.stride)
+                per_px += list(e / npx)
+            for x in (b, pb, net, f):
+                x.close()
             seeds = [seed0, seed0 + n - 1]
         torch.cuda.synchronize()
         e = np.array(per_px)
@@ -198,26 +234,32 @@ def calibrate(out: str = TABLE, log=print) -> dict:
                "energy_per_px_max": top}
         if source == "network":
             ent["ceiling"] = top * (1.0 + MARGIN)
-            tail = ""
+            flags = [False] * len(per_px)  # the ceiling is their maximum: nothing is over
         else:
             r = np.array(ratios)
             ent.update(history=HISTORY, history_factor=HISTORY_FACTOR,
                        history_ratio_median=float(np.median(r)),
                        history_ratio_p99=float(np.percentile(r, 99)),
-                       history_ratio_max=float(r.max()),
-                       history_flags=int((r > HISTORY_FACTOR).sum()))
-            tail = (f"; history ratio median {ent['history_ratio_median']:.3f}, max "
-                    f"{ent['history_ratio_max']:.3f}, flags {ent['history_flags']}")
+                       history_ratio_max=float(r.max()))
+        ent.update(flagged=int(sum(flags)), over_plain_margin=int(sum(over_plain)),
+                   flagged_and_over=int(sum(a and c for a, c in zip(flags, over_plain))))
         entries[key(W, H, source)] = ent
+        table0 = entries
         log(f"{key(W, H, source)}: {e.size} pairs, energy per pixel median "
-            f"{ent['energy_per_px_median']:.3f}, max {top:.3f}" + tail)
+            f"{ent['energy_per_px_median']:.3f}, max {top:.3f}; flagged {ent['flagged']}, over "
+            f"the plain solve's energy {ent['over_plain_margin']}, both "
+            f"{ent['flagged_and_over']}"
+            + ("" if source == "network" else
+               f"; history ratio median {ent['history_ratio_median']:.3f}, "
+               f"max {ent['history_ratio_max']:.3f}"))
     table = {"margin": MARGIN, "entries": entries,
              "command": "python -m reconflow_gb300.fallback --calibrate",
              "what": "network: ceiling = (1 + margin) x the largest learned-solution energy "
                      "per pixel of the calibration set; temporal: a pair falls back when its "
                      "energy per pixel exceeds history_factor x the median of its sequence's "
-                     "last `history` pairs (the ratio's distribution on the calibration "
-                     "sequences recorded)"}
+                     "last `history` pairs (the first pair: the network ceiling); flagged / "
+                     "over_plain_margin / flagged_and_over: pairs the test flags, pairs whose "
+                     "energy exceeds (1 + margin) x their plain solve's, and both"}
     with open(out, "w") as fh:
         json.dump(table, fh, indent=1)
     return table

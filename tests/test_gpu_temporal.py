@@ -73,6 +73,7 @@ def test_sequence_chain_equals_single_pair_warm_solve(torch_cuda, rf):
     (rf_ws_state) and refined for pair 1 in the batch: the result equals the
     single-pair warm solve (rf_solve_warm) from the same warm state bit for
     bit, and the carried grid is close to frame 1's true inverse depth."""
+    from oracle import temporal_oracle as TO
     from reconflow_gb300 import scene as S
     from reconflow_gb300.reconflow import ReconFlowBatch
     from reconflow_gb300.warmstart import SOLVER_WEIGHTS, level_intrinsics, propagate, state
@@ -91,13 +92,24 @@ def test_sequence_chain_equals_single_pair_warm_solve(torch_cuda, rf):
     grid = T.zeros((1, hn, wn, 3), device="cuda")
     propagate([b.deviceResults(0)[4]], w, h, s, [K], [p0["R"]], [p0["t"]], f, grid)
     b.synchronize()
-    truth = np.where(p1["valid"], p1["inv_depth"], np.nan)
-    with np.errstate(invalid="ignore"):
-        tc = np.nanmax(truth[:hn * f, :wn * f].reshape(hn, f, wn, f), axis=(1, 3))
-    ok = np.isfinite(tc)
-    rel = np.abs(grid.cpu().numpy()[0, ..., 2][ok] - tc[ok]) / tc[ok]
-    # the solve's depth is ~5% off at the median on this forward-moving pair
-    assert np.median(rel) < 0.1
+    # the carried grid equals the float32 restatement on the solved depth
+    Z0 = b.copy3dToHost(0)[2][:h, :w]
+    want = TO.propagate_depth_f32(Z0, K, p0["R"], p0["t"], f, (hn, wn))
+    g = grid.cpu().numpy()[0, ..., 2]
+    assert np.array_equal(g.view(np.uint32), want.view(np.uint32))
+    # and is as close to frame 1's true inverse depth (cell means) as the
+    # solve's own depth is to frame 0's: carrying adds no error of its own
+    t0 = np.where(p0["valid"], p0["inv_depth"], np.nan)
+    with np.errstate(invalid="ignore", divide="ignore"):
+        inv0 = 1.0 / Z0
+        ok0 = np.isfinite(t0) & np.isfinite(inv0)
+        e_solve = float(np.median(np.abs(inv0[ok0] - t0[ok0]) / t0[ok0]))
+        truth = np.where(p1["valid"], p1["inv_depth"], np.nan)
+        tc = np.nanmean(truth[:hn * f, :wn * f].reshape(hn, f, wn, f), axis=(1, 3))
+    ok = np.isfinite(tc) & (g > 0)
+    e_carry = float(np.median(np.abs(g[ok] - tc[ok]) / tc[ok]))
+    assert ok.sum() > 0.5 * hn * wn
+    assert e_carry < 1.5 * e_solve + 0.02, (e_carry, e_solve)
     # warm state for pair 1 at level 2, into the batch's warm planes and into
     # tensors of our own for the single-pair solve (the same kernel, the same
     # inputs: the same bits)
