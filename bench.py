@@ -1784,7 +1784,12 @@ def main():
     ap.add_argument("--solve-only", action="store_true",
                     help="only warm-up + timed solves (for profiler launch lists)")
     ap.add_argument("--fallback", default=None, choices=["plain", "none"],
-                    help="c5-stream: the fallback test's reference energy (default plain)")
+                    help="learned workloads: compare with the pair's own plain-solve energy "
+                         "(computed untimed) or take no fallback (default: the calibrated, "
+                         "deployable test)")
+    ap.add_argument("--checkpoint", default=None,
+                    help="learned workloads: the network weights (default: the committed "
+                         "checkpoint)")
     ap.add_argument("--warm", default=None, choices=["temporal", "network"],
                     help="c5-stream: warm start of waves after the first (default temporal)")
     ap.add_argument("--dump", default=None,
@@ -1794,6 +1799,8 @@ def main():
                          "default: the workload's)")
     args = ap.parse_args()
     wl = WORKLOADS[args.workload]
+    if args.checkpoint and "checkpoint" in wl:
+        wl = dict(wl, checkpoint=args.checkpoint)
     world, rank, local = dist_setup(args)
     if args.impl == "reference":
         if "net" in wl:

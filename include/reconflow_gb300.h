@@ -374,6 +374,11 @@ RF_API rf_status rf_batch_import_results(rf_batch* b, int pair, const float* u, 
                                          const float* X, const float* Y, const float* Z,
                                          int pitch);
 RF_API rf_status rf_batch_set_stream(rf_batch* b, void* stream);
+/* The stream the batch's work is enqueued on (the one set by
+ * rf_batch_set_stream, else the batch's own non-blocking stream): kernels
+ * that feed the batch (warm-start features, network, state) go on it so
+ * that they are ordered with the solve.  No reference counterpart. */
+RF_API rf_status rf_batch_get_stream(rf_batch* b, void** stream);
 RF_API rf_status rf_batch_synchronize(rf_batch* b);
 RF_API uint64_t rf_batch_kernel_launches(const rf_batch* b);
 

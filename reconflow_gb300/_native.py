@@ -122,6 +122,7 @@ _SIGS = [
     ("rf_batch_device_results", _I, [_VP, _I, _VP, _VP, _VP, _VP, _VP]),
     ("rf_batch_import_results", _I, [_VP, _I, _VP, _VP, _VP, _VP, _VP, _I]),
     ("rf_batch_set_stream", _I, [_VP, _VP]),
+    ("rf_batch_get_stream", _I, [_VP, ctypes.POINTER(ctypes.c_void_p)]),
     ("rf_batch_synchronize", _I, [_VP]),
     ("rf_batch_kernel_launches", ctypes.c_uint64, [_VP]),
     ("rf_cnn_create", _I, [_I, _I, _I, ctypes.c_ulonglong, ctypes.POINTER(_VP)]),

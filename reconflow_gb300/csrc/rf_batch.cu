@@ -22,6 +22,7 @@
 #include <cstdlib>
 #include <cstring>
 #include <string>
+#include <type_traits>
 #include <vector>
 
 #include <cuda_runtime.h>
@@ -109,6 +110,31 @@ __global__ void __launch_bounds__(kMaxTile) k_batch(BatchCtx ctx, int level, Op 
     const int ix = t.x0 + (int)threadIdx.x, iy = t.y0 + (int)threadIdx.y;
     if (ix >= d.w || iy >= d.h) return;
     op(ctx, t, level, d, ix, iy);
+}
+
+// The same with a register budget for `MINB` resident blocks of kMaxTile
+// threads per SM (RF_BATCH_MINBLOCKS_A / _B select it for the data and the
+// dual step; 1 = the kernel above).
+template <class Op, int MINB>
+__global__ void __launch_bounds__(kMaxTile, MINB) k_batch_occ(BatchCtx ctx, int level, Op op) {
+    prefetch_ahead(ctx, ctx.tiles, (int)blockIdx.x + ctx.prefetch, (int)gridDim.x, level, op);
+    const TileEntry t = ctx.tiles[blockIdx.x];
+    const LevelDims d = ctx.pairs[t.pair].dims[level];
+    const int ix = t.x0 + (int)threadIdx.x, iy = t.y0 + (int)threadIdx.y;
+    if (ix >= d.w || iy >= d.h) return;
+    op(ctx, t, level, d, ix, iy);
+}
+
+// Two rows per thread: the block is the tile's width by half its height;
+// thread (x, y) takes tile rows 2y and 2y + 1 (Op::two), so operations whose
+// neighbouring rows share work (the 5x5 medians) do it once.
+template <class Op>
+__global__ void __launch_bounds__(kMaxTile) k_batch_rows2(BatchCtx ctx, int level, Op op) {
+    const TileEntry t = ctx.tiles[blockIdx.x];
+    const LevelDims d = ctx.pairs[t.pair].dims[level];
+    const int ix = t.x0 + (int)threadIdx.x, iy = t.y0 + 2 * (int)threadIdx.y;
+    if (ix >= d.w || iy >= d.h) return;
+    op.two(t, d, ix, iy);
 }
 
 // WarpImage + ComputeDerivatives fused (warp_deriv_tile): one block = one
@@ -267,6 +293,25 @@ struct OpMedianAdd {
         ou[pos] = a;
         ov[pos] = b;
     }
+    // pixels (ix, iy) and (ix, iy + 1) (the second when inside the level)
+    __device__ void two(const TileEntry& t, LevelDims d, int ix, int iy) const {
+        float mu[2], mv[2];
+        median5_pair2(duhat, dvhat, ix, iy, d, mu, mv, t.off);
+        const int pos = t.off + ix + iy * d.s;
+        const bool has1 = iy + 1 < d.h;
+        const float a0 = u[pos] + mu[0], b0 = v[pos] + mv[0];
+        float a1 = 0.0f, b1 = 0.0f;
+        if (has1) {
+            a1 = u[pos + d.s] + mu[1];
+            b1 = v[pos + d.s] + mv[1];
+        }
+        ou[pos] = a0;
+        ov[pos] = b0;
+        if (has1) {
+            ou[pos + d.s] = a1;
+            ov[pos + d.s] = b1;
+        }
+    }
 };
 
 struct OpMedian5 {
@@ -280,6 +325,17 @@ struct OpMedian5 {
         median5_pair(u, v, ix, iy, d, mu, mv, t.off);
         ou[t.off + ix + iy * d.s] = mu;
         ov[t.off + ix + iy * d.s] = mv;
+    }
+    __device__ void two(const TileEntry& t, LevelDims d, int ix, int iy) const {
+        float mu[2], mv[2];
+        median5_pair2(u, v, ix, iy, d, mu, mv, t.off);
+        const int pos = t.off + ix + iy * d.s;
+        ou[pos] = mu[0];
+        ov[pos] = mv[0];
+        if (iy + 1 < d.h) {
+            ou[pos + d.s] = mu[1];
+            ov[pos + d.s] = mv[1];
+        }
     }
 };
 
@@ -395,6 +451,7 @@ struct rf_batch {
     // iteration apart); 0 = every inner half-iteration over all pairs at once
     int split = 0;
     int prefetch = 0;  // L2 prefetch distance of the inner-iteration launches, in blocks
+    int minb_a = 1, minb_b = 1;  // resident-block target of the data / dual step kernels
     bool solved = false;
     int n_planes = 0;
     // pipelined transfers (rf_batch_stage_upload / rf_batch_stage_download):
@@ -496,7 +553,33 @@ int launch_op(rf_batch* b, int level, const Op& op) {
     int tiles = b->prefix[level * (b->n + 1) + b->n];
     if (tiles <= 0) return 0;
     const dim3 block(b->tile_w[level], b->tile_h[level]);
-    k_batch<Op><<<tiles, block, 0, b->stream>>>(ctx_of(b, level), level, op);
+    constexpr bool is_a = std::is_same<Op, OpReconA>::value;
+    constexpr bool is_b = std::is_same<Op, OpReconB>::value;
+    if constexpr (is_a || is_b) {
+        const int minb = is_a ? b->minb_a : b->minb_b;
+        if (minb == 5)
+            k_batch_occ<Op, 5><<<tiles, block, 0, b->stream>>>(ctx_of(b, level), level, op);
+        else if (minb == 6)
+            k_batch_occ<Op, 6><<<tiles, block, 0, b->stream>>>(ctx_of(b, level), level, op);
+        else
+            k_batch<Op><<<tiles, block, 0, b->stream>>>(ctx_of(b, level), level, op);
+    } else {
+        k_batch<Op><<<tiles, block, 0, b->stream>>>(ctx_of(b, level), level, op);
+    }
+    b->enq++;
+    return rf::launch_status();
+}
+
+// an operation with a two-row form (Op::two) over the level's tiles, two
+// rows per thread where the tile height is even (the one-row kernel if not)
+template <class Op>
+int launch_op_rows2(rf_batch* b, int level, const Op& op) {
+    const int th = b->tile_h[level];
+    if (th % 2 != 0) return launch_op(b, level, op);
+    int tiles = b->prefix[level * (b->n + 1) + b->n];
+    if (tiles <= 0) return 0;
+    k_batch_rows2<Op><<<tiles, dim3(b->tile_w[level], th / 2), 0, b->stream>>>(ctx_of(b, level),
+                                                                              level, op);
     b->enq++;
     return rf::launch_status();
 }
@@ -650,11 +733,11 @@ rf_status enqueue_batch(rf_batch* b, int kind) {
                 if (rs != RF_OK) return rs;
             }
             if (recon) {
-                BL(launch_op(b, level, OpMedianAdd{PB(P(P_DUHAT)), PB(P(P_DVHAT)), PB(u), PB(v),
+                BL(launch_op_rows2(b, level, OpMedianAdd{PB(P(P_DUHAT)), PB(P(P_DVHAT)), PB(u), PB(v),
                                                    PB(tu), PB(tv)}));
-                BL(launch_op(b, level, OpMedian5{PB(tu), PB(tv), PB(u), PB(v)}));
+                BL(launch_op_rows2(b, level, OpMedian5{PB(tu), PB(tv), PB(u), PB(v)}));
             } else {
-                BL(launch_op(b, level, OpMedianAdd{PB(P(P_DUHAT)), PB(P(P_DVHAT)), PB(u), PB(v),
+                BL(launch_op_rows2(b, level, OpMedianAdd{PB(P(P_DUHAT)), PB(P(P_DVHAT)), PB(u), PB(v),
                                                    PB(u), PB(v)}));
             }
         }
@@ -822,6 +905,10 @@ rf_status rf_batch_create(const rf_params* p, int n_pairs, const int* widths, co
         cudaGetDevice(&dev);
         cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
         b->prefetch = waves > 0.0 ? (int)(waves * sms * 16) : 0;
+        const char* ma = std::getenv("RF_BATCH_MINBLOCKS_A");
+        const char* mb = std::getenv("RF_BATCH_MINBLOCKS_B");
+        b->minb_a = ma ? std::atoi(ma) : 1;
+        b->minb_b = mb ? std::atoi(mb) : 1;
     }
     if (e == cudaSuccess) e = fill_tiles(b);
     if (e == cudaSuccess) e = rf::dev_malloc((void**)&b->d_pairs, sizeof(BatchPair) * n_pairs);
@@ -1341,6 +1428,12 @@ rf_status rf_batch_set_stream(rf_batch* b, void* stream) {
     if (!b) return bfail(RF_ERR_INVALID_ARG, "rf_batch_set_stream: null batch");
     BC(cudaStreamSynchronize(b->stream));
     b->stream = stream ? static_cast<cudaStream_t>(stream) : b->own;
+    return RF_OK;
+}
+
+rf_status rf_batch_get_stream(rf_batch* b, void** stream) {
+    if (!b || !stream) return bfail(RF_ERR_INVALID_ARG, "rf_batch_get_stream: null argument");
+    *stream = static_cast<void*>(b->stream);
     return RF_OK;
 }
 

@@ -288,29 +288,44 @@ __global__ void k_plain_tv(const float* __restrict__ duhat, const float* __restr
 // 5x5 medians (medianFilter.cu:3-75): taps clamp along one axis, 0 at corners
 // ---------------------------------------------------------------------------
 // u + median5(duhat): MedianFilter then Add (Reconflow.cu:410-416)
+// Both 5x5 median kernels take two rows per thread (pixels (ix, iy) and
+// (ix, iy + 1), iy even): the windows share 20 taps (median5_pair2).
 __global__ void k_median_add(const float* __restrict__ duhat, const float* __restrict__ dvhat,
                              const float* u, const float* v, float* ou, float* ov, LevelDims d) {
     int ix = blockIdx.x * blockDim.x + threadIdx.x;
-    int iy = blockIdx.y * blockDim.y + threadIdx.y;
+    int iy = 2 * (blockIdx.y * blockDim.y + threadIdx.y);
     if (ix >= d.w || iy >= d.h) return;
-    float mu, mv;
-    median5_pair(duhat, dvhat, ix, iy, d, mu, mv);
-    int pos = ix + iy * d.s;
-    float a = u[pos] + mu;
-    float b = v[pos] + mv;
-    ou[pos] = a;
-    ov[pos] = b;
+    float mu[2], mv[2];
+    median5_pair2(duhat, dvhat, ix, iy, d, mu, mv);
+    const int pos = ix + iy * d.s;
+    const bool has1 = iy + 1 < d.h;
+    const float a0 = u[pos] + mu[0], b0 = v[pos] + mv[0];
+    float a1 = 0.0f, b1 = 0.0f;
+    if (has1) {
+        a1 = u[pos + d.s] + mu[1];
+        b1 = v[pos + d.s] + mv[1];
+    }
+    ou[pos] = a0;
+    ov[pos] = b0;
+    if (has1) {
+        ou[pos + d.s] = a1;
+        ov[pos + d.s] = b1;
+    }
 }
 
 __global__ void k_median5(const float* __restrict__ u, const float* __restrict__ v,
                           float* __restrict__ ou, float* __restrict__ ov, LevelDims d) {
     int ix = blockIdx.x * blockDim.x + threadIdx.x;
-    int iy = blockIdx.y * blockDim.y + threadIdx.y;
+    int iy = 2 * (blockIdx.y * blockDim.y + threadIdx.y);
     if (ix >= d.w || iy >= d.h) return;
-    float mu, mv;
-    median5_pair(u, v, ix, iy, d, mu, mv);
-    ou[ix + iy * d.s] = mu;
-    ov[ix + iy * d.s] = mv;
+    float mu[2], mv[2];
+    median5_pair2(u, v, ix, iy, d, mu, mv);
+    ou[ix + iy * d.s] = mu[0];
+    ov[ix + iy * d.s] = mv[0];
+    if (iy + 1 < d.h) {
+        ou[ix + (iy + 1) * d.s] = mu[1];
+        ov[ix + (iy + 1) * d.s] = mv[1];
+    }
 }
 
 __global__ void k_median3d(const float* __restrict__ X, const float* __restrict__ Y,
@@ -729,13 +744,14 @@ int launch_plain_tv(const float* duhat, const float* dvhat, float* pu1, float* p
 
 int launch_median_add(const float* duhat, const float* dvhat, const float* u, const float* v,
                       float* ou, float* ov, LevelDims d, cudaStream_t st) {
-    k_median_add<<<grid_for(d.w, d.h), dim3(BX, BY), 0, st>>>(duhat, dvhat, u, v, ou, ov, d);
+    k_median_add<<<grid_for(d.w, (d.h + 1) / 2), dim3(BX, BY), 0, st>>>(duhat, dvhat, u, v, ou,
+                                                                       ov, d);
     return check_launch();
 }
 
 int launch_median5(const float* u, const float* v, float* ou, float* ov, LevelDims d,
                    cudaStream_t st) {
-    k_median5<<<grid_for(d.w, d.h), dim3(BX, BY), 0, st>>>(u, v, ou, ov, d);
+    k_median5<<<grid_for(d.w, (d.h + 1) / 2), dim3(BX, BY), 0, st>>>(u, v, ou, ov, d);
     return check_launch();
 }
 

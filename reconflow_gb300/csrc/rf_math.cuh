@@ -379,6 +379,77 @@ __device__ __forceinline__ void sortnet25(float (&s)[25], std::integer_sequence<
     (cmp_exchange<sortnet25_count_or_pair(C, 0), sortnet25_count_or_pair(C, 1)>(s), ...);
 }
 
+// The same construction for any key count N <= 32 (comparators of the
+// 32-key merge sort whose keys are both below N); used for the 20 shared
+// and the 5 own taps of two vertically adjacent 5x5 windows.
+template <int N>
+constexpr int batcher_count_or_pair(int want, int which) {
+    int n = 0;
+    for (int p = 1; p < 32; p <<= 1)
+        for (int k = p; k >= 1; k >>= 1)
+            for (int j = k % p; j + k < 32; j += 2 * k)
+                for (int i = 0; i < k && i < 32 - j - k; i++)
+                    if ((i + j) / (2 * p) == (i + j + k) / (2 * p) && i + j + k < N) {
+                        if (n == want) return which == 0 ? i + j : i + j + k;
+                        n++;
+                    }
+    return n;
+}
+
+template <int N, int A, int B>
+__device__ __forceinline__ void cmp_exchange_n(float (&s)[N]) {
+    const float lo = fminf(s[A], s[B]);
+    s[B] = fmaxf(s[A], s[B]);
+    s[A] = lo;
+}
+
+template <int N, int... C>
+__device__ __forceinline__ void batcher_sort_seq(float (&s)[N], std::integer_sequence<int, C...>) {
+    (cmp_exchange_n<N, batcher_count_or_pair<N>(C, 0), batcher_count_or_pair<N>(C, 1)>(s), ...);
+}
+
+template <int N>
+__device__ __forceinline__ void batcher_sort(float (&s)[N]) {
+    batcher_sort_seq(s, std::make_integer_sequence<int, batcher_count_or_pair<N>(-1, 0)>{});
+}
+
+// Medians of two vertically adjacent 5x5 windows.  `w` holds six rows of
+// five taps: pixel 0's window is rows 0-4, pixel 1's rows 1-5.  The 20 taps
+// of rows 1-4 are sorted once (A) and each pixel's own row (B) on its own;
+// the 13th smallest of the union of the sorted A and B is
+// min over i = 0..5 of max(A[12 - i], B[i - 1]) (i taps taken from B;
+// B[-1] = -inf), the selection of the k-th element of two sorted lists.
+// Without NaN inputs every min / max returns one of its operands, so a
+// non-zero result is bitwise the value the reference's exchange selection
+// returns (equal non-zero floats have equal bits); returns false when an
+// input is NaN, and the caller takes the exchange path (also for a zero
+// result, whose sign the exchange order decides).
+__device__ __forceinline__ bool median25_two(const float (&w)[30], float& m0, float& m1) {
+    bool nan_in = false;
+#pragma unroll
+    for (int k = 0; k < 30; k++) nan_in |= isnan(w[k]);
+    if (nan_in) return false;
+    float A[20], B0[5], B1[5];
+#pragma unroll
+    for (int k = 0; k < 20; k++) A[k] = w[5 + k];
+#pragma unroll
+    for (int k = 0; k < 5; k++) {
+        B0[k] = w[k];
+        B1[k] = w[25 + k];
+    }
+    batcher_sort(A);
+    batcher_sort(B0);
+    batcher_sort(B1);
+    m0 = A[12];
+    m1 = A[12];
+#pragma unroll
+    for (int i = 1; i <= 5; i++) {
+        m0 = fminf(m0, fmaxf(A[12 - i], B0[i - 1]));
+        m1 = fminf(m1, fmaxf(A[12 - i], B1[i - 1]));
+    }
+    return true;
+}
+
 // Median of 25 with the min/max network above, sorting `s` in place.  For
 // inputs without NaN the network's key 12 is the value the exchange
 // selection (median25_exchange) returns, except possibly for the sign of a

@@ -319,6 +319,63 @@ __device__ __forceinline__ void median5_pair(const float* __restrict__ a,
     if (!median25_net(mv, mb)) mb = median25_slow(b, ix, iy, d, base, interior);
 }
 
+// Six rows of five taps around (ix, iy): rows iy-2 .. iy+3, the 5x5
+// windows of (ix, iy) and (ix, iy+1) with the reference's border rules
+// (median5_tap: the rule depends only on the tap's position, so a tap
+// shared by both windows has one value).  `interior`: every tap inside.
+__device__ __forceinline__ void load_window30(const float* __restrict__ a, int ix, int iy,
+                                              LevelDims d, int base, bool interior,
+                                              float (&m)[30]) {
+    if (interior) {
+        const float* p = a + base + ix + iy * d.s;
+#pragma unroll
+        for (int j = 0; j < 6; j++)
+#pragma unroll
+            for (int i = 0; i < 5; i++) m[j * 5 + i] = p[(i - 2) + (j - 2) * d.s];
+    } else {
+#pragma unroll
+        for (int j = 0; j < 6; j++)
+#pragma unroll
+            for (int i = 0; i < 5; i++) {
+                int at = median5_tap(ix + i - 2, iy + j - 2, d.w, d.h, d.s);
+                m[j * 5 + i] = at >= 0 ? a[base + at] : 0.0f;
+            }
+    }
+}
+
+// MedianFilterKernel5 (medianFilter.cu:3-76) of two fields at (ix, iy) and
+// (ix, iy + 1) (the second only when iy + 1 < d.h; its outputs are then
+// unused otherwise): 20 of each window's 25 taps are shared, sorted once
+// (median25_two); NaN inputs or a zero result take the exchange path of the
+// pixel concerned, as median5_pair does.
+__device__ __forceinline__ void median5_pair2(const float* __restrict__ a,
+                                              const float* __restrict__ b, int ix, int iy,
+                                              LevelDims d, float (&ma)[2], float (&mb)[2],
+                                              int base = 0) {
+    const bool in_x = ix >= 2 && ix + 2 < d.w;
+    const bool interior = in_x && iy >= 2 && iy + 3 < d.h;
+    const bool in0 = in_x && iy >= 2 && iy + 2 < d.h;
+    const bool in1 = in_x && iy + 1 >= 2 && iy + 3 < d.h;
+    const bool has1 = iy + 1 < d.h;
+    float w[30];
+    load_window30(a, ix, iy, d, base, interior, w);
+    if (!median25_two(w, ma[0], ma[1])) {
+        ma[0] = median25_slow(a, ix, iy, d, base, in0);
+        ma[1] = has1 ? median25_slow(a, ix, iy + 1, d, base, in1) : 0.0f;
+    } else {
+        if (ma[0] == 0.0f) ma[0] = median25_slow(a, ix, iy, d, base, in0);
+        if (has1 && ma[1] == 0.0f) ma[1] = median25_slow(a, ix, iy + 1, d, base, in1);
+    }
+    load_window30(b, ix, iy, d, base, interior, w);
+    if (!median25_two(w, mb[0], mb[1])) {
+        mb[0] = median25_slow(b, ix, iy, d, base, in0);
+        mb[1] = has1 ? median25_slow(b, ix, iy + 1, d, base, in1) : 0.0f;
+    } else {
+        if (mb[0] == 0.0f) mb[0] = median25_slow(b, ix, iy, d, base, in0);
+        if (has1 && mb[1] == 0.0f) mb[1] = median25_slow(b, ix, iy + 1, d, base, in1);
+    }
+}
+
 // warpImage.cu:15-29
 __device__ __forceinline__ void warp_px(const float* __restrict__ I1, const float* __restrict__ u,
                                         const float* __restrict__ v, LevelDims d,

@@ -549,6 +549,12 @@ class ReconFlowBatch:
     def setStream(self, stream_ptr):
         N.check(self._lib.rf_batch_set_stream(self._h, ctypes.c_void_p(stream_ptr or 0)))
 
+    def stream(self) -> int:
+        """The CUDA stream the batch enqueues on (rf_batch_get_stream)."""
+        st = ctypes.c_void_p()
+        N.check(self._lib.rf_batch_get_stream(self._h, ctypes.byref(st)))
+        return st.value or 0
+
     def synchronize(self):
         N.check(self._lib.rf_batch_synchronize(self._h))
 

@@ -385,16 +385,25 @@ class LearnedBatchSolver:
         self.up = float(self.factor) / float(2 ** warm_level)
         self.planes = [batch.warmPlanes(i) for i in range(n)]
         self.images = [batch.imagePlanes(i, 0) for i in range(n)]
-        self.stream = 0
+        # the buffers above were made on torch's stream; every later kernel
+        # runs on the batch's stream
+        torch.cuda.synchronize()
+
+    @property
+    def stream(self) -> int:
+        """The stream everything runs on: the batch's (ReconFlowBatch.stream)."""
+        return self.batch.stream()
 
     def set_stream(self, stream_ptr):
-        self.stream = stream_ptr or 0
+        """Run the features, the network, the state and the solve on this
+        stream (0 / None: the batch's own)."""
         self.batch.setStream(stream_ptr)
-        self.net.set_stream(stream_ptr)
 
     def predict(self, Ks, Rs, ts):
+        st = self.stream
+        self.net.set_stream(st)
         features([p[0] for p in self.images], [p[1] for p in self.images], self.w, self.h,
-                 self.batch.strides[0], self.factor, Ks, Rs, ts, self.x, self.stream)
+                 self.batch.strides[0], self.factor, Ks, Rs, ts, self.x, st)
         self.net.forward(self.x, self.o16, self.o8)
         return self.o16, self.o8
 
@@ -431,10 +440,13 @@ class TemporalBatchSolver:
         self.warm_level = warm_level
         self.t_warps = warps if temporal_warps is None else temporal_warps
         self.t_iters = iters if temporal_iters is None else temporal_iters
-        self.stream = 0
+        torch.cuda.synchronize()
+
+    @property
+    def stream(self) -> int:
+        return self.batch.stream()
 
     def set_stream(self, stream_ptr):
-        self.stream = stream_ptr or 0
         self.learned.set_stream(stream_ptr)
 
     def first(self, Ks, Rs, ts):

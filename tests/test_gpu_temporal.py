@@ -88,10 +88,13 @@ def test_sequence_chain_equals_single_pair_warm_solve(torch_cuda, rf):
     p0, p1 = q["pairs"][0], q["pairs"][1]
     b.copyImagesToDevice(0, pad_rows(q["frames"][0], s), pad_rows(q["frames"][1], s))
     b.solveR([p0["R"]], [p0["t"]])
+    # the batch solves on its own stream, the kernels below run on the
+    # default stream: order them by synchronising the device in between
+    b.synchronize()
     hn, wn = h // f, w // f
     grid = T.zeros((1, hn, wn, 3), device="cuda")
     propagate([b.deviceResults(0)[4]], w, h, s, [K], [p0["R"]], [p0["t"]], f, grid)
-    b.synchronize()
+    T.cuda.synchronize()
     # the carried grid equals the float32 restatement on the solved depth
     Z0 = b.copy3dToHost(0)[2][:h, :w]
     want = TO.propagate_depth_f32(Z0, K, p0["R"], p0["t"], f, (hn, wn))
@@ -121,6 +124,7 @@ def test_sequence_chain_equals_single_pair_warm_solve(torch_cuda, rf):
     own = [T.zeros((lh + 1) * lsd, device="cuda") for _ in range(5)]
     state(grid, lw, lh, lsd, up, [Kl], [p1["R"]], [p1["t"]], [[t.data_ptr() for t in own]])
     planes = [t.cpu().numpy().reshape(lh + 1, lsd)[:lh] for t in own]
+    T.cuda.synchronize()
     b.solveWarm(wl, [p1["R"]], [p1["t"]], 1, 10)
     u_b, v_b = b.copyOpticalFlowToHost(0)
     b.close()

@@ -220,6 +220,9 @@ def test_learned_batch_pipeline_runs(torch_cuda, rf):
         bt.copyImagesToDevice(i, pad_rows(sc["I0"], 640), pad_rows(sc["I1"], 640))
     ls = LearnedBatchSolver(net, bt, (640, 480), scs[0]["K"], warm_level=2, warps=1, iters=10)
     assert ls.factor == 4 and (ls.hn, ls.wn) == (120, 160)
+    # without set_stream every kernel of the pipeline goes on the batch's own
+    # (non-blocking) stream, ordered with the solve
+    assert ls.stream == bt.stream() != 0
     Ks, Rs, ts = [sc["K"] for sc in scs], [sc["R"] for sc in scs], [sc["t"] for sc in scs]
     ls.solve(Ks, Rs, ts)
     u, v = bt.copyOpticalFlowToHost(1)
