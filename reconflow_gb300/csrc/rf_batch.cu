@@ -22,7 +22,6 @@
 #include <cstdlib>
 #include <cstring>
 #include <string>
-#include <type_traits>
 #include <vector>
 
 #include <cuda_runtime.h>
@@ -104,19 +103,6 @@ __device__ __forceinline__ void prefetch_ahead(const BatchCtx& ctx, const TileEn
 // the block shape; the tile table gives the pair and the tile's origin).
 template <class Op>
 __global__ void __launch_bounds__(kMaxTile) k_batch(BatchCtx ctx, int level, Op op) {
-    prefetch_ahead(ctx, ctx.tiles, (int)blockIdx.x + ctx.prefetch, (int)gridDim.x, level, op);
-    const TileEntry t = ctx.tiles[blockIdx.x];
-    const LevelDims d = ctx.pairs[t.pair].dims[level];
-    const int ix = t.x0 + (int)threadIdx.x, iy = t.y0 + (int)threadIdx.y;
-    if (ix >= d.w || iy >= d.h) return;
-    op(ctx, t, level, d, ix, iy);
-}
-
-// The same with a register budget for `MINB` resident blocks of kMaxTile
-// threads per SM (RF_BATCH_MINBLOCKS_A / _B select it for the data and the
-// dual step; 1 = the kernel above).
-template <class Op, int MINB>
-__global__ void __launch_bounds__(kMaxTile, MINB) k_batch_occ(BatchCtx ctx, int level, Op op) {
     prefetch_ahead(ctx, ctx.tiles, (int)blockIdx.x + ctx.prefetch, (int)gridDim.x, level, op);
     const TileEntry t = ctx.tiles[blockIdx.x];
     const LevelDims d = ctx.pairs[t.pair].dims[level];
@@ -451,7 +437,6 @@ struct rf_batch {
     // iteration apart); 0 = every inner half-iteration over all pairs at once
     int split = 0;
     int prefetch = 0;  // L2 prefetch distance of the inner-iteration launches, in blocks
-    int minb_a = 1, minb_b = 1;  // resident-block target of the data / dual step kernels
     bool solved = false;
     int n_planes = 0;
     // pipelined transfers (rf_batch_stage_upload / rf_batch_stage_download):
@@ -553,19 +538,7 @@ int launch_op(rf_batch* b, int level, const Op& op) {
     int tiles = b->prefix[level * (b->n + 1) + b->n];
     if (tiles <= 0) return 0;
     const dim3 block(b->tile_w[level], b->tile_h[level]);
-    constexpr bool is_a = std::is_same<Op, OpReconA>::value;
-    constexpr bool is_b = std::is_same<Op, OpReconB>::value;
-    if constexpr (is_a || is_b) {
-        const int minb = is_a ? b->minb_a : b->minb_b;
-        if (minb == 5)
-            k_batch_occ<Op, 5><<<tiles, block, 0, b->stream>>>(ctx_of(b, level), level, op);
-        else if (minb == 6)
-            k_batch_occ<Op, 6><<<tiles, block, 0, b->stream>>>(ctx_of(b, level), level, op);
-        else
-            k_batch<Op><<<tiles, block, 0, b->stream>>>(ctx_of(b, level), level, op);
-    } else {
-        k_batch<Op><<<tiles, block, 0, b->stream>>>(ctx_of(b, level), level, op);
-    }
+    k_batch<Op><<<tiles, block, 0, b->stream>>>(ctx_of(b, level), level, op);
     b->enq++;
     return rf::launch_status();
 }
@@ -905,10 +878,6 @@ rf_status rf_batch_create(const rf_params* p, int n_pairs, const int* widths, co
         cudaGetDevice(&dev);
         cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
         b->prefetch = waves > 0.0 ? (int)(waves * sms * 16) : 0;
-        const char* ma = std::getenv("RF_BATCH_MINBLOCKS_A");
-        const char* mb = std::getenv("RF_BATCH_MINBLOCKS_B");
-        b->minb_a = ma ? std::atoi(ma) : 1;
-        b->minb_b = mb ? std::atoi(mb) : 1;
     }
     if (e == cudaSuccess) e = fill_tiles(b);
     if (e == cudaSuccess) e = rf::dev_malloc((void**)&b->d_pairs, sizeof(BatchPair) * n_pairs);

@@ -343,11 +343,24 @@ __device__ __forceinline__ void load_window30(const float* __restrict__ a, int i
     }
 }
 
+// The median of one pixel's window on its own (the network, then the
+// exchange path for NaN or zero): the two-pixel form's answer when either
+// window holds a NaN.  Out of line: it runs only for NaN inputs.
+__device__ __noinline__ float median25_single(const float* __restrict__ a, int ix, int iy,
+                                              LevelDims d, int base, bool interior) {
+    float m[25];
+    load_window25(a, ix, iy, d, base, interior, m);
+    float r;
+    if (!median25_net(m, r)) r = median25_slow(a, ix, iy, d, base, interior);
+    return r;
+}
+
 // MedianFilterKernel5 (medianFilter.cu:3-76) of two fields at (ix, iy) and
 // (ix, iy + 1) (the second only when iy + 1 < d.h; its outputs are then
 // unused otherwise): 20 of each window's 25 taps are shared, sorted once
-// (median25_two); NaN inputs or a zero result take the exchange path of the
-// pixel concerned, as median5_pair does.
+// (median25_two).  A NaN among the 30 taps sends both pixels to the
+// one-window path (the NaN may lie in one window only); a zero result takes
+// the exchange path of the pixel concerned, as median5_pair does.
 __device__ __forceinline__ void median5_pair2(const float* __restrict__ a,
                                               const float* __restrict__ b, int ix, int iy,
                                               LevelDims d, float (&ma)[2], float (&mb)[2],
@@ -360,16 +373,16 @@ __device__ __forceinline__ void median5_pair2(const float* __restrict__ a,
     float w[30];
     load_window30(a, ix, iy, d, base, interior, w);
     if (!median25_two(w, ma[0], ma[1])) {
-        ma[0] = median25_slow(a, ix, iy, d, base, in0);
-        ma[1] = has1 ? median25_slow(a, ix, iy + 1, d, base, in1) : 0.0f;
+        ma[0] = median25_single(a, ix, iy, d, base, in0);
+        ma[1] = has1 ? median25_single(a, ix, iy + 1, d, base, in1) : 0.0f;
     } else {
         if (ma[0] == 0.0f) ma[0] = median25_slow(a, ix, iy, d, base, in0);
         if (has1 && ma[1] == 0.0f) ma[1] = median25_slow(a, ix, iy + 1, d, base, in1);
     }
     load_window30(b, ix, iy, d, base, interior, w);
     if (!median25_two(w, mb[0], mb[1])) {
-        mb[0] = median25_slow(b, ix, iy, d, base, in0);
-        mb[1] = has1 ? median25_slow(b, ix, iy + 1, d, base, in1) : 0.0f;
+        mb[0] = median25_single(b, ix, iy, d, base, in0);
+        mb[1] = has1 ? median25_single(b, ix, iy + 1, d, base, in1) : 0.0f;
     } else {
         if (mb[0] == 0.0f) mb[0] = median25_slow(b, ix, iy, d, base, in0);
         if (has1 && mb[1] == 0.0f) mb[1] = median25_slow(b, ix, iy + 1, d, base, in1);
