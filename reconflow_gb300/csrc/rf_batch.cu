@@ -123,20 +123,6 @@ __global__ void __launch_bounds__(kMaxTile) k_batch_rows2(BatchCtx ctx, int leve
     op.two(t, d, ix, iy);
 }
 
-// WarpImage + ComputeDerivatives fused (warp_deriv_tile): one block = one
-// tile of one pair; the warped image stays in shared memory (dynamic,
-// 2 (tile_w + 4)(tile_h + 4) floats)
-__global__ void __launch_bounds__(kMaxTile) k_batch_warp_deriv(BatchCtx ctx, int level, int I0,
-                                                               int I1, int u, int v, int Ix,
-                                                               int Iy, int Iz) {
-    extern __shared__ float sm[];
-    const TileEntry t = ctx.tiles[blockIdx.x];
-    const LevelDims d = ctx.pairs[t.pair].dims[level];
-    warp_deriv_tile(plane_ptr(ctx, t, I0), plane_ptr(ctx, t, I1), plane_ptr(ctx, t, u),
-                    plane_ptr(ctx, t, v), d, t.x0, t.y0, (int)blockDim.x, (int)blockDim.y, sm,
-                    plane_ptr(ctx, t, Ix), plane_ptr(ctx, t, Iy), plane_ptr(ctx, t, Iz));
-}
-
 // Two operations in one launch on disjoint tile ranges of the level's table
 // (x: [x0, x0 + nx), y: [y0, y0 + ny)), their blocks interleaved (x, y, x,
 // y, ..., then the rest of the longer range) so that every SM holds blocks
@@ -557,18 +543,6 @@ int launch_op_rows2(rf_batch* b, int level, const Op& op) {
     return rf::launch_status();
 }
 
-int launch_warp_deriv(rf_batch* b, int level, int I0, int I1, int u, int v, int Ix, int Iy,
-                      int Iz) {
-    int tiles = b->prefix[level * (b->n + 1) + b->n];
-    if (tiles <= 0) return 0;
-    const int tw = b->tile_w[level], th = b->tile_h[level];
-    const size_t smem = sizeof(float) * 2 * (size_t)(tw + 4) * (th + 4);
-    k_batch_warp_deriv<<<tiles, dim3(tw, th), smem, b->stream>>>(ctx_of(b, level), level, I0, I1,
-                                                                 u, v, Ix, Iy, Iz);
-    b->enq++;
-    return rf::launch_status();
-}
-
 // Tile range of pair group g at `level`: group 0 = pairs [0, split), group
 // 1 = pairs [split, n).
 void group_tiles(const rf_batch* b, int level, int g, int& begin, int& count) {
@@ -664,8 +638,12 @@ rf_status enqueue_batch(rf_batch* b, int kind) {
         const int n_iters = warm ? b->warm_iters[level] : p.n_solver_iters;
         for (int warp = 0; warp < n_warps; warp++) {
             NvtxRange warp_range("batch level %d warp %d", level, warp);
-            BL(launch_warp_deriv(b, level, b->pI0(level), b->pI1(level), u, v, P(P_IX),
-                                 P(P_IY), P(P_IZ)));
+            // WarpImage and ComputeDerivatives as two launches: the fused
+            // shared-memory form recomputes its halo's warped values, which at
+            // the tuned level-0 tile (32 x 2) costs more than the warped
+            // image's round trip (0.312 vs 0.196 ms for 8 720p pairs)
+            BL(launch_op(b, level, OpWarp{b->pI1(level), u, v, P(P_I1W)}));
+            BL(launch_op(b, level, OpDeriv{b->pI0(level), P(P_I1W), P(P_IX), P(P_IY), P(P_IZ)}));
             const ReconFields r = fields_of(
                 b, ReconIdx{u, v, P(P_DUHAT), P(P_DVHAT), P(P_PU1), P(P_PU2), P(P_PV1), P(P_PV2),
                             uproj, vproj, sku, skv, P(P_IX), P(P_IY), P(P_IZ), P(P_X), P(P_Y),

@@ -311,6 +311,125 @@ __global__ void k_add(float* a, const float* b, size_t n) {
 
 inline unsigned blocks_for(size_t n, int t = 256) { return (unsigned)((n + t - 1) / t); }
 
+// ---- inference path on padded activations (rf_tc::k_tc_conv3) -------------
+// A padded buffer holds [B][H + 2][W + 2][C] BF16 with a zero one-pixel
+// border; interior pixel (b, y, x) is at position (b (H + 2) + y + 1)(W + 2)
+// + x + 1.  Borders are zeroed once at creation and never written.
+__device__ __forceinline__ size_t pad_pos(int b, int y, int x, int H, int W) {
+    return ((size_t)b * (H + 2) + y + 1) * (W + 2) + x + 1;
+}
+
+// FP32 input [B][H][W][16] -> padded BF16 interior, 8 channels per thread
+__global__ void k_pad_input(const float* in, int B, int H, int W, bf16* xp) {
+    size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    size_t n = (size_t)B * H * W * 2;
+    if (i >= n) return;
+    const int g = (int)(i % 2);
+    const size_t p = i / 2;
+    const int x = (int)(p % W), r = (int)(p / W), y = r % H, b = r / H;
+    const float* s = in + p * 16 + g * 8;
+    bf16 v[8];
+#pragma unroll
+    for (int e = 0; e < 8; e++) v[e] = __float2bfloat16(s[e]);
+    *(uint4*)(xp + pad_pos(b, y, x, H, W) * 16 + g * 8) = pack8(v);
+}
+
+// padded cat = [nearest 2x upsample of a (Ha x Wa x Ca), b (H x W x Cb)],
+// 8 channels per thread (Ca, Cb multiples of 8)
+__global__ void k_concat_up_pad(const bf16* a, int Ha, int Wa, int Ca, const bf16* bsrc, int Cb,
+                                int Bn, int H, int W, bf16* cat) {
+    const int C = Ca + Cb, G = C / 8;
+    size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    size_t n = (size_t)Bn * H * W * G;
+    if (i >= n) return;
+    const int c = (int)(i % G) * 8;
+    const size_t p = i / G;
+    const int x = (int)(p % W), r = (int)(p / W), y = r % H, bb = r / H;
+    uint4 v = c < Ca ? *(const uint4*)(a + pad_pos(bb, y / 2, x / 2, Ha, Wa) * Ca + c)
+                     : *(const uint4*)(bsrc + pad_pos(bb, y, x, H, W) * Cb + (c - Ca));
+    *(uint4*)(cat + pad_pos(bb, y, x, H, W) * C + c) = v;
+}
+
+// weights [co][tap][ci] -> the direct kernel's [stage][tap][NT / 8][2][8][8]
+// (co = 8 group + row, ci = 16 stage + 8 half + e; rows co >= cout are zero)
+__global__ void k_conv_wc(const bf16* w, int cin, int cout, int NT, bf16* wc) {
+    size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    const int ng = NT / 8;
+    size_t n = (size_t)(cin / 16) * 9 * NT * 16;
+    if (i >= n) return;
+    const int e = (int)(i % 8), r = (int)(i / 8 % 8), kh = (int)(i / 64 % 2);
+    const int gi = (int)(i / 128 % ng), t = (int)(i / (128 * (size_t)ng) % 9);
+    const int j = (int)(i / (128 * (size_t)ng * 9));
+    const int co = gi * 8 + r, ci = 16 * j + 8 * kh + e;
+    wc[i] = co < cout ? w[((size_t)co * 9 + t) * cin + ci] : __float2bfloat16(0.f);
+}
+
+// epilogue of the direct kernel: + bias, optional ReLU; BF16 into the padded
+// output (same geometry as the input) and / or FP32 into an unpadded
+// [B][H][W][cout_f] buffer
+struct ConvOutPadded {
+    const float* bias;
+    int nbias;
+    bf16* y;  // padded [pos][cout] or null
+    int cout;
+    float* yf;  // unpadded FP32 or null
+    int cout_f;
+    int relu, H, W, npos;
+    __device__ int pos(int q) const {
+        if (q >= npos) return -1;
+        const int Wp = W + 2, Hp = H + 2;
+        const int x = q % Wp, r = q / Wp, yy = r % Hp, b = r / Hp;
+        if (x < 1 || x > W || yy < 1 || yy > H) return -1;
+        return (b * H + yy - 1) * W + (x - 1);
+    }
+    __device__ void store(int q, int p, int c, const float (&v)[8]) const {
+        float o[8];
+#pragma unroll
+        for (int e = 0; e < 8; e++) {
+            float t = v[e] + (c + e < nbias ? bias[c + e] : 0.f);
+            o[e] = relu ? fmaxf(t, 0.f) : t;
+        }
+        if (y && c < cout) {
+            bf16 h[8];
+#pragma unroll
+            for (int e = 0; e < 8; e++) h[e] = __float2bfloat16(o[e]);
+            *(uint4*)(y + (size_t)q * cout + c) = pack8(h);
+        }
+        if (yf)
+#pragma unroll
+            for (int e = 0; e < 8; e++)
+                if (c + e < cout_f) yf[(size_t)p * cout_f + c + e] = o[e];
+    }
+};
+
+// the stride-2 layer keeps the im2col GEMM: its input and output padded
+struct TcConvInPadded {
+    static constexpr bool kAsync = true;
+    const bf16* x;
+    int H, W, C, Ho, Wo, stride;
+    __device__ const void* base() const { return x; }
+    __device__ const void* src(int m, int k) const {
+        int ci = k % C, t = k / C, kx = t % 3, ky = t / 3;
+        int xo = m % Wo, r = m / Wo, yo = r % Ho, b = r / Ho;
+        // padded coordinates: the border supplies the zeros of the padding
+        int y = yo * stride + ky, xx = xo * stride + kx;
+        return x + (((size_t)b * (H + 2) + y) * (W + 2) + xx) * C + ci;
+    }
+};
+
+struct ConvOutToPadded {
+    const float* bias;
+    bf16* y;
+    int M, Cout, relu, Ho, Wo;
+    __device__ void operator()(int, int m, int n, float v) const {
+        if (m >= M || n >= Cout) return;
+        v += bias[n];
+        if (relu) v = fmaxf(v, 0.f);
+        int xo = m % Wo, r = m / Wo, yo = r % Ho, b = r / Ho;
+        y[pad_pos(b, yo, xo, Ho, Wo) * Cout + n] = __float2bfloat16(v);
+    }
+};
+
 struct Layer {
     int cin, cout, stride, relu;
     size_t woff, boff;  // offsets into the parameter vector
@@ -341,6 +460,13 @@ struct rf_cnn {
     double* d_loss = nullptr;
     cudaStream_t stream = nullptr;
     uint64_t launches = 0;
+    // inference on padded activations (forward at the allocated size)
+    bool direct = false;
+    bf16 *xp = nullptr, *a1p = nullptr, *a2p = nullptr, *a3p = nullptr, *catp = nullptr,
+         *a4p = nullptr;
+    bf16* wc[6] = {};  // per layer, the direct kernel's weight layout (null: c2)
+    int nt[6] = {};    // per layer, the direct kernel's N tile
+    CUtensorMap map_x{}, map_a2{}, map_a3{}, map_cat{}, map_a4{};
 };
 
 namespace rf_cnn_impl {
@@ -442,11 +568,74 @@ rf_status conv_bwd(rf_cnn* c, const Layer& L, const bf16* x, int B, int H, int W
 rf_status sync_bf16_weights(rf_cnn* c) {
     k_f32_to_bf16<<<blocks_for(c->n_params), 256, 0, c->stream>>>(c->w, c->wb, c->n_params);
     c->launches++;
-    for (const Layer& L : c->layers) {
+    for (size_t li = 0; li < c->layers.size(); li++) {
+        const Layer& L = c->layers[li];
         k_transpose_w<<<blocks_for((size_t)L.cout * 9 * L.cin), 256, 0, c->stream>>>(
             c->wb + L.woff, L.cin, L.cout, c->wt + L.woff);
         c->launches++;
+        if (c->wc[li]) {
+            const size_t n = (size_t)(L.cin / 16) * 9 * c->nt[li] * 16;
+            k_conv_wc<<<blocks_for(n), 256, 0, c->stream>>>(c->wb + L.woff, L.cin, L.cout,
+                                                           c->nt[li], c->wc[li]);
+            c->launches++;
+        }
     }
+    CN(cudaGetLastError());
+    return RF_OK;
+}
+
+// one stride-1 layer on the direct kernel: `map` covers its padded input
+template <int NT>
+rf_status conv3_direct(rf_cnn* c, int li, const CUtensorMap& map, int B, int H, int W,
+                       bf16* y, float* yf) {
+    const Layer& L = c->layers[li];
+    using S = rf_tc::ConvSmem<NT>;
+    rf_tc::ConvGeom g;
+    g.Wp = W + 2;
+    g.npos = B * (H + 2) * (W + 2);
+    g.nbox = (rf_tc::kTM + 2 * (W + 3) + rf_tc::kConvBox - 1) / rf_tc::kConvBox;
+    g.stages = L.cin / 16;
+    const size_t smem = S::bytes(g.nbox);
+    static bool attr_set = false;
+    if (!attr_set) {
+        CN(cudaFuncSetAttribute(rf_tc::k_tc_conv3<NT, ConvOutPadded>,
+                                cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024));
+        attr_set = true;
+    }
+    if (smem > 227 * 1024) return cfail(RF_ERR_UNSUPPORTED, "cnn: row too long for the direct kernel");
+    ConvOutPadded ep{c->w + L.boff, L.cout, y, L.cout, yf, L.cout, L.relu, H, W, g.npos};
+    const unsigned grid = (unsigned)((g.npos + rf_tc::kTM - 1) / rf_tc::kTM);
+    rf_tc::k_tc_conv3<NT, ConvOutPadded><<<grid, rf_tc::kThreads, smem, c->stream>>>(
+        map, c->wc[li], g, ep, c->d_status, c->test_first_wait_polls);
+    c->launches++;
+    CN(cudaGetLastError());
+    return RF_OK;
+}
+
+// inference at the allocated size: padded activations, the stride-1 layers
+// on the direct kernel, the stride-2 layer on the im2col GEMM
+rf_status forward_direct(rf_cnn* c, const float* input, int B) {
+    const int H = c->H, W = c->W, H2 = Ho_of(H, 2), W2 = Ho_of(W, 2);
+    const Layer &c1 = c->layers[0], &c2 = c->layers[1], &c3 = c->layers[2];
+    k_pad_input<<<blocks_for((size_t)B * H * W * 2), 256, 0, c->stream>>>(input, B, H, W, c->xp);
+    c->launches++;
+    rf_status rs = conv3_direct<32>(c, 0, c->map_x, B, H, W, c->a1p, nullptr);
+    if (rs == RF_OK) {
+        const int M = B * H2 * W2, K = 9 * c2.cin;
+        rs = tc_gemm(c, M, c2.cout, K, 1,
+                     TcConvInPadded{c->a1p, H, W, c2.cin, H2, W2, c2.stride},
+                     TcRows{c->wb + c2.woff, K},
+                     ConvOutToPadded{c->w + c2.boff, c->a2p, M, c2.cout, c2.relu, H2, W2});
+    }
+    if (rs == RF_OK) rs = conv3_direct<96>(c, 2, c->map_a2, B, H2, W2, c->a3p, nullptr);
+    if (rs == RF_OK) rs = conv3_direct<16>(c, 3, c->map_a3, B, H2, W2, nullptr, c->o16);
+    if (rs != RF_OK) return rs;
+    k_concat_up_pad<<<blocks_for((size_t)B * H * W * ((c3.cout + c1.cout) / 8)), 256, 0,
+                      c->stream>>>(c->a3p, H2, W2, c3.cout, c->a1p, c1.cout, B, H, W, c->catp);
+    c->launches++;
+    rs = conv3_direct<64>(c, 4, c->map_cat, B, H, W, c->a4p, nullptr);
+    if (rs == RF_OK) rs = conv3_direct<16>(c, 5, c->map_a4, B, H, W, nullptr, c->o8);
+    if (rs != RF_OK) return rs;
     CN(cudaGetLastError());
     return RF_OK;
 }
@@ -516,6 +705,42 @@ rf_status backward(rf_cnn* c, int B, int H, int W) {
     return RF_OK;
 }
 
+// cuTensorMapEncodeTiled through the runtime's driver entry point (no link
+// against libcuda): a 2D map over a padded buffer viewed as [positions][C]
+// BF16, boxes of 8 channels x kConvBox positions, zero fill outside
+typedef CUresult (*EncodeTiledFn)(CUtensorMap*, CUtensorMapDataType, cuuint32_t, void*,
+                                  const cuuint64_t*, const cuuint64_t*, const cuuint32_t*,
+                                  const cuuint32_t*, CUtensorMapInterleave, CUtensorMapSwizzle,
+                                  CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
+
+bool encode_positions_map(CUtensorMap* m, const bf16* base, int C, size_t npos) {
+    static EncodeTiledFn fn = nullptr;
+    if (!fn) {
+        void* p = nullptr;
+        cudaDriverEntryPointQueryResult q{};
+        if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000,
+                                             cudaEnableDefault, &q) != cudaSuccess ||
+            q != cudaDriverEntryPointSuccess || !p)
+            return false;
+        fn = (EncodeTiledFn)p;
+    }
+    const cuuint64_t dims[2] = {(cuuint64_t)C, (cuuint64_t)npos};
+    const cuuint64_t strides[1] = {(cuuint64_t)C * 2};
+    const cuuint32_t box[2] = {8, (cuuint32_t)rf_tc::kConvBox};
+    const cuuint32_t es[2] = {1, 1};
+    return fn(m, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2, (void*)base, dims, strides, box, es,
+              CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
+              CU_TENSOR_MAP_L2_PROMOTION_L2_128B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
+}
+
+// whether the direct kernel's shared memory fits rows of width W
+bool direct_fits(int W) {
+    const int nbox = (rf_tc::kTM + 2 * (W + 3) + rf_tc::kConvBox - 1) / rf_tc::kConvBox;
+    const size_t lim = 227 * 1024;
+    return rf_tc::ConvSmem<32>::bytes(nbox) <= lim && rf_tc::ConvSmem<64>::bytes(nbox) <= lim &&
+           rf_tc::ConvSmem<96>::bytes(nbox) <= lim;
+}
+
 }  // namespace rf_cnn_impl
 
 extern "C" {
@@ -578,6 +803,36 @@ rf_status rf_cnn_create(int max_batch, int height, int width, unsigned long long
     c->part_floats = (size_t)256 * 96 * 9 * 96;  // chunks x largest cout x 9 cin
     alloc(&c->part, c->part_floats * 4);
     alloc(&c->d_loss, sizeof(double));
+    // inference on padded activations: on unless RF_CNN_DIRECT=0 (or rows too long)
+    const char* de = std::getenv("RF_CNN_DIRECT");
+    c->direct = !(de && de[0] == '0') && direct_fits(width);
+    const size_t PP = (size_t)(height + 2) * (width + 2);
+    const size_t PP2 = (size_t)((height + 1) / 2 + 2) * ((width + 1) / 2 + 2);
+    if (c->direct) {
+        alloc(&c->xp, B * PP * 16 * 2); alloc(&c->a1p, B * PP * 32 * 2);
+        alloc(&c->a2p, B * PP2 * 96 * 2); alloc(&c->a3p, B * PP2 * 96 * 2);
+        alloc(&c->catp, B * PP * 128 * 2); alloc(&c->a4p, B * PP * 64 * 2);
+        const int nts[6] = {32, 0, 96, 16, 64, 16};  // c2 (stride 2) keeps the GEMM
+        for (int li = 0; li < 6; li++)
+            if (nts[li]) {
+                c->nt[li] = nts[li];
+                alloc(&c->wc[li], (size_t)(c->layers[li].cin / 16) * 9 * nts[li] * 16 * 2);
+            }
+        // borders are never written: zero every padded buffer once
+        for (auto pb : {std::make_pair(c->xp, B * PP * 16), std::make_pair(c->a1p, B * PP * 32),
+                        std::make_pair(c->a2p, B * PP2 * 96), std::make_pair(c->a3p, B * PP2 * 96),
+                        std::make_pair(c->catp, B * PP * 128), std::make_pair(c->a4p, B * PP * 64)})
+            if (e == cudaSuccess) e = cudaMemset(pb.first, 0, pb.second * 2);
+        if (e == cudaSuccess &&
+            !(encode_positions_map(&c->map_x, c->xp, 16, B * PP) &&
+              encode_positions_map(&c->map_a2, c->a2p, 96, B * PP2) &&
+              encode_positions_map(&c->map_a3, c->a3p, 96, B * PP2) &&
+              encode_positions_map(&c->map_cat, c->catp, 128, B * PP) &&
+              encode_positions_map(&c->map_a4, c->a4p, 64, B * PP))) {
+            rf_cnn_destroy(c);
+            return cfail(RF_ERR_CUDA, "rf_cnn_create: tensor map encoding failed");
+        }
+    }
     if (e == cudaSuccess) e = cudaMemcpy(c->w, hw.data(), off * 4, cudaMemcpyHostToDevice);
     if (e == cudaSuccess) e = cudaMemset(c->m, 0, off * 4);
     if (e == cudaSuccess) e = cudaMemset(c->v, 0, off * 4);
@@ -607,7 +862,10 @@ rf_status rf_cnn_destroy(rf_cnn* c) {
                     (void*)c->a1, (void*)c->a2, (void*)c->a3, (void*)c->cat, (void*)c->a4,
                     (void*)c->o16, (void*)c->o8, (void*)c->g_o16, (void*)c->g_o8, (void*)c->g_a4,
                     (void*)c->g_cat, (void*)c->g_a3, (void*)c->g_a2, (void*)c->g_a1, (void*)c->gb,
-                    (void*)c->part, (void*)c->d_loss})
+                    (void*)c->part, (void*)c->d_loss, (void*)c->xp, (void*)c->a1p,
+                    (void*)c->a2p, (void*)c->a3p, (void*)c->catp, (void*)c->a4p})
+        if (p) cudaFree(p);
+    for (bf16* p : c->wc)
         if (p) cudaFree(p);
     delete c;
     return RF_OK;
@@ -653,7 +911,9 @@ rf_status rf_cnn_forward(rf_cnn* c, const float* input, int B, int H, int W, flo
     rf::NvtxRange range("rf_cnn_forward");
     if (!c || !input) return cfail(RF_ERR_INVALID_ARG, "rf_cnn_forward: null");
     rf_status rs = check_batch(c, B, H, W);
-    if (rs == RF_OK) rs = forward(c, input, B, H, W);
+    if (rs == RF_OK)
+        rs = (c->direct && H == c->H && W == c->W) ? forward_direct(c, input, B)
+                                                   : forward(c, input, B, H, W);
     if (rs != RF_OK) return rs;
     int H2 = (H + 1) / 2, W2 = (W + 1) / 2;
     if (out16)

@@ -27,6 +27,7 @@
 
 #include <cstdint>
 
+#include <cuda.h>
 #include <cuda_bf16.h>
 #include <cuda_runtime.h>
 
@@ -331,6 +332,197 @@ __global__ void __launch_bounds__(kThreads) k_tc_gemm(int M, int N, int K, int k
 #pragma unroll
                 for (int e = 0; e < 8; e++)
                     if (n0 + j + e < N) ep(blockIdx.z, m, n0 + j + e, v[e]);
+        }
+    }
+    tc_fence_before();
+    __syncthreads();
+    if (warp == 0) tmem_dealloc(tmem, S::kCols);
+}
+
+// ---------------------------------------------------------------------------
+// Direct 3x3 convolution (stride 1, padding 1) on padded activations
+// ---------------------------------------------------------------------------
+// Activations are NHWC with a one-pixel zero border: position
+// q = (b (H + 2) + y) (W + 2) + x of a [B][H + 2][W + 2][C] buffer.  For
+// output position q, tap (dy, dx) reads input position
+// q + (dy - 1)(W + 2) + (dx - 1), so 128 consecutive output positions read
+// 128 consecutive input positions for every tap: each tap is one MMA whose
+// A operand is a shifted view of one staged slab, and no im2col copy exists.
+// A CTA computes positions [q0, q0 + 128) (border positions too; their
+// outputs are not stored, so borders stay zero).  Per stage of 16 input
+// channels it stages, by TMA, the slab of input positions
+// [q0 - (W + 3), q0 + 128 + (W + 3)) as two planes of 8 channels (16 bytes
+// per position: the canonical no-swizzle K-major layout, core matrices of 8
+// positions, the two K halves one plane apart), and by a bulk copy the
+// stage's weights for all 9 taps in the same layout (host-prepared), then
+// one thread issues the 9 MMAs (M = 128, N = NT, K = 16) into the TMEM
+// accumulator.  kConvStages ring slots: loads of the next stages run while
+// a stage's MMAs do.  Out-of-range slab positions (before the first image,
+// past the buffer) are filled with zeros by the TMA unit and only reach
+// border outputs.
+constexpr int kConvBox = 128;  // positions per TMA box (2 KB per 8-channel plane)
+
+struct ConvGeom {
+    int Wp;      // padded row length W + 2
+    int npos;    // padded positions of this call: B (H + 2)(W + 2)
+    int nbox;    // TMA boxes per plane: ceil((128 + 2 (W + 3)) / 128)
+    int stages;  // input channels / 16
+};
+
+__device__ __forceinline__ void mbar_expect_tx(uint64_t* bar, uint32_t bytes) {
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)),
+                 "r"(bytes)
+                 : "memory");
+}
+
+// 2D tile of the tensor map at (c0 = channel, c1 = position) into shared memory
+__device__ __forceinline__ void tma_load_2d(void* dst, const void* map, int c0, int c1,
+                                            uint64_t* bar) {
+    asm volatile(
+        "cp.async.bulk.tensor.2d.shared::cluster.global.tile.mbarrier::complete_tx::bytes"
+        " [%0], [%1, {%2, %3}], [%4];" ::"r"(smem_u32(dst)),
+        "l"(map), "r"(c0), "r"(c1), "r"(smem_u32(bar))
+        : "memory");
+}
+
+// contiguous bytes (16-byte aligned, a multiple of 16) into shared memory
+__device__ __forceinline__ void bulk_load(void* dst, const void* src, uint32_t bytes,
+                                          uint64_t* bar) {
+    asm volatile(
+        "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::
+            "r"(smem_u32(dst)),
+        "l"(src), "r"(bytes), "r"(smem_u32(bar))
+        : "memory");
+}
+
+template <int NT>
+struct ConvSmem {
+    static_assert(NT % 16 == 0 && NT >= 16 && NT <= 128, "N tile");
+    static constexpr int kStages = NT >= 96 ? 2 : 3;
+    static constexpr uint32_t kWBytes = 9u * NT * 32u;  // one stage's weights
+    static constexpr uint32_t kCols = NT <= 32 ? 32 : (NT <= 64 ? 64 : 128);
+    __host__ __device__ static uint32_t plane_bytes(int nbox) { return (uint32_t)nbox * kConvBox * 16u; }
+    __host__ __device__ static uint32_t stage_bytes(int nbox) { return 2u * plane_bytes(nbox) + kWBytes; }
+    static size_t bytes(int nbox) { return (size_t)kStages * stage_bytes(nbox) + 2048; }
+};
+
+// `xmap`: CUtensorMap over the padded input viewed as [positions][C] BF16
+// (box: 8 channels x kConvBox positions); `wc`: weights as
+// [stage][tap][NT / 8][2][8][8] BF16.  `status` is set to 1 if a wait gave
+// up (the launch's outputs are then not written); `first_wait_polls` >= 0
+// caps the first slab wait of each CTA (a test hook, as for k_tc_gemm).
+// Every load issued is waited for (with the full limit) before the CTA
+// ends, and the last MMA commit before TMEM is released.
+template <int NT, class EP>
+__global__ void __launch_bounds__(kThreads) k_tc_conv3(const __grid_constant__ CUtensorMap xmap,
+                                                      const __nv_bfloat16* __restrict__ wc,
+                                                      ConvGeom g, EP ep, int* status,
+                                                      int first_wait_polls) {
+    extern __shared__ __align__(1024) unsigned char smem_raw[];
+    using S = ConvSmem<NT>;
+    constexpr int kS = S::kStages;
+    unsigned char* base = (unsigned char*)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
+    const uint32_t plane = S::plane_bytes(g.nbox);
+    const uint32_t stage_bytes = S::stage_bytes(g.nbox);
+    uint64_t* full = (uint64_t*)(base + kS * stage_bytes);
+    uint64_t* empty = full + kS;
+    uint32_t* tslot = (uint32_t*)(empty + kS);
+    int* fail = (int*)(tslot + 1);
+    int* produced = fail + 1;   // stages whose loads were issued
+    int* committed = fail + 2;  // stages whose MMAs were committed
+
+    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+    const int q0 = blockIdx.x * kTM;
+    const int halo = g.Wp + 1;
+    const int nst = g.stages;
+
+    if (tid == 0) {
+        for (int q = 0; q < kS; q++) {
+            mbar_init(&full[q], 1);
+            mbar_init(&empty[q], 1);
+        }
+        *fail = 0;
+        *produced = 0;
+        *committed = 0;
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
+    if (warp == 0) tmem_alloc(tslot, S::kCols);
+    tc_fence_before();
+    __syncthreads();
+    tc_fence_after();
+    const uint32_t tmem = *tslot;
+    constexpr uint32_t idesc = idesc_bf16(kTM, NT);
+
+    auto produce = [&](int j) {
+        const int sl = j % kS;
+        unsigned char* st = base + sl * stage_bytes;
+        mbar_expect_tx(&full[sl], stage_bytes);
+        for (int pl = 0; pl < 2; pl++)
+            for (int b = 0; b < g.nbox; b++)
+                tma_load_2d(st + pl * plane + b * (kConvBox * 16), &xmap, 16 * j + 8 * pl,
+                            q0 - halo + b * kConvBox, &full[sl]);
+        bulk_load(st + 2 * plane, wc + (size_t)j * 9 * NT * 16, S::kWBytes, &full[sl]);
+        *produced = j + 1;
+    };
+
+    if (tid == 0) {
+        for (int j = 0; j < kS && j < nst; j++) produce(j);
+        for (int j = 0; j < nst; j++) {
+            const int sl = j % kS;
+            const unsigned lim = (j == 0 && first_wait_polls >= 0) ? (unsigned)first_wait_polls
+                                                                  : kSpinLimit;
+            if (!mbar_wait(&full[sl], (unsigned)(j / kS) & 1u, lim)) {
+                *fail = 1;
+                break;
+            }
+            tc_fence_after();
+            const uint32_t a0 = smem_u32(base + sl * stage_bytes);
+            const uint32_t b0 = a0 + 2 * plane;
+#pragma unroll
+            for (int t = 0; t < 9; t++) {
+                const int off = halo + (t / 3 - 1) * g.Wp + (t % 3 - 1);
+                const uint64_t da = smem_desc(a0 + (uint32_t)off * 16u, plane, 128);
+                const uint64_t db = smem_desc(b0 + (uint32_t)t * NT * 32u, 128, 256);
+                mma_bf16(tmem, da, db, idesc, (j > 0 || t > 0) ? 1u : 0u);
+            }
+            mma_commit(&empty[sl]);
+            *committed = j + 1;
+            // refill the slot of stage j - 1 once its MMAs are done (stage j's
+            // MMAs stay queued meanwhile)
+            const int pj = j - 1;
+            if (pj >= 0 && pj + kS < nst) {
+                if (!mbar_wait(&empty[pj % kS], (unsigned)(pj / kS) & 1u)) {
+                    *fail = 1;
+                    break;
+                }
+                produce(pj + kS);
+            }
+        }
+    }
+    __syncthreads();
+    // drain: every load issued has landed and the last commit (which covers
+    // every earlier MMA) has arrived, each with the full limit
+    if (tid == 0) {
+        const int np = *produced, nc = *committed;
+        for (int j = nc; j < np; j++)  // loads no MMA waited for
+            if (!mbar_wait(&full[j % kS], (unsigned)(j / kS) & 1u)) *fail = 1;
+        if (nc > 0 && !mbar_wait(&empty[(nc - 1) % kS], (unsigned)((nc - 1) / kS) & 1u))
+            *fail = 1;
+    }
+    tc_fence_before();
+    __syncthreads();
+    tc_fence_after();
+    if (*fail) {
+        if (tid == 0) atomicExch(status, 1);
+    } else if (nst > 0) {
+        const int q = q0 + warp * 32 + lane;
+        const int p = ep.pos(q);  // < 0: a border position or past the call's positions
+        const uint32_t lane_addr = tmem + ((uint32_t)(warp * 32) << 16);
+#pragma unroll 1
+        for (int c = 0; c < NT; c += 8) {
+            float v[8];
+            tmem_ld8(lane_addr + (uint32_t)c, v);
+            if (p >= 0) ep.store(q, p, c, v);
         }
     }
     tc_fence_before();
