@@ -460,10 +460,12 @@ struct rf_cnn {
     double* d_loss = nullptr;
     cudaStream_t stream = nullptr;
     uint64_t launches = 0;
-    // inference on padded activations (forward at the allocated size)
+    // inference on padded activations (rf_cnn_forward; training keeps the GEMMs)
     bool direct = false;
     bf16 *xp = nullptr, *a1p = nullptr, *a2p = nullptr, *a3p = nullptr, *catp = nullptr,
          *a4p = nullptr;
+    int pad_h = -1, pad_w = -1;  // the frame size whose borders the padded buffers hold zero
+    size_t pad_elems[6] = {};    // BF16 elements allocated per padded buffer
     bf16* wc[6] = {};  // per layer, the direct kernel's weight layout (null: c2)
     int nt[6] = {};    // per layer, the direct kernel's N tile
     CUtensorMap map_x{}, map_a2{}, map_a3{}, map_cat{}, map_a4{};
@@ -612,11 +614,21 @@ rf_status conv3_direct(rf_cnn* c, int li, const CUtensorMap& map, int B, int H, 
     return RF_OK;
 }
 
-// inference at the allocated size: padded activations, the stride-1 layers
-// on the direct kernel, the stride-2 layer on the im2col GEMM
-rf_status forward_direct(rf_cnn* c, const float* input, int B) {
-    const int H = c->H, W = c->W, H2 = Ho_of(H, 2), W2 = Ho_of(W, 2);
+// inference: padded activations (laid out for this call's frame size, up to
+// the allocated one), the stride-1 layers on the direct kernel, the stride-2
+// layer on the im2col GEMM
+rf_status forward_direct(rf_cnn* c, const float* input, int B, int H, int W) {
+    const int H2 = Ho_of(H, 2), W2 = Ho_of(W, 2);
     const Layer &c1 = c->layers[0], &c2 = c->layers[1], &c3 = c->layers[2];
+    if (H != c->pad_h || W != c->pad_w) {
+        // a new frame size moves the borders: clear the buffers once (the
+        // kernels never write a border position of the size they run at)
+        bf16* bufs[6] = {c->xp, c->a1p, c->a2p, c->a3p, c->catp, c->a4p};
+        for (int k = 0; k < 6; k++)
+            CN(cudaMemsetAsync(bufs[k], 0, c->pad_elems[k] * 2, c->stream));
+        c->pad_h = H;
+        c->pad_w = W;
+    }
     k_pad_input<<<blocks_for((size_t)B * H * W * 2), 256, 0, c->stream>>>(input, B, H, W, c->xp);
     c->launches++;
     rf_status rs = conv3_direct<32>(c, 0, c->map_x, B, H, W, c->a1p, nullptr);
@@ -818,11 +830,10 @@ rf_status rf_cnn_create(int max_batch, int height, int width, unsigned long long
                 c->nt[li] = nts[li];
                 alloc(&c->wc[li], (size_t)(c->layers[li].cin / 16) * 9 * nts[li] * 16 * 2);
             }
-        // borders are never written: zero every padded buffer once
-        for (auto pb : {std::make_pair(c->xp, B * PP * 16), std::make_pair(c->a1p, B * PP * 32),
-                        std::make_pair(c->a2p, B * PP2 * 96), std::make_pair(c->a3p, B * PP2 * 96),
-                        std::make_pair(c->catp, B * PP * 128), std::make_pair(c->a4p, B * PP * 64)})
-            if (e == cudaSuccess) e = cudaMemset(pb.first, 0, pb.second * 2);
+        // cleared before the first call (forward_direct, per frame size)
+        const size_t elems[6] = {B * PP * 16, B * PP * 32, B * PP2 * 96,
+                                 B * PP2 * 96, B * PP * 128, B * PP * 64};
+        for (int k = 0; k < 6; k++) c->pad_elems[k] = elems[k];
         if (e == cudaSuccess &&
             !(encode_positions_map(&c->map_x, c->xp, 16, B * PP) &&
               encode_positions_map(&c->map_a2, c->a2p, 96, B * PP2) &&
@@ -912,8 +923,7 @@ rf_status rf_cnn_forward(rf_cnn* c, const float* input, int B, int H, int W, flo
     if (!c || !input) return cfail(RF_ERR_INVALID_ARG, "rf_cnn_forward: null");
     rf_status rs = check_batch(c, B, H, W);
     if (rs == RF_OK)
-        rs = (c->direct && H == c->H && W == c->W) ? forward_direct(c, input, B)
-                                                   : forward(c, input, B, H, W);
+        rs = c->direct ? forward_direct(c, input, B, H, W) : forward(c, input, B, H, W);
     if (rs != RF_OK) return rs;
     int H2 = (H + 1) / 2, W2 = (W + 1) / 2;
     if (out16)

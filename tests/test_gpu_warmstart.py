@@ -250,12 +250,14 @@ def test_learned_batch_pipeline_runs(torch_cuda, rf):
 
 
 def test_direct_convolutions_match_the_gemm_path(torch_cuda, monkeypatch):
-    """Inference at the allocated size runs the stride-1 layers as direct 3x3
-    convolutions on padded activations (TMA-staged slabs, nine shifted-view
-    MMAs per 16 input channels); RF_CNN_DIRECT=0 runs every layer as the
-    im2col GEMM.  Both accumulate BF16 products in FP32, in different
-    orders, so the outputs agree to the BF16 rounding of the activations;
-    a call with fewer images than allocated takes the direct path too."""
+    """Inference runs the stride-1 layers as direct 3x3 convolutions on
+    padded activations (TMA-staged slabs, nine shifted-view MMAs per 16
+    input channels); RF_CNN_DIRECT=0 runs every layer as the im2col GEMM.
+    Both accumulate BF16 products in FP32, in different orders, so the
+    outputs agree to the BF16 rounding of the activations.  One network
+    serves calls of several sizes up to its allocation, in turn (the padded
+    layout follows the call's frame size), with fewer images than allocated
+    too."""
     import os
 
     from reconflow_gb300.warmstart import WarmStartNet
@@ -263,22 +265,30 @@ def test_direct_convolutions_match_the_gemm_path(torch_cuda, monkeypatch):
     ckpt = os.path.join(os.path.dirname(os.path.dirname(os.path.abspath(__file__))),
                         "reconflow_gb300", "weights", "warmstart_f125.bin")
     rng = np.random.default_rng(11)
-    for B_alloc, B, H, W in ((2, 2, 12, 10), (4, 3, 91, 161), (1, 1, 37, 45)):
-        x = torch_cuda.as_tensor(rng.normal(0, 0.5, (B, H, W, 16)).astype(np.float32),
-                                 device="cuda")
-        outs = []
-        for flag in ("0", "1"):
-            monkeypatch.setenv("RF_CNN_DIRECT", flag)
-            net = WarmStartNet(B_alloc, H, W, seed=5)
-            net.load(ckpt)
+    alloc = (4, 91, 161)
+    calls = [(3, 90, 160), (4, 91, 161), (2, 12, 10), (1, 37, 45), (3, 90, 160)]
+    xs = [torch_cuda.as_tensor(rng.normal(0, 0.5, (B, H, W, 16)).astype(np.float32),
+                               device="cuda") for B, H, W in calls]
+    xs[4] = xs[0]
+    outs = {}
+    for flag in ("0", "1"):
+        monkeypatch.setenv("RF_CNN_DIRECT", flag)
+        net = WarmStartNet(*alloc, seed=5)
+        net.load(ckpt)
+        outs[flag] = []
+        for x in xs:
             o16, o8 = net.forward(x)
-            outs.append((o16.cpu().numpy(), o8.cpu().numpy()))
-            assert net.wait_gave_up() is False
-            net.close()
-        for a, b in zip(*outs):
+            outs[flag].append((o16.cpu().numpy(), o8.cpu().numpy()))
+        assert net.wait_gave_up() is False
+        net.close()
+    for (B, H, W), ref, got in zip(calls, outs["0"], outs["1"]):
+        for a, b in zip(ref, got):
             scale = float(np.abs(a).max())
             assert np.isfinite(b).all()
             assert np.abs(a - b).max() <= 3e-2 * scale, (B, H, W, np.abs(a - b).max(), scale)
             assert np.abs(a - b).mean() <= 3e-3 * scale, (B, H, W, np.abs(a - b).mean(), scale)
         if H * W > 1000:  # a different accumulation order ran
-            assert not np.array_equal(outs[0][1], outs[1][1])
+            assert not np.array_equal(ref[1], got[1])
+    # the same call before and after other sizes: identical results
+    for a, b in zip(outs["1"][0], outs["1"][4]):
+        assert np.array_equal(a, b)
