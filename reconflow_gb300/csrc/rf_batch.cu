@@ -483,8 +483,10 @@ cudaError_t fill_tiles(rf_batch* b) {
         if (e != cudaSuccess) return e;
         b->tiles_cap = tab.size();
     }
-    return cudaMemcpy(b->d_tiles, tab.data(), sizeof(TileEntry) * tab.size(),
-                      cudaMemcpyHostToDevice);
+    // on the batch's stream (the legacy stream would not order it with the
+    // non-blocking solve stream); the pageable source is staged on return
+    return cudaMemcpyAsync(b->d_tiles, tab.data(), sizeof(TileEntry) * tab.size(),
+                           cudaMemcpyHostToDevice, b->stream);
 }
 
 BatchCtx ctx_of(rf_batch* b, int level) {
@@ -869,6 +871,13 @@ rf_status rf_batch_create(const rf_params* p, int n_pairs, const int* widths, co
         return bfail(RF_ERR_OOM, std::string("rf_batch_create: ") + cudaGetErrorString(e));
     }
     b->stream = b->own;
+    // the pool's clearing memset and the table copies ran on the legacy
+    // default stream (fill_tiles before the stream existed): finish them
+    // before the non-blocking stream can read the pool
+    if (cudaDeviceSynchronize() != cudaSuccess) {
+        rf_batch_destroy(b);
+        return bfail(RF_ERR_CUDA, "rf_batch_create: initialisation");
+    }
     b->K0.assign((size_t)9 * n_pairs, 0.0);
     b->K1.assign((size_t)9 * n_pairs, 0.0);
     b->cams.assign(n_pairs, 0);

@@ -857,6 +857,10 @@ rf_status rf_cnn_create(int max_batch, int height, int width, unsigned long long
         return cfail(RF_ERR_CUDA, "rf_cnn_create: status init");
     }
     rf_status rs = sync_bf16_weights(c);
+    // the initialisation above ran on the legacy default stream; a stream
+    // set later (rf_cnn_set_stream) may be non-blocking: finish it now
+    if (rs == RF_OK && cudaDeviceSynchronize() != cudaSuccess)
+        rs = cfail(RF_ERR_CUDA, "rf_cnn_create: initialisation");
     if (rs != RF_OK) {
         rf_cnn_destroy(c);
         return rs;
@@ -899,8 +903,8 @@ rf_status rf_cnn_get_params(rf_cnn* c, float* host) {
 
 rf_status rf_cnn_set_params(rf_cnn* c, const float* host) {
     if (!c || !host) return cfail(RF_ERR_INVALID_ARG, "rf_cnn_set_params: null");
-    CN(cudaStreamSynchronize(c->stream));
-    CN(cudaMemcpy(c->w, host, c->n_params * 4, cudaMemcpyHostToDevice));
+    // on the network's stream, ahead of the conversion kernels that read it
+    CN(cudaMemcpyAsync(c->w, host, c->n_params * 4, cudaMemcpyHostToDevice, c->stream));
     return sync_bf16_weights(c);
 }
 

@@ -857,6 +857,9 @@ rf_status rf_pose_create(const rf_pose_params* p, int width, int height, rf_pose
         const Tables t = make_tables();
         e = cudaMemcpy(h->d_tab, &t, sizeof(Tables), cudaMemcpyHostToDevice);
     }
+    // the table copy ran on the legacy default stream: finish it before the
+    // handle's non-blocking stream reads the tables
+    if (e == cudaSuccess) e = cudaDeviceSynchronize();
     if (e != cudaSuccess) {
         rf_pose_destroy(h);
         return pfail(RF_ERR_OOM, std::string("rf_pose_create: ") + cudaGetErrorString(e));

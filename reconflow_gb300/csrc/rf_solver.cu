@@ -648,6 +648,14 @@ rf_status rf_create(const rf_params* p, rf_handle** out) {
             return cuda_fail(e, "rf_create: mask init");
         }
     }
+    // the clearing memset and copies above ran on the legacy default stream,
+    // which the handle's non-blocking stream does not wait for: finish them
+    // before any solve can read the pool
+    e = cudaDeviceSynchronize();
+    if (e != cudaSuccess) {
+        rf_destroy(h);
+        return cuda_fail(e, "rf_create: initialisation");
+    }
     *out = h;
     return RF_OK;
 }
@@ -725,9 +733,11 @@ rf_status rf_set_prior_flow(rf_handle* h, const float* u, const float* v, const 
         float* dst = k == 0 ? h->ufn : (k == 1 ? h->vfn : h->mask);
         const float* src = k == 0 ? u : (k == 1 ? v : mask);
         if (!src) {
+            // on the handle's stream, ordered before the next solve (a
+            // pageable source is staged before the call returns)
             std::vector<float> ones((size_t)h->stride * h->height, 1.0f);
-            RF_CUDA(cudaMemcpy(dst, ones.data(), ones.size() * sizeof(float),
-                               cudaMemcpyHostToDevice));
+            RF_CUDA(cudaMemcpyAsync(dst, ones.data(), ones.size() * sizeof(float),
+                                    cudaMemcpyHostToDevice, h->stream));
             continue;
         }
         RF_CUDA(cudaMemcpy2DAsync(dst, sp, src, (size_t)pitch * sizeof(float),
