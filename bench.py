@@ -66,7 +66,7 @@ WORKLOADS = {
     # 1 x 50); plain 5 x 100
     "720p-learned": dict(width=1280, height=720, pairs=64, levels=6, seed=2000, plain_warps=5,
                          plain_iters=100, warm_level=1, warm_warps=[1, 1],
-                         warm_iters=[1, 55], fallback_margin=0.02,
+                         warm_iters=[3, 50], fallback_margin=0.02,
                          checkpoint="reconflow_gb300/weights/warmstart_f125.bin",
                          tiles="reconflow_gb300/tuning/gb300_720p_x64.json"),
     # batched + learned on mixed sizes (the 4K / 1080p stream at a reduced

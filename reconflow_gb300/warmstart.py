@@ -43,7 +43,7 @@ F_NET = 125.0  # focal length (pixels) of the network's input grid
 # scenes: few level-0 iterations, more at the coarser levels.  The temporal
 # warm start of sequences refines with the same schedules.
 SCHEDULES = {
-    (1280, 720): dict(warm_level=1, warps=[1, 1], iters=[1, 55]),
+    (1280, 720): dict(warm_level=1, warps=[1, 1], iters=[3, 50]),
     (1920, 1080): dict(warm_level=2, warps=[1, 1, 1], iters=[4, 60, 80]),
     (3840, 2160): dict(warm_level=3, warps=[1, 1, 1, 1], iters=[4, 30, 60, 80]),
 }
