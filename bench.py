@@ -626,6 +626,7 @@ def run_learned(args, wl, world, rank, local):
     single_tiles = load_tiles(SINGLE_TILES)
     if single_tiles is not None:
         autotune.apply_single(f, single_tiles["levels"], wl["levels"])
+        autotune.apply_iterations_per_launch(lib, single_tiles)
     f.setCameraMatrices(scenes[0]["K"], scenes[0]["K"])
     f.copyImagesToDevice(scenes[0]["I0"], scenes[0]["I1"])
     if not args.solve_only:
@@ -1865,6 +1866,7 @@ def main():
         from reconflow_gb300 import autotune
 
         autotune.apply_single(f, single_tiles["levels"], wl["levels"])
+        autotune.apply_iterations_per_launch(lib, single_tiles)
     f.setCameraMatrices(sc["K"], sc["K"])
     f.copyImagesToDevice(I0, I1)
     flush = torch.empty(L2_FLUSH_BYTES // 4, dtype=torch.float32, device="cuda")
@@ -1976,7 +1978,9 @@ def main():
             "scaling": "weak", "vs_baseline": None, "dtype": "f32",
             "data": "synthetic (seeded scene generator)",
             "config": dict(config_of(wl), tiles=SINGLE_TILES if single_tiles is not None
-                           else "default 32x8"),
+                           else "default 32x8",
+                           cluster_px=(single_tiles or {}).get("iterations_per_launch",
+                                                               {}).get("cluster_px", 0)),
             "e2e": e2e, "roofline": roofline, "cpu_baseline": cpu,
             "clocks": clk.summary(), "gpu_launches": int(launches),
             "wall_s_timed": wall, "accuracy": accuracy,

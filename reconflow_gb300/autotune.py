@@ -1,4 +1,4 @@
-"""Tile-shape autotuner for the batched solver.
+"""Autotuner for the batched and single-pair solvers.
 
 Every step of a batched solve is one launch over the tiles of every pair at
 one pyramid level (``rf_batch.cu``); the tile shape decides how pixels map
@@ -11,10 +11,22 @@ level.  ``tiles_for`` turns a saved table into per-level shapes for a batch
 of any size by the pixel count of the level (summed over pairs).
 
     python -m reconflow_gb300.autotune --size 1280x720 --pairs 64 --out table.json
+
+The tile candidates span 2 to 8 warps per block (32 x 2 .. 16 x 16), so the
+shape search also picks the warps per block.  For one ReconFlow handle a
+second dimension is searched: iterations per launch.  The two-launch loop
+runs one inner iteration per pair of launches (a CUDA graph); the
+thread-block-cluster kernel runs all of a warp's iterations at a level in
+one launch (rf_set_cluster_pixels: every level of at most n pixels).
+`autotune_iterations_per_launch` times whole solves for each threshold and
+keeps the fastest; the table records it under "iterations_per_launch".
+
+    python -m reconflow_gb300.autotune --single --size 1280x720 --out table.json
 """
 from __future__ import annotations
 
 import json
+import os
 
 CANDIDATES = [(32, 8), (64, 4), (128, 2), (32, 4), (64, 2), (16, 16), (32, 2), (16, 8)]
 
@@ -69,6 +81,46 @@ def autotune_single(flow, R1, t1, n_levels, candidates=CANDIDATES, iters=20, log
                 " ".join(f"{k} {v * 1e3:.1f}us" for k, v in sorted(times.items(), key=lambda x: x[1])))
     flow.setTiles([x[0] for x in best], [x[1] for x in best])
     return table
+
+
+# rf_set_cluster_pixels thresholds: 0 = one iteration per launch everywhere;
+# at 1280x720, 1000 = level 5, 4000 = levels 4-5, 16384 = levels 3-5,
+# 60000 = levels 2-5 run a warp's iterations in one cluster launch
+CLUSTER_CANDIDATES = [0, 1000, 4000, 16384, 60000]
+
+
+def autotune_iterations_per_launch(flow, R1, t1, candidates=CLUSTER_CANDIDATES, solves=5,
+                                   log=None):
+    """Time `solves` whole solves of one ReconFlow handle (images and cameras
+    set) for each cluster threshold; set and return the fastest as
+    {"cluster_px": n, "ms": {n: ms per solve}}."""
+    import time
+
+    lib = flow._lib
+    times = {}
+    for px in candidates:
+        lib.rf_set_cluster_pixels(px)
+        for _ in range(2):  # the first solve captures the graph
+            flow.solveR(R1, t1, 5.0)
+        flow.synchronize()
+        t0 = time.perf_counter()
+        for _ in range(solves):
+            flow.solveR(R1, t1, 5.0)
+        flow.synchronize()
+        times[px] = (time.perf_counter() - t0) * 1000.0 / solves
+        if log:
+            log(f"cluster levels up to {px} px: {times[px]:.3f} ms per solve")
+    best = min(times, key=times.get)
+    lib.rf_set_cluster_pixels(best)
+    return {"cluster_px": best, "ms": {str(k): v for k, v in times.items()}}
+
+
+def apply_iterations_per_launch(lib, table):
+    """The single-pair table's iterations-per-launch choice (process-wide:
+    rf_set_cluster_pixels); tables without one leave the default."""
+    ent = table.get("iterations_per_launch") if isinstance(table, dict) else None
+    if ent is not None:
+        lib.rf_set_cluster_pixels(int(ent["cluster_px"]))
 
 
 def tiles_for(batch, table):
@@ -128,8 +180,22 @@ def main(argv=None):
         f.setCameraMatrices(sc["K"], sc["K"])
         f.copyImagesToDevice(sc["I0"], sc["I1"])
         table = autotune_single(f, sc["R"], sc["t"], a.levels, iters=a.iters, log=print)
+        # iterations per launch, on the schedule the drop-in path runs (the
+        # tile search uses a short one)
+        g = ReconFlow()
+        g.initializeR(w, h, 1, a.levels, 2.0, 14, sw["lambda_"], 0.0, sw["lambdaf"],
+                      sw["lambdams"], sw["alphaTv"], sw["alphaProj"], 0.5, sw["tau"], 5, 100,
+                      cvType=5, fix_quirks=sw["fix_quirks"])
+        g.setCameraMatrices(sc["K"], sc["K"])
+        g.copyImagesToDevice(sc["I0"], sc["I1"])
+        apply_single(g, table, a.levels)
+        ipl = autotune_iterations_per_launch(g, sc["R"], sc["t"], log=print)
+        g.close()
         with open(a.out, "w") as fh:
-            json.dump({"device": "GB300", "size": a.size, "pairs": 1, "levels": table}, fh, indent=1)
+            json.dump({"device": "GB300", "size": a.size, "pairs": 1, "levels": table,
+                       "iterations_per_launch": ipl,
+                       "command": f"python -m reconflow_gb300.autotune --single --size {a.size}"
+                                  f" --out {os.path.basename(a.out)}"}, fh, indent=1)
         f.close()
         return
     scs = [make_scene(w, h, seed=7000 + i, device="cuda") for i in range(a.pairs)]

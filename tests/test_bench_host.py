@@ -137,3 +137,22 @@ def test_sequence_guard():
     flags = [g.over(0, e * px, px, 4.0) for e in (8.0, 8.5, 9.0)]  # a lasting jump
     assert flags == [True, True, False]
     assert g.hist[1] == [9.0]
+
+
+def test_iterations_per_launch_table_entry():
+    """The single-pair table's iterations-per-launch choice reaches
+    rf_set_cluster_pixels; a table without one leaves the library alone."""
+    from reconflow_gb300 import autotune
+
+    class Lib:
+        got = []
+
+        def rf_set_cluster_pixels(self, n):
+            self.got.append(n)
+
+    lib = Lib()
+    autotune.apply_iterations_per_launch(lib, {"levels": []})
+    assert lib.got == []
+    autotune.apply_iterations_per_launch(lib, {"iterations_per_launch": {"cluster_px": 4000}})
+    assert lib.got == [4000]
+    assert autotune.CLUSTER_CANDIDATES[0] == 0  # one iteration per launch is always a candidate
