@@ -108,7 +108,7 @@ struct rf_handle {
     // warm start (rf_solve_warm): staging planes and the schedule's start
     float* warm[5] = {nullptr, nullptr, nullptr, nullptr, nullptr};
     int warm_level = -1, warm_warps = 0, warm_iters = 0;
-    int graph_key[3] = {-1, -1, -1};
+    long long graph_key[4] = {-1, -1, -1, -1};  // warm level, warps, iterations; cluster threshold
     // tile shape of the inner-iteration kernels at each level (rf_set_tiles)
     std::vector<int> tile_w, tile_h;
     // energy reduction buffers and the pose of the last solve
@@ -475,10 +475,13 @@ rf_status run_schedule(rf_handle* h, int kind) {
         if (kind == 3) return enqueue_plain(h, ru, rv, true);
         return enqueue_recon(h, ru, rv);
     };
-    const int key[3] = {kind >= 2 ? h->warm_level : -1, kind >= 2 ? h->warm_warps : -1,
-                        kind >= 2 ? h->warm_iters : -1};
+    // a captured schedule is reused while nothing it was captured with has
+    // changed (rf_set_cluster_pixels changes which levels take the cluster
+    // launch)
+    const long long key[4] = {kind >= 2 ? h->warm_level : -1, kind >= 2 ? h->warm_warps : -1,
+                              kind >= 2 ? h->warm_iters : -1, cluster_max_px()};
     if (h->graph && (key[0] != h->graph_key[0] || key[1] != h->graph_key[1] ||
-                     key[2] != h->graph_key[2])) {
+                     key[2] != h->graph_key[2] || key[3] != h->graph_key[3])) {
         cudaGraphExecDestroy(h->graph);
         h->graph = nullptr;
     }
