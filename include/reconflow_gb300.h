@@ -294,6 +294,13 @@ RF_API rf_status rf_batch_solve_warm(rf_batch* b, const double* R0, const double
 /* Energy of every pair's last ReconFlow solution (as rf_energy defines it
  * for one pair); out: n_pairs doubles on the host.  Synchronizes. */
 RF_API rf_status rf_batch_energies(rf_batch* b, double* out);
+/* rf_batch_energies without the wait: the evaluation and the copy of the n
+ * values into `out` are queued on the batch's stream and the call returns
+ * (with `out` in pinned host memory, rf_host_alloc, it returns at once);
+ * the values are valid once the stream has reached them (rf_batch_synchronize
+ * or a wait on the stream).  Lets a serving loop queue the next batch's
+ * solve before it reads this one's energies.  No reference counterpart. */
+RF_API rf_status rf_batch_energies_async(rf_batch* b, double* out);
 /* rf_batch_solve_warm with its own warps / iterations at each level:
  * warps[l], iters[l] for l = 0 .. level (level 0 = the finest). */
 RF_API rf_status rf_batch_solve_warm_levels(rf_batch* b, const double* R0, const double* t0,

@@ -105,6 +105,7 @@ _SIGS = [
     ("rf_batch_solve_flow", _I, [_VP]),
     ("rf_batch_solve_warm", _I, [_VP, _D, _D, _D, _D, _I, _I, _I]),
     ("rf_batch_energies", _I, [_VP, _VP]),
+    ("rf_batch_energies_async", _I, [_VP, _VP]),
     ("rf_batch_solve_warm_levels", _I, [_VP, _D, _D, _D, _D, _I, _VP, _VP]),
     ("rf_batch_warm_planes", _I, [_VP, _I, _VP, _VP, _VP, _VP, _VP]),
     ("rf_batch_image_planes", _I, [_VP, _I, _I, _VP, _VP]),

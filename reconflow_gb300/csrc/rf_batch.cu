@@ -460,6 +460,7 @@ struct rf_batch {
     double* d_energy = nullptr;            // [pair][kEnergyMaxBlocks] partials, then [pair] sums
     EnergyJob* d_ejobs = nullptr;          // [pair]
     EnergyJob* h_ejobs = nullptr;          // pinned staging of d_ejobs
+    cudaEvent_t ejobs_copied = nullptr;    // the last copy out of h_ejobs has run
     uint64_t launches = 0, graph_nodes = 0, enq = 0;
     int res_u = -1, res_v = -1;
     // pipelined inner iterations (pairs [0, split) and [split, n) half an
@@ -937,7 +938,7 @@ rf_status rf_batch_destroy(rf_batch* b) {
             cudaStreamSynchronize(st);
             cudaStreamDestroy(st);
         }
-    for (cudaEvent_t ev : {b->in_staged, b->in_free, b->out_ready, b->out_done})
+    for (cudaEvent_t ev : {b->in_staged, b->in_free, b->out_ready, b->out_done, b->ejobs_copied})
         if (ev) cudaEventDestroy(ev);
     if (b->stage_in) cudaFree(b->stage_in);
     if (b->stage_out) cudaFree(b->stage_out);
@@ -1036,12 +1037,23 @@ rf_status rf_batch_warm_planes(rf_batch* b, int pair, float** u, float** v, floa
 
 rf_status rf_batch_energies(rf_batch* b, double* out) {
     if (!b || !out) return bfail(RF_ERR_INVALID_ARG, "rf_batch_energies: null argument");
+    const rf_status rs = rf_batch_energies_async(b, out);
+    if (rs != RF_OK) return rs;
+    BC(cudaStreamSynchronize(b->stream));
+    return RF_OK;
+}
+
+rf_status rf_batch_energies_async(rf_batch* b, double* out) {
+    if (!b || !out) return bfail(RF_ERR_INVALID_ARG, "rf_batch_energies: null argument");
     if (!b->solved || b->p.method == RF_METHOD_TVL1 || b->last_R1.size() != (size_t)9 * b->n)
         return bfail(RF_ERR_STATE, "rf_batch_energies: needs a ReconFlow solve");
     if (!b->d_energy) BC(rf::dev_malloc((void**)&b->d_energy, sizeof(double) * b->n * (kEnergyMaxBlocks + 1)));
     if (!b->d_ejobs) BC(rf::dev_malloc((void**)&b->d_ejobs, sizeof(EnergyJob) * b->n));
     if (!b->h_ejobs) BC(rf::host_malloc((void**)&b->h_ejobs, sizeof(EnergyJob) * b->n));
-    BC(cudaStreamSynchronize(b->stream));  // the staging buffer is free to refill
+    if (!b->ejobs_copied) BC(cudaEventCreateWithFlags(&b->ejobs_copied, cudaEventDisableTiming));
+    // the pinned job table is free to refill once the last call's copy of it
+    // has run (usually long ago: no wait on the solve itself)
+    BC(cudaEventSynchronize(b->ejobs_copied));
     const int B0 = b->base_idx();
     double* sums = b->d_energy + (size_t)b->n * kEnergyMaxBlocks;
     int blocks = 0;
@@ -1064,11 +1076,11 @@ rf_status rf_batch_energies(rf_batch* b, double* out) {
     }
     BC(cudaMemcpyAsync(b->d_ejobs, b->h_ejobs, sizeof(EnergyJob) * b->n, cudaMemcpyHostToDevice,
                        b->stream));
+    BC(cudaEventRecord(b->ejobs_copied, b->stream));
     if (launch_energy_jobs(b->d_ejobs, b->n, blocks, b->stream) != 0)
         return bfail(RF_ERR_CUDA, "rf_batch_energies: launch");
     b->launches += 2;
     BC(cudaMemcpyAsync(out, sums, sizeof(double) * b->n, cudaMemcpyDeviceToHost, b->stream));
-    BC(cudaStreamSynchronize(b->stream));
     return RF_OK;
 }
 

@@ -471,6 +471,12 @@ class ReconFlowBatch:
         N.check(self._lib.rf_batch_energies(self._h, out.ctypes.data_as(ctypes.c_void_p)))
         return out
 
+    def energiesAsync(self, out_ptr: int):
+        """rf_batch_energies_async: queue the evaluation; the n doubles at
+        out_ptr (pinned host memory) are valid once the batch's stream has
+        reached them."""
+        N.check(self._lib.rf_batch_energies_async(self._h, ctypes.c_void_p(int(out_ptr))))
+
     def warmPlanes(self, pair):
         """Device pointers (u, v, X, Y, Z) of pair's warm-start input planes."""
         ps = [ctypes.c_void_p() for _ in range(5)]

@@ -60,6 +60,21 @@ def test_batch_recon_matches_single_pair(oracle, rf, fix, pipeline, monkeypatch)
         b.copyImagesToDevice(i, pad_rows(I0, s), pad_rows(I1, s))
     b.solveR([d[5] for d in data], [d[6] for d in data])
     E = b.energies()  # one batched evaluation of every pair
+    # the queued form into pinned memory gives the same values once the
+    # batch's stream has reached them
+    import ctypes
+
+    lib = rf.load()
+    pe = ctypes.c_void_p()
+    rf._native.check(lib.rf_host_alloc(8 * b.n, ctypes.byref(pe)))
+    try:
+        b.energiesAsync(pe.value)
+        b.synchronize()
+        Ea = np.ctypeslib.as_array(ctypes.cast(pe, ctypes.POINTER(ctypes.c_double)),
+                                   shape=(b.n,)).copy()
+    finally:
+        lib.rf_host_free(pe)
+    assert Ea.tobytes() == np.asarray(E, np.float64).tobytes()
     for i, (w, h, I0, I1, K, R, t) in enumerate(data):
         s = align_up(w)
         got_u, got_v = b.copyOpticalFlowToHost(i)
