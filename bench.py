@@ -126,14 +126,6 @@ E2E_MODE = ("pipelined: the frames of step k+1 go up and the results of step k c
             "copy streams while step k solves (rf_batch_stage_upload / "
             "rf_batch_stage_download, pinned host memory); every step's copies lie inside the "
             "timed wall time; serial_value: blocking upload_all + step + download_all per step")
-E2E_MODE_TWO_SLOTS = (
-    "pipelined over two batch slots (each its own batch, network, fallback solver and CUDA "
-    "stream): step k+1's solve and energies are queued on the other slot before step k's "
-    "energies are read and its fallback test runs; each slot's frames go up and its results "
-    "come down on copy streams (rf_batch_stage_upload / rf_batch_stage_download, pinned host "
-    "memory); every step's copies, the L2 flush and the fallback test lie inside the timed wall "
-    "time; one_slot_value: the same with one slot; serial_value: blocking upload_all + step + "
-    "download_all per step")
 LEARNED_METRIC = ("720p frame pairs/s, batched + learned warm start (vs the plain solver at "
                   "equal EPE)")
 PLAIN_METRIC = "720p frame pairs/s (ReconFlow flow + depth)"
@@ -282,113 +274,6 @@ def serve_pipelined(items, step, steps, flush=None):
         b.waitDownload()
     torch.cuda.synchronize()
     return time.perf_counter() - t0
-
-
-def serve_learned_two_slots(args, wl, lib, scenes, size, n, e_plain, mode, ceil, margin,
-                            new_batch, f, first, col, s0, flush):
-    """The learned serving loop over two batch slots.  Slot k % 2 solves step
-    k.  Step k+1 is queued (its frames taken from staging, its learned solve
-    and energies launched) before step k's energies are read on the host, so
-    the GPU has the next step's work while the host runs the fallback test
-    and queues the downloads.  Returns {"wall_s", "fallbacks"} of args.steps
-    steps (after two untimed ones)."""
-    import torch
-
-    import reconflow_gb300 as R
-    from reconflow_gb300 import autotune
-    from reconflow_gb300.warmstart import LearnedBatchSolver, WarmStartNet
-
-    W, H = size
-    Ks = [sc["K"] for sc in scenes]
-    Rs = [sc["R"] for sc in scenes]
-    ts = [sc["t"] for sc in scenes]
-    b1, ls1, st1 = first
-    st2 = torch.cuda.Stream()
-    net2 = WarmStartNet(n, (H // 8) + 1, (W // 8) + 1, seed=0)
-    net2.load(os.path.join(ROOT, wl["checkpoint"]))
-    b2 = new_batch(wl["plain_warps"], wl["plain_iters"])
-    b2.setStream(st2.cuda_stream)
-    ls2 = LearnedBatchSolver(net2, b2, (W, H), Ks[0], warm_level=wl["warm_level"],
-                             warps=wl["warm_warps"], iters=wl["warm_iters"])
-    ls2.set_stream(st2.cuda_stream)
-    f2 = R.ReconFlow()
-    f2.initializeR(W, H, 1, wl["levels"], 2.0, SOLVER["method"], SOLVER["lam"], 0.0,
-                   SOLVER["lambdaf"], SOLVER["lambdams"], 1.0 / SOLVER["theta"],
-                   SOLVER["alpha_proj"], 0.5, SOLVER["tau"], wl["plain_warps"], wl["plain_iters"],
-                   cvType=5, fix_quirks=SOLVER["fix_quirks"])
-    f2.setStream(st2.cuda_stream)
-    single_tiles = load_tiles(SINGLE_TILES)
-    if single_tiles is not None:
-        autotune.apply_single(f2, single_tiles["levels"], wl["levels"])
-    nb = H * s0 * 4
-    pinned = []
-
-    def host(nbytes):
-        p_ = ctypes.c_void_p()
-        R._native.check(lib.rf_host_alloc(nbytes, ctypes.byref(p_)))
-        pinned.append(p_)
-        return p_.value
-
-    slots = []
-    for bb, ls_, st_, ff, outs in ((b1, ls1, st1, f, col[2:8]),
-                                    (b2, ls2, st2, f2, [[host(nb) for _ in range(n)]
-                                                        for _ in range(6)])):
-        e_ptr = host(8 * n)
-        e_np = np.ctypeslib.as_array(ctypes.cast(e_ptr, ctypes.POINTER(ctypes.c_double)),
-                                     shape=(n,))
-        slots.append(dict(b=bb, ls=ls_, st=st_, f=ff, outs=outs, e_ptr=e_ptr, e_np=e_np))
-    fallbacks = []
-
-    def enqueue(sl, k, steps):
-        bb = sl["b"]
-        bb.takeUpload()
-        if k + 2 < steps:
-            bb.stageUpload(col[0], col[1], s0)
-        with torch.cuda.stream(sl["st"]):
-            flush.zero_()
-        sl["ls"].solve(Ks, Rs, ts)
-        bb.energiesAsync(sl["e_ptr"])
-
-    def finish(sl, k):
-        bb = sl["b"]
-        sl["st"].synchronize()
-        e = sl["e_np"]
-        bad = [i for i in range(n) if fallback_test(mode, e[i], e_plain[i], W * H, ceil, margin)]
-        for i in bad:  # the plain solve of the pair, from the slot's own frames
-            ff = sl["f"]
-            ff.setCameraMatrices(Ks[i], Ks[i])
-            ff.copyImagesToDeviceFromDevice(*bb.imagePlanes(i, 0), bb.strides[i])
-            ff.solveR(Rs[i], ts[i], 5.0)
-            bb.importResults(i, ff.deviceResults(), ff.stride)
-        fallbacks.append(len(bad))
-        o = sl["outs"]
-        bb.stageDownload(s0, u=o[0], v=o[1], inv_depth=o[2], X=o[3], Y=o[4], Z=o[5])
-
-    def serve(steps):
-        torch.cuda.synchronize()
-        t0 = time.perf_counter()
-        for sl in slots[:min(steps, 2)]:
-            sl["b"].stageUpload(col[0], col[1], s0)
-        enqueue(slots[0], 0, steps)
-        for k in range(steps):
-            if k + 1 < steps:
-                enqueue(slots[(k + 1) % 2], k + 1, steps)
-            finish(slots[k % 2], k)
-        for sl in slots:
-            sl["b"].waitDownload()
-        torch.cuda.synchronize()
-        return time.perf_counter() - t0
-
-    serve(2)
-    fallbacks.clear()
-    wall = serve(args.steps)
-    out = {"wall_s": wall, "fallbacks": list(fallbacks)}
-    torch.cuda.synchronize()
-    for obj in (b2, net2, f2):
-        obj.close()
-    for p_ in pinned:
-        lib.rf_host_free(p_)
-    return out
 
 
 def make_inputs(wl):
@@ -840,13 +725,9 @@ def run_learned(args, wl, world, rank, local):
                 torch.cuda.synchronize()
                 times.append(time.perf_counter() - t1)
             piped = serve_pipelined([(b, col, s0)], step, args.steps, flush)
-        two = serve_learned_two_slots(args, wl, lib, scenes, (W, H), n, e_plain, mode, ceil,
-                                      margin, new_batch, f, (b, ls, stream), col, s0, flush)
-        e2e = {"value": world * n * args.steps / max_over_ranks(two["wall_s"], world),
+        e2e = {"value": world * n * args.steps / max_over_ranks(piped, world),
                "unit": "pairs/s", "h2d_bytes_per_step": 2 * n * W * H * 4,
-               "d2h_bytes_per_step": 6 * n * W * H * 4, "mode": E2E_MODE_TWO_SLOTS,
-               "fallbacks_per_step": two["fallbacks"],
-               "one_slot_value": world * n * args.steps / max_over_ranks(piped, world),
+               "d2h_bytes_per_step": 6 * n * W * H * 4, "mode": E2E_MODE,
                "serial_value": world * n * args.steps / max_over_ranks(sum(times), world)}
         for ptrs in hosts:
             for p_ in ptrs:
