@@ -1424,8 +1424,11 @@ def run_c5_stream(args, wl, world, rank, local):
                 for j in range(n)]
         frames = [[torch.nn.functional.pad(torch.as_tensor(f_, device="cuda"), (0, s - W))
                    .contiguous() for f_ in q["frames"]] for q in seqs]
+        # one stream per size group: the host reads one group's energies
+        # while the other group's wave runs
         groups.append(dict(g=g, W=W, H=H, n=n, s=s, seqs=seqs, frames=frames,
-                           Ks=[q["K"] for q in seqs]))
+                           Ks=[q["K"] for q in seqs], st=torch.cuda.Stream()))
+    torch.cuda.synchronize()  # the frames (default stream) before the groups' streams use them
     gen_s = time.perf_counter() - t0
 
     def new_batch(G, warps, iters):
@@ -1435,7 +1438,7 @@ def run_c5_stream(args, wl, world, rank, local):
                              alphaProj=SOLVER["alpha_proj"], tau=SOLVER["tau"],
                              nWarpIters=warps, nSolverIters=iters,
                              fix_quirks=SOLVER["fix_quirks"])
-        b.setStream(stream.cuda_stream)
+        b.setStream(G["st"].cuda_stream)
         for i, K in enumerate(G["Ks"]):
             b.setCameraMatrices(i, K, K)
         return b
@@ -1470,7 +1473,7 @@ def run_c5_stream(args, wl, world, rank, local):
                                        warm_level=g["warm_level"], warps=g["warm_warps"],
                                        iters=g["warm_iters"], temporal_warps=g["temporal_warps"],
                                        temporal_iters=g["temporal_iters"])
-            tsol.set_stream(stream.cuda_stream)
+            tsol.set_stream(G["st"].cuda_stream)
             G.update(net=net, b=b, tsol=tsol)
             G["mode"], G["ceil_net"] = fallback_setup(args, G["W"], G["H"], "network")
             G["guard"] = FB.SequenceGuard(G["n"])
@@ -1479,7 +1482,7 @@ def run_c5_stream(args, wl, world, rank, local):
                           0.0, SOLVER["lambdaf"], SOLVER["lambdams"], 1.0 / SOLVER["theta"],
                           SOLVER["alpha_proj"], 0.5, SOLVER["tau"], wl["plain_warps"],
                           wl["plain_iters"], cvType=5, fix_quirks=SOLVER["fix_quirks"])
-            f.setStream(stream.cuda_stream)
+            f.setStream(G["st"].cuda_stream)
             G["f"] = f
 
     def solve_wave(G, k):
@@ -1561,7 +1564,11 @@ def run_c5_stream(args, wl, world, rank, local):
             for a, e_ in evs:
                 flush.zero_()
                 a.record(stream)
+                for G in groups:  # each size group works on its own stream
+                    G["st"].wait_stream(stream)
                 stream_once()
+                for G in groups:
+                    stream.wait_stream(G["st"])
                 e_.record(stream)
             torch.cuda.synchronize()
         step_ms = [a.elapsed_time(e_) for a, e_ in evs]
