@@ -126,6 +126,16 @@ E2E_MODE = ("pipelined: the frames of step k+1 go up and the results of step k c
             "copy streams while step k solves (rf_batch_stage_upload / "
             "rf_batch_stage_download, pinned host memory); every step's copies lie inside the "
             "timed wall time; serial_value: blocking upload_all + step + download_all per step")
+E2E_MODE_LAGGED = (
+    "pipelined serving loop with the fallback test one step behind: step k+1's frames are taken "
+    "and its solve and energies (rf_batch_energies_async) queued, after step k's results were "
+    "staged for download, before the host reads step k's energies; a pair that falls back is "
+    "solved again by the plain solver from its pinned host frames and its results downloaded; "
+    "frames go up and results come down on copy streams (rf_batch_stage_upload / "
+    "rf_batch_stage_download, pinned host memory); every step's copies, the L2 flush and the "
+    "fallback test lie inside the timed wall time; in_step_fallback_value: the loop with the "
+    "test inside each step (the host waits for each step's energies before queueing the next); "
+    "serial_value: blocking upload_all + step + download_all per step")
 LEARNED_METRIC = ("720p frame pairs/s, batched + learned warm start (vs the plain solver at "
                   "equal EPE)")
 PLAIN_METRIC = "720p frame pairs/s (ReconFlow flow + depth)"
@@ -274,6 +284,77 @@ def serve_pipelined(items, step, steps, flush=None):
         b.waitDownload()
     torch.cuda.synchronize()
     return time.perf_counter() - t0
+
+
+def serve_learned_lagged(b, ls, f, stream, scenes, size, n, col, s0, flush, steps, test,
+                         fell_back):
+    """The learned serving loop with the fallback test one step behind.
+    Step k+1 is queued (frames taken from staging, the learned solve, the
+    energies into pinned memory, the results staged for download) before the
+    host reads step k's energies, so the GPU has the next step while the host
+    tests this one.  A pair that falls back is solved again by the plain
+    single-pair solver `f` from its pinned host frames, and its results are
+    downloaded (a deployment rotating its output arrays writes them into step
+    k's).  Returns the wall time of `steps` steps."""
+    import torch
+
+    import reconflow_gb300 as R
+
+    mode, ceil, margin, e_plain = test
+    W, H = size
+    Ks = [sc["K"] for sc in scenes]
+    Rs = [sc["R"] for sc in scenes]
+    ts = [sc["t"] for sc in scenes]
+    lib = R.load()
+    pinned = []
+    e_np = []
+    for _ in range(2):
+        p_ = ctypes.c_void_p()
+        R._native.check(lib.rf_host_alloc(8 * n, ctypes.byref(p_)))
+        pinned.append(p_)
+        e_np.append(np.ctypeslib.as_array(ctypes.cast(p_, ctypes.POINTER(ctypes.c_double)),
+                                          shape=(n,)))
+    evs = [torch.cuda.Event(), torch.cuda.Event()]
+
+    def view(ptr):
+        return np.ctypeslib.as_array(ctypes.cast(ctypes.c_void_p(ptr),
+                                                 ctypes.POINTER(ctypes.c_float)), shape=(H, s0))
+
+    def queue(k):
+        b.takeUpload()
+        if k + 1 < steps:
+            b.stageUpload(col[0], col[1], s0)
+        with torch.cuda.stream(stream):
+            flush.zero_()
+        ls.solve(Ks, Rs, ts)
+        b.energiesAsync(pinned[k % 2].value)
+        evs[k % 2].record(stream)
+        b.stageDownload(s0, u=col[2], v=col[3], inv_depth=col[4], X=col[5], Y=col[6], Z=col[7])
+
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    b.stageUpload(col[0], col[1], s0)
+    queue(0)
+    for k in range(steps):
+        if k + 1 < steps:
+            queue(k + 1)
+        evs[k % 2].synchronize()
+        e = e_np[k % 2]
+        bad = [i for i in range(n) if fallback_test(mode, e[i], e_plain[i], W * H, ceil, margin)]
+        for i in bad:
+            f.setCameraMatrices(Ks[i], Ks[i])
+            f.copyImagesToDevice(view(col[0][i]), view(col[1][i]))
+            f.solveR(Rs[i], ts[i], 5.0)
+            f.copyOpticalFlowToHost()
+            f.copy3dToHost()
+            f.copyInverseDepthToHost()
+        fell_back.append(len(bad))
+    b.waitDownload()
+    torch.cuda.synchronize()
+    wall = time.perf_counter() - t0
+    for p_ in pinned:
+        lib.rf_host_free(p_)
+    return wall
 
 
 def make_inputs(wl):
@@ -725,9 +806,17 @@ def run_learned(args, wl, world, rank, local):
                 torch.cuda.synchronize()
                 times.append(time.perf_counter() - t1)
             piped = serve_pipelined([(b, col, s0)], step, args.steps, flush)
-        e2e = {"value": world * n * args.steps / max_over_ranks(piped, world),
+            lag_fb = []
+            serve_learned_lagged(b, ls, f, stream, scenes, (W, H), n, col, s0, flush, 2,
+                                 (mode, ceil, margin, e_plain), lag_fb)
+            lag_fb.clear()
+            lagged = serve_learned_lagged(b, ls, f, stream, scenes, (W, H), n, col, s0, flush,
+                                          args.steps, (mode, ceil, margin, e_plain), lag_fb)
+        e2e = {"value": world * n * args.steps / max_over_ranks(lagged, world),
                "unit": "pairs/s", "h2d_bytes_per_step": 2 * n * W * H * 4,
-               "d2h_bytes_per_step": 6 * n * W * H * 4, "mode": E2E_MODE,
+               "d2h_bytes_per_step": 6 * n * W * H * 4, "mode": E2E_MODE_LAGGED,
+               "fallbacks_per_step": lag_fb,
+               "in_step_fallback_value": world * n * args.steps / max_over_ranks(piped, world),
                "serial_value": world * n * args.steps / max_over_ranks(sum(times), world)}
         for ptrs in hosts:
             for p_ in ptrs:
