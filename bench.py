@@ -1282,6 +1282,10 @@ def run_learned_mixed(args, wl, world, rank, local):
             f.copyImagesToDevice(G["scenes"][0]["I0"], G["scenes"][0]["I1"])
             f.solveR(G["Rs"][0], G["ts"][0], 5.0)
             G["single_ms"] = statistics.median(timed(lambda: f.solveR(G["Rs"][0], G["ts"][0], 5.0), 2))
+            # the learned step runs each size group on its own stream
+            G["st"] = torch.cuda.Stream()
+            torch.cuda.synchronize()
+            f.setStream(G["st"].cuda_stream)
             G["f"] = f
             fct = net_factor(G["Ks"][0])
             net = WarmStartNet(G["n"], G["H"] // fct + 1, G["W"] // fct + 1, seed=0)
@@ -1291,16 +1295,20 @@ def run_learned_mixed(args, wl, world, rank, local):
             G["ls"] = LearnedBatchSolver(net, b, (G["W"], G["H"]), G["Ks"][0],
                                          warm_level=G["g"]["warm_level"],
                                          warps=G["g"]["warm_warps"], iters=G["g"]["warm_iters"])
-            G["ls"].set_stream(stream.cuda_stream)
+            G["ls"].set_stream(G["st"].cuda_stream)
     margin = wl["fallback_margin"]
     fallbacks = []
     for G in groups:
         G["mode"], G["ceil"] = fallback_setup(args, G["W"], G["H"], "network")
 
     def step():
+        # both groups' solves are queued before the first group's energies
+        # are read: one group's solve runs while the host tests the other
         nbad = 0
         for G in groups:
+            G["st"].wait_stream(stream)
             G["ls"].solve(G["Ks"], G["Rs"], G["ts"])
+        for G in groups:
             e = G["b"].energies()
             bad = [i for i in range(G["n"])
                    if fallback_test(G["mode"], e[i], G["e_plain"][i], G["W"] * G["H"], G["ceil"],
@@ -1312,6 +1320,8 @@ def run_learned_mixed(args, wl, world, rank, local):
                 f.solveR(G["Rs"][i], G["ts"][i], 5.0)
                 G["b"].importResults(i, f.deviceResults(), f.stride)
             nbad += len(bad)
+        for G in groups:
+            stream.wait_stream(G["st"])
         fallbacks.append(nbad)
 
     with torch.cuda.stream(stream):
