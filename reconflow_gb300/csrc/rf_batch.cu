@@ -45,6 +45,7 @@ constexpr int kMaxLevels = 16;
 
 struct BatchPair {
     LevelDims dims[kMaxLevels];
+    int off;  // the pair's region: floats into every plane
 };
 
 // One block of a level: the tile whose first pixel is (x0, y0) in pair
@@ -121,6 +122,20 @@ __global__ void __launch_bounds__(kMaxTile) k_batch_rows2(BatchCtx ctx, int leve
     const int ix = t.x0 + (int)threadIdx.x, iy = t.y0 + 2 * (int)threadIdx.y;
     if (ix >= d.w || iy >= d.h) return;
     op.two(t, d, ix, iy);
+}
+
+// Level-0 row copies (the staging gathers): one warp per row of a pair's
+// level 0, block (pair, chunk of 8 rows, striding by the grid's chunks);
+// Op::row(e0, w, lane) moves the row's w elements starting at element e0
+// of every plane.
+constexpr int kRowWarps = 8;
+template <class Op>
+__global__ void __launch_bounds__(32 * kRowWarps) k_batch_rows_l0(const BatchPair* pairs, Op op) {
+    const BatchPair& p = pairs[blockIdx.x];
+    const LevelDims d = p.dims[0];
+    for (int row = (int)blockIdx.y * kRowWarps + ((int)threadIdx.x >> 5); row < d.h;
+         row += (int)gridDim.y * kRowWarps)
+        op.row((size_t)p.off + (size_t)row * d.s, d.w, (int)threadIdx.x & 31);
 }
 
 // Two operations in one launch on disjoint tile ranges of the level's table
@@ -348,23 +363,40 @@ struct OpUpscale {
 
 // staged frames -> the pairs' level-0 image planes (rf_batch_take_upload):
 // the same pixels the per-pair copies of rf_batch_upload_images write, in
-// one launch over the level's tiles (staging and pool share the layout)
+// one launch over every pair's rows (staging and pool share the layout)
 struct OpStageIn {
     const float* s0;
     const float* s1;
     float* d0;
     float* d1;
-    __device__ void operator()(const BatchCtx&, const TileEntry& t, int, LevelDims d, int ix,
-                               int iy) const {
-        const size_t e = (size_t)t.off + ix + (size_t)iy * d.s;
-        const float a = s0[e], c = s1[e];
-        d0[e] = a;
-        d1[e] = c;
+    // k_batch_rows_l0: lane `lane` takes columns lane, lane + 32, ...; four
+    // columns' loads go out before their stores
+    __device__ void row(size_t e0, int w, int lane) const {
+        int c = lane;
+        for (; c + 96 < w; c += 128) {
+            float a[4], b[4];
+#pragma unroll
+            for (int k = 0; k < 4; k++) {
+                a[k] = s0[e0 + c + 32 * k];
+                b[k] = s1[e0 + c + 32 * k];
+            }
+#pragma unroll
+            for (int k = 0; k < 4; k++) {
+                d0[e0 + c + 32 * k] = a[k];
+                d1[e0 + c + 32 * k] = b[k];
+            }
+        }
+        for (; c < w; c += 32) {
+            const float a = s0[e0 + c], b = s1[e0 + c];
+            d0[e0 + c] = a;
+            d1[e0 + c] = b;
+        }
     }
 };
 
 // the pairs' results -> the download staging planes (u, v, 1/Z, X, Y, Z
-// at k * total; bit k of `mask` selects output k), one launch for every pair
+// at k * total; bit k of `mask` selects output k), one launch over every
+// pair's rows
 struct OpStageOut {
     const float* u;
     const float* v;
@@ -374,9 +406,8 @@ struct OpStageOut {
     float* out;
     size_t total;
     int mask;
-    __device__ void operator()(const BatchCtx&, const TileEntry& t, int, LevelDims d, int ix,
-                               int iy) const {
-        const size_t e = (size_t)t.off + ix + (size_t)iy * d.s;
+    // element e of every requested output
+    __device__ __forceinline__ void at(size_t e) const {
         if (mask & 1) out[e] = u[e];
         if (mask & 2) out[total + e] = v[e];
         if (mask & 60) {
@@ -386,6 +417,34 @@ struct OpStageOut {
             if (mask & 16) out[4 * total + e] = Y[e];
             if (mask & 32) out[5 * total + e] = z;
         }
+    }
+    // k_batch_rows_l0: as OpStageIn::row, the requested fields of four
+    // columns loaded before their stores
+    __device__ void row(size_t e0, int w, int lane) const {
+        int c = lane;
+        for (; c + 96 < w; c += 128) {
+            float fu[4], fv[4], fx[4], fy[4], fz[4];
+#pragma unroll
+            for (int k = 0; k < 4; k++) {
+                const size_t e = e0 + c + 32 * k;
+                fu[k] = (mask & 1) ? u[e] : 0.0f;
+                fv[k] = (mask & 2) ? v[e] : 0.0f;
+                fz[k] = (mask & 60) ? Z[e] : 0.0f;
+                fx[k] = (mask & 8) ? X[e] : 0.0f;
+                fy[k] = (mask & 16) ? Y[e] : 0.0f;
+            }
+#pragma unroll
+            for (int k = 0; k < 4; k++) {
+                const size_t e = e0 + c + 32 * k;
+                if (mask & 1) out[e] = fu[k];
+                if (mask & 2) out[total + e] = fv[k];
+                if (mask & 4) out[2 * total + e] = 1.0f / fz[k];
+                if (mask & 8) out[3 * total + e] = fx[k];
+                if (mask & 16) out[4 * total + e] = fy[k];
+                if (mask & 32) out[5 * total + e] = fz[k];
+            }
+        }
+        for (; c < w; c += 32) at(e0 + c);
     }
 };
 
@@ -571,6 +630,19 @@ int launch_op(rf_batch* b, int level, const Op& op) {
     if (tiles <= 0) return 0;
     const dim3 block(b->tile_w[level], b->tile_h[level]);
     k_batch<Op><<<tiles, block, 0, b->stream>>>(ctx_of(b, level), level, op);
+    b->enq++;
+    return rf::launch_status();
+}
+
+// a level-0 row operation (Op::row) over every pair's rows in one launch
+template <class Op>
+int launch_rows_l0(rf_batch* b, const Op& op) {
+    int max_h = 0;
+    for (int i = 0; i < b->n; i++) max_h = b->dims[i][0].h > max_h ? b->dims[i][0].h : max_h;
+    int chunks = (max_h + kRowWarps - 1) / kRowWarps;
+    if (chunks <= 0) return 0;
+    if (chunks > 65535) chunks = 65535;  // the grid's y limit; blocks stride over the rest
+    k_batch_rows_l0<Op><<<dim3(b->n, chunks), 32 * kRowWarps, 0, b->stream>>>(b->d_pairs, op);
     b->enq++;
     return rf::launch_status();
 }
@@ -884,8 +956,10 @@ rf_status rf_batch_create(const rf_params* p, int n_pairs, const int* widths, co
     cudaError_t e = rf::dev_malloc((void**)&b->pool, pool_floats * sizeof(float));
     if (e == cudaSuccess) e = cudaMemset(b->pool, 0, pool_floats * sizeof(float));
     std::vector<BatchPair> hp(n_pairs);
-    for (int i = 0; i < n_pairs; i++)
+    for (int i = 0; i < n_pairs; i++) {
         for (int l = 0; l < b->L; l++) hp[i].dims[l] = b->dims[i][l];
+        hp[i].off = (int)b->base_off[i];
+    }
     b->tile_w.assign(b->L, BX);
     b->tile_h.assign(b->L, BY);
     {
@@ -1056,7 +1130,7 @@ rf_status rf_batch_energies_async(rf_batch* b, double* out) {
     BC(cudaEventSynchronize(b->ejobs_copied));
     const int B0 = b->base_idx();
     double* sums = b->d_energy + (size_t)b->n * kEnergyMaxBlocks;
-    int blocks = 0;
+    int blocks = 0, max_blocks = 0;
     // every pair's evaluation in one launch (blocks in pair order) and the
     // sums in a second; each pair's value is its single-pair evaluation's
     for (int i = 0; i < b->n; i++) {
@@ -1073,11 +1147,12 @@ rf_status rf_batch_energies_async(rf_batch* b, double* out) {
         j.partial = b->d_energy + (size_t)i * kEnergyMaxBlocks;
         j.out = sums + i;
         blocks += j.nblocks;
+        if (j.nblocks > max_blocks) max_blocks = j.nblocks;
     }
     BC(cudaMemcpyAsync(b->d_ejobs, b->h_ejobs, sizeof(EnergyJob) * b->n, cudaMemcpyHostToDevice,
                        b->stream));
     BC(cudaEventRecord(b->ejobs_copied, b->stream));
-    if (launch_energy_jobs(b->d_ejobs, b->n, blocks, b->stream) != 0)
+    if (launch_energy_jobs(b->d_ejobs, b->n, blocks, max_blocks, b->stream) != 0)
         return bfail(RF_ERR_CUDA, "rf_batch_energies: launch");
     b->launches += 2;
     BC(cudaMemcpyAsync(out, sums, sizeof(double) * b->n, cudaMemcpyDeviceToHost, b->stream));
@@ -1337,10 +1412,10 @@ rf_status rf_batch_take_upload(rf_batch* b) {
     if (!b) return bfail(RF_ERR_INVALID_ARG, "rf_batch_take_upload: null batch");
     if (!b->up_staged) return bfail(RF_ERR_STATE, "rf_batch_take_upload: no frames staged");
     BC(cudaStreamWaitEvent(b->stream, b->in_staged, 0));
-    // one kernel for every pair (128 pitched device copies cost ~2 ms of
-    // the solve stream for 64 720p pairs; the kernel moves 0.47 GB at HBM speed)
-    BL(launch_op(b, 0, OpStageIn{b->stage_in, b->stage_in + b->total,
-                                 plane_base(b, b->pI0(0)), plane_base(b, b->pI1(0))}));
+    // one kernel for every pair, a warp per row (128 pitched device copies
+    // cost ~2 ms of the solve stream for 64 720p pairs)
+    BL(launch_rows_l0(b, OpStageIn{b->stage_in, b->stage_in + b->total,
+                                   plane_base(b, b->pI0(0)), plane_base(b, b->pI1(0))}));
     b->launches++;
     for (int i = 0; i < b->n; i++) b->imgs[i] = 1;
     BC(cudaEventRecord(b->in_free, b->stream));
@@ -1371,11 +1446,11 @@ rf_status rf_batch_stage_download(rf_batch* b, float* const* u, float* const* v,
     // one kernel gathers the requested results (and 1/Z) of every pair
     if (mask) {
         const float* none = nullptr;
-        BL(launch_op(b, 0, OpStageOut{plane_base(b, b->res_u), plane_base(b, b->res_v),
-                                      recon ? plane_base(b, B0 + P_X) : none,
-                                      recon ? plane_base(b, B0 + P_Y) : none,
-                                      recon ? plane_base(b, B0 + P_Z) : none, b->stage_out,
-                                      b->total, mask}));
+        BL(launch_rows_l0(b, OpStageOut{plane_base(b, b->res_u), plane_base(b, b->res_v),
+                                        recon ? plane_base(b, B0 + P_X) : none,
+                                        recon ? plane_base(b, B0 + P_Y) : none,
+                                        recon ? plane_base(b, B0 + P_Z) : none, b->stage_out,
+                                        b->total, mask}));
         b->launches++;
     }
     BC(cudaEventRecord(b->out_ready, b->stream));

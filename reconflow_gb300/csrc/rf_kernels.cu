@@ -462,47 +462,74 @@ __global__ void k_flow_color(const float* __restrict__ u, const float* __restric
 // partials in a fixed order, so the result is deterministic.
 constexpr int kEnergyThreads = 256;
 
+// One pixel's energy: per-pixel terms in FP32 (GB300's FP64 division and
+// square root would bound the kernel).
+__device__ __forceinline__ float energy_px(const EnergyArgs& a, LevelDims d, int ix, int iy) {
+    const int s = d.s, pos = ix + iy * s;
+    float x = ((float)ix + a.u[pos] + 0.5f) / (float)d.w;
+    float y = ((float)iy + a.v[pos] + 0.5f) / (float)d.h;
+    float i1w = tex2d(a.I1, d.w, d.h, s, x, y);
+    const float u0 = a.u[pos], v0 = a.v[pos];
+    const float data = a.lambda * fabsf(i1w - a.I0[pos]);
+    const float ux = ix + 1 < d.w ? a.u[pos + 1] - u0 : 0.0f;
+    const float uy = iy + 1 < d.h ? a.u[pos + s] - u0 : 0.0f;
+    const float vx = ix + 1 < d.w ? a.v[pos + 1] - v0 : 0.0f;
+    const float vy = iy + 1 < d.h ? a.v[pos + s] - v0 : 0.0f;
+    const float tv = sqrtf(ux * ux + uy * uy) + sqrtf(vx * vx + vy * vy);
+    float proj = 0.0f;
+    if (a.recon) {
+        const float Xp = a.X[pos], Yp = a.Y[pos], Zp = a.Z[pos];
+        const float X2 = a.R1f[0] * Xp + a.R1f[1] * Yp + a.R1f[2] * Zp + a.t1f[0];
+        const float Y2 = a.R1f[3] * Xp + a.R1f[4] * Yp + a.R1f[5] * Zp + a.t1f[1];
+        const float Z2 = a.R1f[6] * Xp + a.R1f[7] * Yp + a.R1f[8] * Zp + a.t1f[2];
+        const float uc = a.fxf * X2 / Z2 + a.cxf - (float)ix;
+        const float vc = a.fxf * Y2 / Z2 + a.cyf - (float)iy;
+        const float du = u0 - uc, dv = v0 - vc;
+        float r2 = du * du + dv * dv;
+        if (!(r2 < 1.0f)) r2 = 1.0f;  // truncated at 1 px^2 (NaN included)
+        proj = 0.5f * a.alpha_proj * r2;
+    }
+    float px_e = data + tv + proj;
+    // a pixel whose flow is not finite (a NaN or infinite gradient) counts
+    // each term at its cap: a unit brightness residual, unit gradients of u
+    // and v, the truncated reprojection residual
+    if (!isfinite(px_e)) px_e = a.lambda + 2.0f + (a.recon ? 0.5f * a.alpha_proj : 0.0f);
+    return px_e;
+}
+
 // Block `blk` of `nblk` of one energy evaluation: its grid-stride share of
-// the pixels, summed in double in a fixed order, into partial[blk].
+// the pixels (pixel i = iy * w + ix, then i + step, ...), summed in double
+// in that order, into partial[blk].
 __device__ __forceinline__ void energy_block(const EnergyArgs& a, LevelDims d, int blk, int nblk,
                                              double* partial) {
     __shared__ double red[kEnergyThreads / 32];
     double e = 0.0;
     const int npx = d.w * d.h;
-    for (int i = blk * kEnergyThreads + threadIdx.x; i < npx; i += nblk * kEnergyThreads) {
-        const int ix = i % d.w, iy = i / d.w, s = d.s, pos = ix + iy * s;
-        float x = ((float)ix + a.u[pos] + 0.5f) / (float)d.w;
-        float y = ((float)iy + a.v[pos] + 0.5f) / (float)d.h;
-        float i1w = tex2d(a.I1, d.w, d.h, s, x, y);
-        // per-pixel terms in FP32 (GB300's FP64 division and square root
-        // would bound the kernel), summed in double
-        const float u0 = a.u[pos], v0 = a.v[pos];
-        const float data = a.lambda * fabsf(i1w - a.I0[pos]);
-        const float ux = ix + 1 < d.w ? a.u[pos + 1] - u0 : 0.0f;
-        const float uy = iy + 1 < d.h ? a.u[pos + s] - u0 : 0.0f;
-        const float vx = ix + 1 < d.w ? a.v[pos + 1] - v0 : 0.0f;
-        const float vy = iy + 1 < d.h ? a.v[pos + s] - v0 : 0.0f;
-        const float tv = sqrtf(ux * ux + uy * uy) + sqrtf(vx * vx + vy * vy);
-        float proj = 0.0f;
-        if (a.recon) {
-            const float Xp = a.X[pos], Yp = a.Y[pos], Zp = a.Z[pos];
-            const float X2 = a.R1f[0] * Xp + a.R1f[1] * Yp + a.R1f[2] * Zp + a.t1f[0];
-            const float Y2 = a.R1f[3] * Xp + a.R1f[4] * Yp + a.R1f[5] * Zp + a.t1f[1];
-            const float Z2 = a.R1f[6] * Xp + a.R1f[7] * Yp + a.R1f[8] * Zp + a.t1f[2];
-            const float uc = a.fxf * X2 / Z2 + a.cxf - (float)ix;
-            const float vc = a.fxf * Y2 / Z2 + a.cyf - (float)iy;
-            const float du = u0 - uc, dv = v0 - vc;
-            float r2 = du * du + dv * dv;
-            if (!(r2 < 1.0f)) r2 = 1.0f;  // truncated at 1 px^2 (NaN included)
-            proj = 0.5f * a.alpha_proj * r2;
+    const int step = nblk * kEnergyThreads;
+    int i = blk * kEnergyThreads + (int)threadIdx.x;
+    // (ix, iy) of pixel i, advanced by `step` without a division per pixel
+    int iy = i / d.w, ix = i - iy * d.w;
+    const int sy = step / d.w, sx = step - sy * d.w;
+    // two pixels per pass, so that their loads overlap; added in order
+    while (i + step < npx) {
+        int ix1 = ix + sx, iy1 = iy + sy;
+        if (ix1 >= d.w) {
+            ix1 -= d.w;
+            iy1++;
         }
-        float px_e = data + tv + proj;
-        // a pixel whose flow is not finite (a NaN or infinite gradient)
-        // counts each term at its cap: a unit brightness residual, unit
-        // gradients of u and v, the truncated reprojection residual
-        if (!isfinite(px_e)) px_e = a.lambda + 2.0f + (a.recon ? 0.5f * a.alpha_proj : 0.0f);
-        e += (double)px_e;
+        const float e0 = energy_px(a, d, ix, iy);
+        const float e1 = energy_px(a, d, ix1, iy1);
+        e += (double)e0;
+        e += (double)e1;
+        i += 2 * step;
+        ix = ix1 + sx;
+        iy = iy1 + sy;
+        if (ix >= d.w) {
+            ix -= d.w;
+            iy++;
+        }
     }
+    if (i < npx) e += (double)energy_px(a, d, ix, iy);
     for (int o = 16; o > 0; o >>= 1) e += __shfl_down_sync(0xffffffffu, e, o);
     if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = e;
     __syncthreads();
@@ -548,6 +575,14 @@ __global__ void __launch_bounds__(kEnergyThreads) k_energy_partial_jobs(const En
     }
     const EnergyJob& j = jobs[lo];
     energy_block(j.a, j.d, b - j.first_block, j.nblocks, j.partial);
+}
+
+// The same blocks on a 2D grid: blockIdx.y = the job, blockIdx.x = its
+// block (blocks past the job's count return), no search.
+__global__ void __launch_bounds__(kEnergyThreads) k_energy_partial_grid(const EnergyJob* jobs) {
+    const EnergyJob& j = jobs[blockIdx.y];
+    if ((int)blockIdx.x >= j.nblocks) return;
+    energy_block(j.a, j.d, (int)blockIdx.x, j.nblocks, j.partial);
 }
 
 __global__ void k_energy_final_jobs(const EnergyJob* jobs) {
@@ -841,9 +876,13 @@ int energy_blocks(LevelDims d) {
     return nb < kEnergyMaxBlocks ? nb : kEnergyMaxBlocks;
 }
 
-int launch_energy_jobs(const EnergyJob* jobs, int n, int total_blocks, cudaStream_t st) {
+int launch_energy_jobs(const EnergyJob* jobs, int n, int total_blocks, int max_blocks,
+                       cudaStream_t st) {
     if (n <= 0 || total_blocks <= 0) return 0;
-    k_energy_partial_jobs<<<total_blocks, kEnergyThreads, 0, st>>>(jobs, n);
+    if (n <= 65535 && max_blocks > 0)
+        k_energy_partial_grid<<<dim3(max_blocks, n), kEnergyThreads, 0, st>>>(jobs);
+    else
+        k_energy_partial_jobs<<<total_blocks, kEnergyThreads, 0, st>>>(jobs, n);
     k_energy_final_jobs<<<n, 32, 0, st>>>(jobs);
     return check_launch();
 }

@@ -202,7 +202,8 @@ constexpr int kEnergyMaxBlocks = 1024;
 int energy_blocks(LevelDims d);
 // every job of the device array `jobs` (blocks in job order, total_blocks in
 // all): the same partials and sums as launch_energy of each job alone
-int launch_energy_jobs(const EnergyJob* jobs, int n, int total_blocks, cudaStream_t st);
+int launch_energy_jobs(const EnergyJob* jobs, int n, int total_blocks, int max_blocks,
+                       cudaStream_t st);
 
 // Solution energy on one level (data + TV + reprojection) into *out (device
 // double); `partial` holds `nblocks` doubles.
