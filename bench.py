@@ -135,7 +135,10 @@ E2E_MODE_LAGGED = (
     "rf_batch_stage_download, pinned host memory); every step's copies, the L2 flush and the "
     "fallback test lie inside the timed wall time; in_step_fallback_value: the loop with the "
     "test inside each step (the host waits for each step's energies before queueing the next); "
-    "serial_value: blocking upload_all + step + download_all per step")
+    "serial_value: blocking upload_all + step + download_all per step; value and "
+    "in_step_fallback_value: the median of three timed runs of `steps` steps each (all three in "
+    "*_runs), because the host link is shared with the other GPUs' jobs on the machine")
+E2E_RUNS = 3
 LEARNED_METRIC = ("720p frame pairs/s, batched + learned warm start (vs the plain solver at "
                   "equal EPE)")
 PLAIN_METRIC = "720p frame pairs/s (ReconFlow flow + depth)"
@@ -805,19 +808,30 @@ def run_learned(args, wl, world, rank, local):
                 e2e_step()
                 torch.cuda.synchronize()
                 times.append(time.perf_counter() - t1)
-            piped = serve_pipelined([(b, col, s0)], step, args.steps, flush)
+            piped_runs = [serve_pipelined([(b, col, s0)], step, args.steps, flush)
+                          for _ in range(E2E_RUNS)]
             lag_fb = []
             serve_learned_lagged(b, ls, f, stream, scenes, (W, H), n, col, s0, flush, 2,
                                  (mode, ceil, margin, e_plain), lag_fb)
             lag_fb.clear()
-            lagged = serve_learned_lagged(b, ls, f, stream, scenes, (W, H), n, col, s0, flush,
-                                          args.steps, (mode, ceil, margin, e_plain), lag_fb)
-        e2e = {"value": world * n * args.steps / max_over_ranks(lagged, world),
+            lagged_runs = []
+            for _ in range(E2E_RUNS):
+                run_fb = []
+                lagged_runs.append(serve_learned_lagged(
+                    b, ls, f, stream, scenes, (W, H), n, col, s0, flush, args.steps,
+                    (mode, ceil, margin, e_plain), run_fb))
+                lag_fb.extend(run_fb)
+        rate = lambda t: world * n * args.steps / max_over_ranks(t, world)  # noqa: E731
+        lag_values = [rate(t) for t in lagged_runs]
+        piped_values = [rate(t) for t in piped_runs]
+        e2e = {"value": float(np.median(lag_values)),
                "unit": "pairs/s", "h2d_bytes_per_step": 2 * n * W * H * 4,
                "d2h_bytes_per_step": 6 * n * W * H * 4, "mode": E2E_MODE_LAGGED,
+               "value_runs": lag_values,
                "fallbacks_per_step": lag_fb,
-               "in_step_fallback_value": world * n * args.steps / max_over_ranks(piped, world),
-               "serial_value": world * n * args.steps / max_over_ranks(sum(times), world)}
+               "in_step_fallback_value": float(np.median(piped_values)),
+               "in_step_fallback_runs": piped_values,
+               "serial_value": rate(sum(times))}
         for ptrs in hosts:
             for p_ in ptrs:
                 lib.rf_host_free(p_)
