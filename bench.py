@@ -821,7 +821,10 @@ def run_learned(args, wl, world, rank, local):
                     b, ls, f, stream, scenes, (W, H), n, col, s0, flush, args.steps,
                     (mode, ceil, margin, e_plain), run_fb))
                 lag_fb.extend(run_fb)
-        rate = lambda t: world * n * args.steps / max_over_ranks(t, world)  # noqa: E731
+
+        def rate(t):  # pairs/s of `args.steps` steps in t seconds, slowest rank
+            return world * n * args.steps / max_over_ranks(t, world)
+
         lag_values = [rate(t) for t in lagged_runs]
         piped_values = [rate(t) for t in piped_runs]
         e2e = {"value": float(np.median(lag_values)),
