@@ -162,13 +162,14 @@ RF_API rf_status rf_solve_warm(rf_handle* h, const double R0[9], const double t0
 RF_API rf_status rf_solve_flow_warm(rf_handle* h, int level, const float* u, const float* v,
                                     int pitch, int on_device, int warps, int iters);
 
-/* Energy of the last solution (no reference counterpart), summed in double
- * over the level-0 pixels: lambda * |I1(x + u) - I0(x)| + |grad u| +
+/* Energy of the last solution (no reference counterpart), summed over the
+ * level-0 pixels: lambda * |I1(x + u) - I0(x)| + |grad u| +
  * |grad v| (+ alpha_proj / 2 * min(|(u, v) - uc(X)|^2, 1) for ReconFlow, uc
  * the projection of the solved point as SolveUc computes it; the
  * reprojection residual is truncated at 1 px^2, so a few pixels whose point
- * projects near infinity cannot dominate the sum).  Per-pixel terms in FP32,
- * the sum in double.  Blocking. */
+ * projects near infinity cannot dominate the sum).  Per-pixel terms in FP32;
+ * each GPU thread adds its own few dozen pixels in FP32, and the thread sums
+ * are added in double in a fixed order.  Blocking. */
 RF_API rf_status rf_energy(rf_handle* h, double* energy);
 
 /* CudaFlow::copyOpticalFlowToHost(u, v) (Cudaflow.cu:320-325). Blocking. */

@@ -498,12 +498,14 @@ __device__ __forceinline__ float energy_px(const EnergyArgs& a, LevelDims d, int
 }
 
 // Block `blk` of `nblk` of one energy evaluation: its grid-stride share of
-// the pixels (pixel i = iy * w + ix, then i + step, ...), summed in double
-// in that order, into partial[blk].
+// the pixels (pixel i = iy * w + ix, then i + step, ...).  Each thread sums
+// its own pixels in FP32 in that order (at most a few dozen: GB300's FP64
+// pipe, not memory, bounded a per-pixel double sum), then the warp and the
+// block add the thread sums in double, in a fixed order, into partial[blk].
 __device__ __forceinline__ void energy_block(const EnergyArgs& a, LevelDims d, int blk, int nblk,
                                              double* partial) {
     __shared__ double red[kEnergyThreads / 32];
-    double e = 0.0;
+    float et = 0.0f;
     const int npx = d.w * d.h;
     const int step = nblk * kEnergyThreads;
     int i = blk * kEnergyThreads + (int)threadIdx.x;
@@ -519,8 +521,8 @@ __device__ __forceinline__ void energy_block(const EnergyArgs& a, LevelDims d, i
         }
         const float e0 = energy_px(a, d, ix, iy);
         const float e1 = energy_px(a, d, ix1, iy1);
-        e += (double)e0;
-        e += (double)e1;
+        et += e0;
+        et += e1;
         i += 2 * step;
         ix = ix1 + sx;
         iy = iy1 + sy;
@@ -529,7 +531,8 @@ __device__ __forceinline__ void energy_block(const EnergyArgs& a, LevelDims d, i
             iy++;
         }
     }
-    if (i < npx) e += (double)energy_px(a, d, ix, iy);
+    if (i < npx) et += energy_px(a, d, ix, iy);
+    double e = (double)et;
     for (int o = 16; o > 0; o >>= 1) e += __shfl_down_sync(0xffffffffu, e, o);
     if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = e;
     __syncthreads();
@@ -871,9 +874,12 @@ int launch_energy(const float* I0, const float* I1, const float* u, const float*
     return check_launch();
 }
 
+// at least 8 pixels per thread (fewer thread sums to add in double), at
+// most kEnergyMaxBlocks blocks
 int energy_blocks(LevelDims d) {
-    const int nb = (d.w * d.h + kEnergyThreads - 1) / kEnergyThreads;
-    return nb < kEnergyMaxBlocks ? nb : kEnergyMaxBlocks;
+    const long long per_block = 8LL * kEnergyThreads;
+    const long long nb = ((long long)d.w * d.h + per_block - 1) / per_block;
+    return nb < kEnergyMaxBlocks ? (int)nb : kEnergyMaxBlocks;
 }
 
 int launch_energy_jobs(const EnergyJob* jobs, int n, int total_blocks, int max_blocks,

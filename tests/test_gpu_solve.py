@@ -368,7 +368,8 @@ def test_energy_matches_oracle(oracle, rf, method):
     else:
         e_ref = oracle.energy(I0, I1, res["u"], res["v"], res["X"], res["Y"], res["Z"], w, h, s,
                               50.0, 60.0, R, t, K)
-    # per-pixel terms in FP32 on the GPU, FP64 in the oracle; both sum in double
+    # per-pixel terms and each thread's few pixels in FP32 on the GPU, FP64 in
+    # the oracle; the GPU adds the thread sums in double
     assert e_gpu == pytest.approx(e_ref, rel=1e-5)
 
 
